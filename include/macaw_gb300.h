@@ -1,0 +1,226 @@
+/*
+ * macaw_gb300.h -- C ABI of the GB300 particle tracker.
+ *
+ * The hot path MaCaw runs through MOOSE's ray tracing module and OpenMC
+ * (source birth, tet-to-tet walk, cross-section lookup, distance sampling,
+ * collision, element track-length tallies) is exposed here as batch-level
+ * calls with plain pointers and sizes.  Every call returns 0 on success or
+ * a non-zero MC_ERR_* code; mc_last_error() then holds a message.  A context
+ * is bound to one CUDA device and one stream, and its calls are serialised
+ * by an internal mutex.  Device-side failures (lost or stuck particles, bad
+ * cross sections) never trap: they are counted in mc_stats and reported as
+ * status codes in per-history traces.
+ *
+ * Each entry point names the reference interface it stands in for, by file
+ * and line in idaholab/macaw.
+ */
+#ifndef MACAW_GB300_H
+#define MACAW_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MC_OK 0
+#define MC_ERR_ARG 1     /* invalid argument (paramError / mooseError) */
+#define MC_ERR_STATE 2   /* call out of order (missing mesh, data, source) */
+#define MC_ERR_CUDA 3    /* CUDA runtime failure */
+#define MC_ERR_DEVICE 4  /* device-side status word reported a failure */
+#define MC_ERR_NOMEM 5   /* device or host allocation failed */
+
+/* boundary condition types: MOOSE KillRayBC / ReflectRayBC as used in
+ * test/tests/study/openmc_study.i:49-54 */
+#define MC_BC_VACUUM 0
+#define MC_BC_REFLECT 1
+
+/* precision forms */
+#define MC_PREC_FP64 0   /* plain FP64, per-history traces bit-exact to the oracle */
+#define MC_PREC_MIXED 1  /* FP32 walk/XS, FP64 near faces/edges and for tallies */
+
+/* execution forms */
+#define MC_MODE_HISTORY 0    /* one thread per history, persistent grid */
+#define MC_MODE_EVENT 1      /* event queues: birth, xs, advance, collide */
+
+/* source kinds */
+#define MC_SRC_POINT 0
+#define MC_SRC_BOX 1
+#define MC_SRC_CYLINDERS 2
+#define MC_SRC_WATT 0
+#define MC_SRC_MONO 1
+
+/* tally readback kinds */
+#define MC_TALLY_BATCH 0   /* raw sum of wgt*track length of the current batch */
+#define MC_TALLY_SUM 1     /* OpenMC results SUM: sum over batches of batch/weight */
+#define MC_TALLY_SUM_SQ 2  /* OpenMC results SUM_SQ */
+
+/* history end states (mc_trace.status) */
+#define MC_ST_LEAKED 1
+#define MC_ST_ABSORBED 2
+#define MC_ST_CUTOFF 3
+#define MC_ST_STUCK 4
+#define MC_ST_LOST 5
+#define MC_ST_BADXS 6
+
+typedef struct mc_ctx mc_ctx;
+
+/* Fixed source (the settings.xml <source> that OpenMCStudy::defineRays
+ * samples per history; src/userobjects/OpenMCStudy.C:317-360). */
+typedef struct {
+  int32_t space;  /* MC_SRC_POINT | MC_SRC_BOX | MC_SRC_CYLINDERS */
+  int32_t energy; /* MC_SRC_WATT | MC_SRC_MONO */
+  double point[3];
+  double box_lo[3];
+  double box_hi[3];
+  int32_t n_cyl;
+  int32_t pad;
+  const double* cyl_xy; /* 2*n_cyl cylinder axis positions (x, y) */
+  double cyl_r, cyl_z0, cyl_z1;
+  double watt_a, watt_b; /* eV, 1/eV */
+  double mono_E;         /* eV */
+} mc_source_desc;
+
+/* One source site: the ray MaCaw defines per history (start point,
+ * direction, aux energy and weight; src/userobjects/OpenMCStudy.C:335-360).
+ * The tracking stream is seeded from the history index, as for sites the
+ * library samples itself. */
+typedef struct {
+  double x, y, z;
+  double u, v, w;
+  double E;
+  double wgt;
+} mc_site;
+
+/* One batch of histories (OpenMCStudy::generateRays + execute +
+ * postExecuteStudy for a fixed-source batch;
+ * src/userobjects/OpenMCStudy.C:218-242,366-402). */
+typedef struct {
+  int64_t first_history;   /* 0-based global index of the first history; id = index + 1 */
+  int64_t n_histories;
+  int64_t bank_size;       /* particles in flight (event mode); 0 = all */
+  uint64_t seed;           /* master seed */
+  int32_t precision;       /* MC_PREC_* */
+  int32_t mode;            /* MC_MODE_* */
+  int32_t block_size;      /* threads per block; 0 = default */
+  int32_t max_seg_per_advance; /* event mode: segments per advance launch; 0 = until event */
+  int32_t record_traces;   /* 1: fill one mc_trace per history */
+  int32_t accumulate;      /* 1: fold this batch into SUM/SUM_SQ and clear the batch tally */
+  int32_t sort_queue;      /* event mode: 1 sorts the advance queue by element */
+  int32_t profile;         /* 1: time every advance launch with CUDA events (mc_stats.ms_advance) */
+  const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
+} mc_run_desc;
+
+/* Per-history outcome: element sequence hash, counts, end state. */
+typedef struct {
+  int64_t id;
+  uint64_t hash;
+  int32_t status;
+  int32_t n_seg;
+  int32_t n_coll;
+  int32_t elem;
+  int32_t face;
+  int32_t pad;
+  double E;
+  double x, y, z;
+} mc_trace;
+
+typedef struct {
+  int64_t n_hist, n_seg, n_coll, n_leak, n_absorb, n_cutoff, n_stuck, n_lost, n_badxs;
+  int64_t n_fallback;   /* mixed form: segments re-solved in FP64 */
+  int64_t n_xs;         /* macroscopic XS evaluations */
+  int64_t n_launch;     /* kernels launched by the last mc_run */
+  double leak_weight;
+  double ms_total;      /* device time of the last mc_run (CUDA events) */
+  double ms_advance;    /* device time in the segment-walk kernels */
+  int64_t n_advance_launch;
+} mc_stats;
+
+/* ---- context --------------------------------------------------------- */
+/* Replaces: OpenMCStudy construction, openmc_init + openmc_simulation_init
+ * (src/userobjects/OpenMCStudy.C:78-204). */
+int mc_ctx_create(int device, mc_ctx** out);
+/* Replaces: OpenMCStudy::~OpenMCStudy / openmc_finalize (OpenMCStudy.C:207-216). */
+int mc_ctx_destroy(mc_ctx* ctx);
+/* Replaces: mooseError / openmc_err_msg (OpenMCStudy.C:129-131). */
+const char* mc_last_error(mc_ctx* ctx);
+int mc_version(void);
+
+/* ---- mesh (the libMesh mesh MOOSE traces on; one cell per element,
+ * one universe per subdomain: OpenMCStudy.C:152-187) ------------------- */
+/* tet_side_bid: optional 4*n_tet sideset ids (-1 interior/none); side f is
+ * the face opposite local vertex f.  Builds face adjacency, outward face
+ * planes and the start-point locator, and uploads them. */
+int mc_mesh_upload(mc_ctx* ctx, int64_t n_vtx, const double* xyz, int64_t n_tet,
+                   const int32_t* tet_vtx, const int32_t* tet_block, const int32_t* tet_side_bid);
+/* Replaces: [RayBCs] ReflectRayBC / KillRayBC boundary lists
+ * (test/tests/study/openmc_study.i:49-54). */
+int mc_bc_set(mc_ctx* ctx, int32_t boundary_id, int32_t type);
+
+/* ---- cross sections (OpenMC nuclide/material data the collision kernel
+ * evaluates; CollisionKernel.C:143) ------------------------------------- */
+int mc_nuclide_add(mc_ctx* ctx, int64_t n_pts, const double* E, const double* sig_t,
+                   const double* sig_s, double awr, int32_t* out_index);
+int mc_material_add(mc_ctx* ctx, int32_t material_id, int32_t n, const int32_t* nuclides,
+                    const double* densities);
+/* Replaces: CollisionKernel 'blocks'/'materials' params and the
+ * block -> material map (src/raykernels/CollisionKernel.C:34-37,63-69,110). */
+int mc_block_material_map(mc_ctx* ctx, int32_t n, const int32_t* blocks,
+                          const int32_t* materials);
+int mc_set_hash_bins(mc_ctx* ctx, int32_t n_bins);
+
+/* ---- source ---------------------------------------------------------- */
+int mc_source_set(mc_ctx* ctx, const mc_source_desc* src);
+
+/* ---- run ------------------------------------------------------------- */
+/* Replaces: one batch of OpenMCStudy::generateRays / execute /
+ * postExecuteStudy, whose per-segment work is CollisionKernel::onSegment
+ * (src/raykernels/CollisionKernel.C:98-275).  Asynchronous on the context
+ * stream unless traces or accumulation need a sync; mc_sync waits. */
+int mc_run(mc_ctx* ctx, const mc_run_desc* desc);
+int mc_sync(mc_ctx* ctx);
+/* Replaces: the loop over openmc::initialize_history in
+ * OpenMCStudy::defineRays (src/userobjects/OpenMCStudy.C:317-360): samples
+ * the source sites of histories [first, first+n) on the device and copies
+ * them to the HOST array out. */
+int mc_source_sample(mc_ctx* ctx, int64_t first, int64_t n, uint64_t seed, mc_site* out);
+/* Work of this context goes to the given cudaStream_t (NULL: the context's
+ * own stream). */
+int mc_ctx_set_stream(mc_ctx* ctx, void* stream);
+
+/* ---- results --------------------------------------------------------- */
+/* Replaces: OpenMCTallyAux::computeValue element readback
+ * (src/auxkernels/OpenMCTallyAux.C:187-205), for the element flux tally. */
+int mc_tally_download(mc_ctx* ctx, int32_t kind, double* out, int64_t n);
+int mc_tally_reset(mc_ctx* ctx);
+int mc_trace_download(mc_ctx* ctx, mc_trace* out, int64_t n);
+int mc_stats_get(mc_ctx* ctx, mc_stats* out);
+/* Number of completed accumulated batches (OpenMC n_realizations). */
+int mc_batches_done(mc_ctx* ctx, int64_t* out);
+
+/* ---- synthetic problem generators (host only; no device needed) ------ */
+/* Cube [0,L]^3 of n^3 hexes, six Kuhn tets each; sidesets 0..5 as MOOSE's
+ * GeneratedMesh (back, bottom, right, top, left, front). */
+int mc_gen_cube_sizes(int32_t n, int64_t* n_vtx, int64_t* n_tet);
+int mc_gen_cube(int32_t n, double L, double* xyz, int32_t* tet_vtx, int32_t* tet_block,
+                int32_t* tet_side_bid);
+/* Square lattice of nx*ny pin cells (pitch, height, nz axial layers, n_sec
+ * azimuthal sectors), rings at r_fuel / r_clad; blocks 1 fuel, 2 clad,
+ * 3 moderator; outer sidesets 0..5. */
+int mc_gen_lattice_sizes(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int32_t n_fuel_rings,
+                         int64_t* n_vtx, int64_t* n_tet);
+int mc_gen_lattice(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int32_t n_fuel_rings,
+                   double pitch, double height, double r_fuel, double r_clad, double* xyz,
+                   int32_t* tet_vtx, int32_t* tet_block, int32_t* tet_side_bid);
+/* Synthetic nuclide: n_pts log-uniform energies in [E_min, E_max] eV,
+ * sigma_t = a/sqrt(E) + n_peaks Lorentzians, sigma_s = f_s*sigma_t,
+ * awr; all drawn from (seed, index). */
+int mc_gen_nuclide(uint64_t seed, int32_t index, int64_t n_pts, double E_min, double E_max,
+                   int32_t n_peaks, double* E, double* sig_t, double* sig_s, double* awr);
+/* n atom densities uniform in [lo, hi] drawn from (seed, index). */
+int mc_gen_densities(uint64_t seed, int32_t index, int32_t n, double lo, double hi, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

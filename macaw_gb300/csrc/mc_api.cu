@@ -1,0 +1,670 @@
+// mc_api.cu -- context, uploads, run loop and readback behind the C ABI.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/macaw_gb300.h"
+#include "mc_host.h"
+#include "mc_kernels.h"
+
+using namespace mc;
+
+namespace {
+
+// Owning device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t alloc(size_t n) {
+    if (n == bytes && p) return cudaSuccess;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    else p = nullptr;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return (T*)p;
+  }
+};
+
+}  // namespace
+
+struct mc_ctx {
+  int device = 0;
+  int n_sm = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  std::vector<cudaEvent_t> prof_ev;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a0 = nullptr, ev_a1 = nullptr;
+  std::mutex mu;
+  std::string err;
+
+  // host model
+  MeshTables mesh;
+  bool have_mesh = false;
+  std::vector<int32_t> bc_type = std::vector<int32_t>(1024, MC_BC_VACUUM);
+  std::vector<Nuclide> nucs;
+  std::vector<Material> mats;
+  std::vector<int32_t> map_blocks, map_mats;
+  int32_t n_bins = 8000;
+  XSTables xs;
+  bool xs_dirty = true, tmat_dirty = true, bc_dirty = true;
+  mc_source_desc src{};
+  std::vector<double> src_cyl;
+  bool have_src = false;
+
+  // device copies
+  DevBuf d_planes, d_planes32, d_nbr, d_tmat, d_bc, d_gstart, d_gtets;
+  DevBuf d_pts, d_nuc_off, d_nuc_n, d_hidx, d_awr, d_mat_off, d_mat_nuc, d_mat_dens;
+  DevBuf d_cyl;
+  DevBuf d_tally, d_sum, d_sumsq;
+  DevBuf d_counters, d_leak_w;
+  DevBuf d_traces;
+  int64_t trace_n = 0;
+  DevBuf d_sites;
+  // event bank
+  DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
+  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero;
+  DevBuf q_xs0, q_xs1, q_adv0, q_adv1, q_coll, q_free, d_ctl;
+  int64_t bank_cap = 0;
+
+  int64_t batches = 0;
+  mc_stats last{};
+};
+
+namespace {
+
+int set_err(mc_ctx* c, int code, const std::string& msg) {
+  c->err = msg;
+  return code;
+}
+
+int cuda_err(mc_ctx* c, cudaError_t e, const char* what) {
+  c->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return MC_ERR_CUDA;
+}
+
+template <class T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+  cudaError_t e = b.alloc(std::max<size_t>(16, v.size() * sizeof(T)));
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+#define CK(expr, what)                      \
+  do {                                      \
+    cudaError_t e_ = (expr);                \
+    if (e_ != cudaSuccess) return cuda_err(c, e_, what); \
+  } while (0)
+
+int ensure_device_tables(mc_ctx* c) {
+  if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh uploaded (mc_mesh_upload)");
+  if (c->nucs.empty()) return set_err(c, MC_ERR_STATE, "no nuclides (mc_nuclide_add)");
+  if (c->mats.empty()) return set_err(c, MC_ERR_STATE, "no materials (mc_material_add)");
+  if (c->xs_dirty) {
+    std::string m = build_xs_tables(c->nucs, c->mats, c->n_bins, c->xs);
+    if (!m.empty()) return set_err(c, MC_ERR_ARG, m);
+    CK(upload(c->d_pts, c->xs.pts, c->stream), "upload xs points");
+    CK(upload(c->d_nuc_off, c->xs.nuc_off, c->stream), "upload xs offsets");
+    CK(upload(c->d_nuc_n, c->xs.nuc_n, c->stream), "upload xs sizes");
+    CK(upload(c->d_hidx, c->xs.hidx, c->stream), "upload xs hash index");
+    CK(upload(c->d_awr, c->xs.awr, c->stream), "upload awr");
+    CK(upload(c->d_mat_off, c->xs.mat_off, c->stream), "upload materials");
+    CK(upload(c->d_mat_nuc, c->xs.mat_nuc, c->stream), "upload materials");
+    CK(upload(c->d_mat_dens, c->xs.mat_dens, c->stream), "upload materials");
+    c->xs_dirty = false;
+    c->tmat_dirty = true;
+  }
+  if (c->tmat_dirty) {
+    // element -> material index via the block map (material id, then the
+    // index of that id among the uploaded materials)
+    std::vector<int32_t> tmat((size_t)c->mesh.n_tet, -1);
+    for (int64_t t = 0; t < c->mesh.n_tet; ++t) {
+      const int32_t blk = c->mesh.block[t];
+      for (size_t i = 0; i < c->map_blocks.size(); ++i)
+        if (c->map_blocks[i] == blk) {
+          for (size_t m = 0; m < c->xs.mat_ids.size(); ++m)
+            if (c->xs.mat_ids[m] == c->map_mats[i]) {
+              tmat[t] = (int32_t)m;
+              break;
+            }
+          break;
+        }
+    }
+    CK(upload(c->d_tmat, tmat, c->stream), "upload element materials");
+    c->tmat_dirty = false;
+  }
+  if (c->bc_dirty) {
+    CK(upload(c->d_bc, c->bc_type, c->stream), "upload boundary conditions");
+    c->bc_dirty = false;
+  }
+  return MC_OK;
+}
+
+DevMesh dev_mesh(mc_ctx* c) {
+  DevMesh M;
+  M.planes = c->d_planes.as<double4_32a>();
+  M.planes32 = c->d_planes32.as<float4>();
+  M.nbr = c->d_nbr.as<int4>();
+  M.tmat = c->d_tmat.as<int>();
+  M.bc_type = c->d_bc.as<int>();
+  M.n_bid = (int)c->bc_type.size();
+  M.n_tet = c->mesh.n_tet;
+  for (int k = 0; k < 3; ++k) {
+    M.glo[k] = c->mesh.glo[k];
+    M.gh[k] = c->mesh.gh[k];
+    M.gn[k] = c->mesh.gn[k];
+  }
+  M.gstart = c->d_gstart.as<int64_t>();
+  M.gtets = c->d_gtets.as<int>();
+  return M;
+}
+
+DevXS dev_xs(mc_ctx* c) {
+  DevXS X;
+  X.pts = c->d_pts.as<double4_32a>();
+  X.nuc_off = c->d_nuc_off.as<int64_t>();
+  X.nuc_n = c->d_nuc_n.as<int>();
+  X.hidx = c->d_hidx.as<int>();
+  X.awr = c->d_awr.as<double>();
+  X.mat_off = c->d_mat_off.as<int>();
+  X.mat_nuc = c->d_mat_nuc.as<int>();
+  X.mat_dens = c->d_mat_dens.as<double>();
+  X.n_nuc = (int)c->xs.nuc_n.size();
+  X.n_bins = c->xs.n_bins;
+  X.E_lo = c->xs.E_lo;
+  X.E_hi = c->xs.E_hi;
+  X.lE_lo = c->xs.lE_lo;
+  X.du = c->xs.du;
+  return X;
+}
+
+DevSource dev_source(mc_ctx* c) {
+  DevSource S;
+  S.space = c->src.space;
+  S.energy = c->src.energy;
+  for (int k = 0; k < 3; ++k) {
+    S.point[k] = c->src.point[k];
+    S.box_lo[k] = c->src.box_lo[k];
+    S.box_hi[k] = c->src.box_hi[k];
+  }
+  S.n_cyl = c->src.n_cyl;
+  S.cyl_xy = c->d_cyl.as<double>();
+  S.cyl_r = c->src.cyl_r;
+  S.cyl_z0 = c->src.cyl_z0;
+  S.cyl_z1 = c->src.cyl_z1;
+  S.watt_a = c->src.watt_a;
+  S.watt_b = c->src.watt_b;
+  S.mono_E = c->src.mono_E;
+  return S;
+}
+
+int ensure_bank(mc_ctx* c, int64_t cap) {
+  if (c->bank_cap == cap) return MC_OK;
+  const size_t n = (size_t)cap;
+  DevBuf* d8[] = {&c->b_x, &c->b_y, &c->b_z, &c->b_u, &c->b_v, &c->b_w, &c->b_E,
+                  &c->b_wgt, &c->b_sigt, &c->b_seed, &c->b_hash, &c->b_id};
+  for (DevBuf* b : d8) CK(b->alloc(n * 8), "allocate particle bank");
+  DevBuf* d4[] = {&c->b_elem, &c->b_mat, &c->b_nseg, &c->b_ncoll, &c->b_zero,
+                  &c->q_xs0, &c->q_xs1, &c->q_adv0, &c->q_adv1, &c->q_coll, &c->q_free};
+  for (DevBuf* b : d4) CK(b->alloc(n * 4), "allocate particle bank");
+  CK(c->d_ctl.alloc(sizeof(EventCtl)), "allocate event control");
+  c->bank_cap = cap;
+  return MC_OK;
+}
+
+Bank dev_bank(mc_ctx* c) {
+  Bank B;
+  B.x = c->b_x.as<double>(); B.y = c->b_y.as<double>(); B.z = c->b_z.as<double>();
+  B.u = c->b_u.as<double>(); B.v = c->b_v.as<double>(); B.w = c->b_w.as<double>();
+  B.E = c->b_E.as<double>(); B.wgt = c->b_wgt.as<double>(); B.sigt = c->b_sigt.as<double>();
+  B.seed = c->b_seed.as<uint64_t>(); B.hash = c->b_hash.as<uint64_t>(); B.id = c->b_id.as<int64_t>();
+  B.elem = c->b_elem.as<int>(); B.mat = c->b_mat.as<int>(); B.n_seg = c->b_nseg.as<int>();
+  B.n_coll = c->b_ncoll.as<int>(); B.zero_run = c->b_zero.as<int>();
+  B.cap = c->bank_cap;
+  return B;
+}
+
+EventQueues dev_queues(mc_ctx* c) {
+  EventQueues Q;
+  Q.xs[0] = c->q_xs0.as<int>();
+  Q.xs[1] = c->q_xs1.as<int>();
+  Q.adv[0] = c->q_adv0.as<int>();
+  Q.adv[1] = c->q_adv1.as<int>();
+  Q.coll = c->q_coll.as<int>();
+  Q.free_slots = c->q_free.as<int>();
+  return Q;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int mc_version(void) { return 1; }
+
+int mc_ctx_create(int device, mc_ctx** out) {
+  if (!out) return MC_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return MC_ERR_CUDA;
+  if (device < 0 || device >= n) return MC_ERR_ARG;
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return MC_ERR_CUDA;
+  mc_ctx* c = new mc_ctx();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaEventCreate(&c->ev_a0) != cudaSuccess || cudaEventCreate(&c->ev_a1) != cudaSuccess) {
+    delete c;
+    return MC_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  if (c->d_counters.alloc(sizeof(unsigned long long) * kNumCounters) != cudaSuccess ||
+      c->d_leak_w.alloc(sizeof(double)) != cudaSuccess) {
+    delete c;
+    return MC_ERR_NOMEM;
+  }
+  *out = c;
+  return MC_OK;
+}
+
+int mc_ctx_destroy(mc_ctx* c) {
+  if (!c) return MC_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+  }
+  cudaEventDestroy(c->ev0);
+  cudaEventDestroy(c->ev1);
+  cudaEventDestroy(c->ev_a0);
+  cudaEventDestroy(c->ev_a1);
+  for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+  cudaStreamDestroy(c->own_stream);
+  delete c;
+  return MC_OK;
+}
+
+const char* mc_last_error(mc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int mc_mesh_upload(mc_ctx* c, int64_t n_vtx, const double* xyz, int64_t n_tet,
+                   const int32_t* tet_vtx, const int32_t* tet_block, const int32_t* tet_side_bid) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!xyz || !tet_vtx || !tet_block) return set_err(c, MC_ERR_ARG, "null mesh array");
+  MeshTables M;
+  std::string m = build_mesh_tables(n_vtx, xyz, n_tet, tet_vtx, tet_block, tet_side_bid, M);
+  if (!m.empty()) return set_err(c, MC_ERR_ARG, m);
+  for (int64_t s = 0; s < 4 * n_tet; ++s)
+    if (M.nbr[s] < 0 && -1 - M.nbr[s] >= (int64_t)c->bc_type.size())
+      return set_err(c, MC_ERR_ARG, "sideset id out of range [0, 1024)");
+  cudaSetDevice(c->device);
+  c->mesh = std::move(M);
+  CK(upload(c->d_planes, c->mesh.planes, c->stream), "upload planes");
+  CK(upload(c->d_planes32, c->mesh.planes32, c->stream), "upload planes");
+  CK(upload(c->d_nbr, c->mesh.nbr, c->stream), "upload neighbours");
+  CK(upload(c->d_gstart, c->mesh.gstart, c->stream), "upload locator");
+  CK(upload(c->d_gtets, c->mesh.gtets, c->stream), "upload locator");
+  CK(c->d_tally.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
+  CK(c->d_sum.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
+  CK(c->d_sumsq.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
+  CK(cudaMemsetAsync(c->d_tally.p, 0, c->d_tally.bytes, c->stream), "clear tally");
+  CK(cudaMemsetAsync(c->d_sum.p, 0, c->d_sum.bytes, c->stream), "clear tally");
+  CK(cudaMemsetAsync(c->d_sumsq.p, 0, c->d_sumsq.bytes, c->stream), "clear tally");
+  CK(cudaStreamSynchronize(c->stream), "mesh upload");
+  c->have_mesh = true;
+  c->tmat_dirty = true;
+  c->batches = 0;
+  return MC_OK;
+}
+
+int mc_bc_set(mc_ctx* c, int32_t bid, int32_t type) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (bid < 0 || bid >= (int32_t)c->bc_type.size()) return set_err(c, MC_ERR_ARG, "boundary id out of range [0, 1024)");
+  if (type != MC_BC_VACUUM && type != MC_BC_REFLECT) return set_err(c, MC_ERR_ARG, "unknown boundary condition type");
+  c->bc_type[bid] = type;
+  c->bc_dirty = true;
+  return MC_OK;
+}
+
+int mc_nuclide_add(mc_ctx* c, int64_t n_pts, const double* E, const double* sig_t,
+                   const double* sig_s, double awr, int32_t* out_index) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n_pts < 2 || !E || !sig_t || !sig_s) return set_err(c, MC_ERR_ARG, "nuclide grid needs at least 2 points");
+  if (n_pts > (int64_t)1 << 30) return set_err(c, MC_ERR_ARG, "nuclide grid too large");
+  if (!(E[0] > 0.0)) return set_err(c, MC_ERR_ARG, "nuclide energies must be positive");
+  for (int64_t i = 0; i + 1 < n_pts; ++i)
+    if (!(E[i] < E[i + 1])) return set_err(c, MC_ERR_ARG, "nuclide energy grid must be strictly increasing");
+  for (int64_t i = 0; i < n_pts; ++i)
+    if (!(sig_t[i] >= 0.0) || !(sig_s[i] >= 0.0) || sig_s[i] > sig_t[i])
+      return set_err(c, MC_ERR_ARG, "cross sections must satisfy 0 <= sigma_s <= sigma_t");
+  if (!(awr > 0.0)) return set_err(c, MC_ERR_ARG, "atomic weight ratio must be positive");
+  Nuclide n;
+  n.E.assign(E, E + n_pts);
+  n.st.assign(sig_t, sig_t + n_pts);
+  n.ss.assign(sig_s, sig_s + n_pts);
+  n.awr = awr;
+  c->nucs.push_back(std::move(n));
+  if (out_index) *out_index = (int32_t)c->nucs.size() - 1;
+  c->xs_dirty = true;
+  return MC_OK;
+}
+
+int mc_material_add(mc_ctx* c, int32_t material_id, int32_t n, const int32_t* nuclides,
+                    const double* densities) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n < 1 || !nuclides || !densities) return set_err(c, MC_ERR_ARG, "material needs at least one nuclide");
+  for (int i = 0; i < n; ++i) {
+    if (nuclides[i] < 0 || nuclides[i] >= (int32_t)c->nucs.size())
+      return set_err(c, MC_ERR_ARG, "material nuclide index out of range");
+    if (!(densities[i] >= 0.0)) return set_err(c, MC_ERR_ARG, "atom densities must be non-negative");
+  }
+  for (const auto& m : c->mats)
+    if (m.id == material_id) return set_err(c, MC_ERR_ARG, "duplicate material id");
+  Material m;
+  m.id = material_id;
+  m.nuc.assign(nuclides, nuclides + n);
+  m.dens.assign(densities, densities + n);
+  c->mats.push_back(std::move(m));
+  c->xs_dirty = true;
+  return MC_OK;
+}
+
+int mc_block_material_map(mc_ctx* c, int32_t n, const int32_t* blocks, const int32_t* materials) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n < 0 || (n > 0 && (!blocks || !materials))) return set_err(c, MC_ERR_ARG, "null block map");
+  c->map_blocks.assign(blocks, blocks + n);
+  c->map_mats.assign(materials, materials + n);
+  c->tmat_dirty = true;
+  return MC_OK;
+}
+
+int mc_set_hash_bins(mc_ctx* c, int32_t n_bins) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n_bins < 1 || n_bins > (1 << 24)) return set_err(c, MC_ERR_ARG, "hash bins must be in [1, 2^24]");
+  c->n_bins = n_bins;
+  c->xs_dirty = true;
+  return MC_OK;
+}
+
+int mc_source_set(mc_ctx* c, const mc_source_desc* s) {
+  if (!c || !s) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (s->space < 0 || s->space > 2) return set_err(c, MC_ERR_ARG, "unknown source space kind");
+  if (s->energy < 0 || s->energy > 1) return set_err(c, MC_ERR_ARG, "unknown source energy kind");
+  if (s->space == MC_SRC_CYLINDERS && (s->n_cyl < 1 || !s->cyl_xy || !(s->cyl_r > 0.0)))
+    return set_err(c, MC_ERR_ARG, "cylinder source needs cylinders and a positive radius");
+  if (s->energy == MC_SRC_WATT && (!(s->watt_a > 0.0) || !(s->watt_b > 0.0)))
+    return set_err(c, MC_ERR_ARG, "Watt parameters must be positive");
+  if (s->energy == MC_SRC_MONO && !(s->mono_E > 0.0))
+    return set_err(c, MC_ERR_ARG, "source energy must be positive");
+  c->src = *s;
+  if (s->space == MC_SRC_CYLINDERS) {
+    c->src_cyl.assign(s->cyl_xy, s->cyl_xy + 2 * (size_t)s->n_cyl);
+    cudaSetDevice(c->device);
+    CK(upload(c->d_cyl, c->src_cyl, c->stream), "upload source");
+    CK(cudaStreamSynchronize(c->stream), "upload source");
+  }
+  c->src.cyl_xy = nullptr;
+  c->have_src = true;
+  return MC_OK;
+}
+
+int mc_run(mc_ctx* c, const mc_run_desc* d) {
+  if (!c || !d) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (d->n_histories < 0 || d->first_history < 0) return set_err(c, MC_ERR_ARG, "negative history range");
+  if (d->precision != MC_PREC_FP64 && d->precision != MC_PREC_MIXED)
+    return set_err(c, MC_ERR_ARG, "unknown precision form");
+  if (d->precision == MC_PREC_MIXED) return set_err(c, MC_ERR_ARG, "mixed precision form not available");
+  if (d->mode != MC_MODE_HISTORY && d->mode != MC_MODE_EVENT) return set_err(c, MC_ERR_ARG, "unknown execution form");
+  if (!c->have_src) return set_err(c, MC_ERR_STATE, "no source (mc_source_set)");
+  cudaSetDevice(c->device);
+  int rc = ensure_device_tables(c);
+  if (rc) return rc;
+  const int block = d->block_size > 0 ? d->block_size : 256;
+  if (block % 32 != 0 || block > 256) return set_err(c, MC_ERR_ARG, "block size must be a multiple of 32, at most 256");
+  if (d->record_traces) {
+    if (c->trace_n < d->n_histories) {
+      CK(c->d_traces.alloc(sizeof(mc_trace) * (size_t)std::max<int64_t>(1, d->n_histories)), "allocate traces");
+      c->trace_n = d->n_histories;
+    }
+  }
+  CK(cudaMemsetAsync(c->d_counters.p, 0, c->d_counters.bytes, c->stream), "clear counters");
+  CK(cudaMemsetAsync(c->d_leak_w.p, 0, sizeof(double), c->stream), "clear counters");
+  RunArgs a;
+  a.first = d->first_history;
+  a.n = d->n_histories;
+  a.master = d->seed;
+  a.tally = c->d_tally.as<double>();
+  a.traces = d->record_traces ? c->d_traces.as<mc_trace>() : nullptr;
+  a.counters = c->d_counters.as<unsigned long long>();
+  a.leak_w = c->d_leak_w.as<double>();
+  a.precision = d->precision;
+  a.max_seg = d->max_seg_per_advance;
+  a.sites = nullptr;
+  if (d->sites && d->n_histories > 0) {
+    CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)d->n_histories)), "allocate sites");
+    CK(cudaMemcpyAsync(c->d_sites.p, d->sites, sizeof(mc_site) * (size_t)d->n_histories,
+                       cudaMemcpyHostToDevice, c->stream),
+       "upload sites");
+    a.sites = c->d_sites.as<mc_site>();
+  }
+  const DevMesh M = dev_mesh(c);
+  const DevXS X = dev_xs(c);
+  const DevSource S = dev_source(c);
+  const int per_sm = 2048 / block;
+  const int grid = std::max(1, c->n_sm * per_sm);
+  int n_launch = 0, n_adv = 0;
+  float ms_adv = 0.0f;
+  CK(cudaEventRecord(c->ev0, c->stream), "event");
+  if (d->n_histories > 0) {
+    if (d->mode == MC_MODE_HISTORY) {
+      CK(launch_history(M, X, S, a, block, grid, c->stream), "launch history kernel");
+      n_launch = 1;
+      n_adv = 1;
+    } else {
+      int64_t cap = d->bank_size > 0 ? std::min(d->bank_size, d->n_histories) : d->n_histories;
+      cap = std::max<int64_t>(cap, 1);
+      if (cap > ((int64_t)1 << 30)) return set_err(c, MC_ERR_ARG, "bank too large");
+      rc = ensure_bank(c, std::max(cap, c->bank_cap));
+      if (rc) return rc;
+      const Bank B = dev_bank(c);
+      const EventQueues Q = dev_queues(c);
+      EventCtl* ctl = c->d_ctl.as<EventCtl>();
+      CK(launch_event_init(M, X, S, a, B, Q, ctl, block, grid, c->stream), "launch event init");
+      n_launch = 1;
+      int par = 0;
+      EventCtl h;
+      const int kGroup = 4;
+      const int64_t tail = std::max<int64_t>(4096, cap / 64);
+      for (int64_t it = 0;; ++it) {
+        for (int gi = 0; gi < kGroup; ++gi) {
+          cudaEvent_t e0 = nullptr, e1 = nullptr;
+          if (d->profile) {
+            while (c->prof_ev.size() < (size_t)(2 * n_adv + 2)) {
+              cudaEvent_t e;
+              CK(cudaEventCreate(&e), "event");
+              c->prof_ev.push_back(e);
+            }
+            e0 = c->prof_ev[2 * n_adv];
+            e1 = c->prof_ev[2 * n_adv + 1];
+          }
+          CK(launch_event_iteration(M, X, S, a, B, Q, ctl, par, block, grid, c->stream, &n_launch, e0, e1),
+             "launch event iteration");
+          n_adv += 1;
+          par ^= 1;
+        }
+        CK(cudaMemcpyAsync(&h, ctl, sizeof(EventCtl), cudaMemcpyDeviceToHost, c->stream), "read event control");
+        CK(cudaStreamSynchronize(c->stream), "event loop");
+        const int64_t inflight = (int64_t)h.n_xs[par] + h.n_adv[par];
+        if (inflight == 0 && h.next_hist >= a.n) break;
+        if (h.next_hist >= a.n && inflight <= tail) {
+          CK(launch_event_finish(M, X, S, a, B, Q, ctl, par, block, grid, c->stream), "launch event finish");
+          ++n_launch;
+          break;
+        }
+        if (it > 10000000) return set_err(c, MC_ERR_DEVICE, "event loop did not terminate");
+      }
+    }
+  }
+  CK(cudaEventRecord(c->ev1, c->stream), "event");
+  if (d->accumulate) {
+    const double inv_w = d->n_histories > 0 ? 1.0 / (double)d->n_histories : 0.0;
+    CK(launch_accumulate(c->d_tally.as<double>(), c->d_sum.as<double>(), c->d_sumsq.as<double>(),
+                         c->mesh.n_tet, inv_w, c->stream),
+       "launch accumulate");
+    c->batches += 1;
+  }
+  unsigned long long cnt[kNumCounters];
+  double leak_w = 0.0;
+  CK(cudaMemcpyAsync(cnt, c->d_counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream), "read counters");
+  CK(cudaMemcpyAsync(&leak_w, c->d_leak_w.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "read counters");
+  CK(cudaStreamSynchronize(c->stream), "run");
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  if (d->mode == MC_MODE_HISTORY) {
+    ms_adv = ms;
+  } else if (d->profile) {
+    for (int i = 0; i < n_adv; ++i) {
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, c->prof_ev[2 * i], c->prof_ev[2 * i + 1]);
+      ms_adv += t;
+    }
+  }
+  mc_stats& s = c->last;
+  s.n_hist = (int64_t)cnt[kCntHist];
+  s.n_seg = (int64_t)cnt[kCntSeg];
+  s.n_coll = (int64_t)cnt[kCntColl];
+  s.n_leak = (int64_t)cnt[kCntLeak];
+  s.n_absorb = (int64_t)cnt[kCntAbsorb];
+  s.n_cutoff = (int64_t)cnt[kCntCutoff];
+  s.n_stuck = (int64_t)cnt[kCntStuck];
+  s.n_lost = (int64_t)cnt[kCntLost];
+  s.n_badxs = (int64_t)cnt[kCntBadXS];
+  s.n_fallback = (int64_t)cnt[kCntFallback];
+  s.n_xs = (int64_t)cnt[kCntXS];
+  s.n_launch = n_launch;
+  s.leak_weight = leak_w;
+  s.ms_total = ms;
+  s.ms_advance = ms_adv;
+  s.n_advance_launch = n_adv;
+  if (s.n_hist != d->n_histories)
+    return set_err(c, MC_ERR_DEVICE, "device finished " + std::to_string(s.n_hist) + " of " +
+                                         std::to_string(d->n_histories) + " histories");
+  return MC_OK;
+}
+
+int mc_source_sample(mc_ctx* c, int64_t first, int64_t n, uint64_t seed, mc_site* out) {
+  if (!c || (!out && n > 0)) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n < 0 || first < 0) return set_err(c, MC_ERR_ARG, "negative history range");
+  if (!c->have_src) return set_err(c, MC_ERR_STATE, "no source (mc_source_set)");
+  if (n == 0) return MC_OK;
+  cudaSetDevice(c->device);
+  int rc = ensure_device_tables(c);
+  if (rc) return rc;
+  CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)n)), "allocate sites");
+  CK(launch_sample(dev_xs(c), dev_source(c), first, n, seed, c->d_sites.as<mc_site>(), c->stream),
+     "launch source sampling");
+  CK(cudaMemcpyAsync(out, c->d_sites.p, sizeof(mc_site) * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+     "download sites");
+  CK(cudaStreamSynchronize(c->stream), "source sampling");
+  return MC_OK;
+}
+
+int mc_ctx_set_stream(mc_ctx* c, void* stream) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  CK(cudaStreamSynchronize(c->stream), "sync before stream change");
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return MC_OK;
+}
+
+int mc_sync(mc_ctx* c) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return MC_OK;
+}
+
+int mc_tally_download(mc_ctx* c, int32_t kind, double* out, int64_t n) {
+  if (!c || !out) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh");
+  if (n != c->mesh.n_tet) return set_err(c, MC_ERR_ARG, "tally length must equal the number of tets");
+  DevBuf* b = kind == MC_TALLY_BATCH ? &c->d_tally : kind == MC_TALLY_SUM ? &c->d_sum
+              : kind == MC_TALLY_SUM_SQ ? &c->d_sumsq : nullptr;
+  if (!b) return set_err(c, MC_ERR_ARG, "unknown tally kind");
+  cudaSetDevice(c->device);
+  CK(cudaMemcpyAsync(out, b->p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "download tally");
+  CK(cudaStreamSynchronize(c->stream), "download tally");
+  return MC_OK;
+}
+
+int mc_tally_reset(mc_ctx* c) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh");
+  cudaSetDevice(c->device);
+  CK(cudaMemsetAsync(c->d_tally.p, 0, c->d_tally.bytes, c->stream), "clear tally");
+  CK(cudaMemsetAsync(c->d_sum.p, 0, c->d_sum.bytes, c->stream), "clear tally");
+  CK(cudaMemsetAsync(c->d_sumsq.p, 0, c->d_sumsq.bytes, c->stream), "clear tally");
+  CK(cudaStreamSynchronize(c->stream), "clear tally");
+  c->batches = 0;
+  return MC_OK;
+}
+
+int mc_trace_download(mc_ctx* c, mc_trace* out, int64_t n) {
+  if (!c || !out) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n > c->trace_n) return set_err(c, MC_ERR_ARG, "more traces requested than recorded");
+  cudaSetDevice(c->device);
+  CK(cudaMemcpyAsync(out, c->d_traces.p, sizeof(mc_trace) * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+     "download traces");
+  CK(cudaStreamSynchronize(c->stream), "download traces");
+  return MC_OK;
+}
+
+int mc_stats_get(mc_ctx* c, mc_stats* out) {
+  if (!c || !out) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  *out = c->last;
+  return MC_OK;
+}
+
+int mc_batches_done(mc_ctx* c, int64_t* out) {
+  if (!c || !out) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  *out = c->batches;
+  return MC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,376 @@
+// mc_device.cuh -- device data views and the per-particle tracking steps.
+//
+// The steps restate, for a tet mesh and tabulated cross sections, what
+// MaCaw does per ray segment in CollisionKernel::onSegment
+// (src/raykernels/CollisionKernel.C:98-275) inside MOOSE's element walk:
+//   xs      macroscopic total XS at (E, material)        CollisionKernel.C:143
+//   sample  d = -ln(xi)/Sigma_t, one draw per segment      CollisionKernel.C:150
+//   score   wgt*min(d, L) into the element flux tally      CollisionKernel.C:153-154
+//   cross   d > L: move to the exit face, neighbour or BC  CollisionKernel.C:163-169
+//   collide end-(L-d)*u, nuclide, absorb/scatter           CollisionKernel.C:173-230
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/macaw_gb300.h"
+#include "mc_core.cuh"
+
+namespace mc {
+
+struct DevMesh {
+  const double4_32a* __restrict__ planes;   // 4 per tet (nx, ny, nz, d), outward
+  const float4* __restrict__ planes32;  // same in float
+  const int4* __restrict__ nbr;         // neighbour per side, or -1-boundary_id
+  const int* __restrict__ tmat;         // material index per tet (-1: none)
+  const int* __restrict__ bc_type;      // per boundary id: 0 vacuum, 1 reflect
+  int n_bid;
+  int64_t n_tet;
+  double glo[3], gh[3];
+  int gn[3];
+  const int64_t* __restrict__ gstart;
+  const int* __restrict__ gtets;
+};
+
+struct DevXS {
+  const double4_32a* __restrict__ pts;      // (E, sigma_t, sigma_s, 0) per point
+  const int64_t* __restrict__ nuc_off;
+  const int* __restrict__ nuc_n;
+  const int* __restrict__ hidx;         // (n_bins+1) x n_nuc, bin-major
+  const double* __restrict__ awr;
+  const int* __restrict__ mat_off;
+  const int* __restrict__ mat_nuc;
+  const double* __restrict__ mat_dens;
+  int n_nuc, n_bins;
+  double E_lo, E_hi, lE_lo, du;
+};
+
+struct DevSource {
+  int space, energy;
+  double point[3], box_lo[3], box_hi[3];
+  int n_cyl;
+  const double* __restrict__ cyl_xy;
+  double cyl_r, cyl_z0, cyl_z1;
+  double watt_a, watt_b, mono_E;
+};
+
+struct Particle {
+  double x, y, z, u, v, w, E, wgt, sigt;
+  uint64_t seed, hash;
+  int64_t id;
+  int elem, mat, n_seg, n_coll, status, face, zero_run;
+};
+
+// ---------------------------------------------------------------------------
+// Cross sections.
+__device__ __forceinline__ int xs_bucket(const DevXS& X, double lE) {
+  const double q = (lE - X.lE_lo) / X.du;
+  if (!(q >= 0.0)) return 0;
+  if (q >= (double)X.n_bins) return X.n_bins - 1;
+  int k = (int)q;
+  if (k > X.n_bins - 1) k = X.n_bins - 1;
+  return k;
+}
+
+// Bisection inside the hash bin, guarded so a bin estimate that is off by
+// rounding still ends on the right interval.
+__device__ __forceinline__ int xs_index(const DevXS& X, int nuc, int k, double E) {
+  const double4_32a* P = X.pts + X.nuc_off[nuc];
+  int lo = __ldg(X.hidx + (size_t)k * X.n_nuc + nuc);
+  int hi = __ldg(X.hidx + (size_t)(k + 1) * X.n_nuc + nuc) + 1;
+  const int last = X.nuc_n[nuc] - 1;
+  if (hi > last) hi = last;
+  while (lo > 0 && E < __ldg(&P[lo].x)) --lo;
+  while (hi < last && E >= __ldg(&P[hi].x)) ++hi;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (E < __ldg(&P[mid].x)) hi = mid;
+    else lo = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void micro_xs(const DevXS& X, int nuc, int k, double E, double& st,
+                                         double& ss) {
+  const double4_32a* P = X.pts + X.nuc_off[nuc];
+  const int i = xs_index(X, nuc, k, E);
+  const double4_32a a = P[i];
+  const double4_32a b = P[i + 1];
+  const double f = (E - a.x) / (b.x - a.x);
+  st = a.y + f * (b.y - a.y);
+  ss = a.z + f * (b.z - a.z);
+}
+
+// Sigma_t = sum_i N_i sigma_t,i(E), in material order (OpenMC
+// Material::calculate_xs, called through event_calculate_xs).
+__device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E) {
+  const int k = xs_bucket(X, mc::log64(E));
+  double acc = 0.0;
+  const int j1 = __ldg(X.mat_off + mat + 1);
+  for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
+    double st, ss;
+    micro_xs(X, __ldg(X.mat_nuc + j), k, E, st, ss);
+    acc = acc + __ldg(X.mat_dens + j) * st;
+  }
+  return acc;
+}
+
+// ---------------------------------------------------------------------------
+// Start element (stands in for MOOSE ClaimRays): lowest-id tet containing x
+// (all four half-spaces within kLocateTol) whose interior the direction
+// enters; else the lowest-id containing tet; else -1.
+__device__ __forceinline__ int locate(const DevMesh& M, double x, double y, double z, double u,
+                                      double v, double w) {
+  const double xs[3] = {x, y, z};
+  int ci[3];
+  for (int k = 0; k < 3; ++k) {
+    const double q = (xs[k] - M.glo[k]) / M.gh[k];
+    int c = (int)floor(q);
+    if (!(q >= 0.0)) c = 0;
+    if (c > M.gn[k] - 1) c = M.gn[k] - 1;
+    if (c < 0) c = 0;
+    ci[k] = c;
+  }
+  const int64_t cell = ((int64_t)ci[2] * M.gn[1] + ci[1]) * M.gn[0] + ci[0];
+  int best_in = -1, best_any = -1;
+  for (int64_t q = M.gstart[cell]; q < M.gstart[cell + 1]; ++q) {
+    const int t = M.gtets[q];
+    bool inside = true, enters = true;
+    for (int f = 0; f < 4; ++f) {
+      const double4_32a pl = M.planes[4 * (int64_t)t + f];
+      const double s = pl.x * x + pl.y * y + pl.z * z - pl.w;
+      if (s > kLocateTol) {
+        inside = false;
+        break;
+      }
+      if (s >= -kLocateTol) {
+        const double dn = pl.x * u + pl.y * v + pl.z * w;
+        if (!(dn < 0.0)) enters = false;
+      }
+    }
+    if (!inside) continue;
+    if (enters && (best_in < 0 || t < best_in)) best_in = t;
+    if (best_any < 0 || t < best_any) best_any = t;
+  }
+  return best_in >= 0 ? best_in : best_any;
+}
+
+// ---------------------------------------------------------------------------
+// Source site of history index h (OpenMCStudy::defineRays with OpenMC's
+// initialize_history, OpenMCStudy.C:317-360): position, direction, energy
+// drawn from the source stream of particle id h+1.
+__device__ __forceinline__ void sample_source(const DevXS& X, const DevSource& S, int64_t h,
+                                              uint64_t master, mc_site& o) {
+  const Skip k = skip_ahead((uint64_t)(h + 1) * kPrnStride);
+  uint64_t ss = stream_seed(k, master, kStreamSource);
+  if (S.space == 0) {
+    o.x = S.point[0];
+    o.y = S.point[1];
+    o.z = S.point[2];
+  } else if (S.space == 1) {
+    o.x = S.box_lo[0] + prn(ss) * (S.box_hi[0] - S.box_lo[0]);
+    o.y = S.box_lo[1] + prn(ss) * (S.box_hi[1] - S.box_lo[1]);
+    o.z = S.box_lo[2] + prn(ss) * (S.box_hi[2] - S.box_lo[2]);
+  } else {
+    int c = (int)(prn(ss) * (double)S.n_cyl);
+    if (c > S.n_cyl - 1) c = S.n_cyl - 1;
+    const double r = S.cyl_r * sqrt(prn(ss));
+    double ct, st;
+    sample_azimuth(ss, ct, st);
+    o.x = S.cyl_xy[2 * c] + r * ct;
+    o.y = S.cyl_xy[2 * c + 1] + r * st;
+    o.z = S.cyl_z0 + prn(ss) * (S.cyl_z1 - S.cyl_z0);
+  }
+  const double mu = 2.0 * prn(ss) - 1.0;
+  double cp, sp;
+  sample_azimuth(ss, cp, sp);
+  const double sm = sqrt(fmax0(1.0 - mu * mu));
+  o.u = mu;
+  o.v = sm * cp;
+  o.w = sm * sp;
+  o.E = (S.energy == 1) ? S.mono_E : sample_watt(ss, S.watt_a, S.watt_b, X.E_lo, X.E_hi);
+  o.wgt = 1.0;
+}
+
+// A history starts at its site: tracking stream of particle id h+1, start
+// element located (stands in for MOOSE ClaimRays).
+__device__ __forceinline__ void start(const DevMesh& M, const mc_site& o, int64_t h, uint64_t master,
+                                      Particle& p) {
+  p.id = h + 1;
+  const Skip k = skip_ahead((uint64_t)p.id * kPrnStride);
+  p.seed = stream_seed(k, master, kStreamTracking);
+  p.x = o.x;
+  p.y = o.y;
+  p.z = o.z;
+  p.u = o.u;
+  p.v = o.v;
+  p.w = o.w;
+  p.E = o.E;
+  p.wgt = o.wgt;
+  p.hash = kFnvOffset;
+  p.status = kAlive;
+  p.n_seg = 0;
+  p.n_coll = 0;
+  p.face = -1;
+  p.zero_run = 0;
+  p.mat = -2;
+  p.sigt = 0.0;
+  p.elem = locate(M, p.x, p.y, p.z, p.u, p.v, p.w);
+  if (p.elem < 0) p.status = kLost;
+}
+
+// ---------------------------------------------------------------------------
+// Collision at the current position (OpenMC event_collide as MaCaw calls
+// it, CollisionKernel.C:185-230): nuclide by cumulative N_i sigma_t,i,
+// absorption if xi*sigma_t < sigma_a, else elastic scattering isotropic in
+// the centre-of-mass frame off a target at rest.  Absorption and energy
+// cutoff end the history; secondaries are not tracked (CollisionKernel.C:236).
+__device__ __forceinline__ void collide(const DevXS& X, Particle& p) {
+  const int mat = p.mat;
+  const int k = xs_bucket(X, mc::log64(p.E));
+  const double cutoff = prn(p.seed) * p.sigt;
+  double acc = 0.0, st = 0.0, ss = 0.0;
+  const int j0 = __ldg(X.mat_off + mat), j1 = __ldg(X.mat_off + mat + 1);
+  int pick = -1;
+  for (int j = j0; j < j1; ++j) {
+    micro_xs(X, __ldg(X.mat_nuc + j), k, p.E, st, ss);
+    acc = acc + __ldg(X.mat_dens + j) * st;
+    if (acc >= cutoff) {
+      pick = j;
+      break;
+    }
+  }
+  if (pick < 0) pick = j1 - 1;
+  const double sa = st - ss;
+  if (prn(p.seed) * st < sa) {
+    p.status = kAbsorbed;
+    return;
+  }
+  const double A = __ldg(X.awr + __ldg(X.mat_nuc + pick));
+  const double mu_cm = 2.0 * prn(p.seed) - 1.0;
+  const double q = A * A + 2.0 * A * mu_cm + 1.0;
+  const double Ap1 = A + 1.0;
+  const double E2 = p.E * q / (Ap1 * Ap1);
+  double cp, sp;
+  sample_azimuth(p.seed, cp, sp);
+  if (!(q > 0.0) || !(E2 >= X.E_lo)) {
+    p.E = E2;
+    p.status = kCutoff;
+    return;
+  }
+  double mu_lab = (1.0 + A * mu_cm) / sqrt(q);
+  if (mu_lab > 1.0) mu_lab = 1.0;
+  if (mu_lab < -1.0) mu_lab = -1.0;
+  rotate_dir(p.u, p.v, p.w, mu_lab, cp, sp);
+  p.E = E2;
+  p.mat = -2;  // energy changed: cross sections are recomputed
+}
+
+// ---------------------------------------------------------------------------
+// One segment of the FP64 walk.  Returns 0 when the particle crossed a face
+// (or reflected) and continues, 1 when a collision was sampled inside the
+// element (position already moved to the collision point), 2 when the
+// history ended (leak, stuck, bad XS).
+//
+// The distance-to-collision test first compares -logf(xi) against
+// L*Sigma_t in float with a margin that covers float rounding and logf's
+// error bound; only when that comparison is not decisive is the FP64 log
+// evaluated.  Either way the outcome and the score (L when d > L) are the
+// values the FP64 arithmetic gives.
+template <bool kCountXS>
+__device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Particle& p,
+                                            double* __restrict__ tally, float& sigt32,
+                                            unsigned long long& n_xs) {
+  if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
+    p.status = kStuck;
+    return 2;
+  }
+  const int mat = __ldg(M.tmat + p.elem);
+  if (mat < 0) {
+    p.status = kBadXS;
+    return 2;
+  }
+  if (mat != p.mat) {
+    p.sigt = macro_total(X, mat, p.E);
+    p.mat = mat;
+    sigt32 = (float)p.sigt;
+    if (kCountXS) ++n_xs;
+    if (!(p.sigt > 0.0) || p.sigt != p.sigt) {
+      p.status = kBadXS;
+      return 2;
+    }
+  }
+  const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
+  int bf = -1;
+  double bnum = 0.0, bden = 1.0;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const double4_32a pl = P[f];
+    const double den = pl.x * p.u + pl.y * p.v + pl.z * p.w;
+    if (den > 0.0) {
+      const double num = pl.w - (pl.x * p.x + pl.y * p.y + pl.z * p.z);
+      if (bf < 0 || num * bden < bnum * den) {
+        bf = f;
+        bnum = num;
+        bden = den;
+      }
+    }
+  }
+  if (bf < 0) {
+    p.status = kStuck;
+    return 2;
+  }
+  double L = bnum / bden;
+  if (!(L > 0.0)) L = 0.0;
+  const double xi = prn(p.seed);
+  const float lf = -logf((float)xi);
+  const float thr = (float)L * sigt32;
+  bool cross;
+  double dist = 0.0;
+  if (lf > thr * 1.00001f + 1e-6f) {
+    cross = true;
+  } else {
+    dist = -mc::log64(xi) / p.sigt;
+    cross = dist > L;
+  }
+  const double score = cross ? L : dist;  // (L < dist) ? L : dist
+  atomicAdd(tally + p.elem, p.wgt * score);
+  ++p.n_seg;
+  if (L == 0.0) ++p.zero_run;
+  else p.zero_run = 0;
+  if (cross) {
+    p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
+    p.x = p.x + L * p.u;
+    p.y = p.y + L * p.v;
+    p.z = p.z + L * p.w;
+    const int4 nb4 = M.nbr[p.elem];
+    const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+    if (nb >= 0) {
+      p.elem = nb;
+      return 0;
+    }
+    const int bid = -1 - nb;
+    if (bid < M.n_bid && M.bc_type[bid] == 1) {
+      const double4_32a pl = P[bf];
+      const double dn = p.u * pl.x + p.v * pl.y + p.w * pl.z;
+      const double t2 = 2.0 * dn;
+      p.u = p.u - t2 * pl.x;
+      p.v = p.v - t2 * pl.y;
+      p.w = p.w - t2 * pl.z;
+      return 0;
+    }
+    p.status = kLeaked;
+    p.face = bf;
+    return 2;
+  }
+  p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
+  const double ex = p.x + L * p.u, ey = p.y + L * p.v, ez = p.z + L * p.w;
+  const double back = L - dist;
+  p.x = ex - back * p.u;
+  p.y = ey - back * p.v;
+  p.z = ez - back * p.w;
+  ++p.n_coll;
+  p.zero_run = 0;
+  return 1;
+}
+
+}  // namespace mc

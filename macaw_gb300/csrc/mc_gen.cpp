@@ -1,0 +1,347 @@
+// mc_gen.cpp -- synthetic meshes and cross-section tables.
+//
+// The reference's own inputs (BEAVRS meshes, ENDF data) are not available,
+// so problems are generated from a seed.  Every value is produced with the
+// tracker's own arithmetic (mc::exp/mc::log, IEEE sqrt and division, no
+// fused multiply-add), so the same seed yields bit-identical tables on every
+// host architecture.
+#include <math.h>
+
+#include <algorithm>
+#include <map>
+#include <utility>
+#include <vector>
+
+#include "../../include/macaw_gb300.h"
+#include "mc_core.cuh"
+
+namespace {
+
+// Independent generator stream per (seed, purpose, index).
+struct Gen {
+  uint64_t s;
+  Gen(uint64_t seed, uint64_t purpose, uint64_t index) {
+    mc::Skip k = mc::skip_ahead((index + 1) * mc::kPrnStride);
+    s = k.G * (seed + 101 * purpose + 7) + k.C;
+  }
+  double u() { return mc::prn(s); }
+  double uniform(double lo, double hi) { return lo + u() * (hi - lo); }
+  double log_uniform(double lo, double hi) {
+    const double a = mc::log64(lo), b = mc::log64(hi);
+    return mc::exp64(a + u() * (b - a));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Cube of n^3 hexes, each split into the six Kuhn tets along its main diagonal.
+void cube_vertex_index(int n, int i, int j, int k, int32_t* id) {
+  *id = (int32_t)(((int64_t)k * (n + 1) + j) * (n + 1) + i);
+}
+
+// MOOSE GeneratedMesh 3D sideset ids: back=0 (z-), bottom=1 (y-), right=2
+// (x+), top=3 (y+), left=4 (x-), front=5 (z+).
+int box_side_id(const int* lo_hit, const int* hi_hit) {
+  if (lo_hit[2]) return 0;
+  if (lo_hit[1]) return 1;
+  if (hi_hit[0]) return 2;
+  if (hi_hit[1]) return 3;
+  if (lo_hit[0]) return 4;
+  if (hi_hit[2]) return 5;
+  return -1;
+}
+
+const int kFaceVtx[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+
+}  // namespace
+
+extern "C" int mc_gen_cube_sizes(int32_t n, int64_t* n_vtx, int64_t* n_tet) {
+  if (n < 1 || n > 1000) return MC_ERR_ARG;
+  *n_vtx = (int64_t)(n + 1) * (n + 1) * (n + 1);
+  *n_tet = (int64_t)6 * n * n * n;
+  return MC_OK;
+}
+
+extern "C" int mc_gen_cube(int32_t n, double L, double* xyz, int32_t* tet_vtx, int32_t* tet_block,
+                           int32_t* tet_side_bid) {
+  if (n < 1 || n > 1000 || !(L > 0.0)) return MC_ERR_ARG;
+  const double h = L / n;
+  for (int k = 0; k <= n; ++k)
+    for (int j = 0; j <= n; ++j)
+      for (int i = 0; i <= n; ++i) {
+        int32_t v;
+        cube_vertex_index(n, i, j, k, &v);
+        xyz[3 * (int64_t)v + 0] = (i == n) ? L : i * h;
+        xyz[3 * (int64_t)v + 1] = (j == n) ? L : j * h;
+        xyz[3 * (int64_t)v + 2] = (k == n) ? L : k * h;
+      }
+  static const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  int64_t t = 0;
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i)
+        for (int p = 0; p < 6; ++p, ++t) {
+          int c[3] = {i, j, k};
+          int cell[4][3];
+          for (int a = 0; a < 3; ++a) cell[0][a] = c[a];
+          for (int s = 1; s < 4; ++s) {
+            for (int a = 0; a < 3; ++a) cell[s][a] = cell[s - 1][a];
+            cell[s][perms[p][s - 1]] += 1;
+          }
+          for (int s = 0; s < 4; ++s) cube_vertex_index(n, cell[s][0], cell[s][1], cell[s][2], &tet_vtx[4 * t + s]);
+          tet_block[t] = 0;
+          if (tet_side_bid) {
+            for (int f = 0; f < 4; ++f) {
+              int lo_hit[3] = {1, 1, 1}, hi_hit[3] = {1, 1, 1};
+              for (int q = 0; q < 3; ++q) {
+                const int* v = cell[kFaceVtx[f][q]];
+                for (int a = 0; a < 3; ++a) {
+                  if (v[a] != 0) lo_hit[a] = 0;
+                  if (v[a] != n) hi_hit[a] = 0;
+                }
+              }
+              tet_side_bid[4 * t + f] = box_side_id(lo_hit, hi_hit);
+            }
+          }
+        }
+  return MC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pin-cell lattice.  Each square cell (pitch p) is triangulated in 2-D with
+// a centre fan, n_fuel_rings rings inside r_fuel, one ring to r_clad and
+// one ring out to the cell square, all on n_sec azimuthal sectors (n_sec a
+// multiple of 8, so sector rays hit the cell corners).  Points on the cell
+// square are placed by a per-edge formula so neighbouring cells produce
+// bit-identical shared vertices.  The 2-D mesh is extruded into nz layers
+// of prisms, each cut into three tets with every quad diagonal starting at
+// the lower-layer vertex of the smaller 2-D id (a conforming split).
+namespace {
+
+struct Lattice2D {
+  std::vector<double> x, y;
+  std::vector<uint8_t> on_x0, on_x1, on_y0, on_y1;
+  std::vector<int32_t> tri;  // 3 per triangle
+  std::vector<int32_t> tri_block;
+};
+
+int lattice2d(int nx, int ny, int n_sec, int n_fr, double pitch, double r_fuel, double r_clad,
+              Lattice2D& G) {
+  if (nx < 1 || ny < 1 || n_sec < 8 || n_sec % 8 != 0 || n_fr < 1) return MC_ERR_ARG;
+  if (!(r_fuel > 0.0) || !(r_clad > r_fuel) || !(pitch > 2.0 * r_clad)) return MC_ERR_ARG;
+  const double twopi = 6.283185307179586;
+  const int q = n_sec / 8;
+  // cos/sin of the sector angles by Taylor series after reduction to
+  // [-pi/4, pi/4] around the nearest multiple of pi/2 (exact at the axes).
+  std::vector<double> cs(n_sec), sn(n_sec), tn(2 * q + 1);
+  for (int k = 0; k < n_sec; ++k) {
+    const double a = twopi * k / n_sec;
+    const int quad = (k + q) / (2 * q);  // nearest multiple of pi/2
+    const int oct = quad % 4;
+    const double r = a - quad * (twopi / 4.0);
+    double c = 0.0, s = 0.0, term_c = 1.0, term_s = r;
+    for (int m = 0; m < 12; ++m) {
+      c += term_c;
+      s += term_s;
+      term_c = -term_c * r * r / ((2.0 * m + 1.0) * (2.0 * m + 2.0));
+      term_s = -term_s * r * r / ((2.0 * m + 2.0) * (2.0 * m + 3.0));
+    }
+    if (k % (2 * q) == 0) {
+      c = 1.0;
+      s = 0.0;
+    }
+    double C, S;
+    switch (oct) {
+      case 0: C = c; S = s; break;
+      case 1: C = -s; S = c; break;
+      case 2: C = -c; S = -s; break;
+      default: C = s; S = -c; break;
+    }
+    cs[k] = C;
+    sn[k] = S;
+  }
+  for (int m = 0; m <= q; ++m) {
+    // tan of m/q * 45 degrees, from the sector cos/sin
+    tn[q + m] = (m == q) ? 1.0 : sn[m] / cs[m];
+    tn[q - m] = -tn[q + m];
+  }
+  std::map<std::pair<uint64_t, uint64_t>, int32_t> shared;
+  auto add_pt = [&](double x, double y, bool dedup, int fx0, int fx1, int fy0, int fy1) -> int32_t {
+    if (dedup) {
+      auto key = std::make_pair(mc::dbits(x), mc::dbits(y));
+      auto it = shared.find(key);
+      if (it != shared.end()) return it->second;
+      shared[key] = (int32_t)G.x.size();
+    }
+    G.x.push_back(x);
+    G.y.push_back(y);
+    G.on_x0.push_back((uint8_t)fx0);
+    G.on_x1.push_back((uint8_t)fx1);
+    G.on_y0.push_back((uint8_t)fy0);
+    G.on_y1.push_back((uint8_t)fy1);
+    return (int32_t)G.x.size() - 1;
+  };
+  auto tri = [&](int32_t a, int32_t b, int32_t c, int32_t blk) {
+    G.tri.push_back(a);
+    G.tri.push_back(b);
+    G.tri.push_back(c);
+    G.tri_block.push_back(blk);
+  };
+  const double h = pitch * 0.5;
+  const int n_rings = n_fr + 1;  // fuel rings + clad ring
+  std::vector<int32_t> ring((size_t)n_rings * n_sec), sq(n_sec);
+  for (int cj = 0; cj < ny; ++cj)
+    for (int ci = 0; ci < nx; ++ci) {
+      const double X0 = ci * pitch, X1 = (ci + 1) * pitch, Y0 = cj * pitch, Y1 = (cj + 1) * pitch;
+      const double cx = (X0 + X1) * 0.5, cy = (Y0 + Y1) * 0.5;
+      const int32_t ctr = add_pt(cx, cy, false, 0, 0, 0, 0);
+      for (int r = 0; r < n_rings; ++r) {
+        const double rad = (r < n_fr) ? r_fuel * (r + 1) / n_fr : r_clad;
+        for (int k = 0; k < n_sec; ++k) ring[(size_t)r * n_sec + k] = add_pt(cx + rad * cs[k], cy + rad * sn[k], false, 0, 0, 0, 0);
+      }
+      for (int k = 0; k < n_sec; ++k) {
+        double x, y;
+        if (k == q) { x = X1; y = Y1; }
+        else if (k == 3 * q) { x = X0; y = Y1; }
+        else if (k == 5 * q) { x = X0; y = Y0; }
+        else if (k == 7 * q) { x = X1; y = Y0; }
+        else if (k < q || k > 7 * q) { x = X1; y = cy + h * tn[q + (k < q ? k : k - n_sec)]; }
+        else if (k < 3 * q) { x = cx + h * tn[q + 2 * q - k]; y = Y1; }
+        else if (k < 5 * q) { x = X0; y = cy + h * tn[q + 4 * q - k]; }
+        else { x = cx + h * tn[q + k - 6 * q]; y = Y0; }
+        const int fx0 = (x == X0 && ci == 0), fx1 = (x == X1 && ci == nx - 1);
+        const int fy0 = (y == Y0 && cj == 0), fy1 = (y == Y1 && cj == ny - 1);
+        sq[k] = add_pt(x, y, true, fx0, fx1, fy0, fy1);
+      }
+      for (int k = 0; k < n_sec; ++k) {
+        const int k1 = (k + 1) % n_sec;
+        tri(ctr, ring[k], ring[k1], 1);
+        for (int r = 0; r + 1 < n_rings; ++r) {
+          const int32_t a = ring[(size_t)r * n_sec + k], b = ring[(size_t)r * n_sec + k1];
+          const int32_t c = ring[(size_t)(r + 1) * n_sec + k1], d = ring[(size_t)(r + 1) * n_sec + k];
+          const int32_t blk = (r + 1 < n_fr) ? 1 : 2;
+          tri(a, b, c, blk);
+          tri(a, c, d, blk);
+        }
+        const int32_t a = ring[(size_t)(n_rings - 1) * n_sec + k], b = ring[(size_t)(n_rings - 1) * n_sec + k1];
+        tri(a, b, sq[k1], 3);
+        tri(a, sq[k1], sq[k], 3);
+      }
+    }
+  return MC_OK;
+}
+
+}  // namespace
+
+extern "C" int mc_gen_lattice_sizes(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int32_t n_fr,
+                                    int64_t* n_vtx, int64_t* n_tet) {
+  Lattice2D G;
+  if (nz < 1) return MC_ERR_ARG;
+  int rc = lattice2d(nx, ny, n_sec, n_fr, 1.26, 0.41, 0.475, G);
+  if (rc) return rc;
+  *n_vtx = (int64_t)G.x.size() * (nz + 1);
+  *n_tet = (int64_t)G.tri_block.size() * nz * 3;
+  return MC_OK;
+}
+
+extern "C" int mc_gen_lattice(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int32_t n_fr,
+                              double pitch, double height, double r_fuel, double r_clad,
+                              double* xyz, int32_t* tet_vtx, int32_t* tet_block,
+                              int32_t* tet_side_bid) {
+  Lattice2D G;
+  if (nz < 1 || !(height > 0.0)) return MC_ERR_ARG;
+  int rc = lattice2d(nx, ny, n_sec, n_fr, pitch, r_fuel, r_clad, G);
+  if (rc) return rc;
+  const int64_t n2 = (int64_t)G.x.size();
+  for (int l = 0; l <= nz; ++l) {
+    const double z = (l == nz) ? height : height * l / nz;
+    for (int64_t v = 0; v < n2; ++v) {
+      const int64_t id = (int64_t)l * n2 + v;
+      xyz[3 * id] = G.x[v];
+      xyz[3 * id + 1] = G.y[v];
+      xyz[3 * id + 2] = z;
+    }
+  }
+  const int64_t nt2 = (int64_t)G.tri_block.size();
+  int64_t t = 0;
+  for (int l = 0; l < nz; ++l)
+    for (int64_t f = 0; f < nt2; ++f) {
+      int32_t v[3] = {G.tri[3 * f], G.tri[3 * f + 1], G.tri[3 * f + 2]};
+      std::sort(v, v + 3);
+      const int32_t a0 = (int32_t)(l * n2 + v[0]), b0 = (int32_t)(l * n2 + v[1]), c0 = (int32_t)(l * n2 + v[2]);
+      const int32_t a1 = (int32_t)((l + 1) * n2 + v[0]), b1 = (int32_t)((l + 1) * n2 + v[1]),
+                    c1 = (int32_t)((l + 1) * n2 + v[2]);
+      const int32_t tets[3][4] = {{a0, b0, c0, c1}, {a0, b0, b1, c1}, {a0, a1, b1, c1}};
+      for (int s = 0; s < 3; ++s, ++t) {
+        for (int a = 0; a < 4; ++a) tet_vtx[4 * t + a] = tets[s][a];
+        tet_block[t] = G.tri_block[f];
+        if (tet_side_bid) {
+          for (int fc = 0; fc < 4; ++fc) {
+            int lo_hit[3] = {1, 1, 1}, hi_hit[3] = {1, 1, 1};
+            for (int qv = 0; qv < 3; ++qv) {
+              const int32_t g = tets[s][kFaceVtx[fc][qv]];
+              const int64_t g2 = g % n2;
+              const int64_t lay = g / n2;
+              if (!G.on_x0[g2]) lo_hit[0] = 0;
+              if (!G.on_x1[g2]) hi_hit[0] = 0;
+              if (!G.on_y0[g2]) lo_hit[1] = 0;
+              if (!G.on_y1[g2]) hi_hit[1] = 0;
+              if (lay != 0) lo_hit[2] = 0;
+              if (lay != nz) hi_hit[2] = 0;
+            }
+            tet_side_bid[4 * t + fc] = box_side_id(lo_hit, hi_hit);
+          }
+        }
+      }
+    }
+  return MC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic nuclide: log-uniform grid, 1/sqrt(E) background with amplitude
+// U[1,10] b, n_peaks Lorentzians (centres log-U[1 eV, 100 keV], full widths
+// log-U[1e-3, 1e-1] x centre, heights U[10, 1000] b), constant scatter
+// fraction U[0.5, 0.99], target mass ratio U[1, 240].
+extern "C" int mc_gen_nuclide(uint64_t seed, int32_t index, int64_t n_pts, double E_min,
+                              double E_max, int32_t n_peaks, double* E, double* sig_t,
+                              double* sig_s, double* awr) {
+  if (n_pts < 2 || !(E_min > 0.0) || !(E_max > E_min) || n_peaks < 0) return MC_ERR_ARG;
+  Gen g(seed, 1, (uint64_t)index);
+  const double amp = g.uniform(1.0, 10.0);
+  std::vector<double> ec(n_peaks), hw(n_peaks), ht(n_peaks);
+  for (int p = 0; p < n_peaks; ++p) {
+    ec[p] = g.log_uniform(1.0, 1.0e5);
+    hw[p] = 0.5 * g.log_uniform(1.0e-3, 1.0e-1) * ec[p];
+    ht[p] = g.uniform(10.0, 1000.0);
+  }
+  const double fs = g.uniform(0.5, 0.99);
+  *awr = g.uniform(1.0, 240.0);
+  const double la = mc::log64(E_min), lb = mc::log64(E_max);
+  for (int64_t k = 0; k < n_pts; ++k) {
+    double e;
+    if (k == 0) e = E_min;
+    else if (k == n_pts - 1) e = E_max;
+    else e = mc::exp64(la + (lb - la) * ((double)k / (double)(n_pts - 1)));
+    E[k] = e;
+  }
+  for (int64_t k = 1; k < n_pts; ++k)
+    if (!(E[k] > E[k - 1])) return MC_ERR_ARG;
+  for (int64_t k = 0; k < n_pts; ++k) {
+    const double e = E[k];
+    double s = amp / sqrt(e);
+    for (int p = 0; p < n_peaks; ++p) {
+      const double z = (e - ec[p]) / hw[p];
+      s = s + ht[p] / (1.0 + z * z);
+    }
+    sig_t[k] = s;
+    sig_s[k] = fs * s;
+  }
+  return MC_OK;
+}
+
+extern "C" int mc_gen_densities(uint64_t seed, int32_t index, int32_t n, double lo, double hi,
+                                double* out) {
+  if (n < 0 || !(hi >= lo)) return MC_ERR_ARG;
+  Gen g(seed, 2, (uint64_t)index);
+  for (int i = 0; i < n; ++i) out[i] = g.uniform(lo, hi);
+  return MC_OK;
+}

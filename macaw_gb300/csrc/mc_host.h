@@ -1,0 +1,62 @@
+// mc_host.h -- host-side data model of the tracker context.
+#pragma once
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace mc {
+
+// Face adjacency, outward planes and start-point locator of a tet mesh, in
+// the layouts the kernels read.  Side f of a tet is the face opposite its
+// local vertex f.
+struct MeshTables {
+  int64_t n_vtx = 0, n_tet = 0;
+  std::vector<double> planes;   // 16 per tet: (nx, ny, nz, d) per side
+  std::vector<float> planes32;  // same, rounded to float
+  std::vector<int32_t> nbr;     // 4 per tet: neighbour id, or -1-boundary_id
+  std::vector<int32_t> block;   // subdomain id per tet
+  // uniform-grid locator: cells hold ascending ids of tets whose bounding
+  // box (grown by the locate tolerance) overlaps the cell
+  double glo[3] = {0, 0, 0}, gh[3] = {1, 1, 1};
+  int32_t gn[3] = {1, 1, 1};
+  std::vector<int64_t> gstart;
+  std::vector<int32_t> gtets;
+  double bbox_lo[3] = {0, 0, 0}, bbox_hi[3] = {0, 0, 0};
+};
+
+// Builds MeshTables; returns an empty string or an error message.
+std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
+                              const int32_t* tet_vtx, const int32_t* tet_block,
+                              const int32_t* tet_side_bid, MeshTables& out);
+
+struct Nuclide {
+  std::vector<double> E, st, ss;
+  double awr = 1.0;
+};
+
+struct Material {
+  int32_t id = 0;
+  std::vector<int32_t> nuc;
+  std::vector<double> dens;
+};
+
+// Flattened cross-section tables in the layouts the kernels read.
+struct XSTables {
+  std::vector<double> pts;      // 4 per point: (E, sigma_t, sigma_s, 0), nuclides concatenated
+  std::vector<int64_t> nuc_off; // first point of each nuclide
+  std::vector<int32_t> nuc_n;   // points per nuclide
+  std::vector<int32_t> hidx;    // (n_bins+1) x n_nuc, bin-major
+  std::vector<double> awr;
+  std::vector<int32_t> mat_off; // n_mat+1
+  std::vector<int32_t> mat_nuc;
+  std::vector<double> mat_dens;
+  std::vector<int32_t> mat_ids;
+  int32_t n_bins = 8000;
+  double E_lo = 0, E_hi = 0, lE_lo = 0, du = 0;
+};
+
+std::string build_xs_tables(const std::vector<Nuclide>& nucs, const std::vector<Material>& mats,
+                            int32_t n_bins, XSTables& out);
+
+}  // namespace mc

@@ -1,0 +1,403 @@
+// mc_kernels.cu -- tracking kernels for sm_103a.
+//
+// Two execution forms over the same per-particle steps (mc_device.cuh):
+//  * history: a persistent grid where each thread runs whole histories,
+//    birth to death, one after another;
+//  * event: a device-resident particle bank and four event queues (XS
+//    lookup, advance, collide, refill).  Each launch works on one event
+//    type, so warps stay coherent; queues are filled with warp-aggregated
+//    atomics.  Grids are persistent and loop over the device-side queue
+//    lengths, so the host never needs the counts to launch.
+#include <cooperative_groups.h>
+
+#include "mc_kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace mc {
+
+namespace {
+
+struct LocalCounters {
+  unsigned long long c[kNumCounters];
+  double leak_w;
+  __device__ void zero() {
+#pragma unroll
+    for (int i = 0; i < kNumCounters; ++i) c[i] = 0;
+    leak_w = 0.0;
+  }
+};
+
+__device__ __forceinline__ void flush(LocalCounters& L, unsigned long long* g, double* leak_w) {
+#pragma unroll
+  for (int i = 0; i < kNumCounters; ++i) {
+    unsigned long long v = L.c[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(g + i, v);
+  }
+  double w = L.leak_w;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+  if ((threadIdx.x & 31) == 0 && w != 0.0) atomicAdd(leak_w, w);
+}
+
+// End of a history: closing hash word, counters, optional trace record.
+__device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCounters& L) {
+  p.hash = fnv(p.hash, (uint64_t)(16 + p.status));
+  L.c[kCntSeg] += (unsigned long long)p.n_seg;
+  L.c[kCntColl] += (unsigned long long)p.n_coll;
+  L.c[kCntHist] += 1;
+  switch (p.status) {
+    case kLeaked: L.c[kCntLeak] += 1; L.leak_w += p.wgt; break;
+    case kAbsorbed: L.c[kCntAbsorb] += 1; break;
+    case kCutoff: L.c[kCntCutoff] += 1; break;
+    case kStuck: L.c[kCntStuck] += 1; break;
+    case kLost: L.c[kCntLost] += 1; break;
+    default: L.c[kCntBadXS] += 1; break;
+  }
+  if (a.traces) {
+    mc_trace t;
+    t.id = p.id;
+    t.hash = p.hash;
+    t.status = p.status;
+    t.n_seg = p.n_seg;
+    t.n_coll = p.n_coll;
+    t.elem = p.elem;
+    t.face = p.face;
+    t.pad = 0;
+    t.E = p.E;
+    t.x = p.x;
+    t.y = p.y;
+    t.z = p.z;
+    a.traces[p.id - 1 - a.first] = t;
+  }
+}
+
+// Macroscopic XS for the particle's current element; false if unusable.
+__device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, Particle& p,
+                                          LocalCounters& L) {
+  const int mat = __ldg(M.tmat + p.elem);
+  if (mat < 0) {
+    p.status = kBadXS;
+    return false;
+  }
+  p.sigt = macro_total(X, mat, p.E);
+  p.mat = mat;
+  L.c[kCntXS] += 1;
+  if (!(p.sigt > 0.0) || p.sigt != p.sigt) {
+    p.status = kBadXS;
+    return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void load(const Bank& B, int s, Particle& p) {
+  p.x = B.x[s]; p.y = B.y[s]; p.z = B.z[s];
+  p.u = B.u[s]; p.v = B.v[s]; p.w = B.w[s];
+  p.E = B.E[s]; p.wgt = B.wgt[s]; p.sigt = B.sigt[s];
+  p.seed = B.seed[s]; p.hash = B.hash[s]; p.id = B.id[s];
+  p.elem = B.elem[s]; p.mat = B.mat[s]; p.n_seg = B.n_seg[s]; p.n_coll = B.n_coll[s];
+  p.zero_run = B.zero_run[s];
+  p.status = kAlive;
+  p.face = -1;
+}
+
+__device__ __forceinline__ void store(const Bank& B, int s, const Particle& p) {
+  B.x[s] = p.x; B.y[s] = p.y; B.z[s] = p.z;
+  B.u[s] = p.u; B.v[s] = p.v; B.w[s] = p.w;
+  B.E[s] = p.E; B.wgt[s] = p.wgt; B.sigt[s] = p.sigt;
+  B.seed[s] = p.seed; B.hash[s] = p.hash; B.id[s] = p.id;
+  B.elem[s] = p.elem; B.mat[s] = p.mat; B.n_seg[s] = p.n_seg; B.n_coll[s] = p.n_coll;
+  B.zero_run[s] = p.zero_run;
+}
+
+__device__ __forceinline__ void birth(const DevMesh& M, const DevXS& X, const DevSource& S,
+                                      const RunArgs& a, int64_t h, Particle& p) {
+  mc_site o;
+  if (a.sites) o = a.sites[h - a.first];
+  else sample_source(X, S, h, a.master, o);
+  start(M, o, h, a.master, p);
+}
+
+// Append slot to a queue with one atomic per converged group of lanes.
+__device__ __forceinline__ void push(int* q, int* cnt, int slot) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(cnt, (int)g.size());
+  base = g.shfl(base, 0);
+  q[base + g.thread_rank()] = slot;
+}
+
+// ---------------------------------------------------------------------------
+// History form.
+__global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S, RunArgs a) {
+  LocalCounters L;
+  L.zero();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    Particle p;
+    birth(M, X, S, a, a.first + i, p);
+    float sigt32 = 0.0f;
+    unsigned long long nxs = 0;
+    while (p.status == kAlive) {
+      const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
+      if (r == 1) collide(X, p);
+    }
+    L.c[kCntXS] += nxs;
+    finish(p, a, L);
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
+// ---------------------------------------------------------------------------
+// Event form.
+
+// Births of histories [0, min(n, cap)) into slots of the same index.
+__global__ void __launch_bounds__(256) k_ev_init(DevMesh M, DevXS X, DevSource S, RunArgs a,
+                                                 Bank B, EventQueues Q, EventCtl* ctl) {
+  LocalCounters L;
+  L.zero();
+  const int64_t m = a.n < B.cap ? a.n : B.cap;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+    Particle p;
+    birth(M, X, S, a, a.first + i, p);
+    if (p.status != kAlive) {
+      finish(p, a, L);
+      push(Q.free_slots, &ctl->n_free, (int)i);
+      continue;
+    }
+    store(B, (int)i, p);
+    push(Q.xs[0], &ctl->n_xs[0], (int)i);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->next_hist = m;
+  flush(L, a.counters, a.leak_w);
+}
+
+__global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Bank B,
+                                               EventQueues Q, EventCtl* ctl, int par) {
+  LocalCounters L;
+  L.zero();
+  const int n = *(volatile int*)&ctl->n_xs[par];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = Q.xs[par][i];
+    Particle p;
+    p.E = B.E[s];
+    p.elem = B.elem[s];
+    p.status = kAlive;
+    if (refresh_xs(M, X, p, L)) {
+      B.sigt[s] = p.sigt;
+      B.mat[s] = p.mat;
+      push(Q.adv[par], &ctl->n_adv[par], s);
+    } else {
+      load(B, s, p);
+      p.status = kBadXS;
+      finish(p, a, L);
+      push(Q.free_slots, &ctl->n_free, s);
+    }
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
+__global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs a, Bank B,
+                                                    EventQueues Q, EventCtl* ctl, int par) {
+  LocalCounters L;
+  L.zero();
+  const int n = *(volatile int*)&ctl->n_adv[par];
+  const int nxt = par ^ 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = Q.adv[par][i];
+    Particle p;
+    load(B, s, p);
+    float sigt32 = (float)p.sigt;
+    unsigned long long nxs = 0;
+    int r = 0;
+    int k = 0;
+    for (;;) {
+      // a new material needs a cross-section event before the next segment
+      if (p.n_seg < kMaxSegments && p.zero_run < kMaxZeroRun && __ldg(M.tmat + p.elem) != p.mat) {
+        r = 3;
+        break;
+      }
+      r = segment_fp64<false>(M, X, p, a.tally, sigt32, nxs);
+      if (r != 0) break;
+      if (a.max_seg > 0 && ++k >= a.max_seg) {
+        r = 4;
+        break;
+      }
+    }
+    if (r == 2) {
+      finish(p, a, L);
+      push(Q.free_slots, &ctl->n_free, s);
+      continue;
+    }
+    store(B, s, p);
+    if (r == 1) push(Q.coll, &ctl->n_coll, s);
+    else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+    else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
+__global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs a, Bank B,
+                                                    EventQueues Q, EventCtl* ctl, int par) {
+  LocalCounters L;
+  L.zero();
+  const int n = *(volatile int*)&ctl->n_coll;
+  const int nxt = par ^ 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = Q.coll[i];
+    Particle p;
+    load(B, s, p);
+    collide(X, p);
+    if (p.status != kAlive) {
+      finish(p, a, L);
+      push(Q.free_slots, &ctl->n_free, s);
+      continue;
+    }
+    B.u[s] = p.u; B.v[s] = p.v; B.w[s] = p.w;
+    B.E[s] = p.E; B.seed[s] = p.seed; B.mat[s] = p.mat;
+    push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
+// New histories into the slots freed this iteration: free slot i takes
+// history next_hist + i while histories remain.
+__global__ void __launch_bounds__(256) k_ev_refill(DevMesh M, DevXS X, DevSource S, RunArgs a,
+                                                   Bank B, EventQueues Q, EventCtl* ctl, int par) {
+  LocalCounters L;
+  L.zero();
+  const int nf = *(volatile int*)&ctl->n_free;
+  const long long base = *(volatile long long*)&ctl->next_hist;
+  const long long left = a.n - base;
+  const int n = (int)(left < (long long)nf ? (left > 0 ? left : 0) : nf);
+  const int nxt = par ^ 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = Q.free_slots[i];
+    Particle p;
+    birth(M, X, S, a, a.first + base + i, p);
+    if (p.status != kAlive) {
+      finish(p, a, L);
+      continue;  // slot stays empty for the rest of the batch
+    }
+    store(B, s, p);
+    push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
+// End of an iteration: consumed queues emptied, births committed.  Free
+// slots never outlive an iteration: either all were refilled, or every
+// remaining history was born and the spare slots are not needed again.
+__global__ void k_ev_reset(EventCtl* ctl, int par, int64_t n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    long long nh = ctl->next_hist + (long long)ctl->n_free;
+    ctl->next_hist = nh < n ? nh : n;
+    ctl->n_free = 0;
+    ctl->n_xs[par] = 0;
+    ctl->n_adv[par] = 0;
+    ctl->n_coll = 0;
+  }
+}
+
+// Tail of a batch: every particle still queued runs to completion in one
+// launch, one thread per particle, with cross sections and collisions inline.
+__global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a, Bank B,
+                                                   EventQueues Q, EventCtl* ctl, int par) {
+  LocalCounters L;
+  L.zero();
+  const int nx = *(volatile int*)&ctl->n_xs[par];
+  const int na = *(volatile int*)&ctl->n_adv[par];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx + na; i += gridDim.x * blockDim.x) {
+    const int s = (i < nx) ? Q.xs[par][i] : Q.adv[par][i - nx];
+    Particle p;
+    load(B, s, p);
+    if (i < nx) p.mat = -2;
+    float sigt32 = (float)p.sigt;
+    unsigned long long nxs = 0;
+    while (p.status == kAlive) {
+      const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
+      if (r == 1) collide(X, p);
+    }
+    L.c[kCntXS] += nxs;
+    finish(p, a, L);
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
+__global__ void __launch_bounds__(256) k_sample(DevXS X, DevSource S, int64_t first, int64_t n,
+                                                uint64_t master, mc_site* out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    mc_site o;
+    sample_source(X, S, first + i, master, o);
+    out[i] = o;
+  }
+}
+
+__global__ void k_accumulate(double* __restrict__ batch, double* __restrict__ sum,
+                             double* __restrict__ sumsq, int64_t n, double inv_w) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double v = batch[i] * inv_w;
+    sum[i] += v;
+    sumsq[i] += v * v;
+    batch[i] = 0.0;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
+                           int block, int grid, cudaStream_t st) {
+  k_history<<<grid, block, 0, st>>>(M, X, S, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_event_init(const DevMesh& M, const DevXS& X, const DevSource& S,
+                              const RunArgs& a, const Bank& B, const EventQueues& Q,
+                              EventCtl* ctl, int block, int grid, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(EventCtl), st);
+  if (e != cudaSuccess) return e;
+  k_ev_init<<<grid, block, 0, st>>>(M, X, S, a, B, Q, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSource& S,
+                                   const RunArgs& a, const Bank& B, const EventQueues& Q,
+                                   EventCtl* ctl, int par, int block, int grid, cudaStream_t st,
+                                   int* n_launch, cudaEvent_t adv0, cudaEvent_t adv1) {
+  k_ev_xs<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (adv0) cudaEventRecord(adv0, st);
+  k_ev_advance<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (adv1) cudaEventRecord(adv1, st);
+  k_ev_collide<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  k_ev_refill<<<grid, block, 0, st>>>(M, X, S, a, B, Q, ctl, par);
+  k_ev_reset<<<1, 32, 0, st>>>(ctl, par, a.n);
+  if (n_launch) *n_launch += 5;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_event_finish(const DevMesh& M, const DevXS& X, const DevSource& S,
+                                const RunArgs& a, const Bank& B, const EventQueues& Q,
+                                EventCtl* ctl, int par, int block, int grid, cudaStream_t st) {
+  (void)S;
+  k_ev_finish<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample(const DevXS& X, const DevSource& S, int64_t first, int64_t n,
+                          uint64_t master, mc_site* out, cudaStream_t st) {
+  k_sample<<<1216, 256, 0, st>>>(X, S, first, n, master, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate(double* batch, double* sum, double* sumsq, int64_t n, double inv_w,
+                              cudaStream_t st) {
+  k_accumulate<<<1216, 256, 0, st>>>(batch, sum, sumsq, n, inv_w);
+  return cudaGetLastError();
+}
+
+}  // namespace mc

@@ -1,0 +1,88 @@
+// mc_kernels.h -- launchers for the tracking kernels (host-callable).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/macaw_gb300.h"
+#include "mc_device.cuh"
+
+namespace mc {
+
+// Device counters, one 64-bit slot each.
+enum Counter : int {
+  kCntSeg = 0,
+  kCntColl,
+  kCntLeak,
+  kCntAbsorb,
+  kCntCutoff,
+  kCntStuck,
+  kCntLost,
+  kCntBadXS,
+  kCntXS,
+  kCntFallback,
+  kCntHist,
+  kNumCounters
+};
+
+// Particle bank in structure-of-arrays form.
+struct Bank {
+  double *x, *y, *z, *u, *v, *w, *E, *wgt, *sigt;
+  uint64_t *seed, *hash;
+  int64_t* id;
+  int *elem, *mat, *n_seg, *n_coll, *zero_run;
+  int64_t cap;
+};
+
+// Event-loop control block (device memory).
+struct EventCtl {
+  int n_xs[2], n_adv[2], n_coll;   // queue lengths, double-buffered by iteration parity
+  int n_free;                       // slots freed this iteration
+  int alive;                        // particles in flight
+  int pad;
+  long long next_hist;              // next history (relative to the batch) to be born
+  long long leak_w_bits;            // unused
+};
+
+struct EventQueues {
+  int* xs[2];
+  int* adv[2];
+  int* coll;
+  int* free_slots;
+};
+
+struct RunArgs {
+  int64_t first, n;
+  uint64_t master;
+  double* tally;
+  mc_trace* traces;
+  unsigned long long* counters;
+  double* leak_w;
+  const mc_site* sites;  // device copy of caller-supplied sites, or null
+  int precision;
+  int max_seg;  // event mode: segments per advance launch (<= 0: until event)
+};
+
+cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
+                           int block, int grid, cudaStream_t st);
+
+// Event mode, one call per phase; grids are persistent (grid-stride over the
+// device-side queue lengths), so the launch shapes never depend on counts.
+cudaError_t launch_event_init(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
+                              const Bank& B, const EventQueues& Q, EventCtl* ctl, int block,
+                              int grid, cudaStream_t st);
+cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSource& S,
+                                   const RunArgs& a, const Bank& B, const EventQueues& Q,
+                                   EventCtl* ctl, int parity, int block, int grid,
+                                   cudaStream_t st, int* n_launch, cudaEvent_t adv0 = nullptr,
+                                   cudaEvent_t adv1 = nullptr);
+cudaError_t launch_event_finish(const DevMesh& M, const DevXS& X, const DevSource& S,
+                                const RunArgs& a, const Bank& B, const EventQueues& Q,
+                                EventCtl* ctl, int parity, int block, int grid, cudaStream_t st);
+
+cudaError_t launch_sample(const DevXS& X, const DevSource& S, int64_t first, int64_t n,
+                          uint64_t master, mc_site* out, cudaStream_t st);
+
+cudaError_t launch_accumulate(double* batch, double* sum, double* sumsq, int64_t n, double inv_w,
+                              cudaStream_t st);
+
+}  // namespace mc

@@ -1,0 +1,164 @@
+"""Synthetic fixed-source problems (meshes, cross sections, sources).
+
+The reference's inputs (BEAVRS meshes, ENDF/HDF5 nuclear data) are not
+shipped with it and cannot be downloaded here, so problems are generated
+from one seed by the library's own generators (mc_gen_*), which produce
+bit-identical tables on every host architecture.
+
+cube_problem     -- 20 cm cube, 20^3 hexes x 6 tets (48,000 tets), one
+                    material of 10 nuclides, 10,000-point grids, point source
+                    at the centre, Watt spectrum, vacuum boundary.
+lattice_problem  -- 17x17 pin cells, pitch 1.26 cm, 50 cm tall, fuel/clad/
+                    moderator rings (15/4/3 nuclides, 20,000-point grids),
+                    about 2.0M tets, uniform source in the fuel cylinders.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import MC_BC_VACUUM, MC_SRC_CYLINDERS, MC_SRC_POINT, MC_SRC_WATT, lib, ptr
+
+WATT_A = 0.988e6   # eV
+WATT_B = 2.249e-6  # 1/eV
+E_MIN, E_MAX = 1.0e-5, 2.0e7  # eV
+
+
+@dataclass
+class Nuclide:
+    E: np.ndarray
+    sig_t: np.ndarray
+    sig_s: np.ndarray
+    awr: float
+
+
+@dataclass
+class Material:
+    id: int
+    nuclides: np.ndarray  # int32 indices into Problem.nuclides
+    densities: np.ndarray  # atom/b-cm
+
+
+@dataclass
+class Source:
+    space: int = MC_SRC_POINT
+    energy: int = MC_SRC_WATT
+    point: tuple = (0.0, 0.0, 0.0)
+    box_lo: tuple = (0.0, 0.0, 0.0)
+    box_hi: tuple = (0.0, 0.0, 0.0)
+    cyl_xy: np.ndarray | None = None
+    cyl_r: float = 0.0
+    cyl_z0: float = 0.0
+    cyl_z1: float = 0.0
+    watt_a: float = WATT_A
+    watt_b: float = WATT_B
+    mono_E: float = 0.0
+
+
+@dataclass
+class Problem:
+    name: str
+    xyz: np.ndarray
+    tet_vtx: np.ndarray
+    tet_block: np.ndarray
+    tet_side_bid: np.ndarray
+    nuclides: list
+    materials: list
+    blocks: np.ndarray
+    block_materials: np.ndarray
+    source: Source
+    bcs: dict = field(default_factory=dict)  # boundary id -> MC_BC_*
+    hash_bins: int = 8000
+
+    @property
+    def n_tet(self) -> int:
+        return int(self.tet_vtx.shape[0])
+
+    def footprint_bytes(self) -> int:
+        pts = sum(n.E.size for n in self.nuclides)
+        return self.n_tet * (128 + 64 + 16 + 4 + 3 * 8) + pts * 32
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what} failed with code {rc}")
+
+
+def cube_mesh(n: int = 20, L: float = 20.0):
+    nv, nt = C.c_int64(), C.c_int64()
+    _check(lib.mc_gen_cube_sizes(n, C.byref(nv), C.byref(nt)), "mc_gen_cube_sizes")
+    xyz = np.zeros((nv.value, 3), np.float64)
+    tv = np.zeros((nt.value, 4), np.int32)
+    blk = np.zeros(nt.value, np.int32)
+    bid = np.zeros((nt.value, 4), np.int32)
+    _check(lib.mc_gen_cube(n, L, ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_cube")
+    return xyz, tv, blk, bid
+
+
+def lattice_mesh(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fuel_rings: int = 2,
+                 pitch: float = 1.26, height: float = 50.0, r_fuel: float = 0.41, r_clad: float = 0.475):
+    nv, nt = C.c_int64(), C.c_int64()
+    _check(lib.mc_gen_lattice_sizes(nx, ny, nz, n_sec, n_fuel_rings, C.byref(nv), C.byref(nt)),
+           "mc_gen_lattice_sizes")
+    xyz = np.zeros((nv.value, 3), np.float64)
+    tv = np.zeros((nt.value, 4), np.int32)
+    blk = np.zeros(nt.value, np.int32)
+    bid = np.zeros((nt.value, 4), np.int32)
+    _check(lib.mc_gen_lattice(nx, ny, nz, n_sec, n_fuel_rings, pitch, height, r_fuel, r_clad,
+                              ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_lattice")
+    return xyz, tv, blk, bid
+
+
+def make_nuclide(seed: int, index: int, n_pts: int, n_peaks: int = 20,
+                 E_min: float = E_MIN, E_max: float = E_MAX) -> Nuclide:
+    E = np.zeros(n_pts)
+    st = np.zeros(n_pts)
+    ss = np.zeros(n_pts)
+    awr = C.c_double()
+    _check(lib.mc_gen_nuclide(seed, index, n_pts, E_min, E_max, n_peaks, ptr(E), ptr(st), ptr(ss),
+                              C.byref(awr)), "mc_gen_nuclide")
+    return Nuclide(E, st, ss, awr.value)
+
+
+def make_densities(seed: int, index: int, n: int, lo: float = 1e-4, hi: float = 5e-2) -> np.ndarray:
+    out = np.zeros(n)
+    _check(lib.mc_gen_densities(seed, index, n, lo, hi, ptr(out)), "mc_gen_densities")
+    return out
+
+
+def cube_problem(n: int = 20, L: float = 20.0, n_nuc: int = 10, n_pts: int = 10000, n_peaks: int = 20,
+                 seed: int = 20240611) -> Problem:
+    """The 48,000-tet cube of the plain FP64 configuration (at n=20)."""
+    xyz, tv, blk, bid = cube_mesh(n, L)
+    nucs = [make_nuclide(seed, i, n_pts, n_peaks) for i in range(n_nuc)]
+    mat = Material(1, np.arange(n_nuc, dtype=np.int32), make_densities(seed, 0, n_nuc))
+    src = Source(space=MC_SRC_POINT, point=(L / 2, L / 2, L / 2))
+    return Problem(f"cube{n}", xyz, tv, blk, bid, nucs, [mat], np.array([0], np.int32),
+                   np.array([1], np.int32), src, {b: MC_BC_VACUUM for b in range(6)})
+
+
+def lattice_problem(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fuel_rings: int = 2,
+                    pitch: float = 1.26, height: float = 50.0, n_pts: int = 20000, n_peaks: int = 20,
+                    nuclides_per_material=(15, 4, 3), seed: int = 20240611) -> Problem:
+    """17x17 pin lattice (about 2.0M tets at the defaults): blocks 1 fuel,
+    2 clad, 3 moderator mapped to materials 1, 2, 3."""
+    xyz, tv, blk, bid = lattice_mesh(nx, ny, nz, n_sec, n_fuel_rings, pitch, height)
+    nucs, mats = [], []
+    k = 0
+    for m, cnt in enumerate(nuclides_per_material):
+        idx = []
+        for _ in range(cnt):
+            nucs.append(make_nuclide(seed, k, n_pts, n_peaks))
+            idx.append(k)
+            k += 1
+        mats.append(Material(m + 1, np.array(idx, np.int32), make_densities(seed, m, cnt)))
+    cx = (np.arange(nx) + 0.5) * pitch
+    cy = (np.arange(ny) + 0.5) * pitch
+    centres = np.array([(x, y) for y in cy for x in cx], np.float64)
+    src = Source(space=MC_SRC_CYLINDERS, cyl_xy=np.ascontiguousarray(centres), cyl_r=0.41,
+                 cyl_z0=0.0, cyl_z1=height)
+    return Problem(f"lattice{nx}x{ny}x{nz}", xyz, tv, blk, bid, nucs, mats,
+                   np.array([1, 2, 3], np.int32), np.array([1, 2, 3], np.int32), src,
+                   {b: MC_BC_VACUUM for b in range(6)})

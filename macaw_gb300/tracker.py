@@ -1,0 +1,165 @@
+"""Thin Python handle over the C ABI (used by tests, bench and the serving loop).
+
+Tracker.load(problem) uploads mesh, boundary conditions, nuclides,
+materials, block map and source; Tracker.run(...) runs one batch of
+histories on the GPU.  Every call checks the return code and raises
+MCError with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (MC_MODE_EVENT, MC_PREC_FP64, MC_TALLY_BATCH, MC_TALLY_SUM, MC_TALLY_SUM_SQ,
+                   SITE_DTYPE, TRACE_DTYPE, MCError, RunDesc, SourceDesc, Stats, lib, ptr)
+from .problems import Problem, Source
+
+
+class Tracker:
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        rc = lib.mc_ctx_create(device, C.byref(h))
+        if rc != 0:
+            raise MCError(rc, f"mc_ctx_create(device={device}) failed (no usable CUDA device?)")
+        self._h = h
+        self.n_tet = 0
+
+    # -- plumbing ---------------------------------------------------------
+    def _ck(self, rc: int, what: str) -> None:
+        if rc != 0:
+            msg = lib.mc_last_error(self._h)
+            raise MCError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self) -> None:
+        if self._h:
+            lib.mc_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- setup ------------------------------------------------------------
+    def upload_mesh(self, xyz, tet_vtx, tet_block, tet_side_bid=None) -> None:
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        tv = np.ascontiguousarray(tet_vtx, np.int32)
+        blk = np.ascontiguousarray(tet_block, np.int32)
+        bid = None if tet_side_bid is None else np.ascontiguousarray(tet_side_bid, np.int32)
+        self._ck(lib.mc_mesh_upload(self._h, xyz.shape[0], ptr(xyz), tv.shape[0], ptr(tv), ptr(blk), ptr(bid)),
+                 "mc_mesh_upload")
+        self.n_tet = tv.shape[0]
+
+    def set_bc(self, boundary_id: int, bc_type: int) -> None:
+        self._ck(lib.mc_bc_set(self._h, boundary_id, bc_type), "mc_bc_set")
+
+    def add_nuclide(self, E, sig_t, sig_s, awr) -> int:
+        E, st, ss = (np.ascontiguousarray(a, np.float64) for a in (E, sig_t, sig_s))
+        idx = C.c_int32()
+        self._ck(lib.mc_nuclide_add(self._h, E.size, ptr(E), ptr(st), ptr(ss), float(awr), C.byref(idx)),
+                 "mc_nuclide_add")
+        return idx.value
+
+    def add_material(self, material_id: int, nuclides, densities) -> None:
+        n = np.ascontiguousarray(nuclides, np.int32)
+        d = np.ascontiguousarray(densities, np.float64)
+        self._ck(lib.mc_material_add(self._h, material_id, n.size, ptr(n), ptr(d)), "mc_material_add")
+
+    def block_material_map(self, blocks, materials) -> None:
+        b = np.ascontiguousarray(blocks, np.int32)
+        m = np.ascontiguousarray(materials, np.int32)
+        self._ck(lib.mc_block_material_map(self._h, b.size, ptr(b), ptr(m)), "mc_block_material_map")
+
+    def set_hash_bins(self, n: int) -> None:
+        self._ck(lib.mc_set_hash_bins(self._h, n), "mc_set_hash_bins")
+
+    def set_source(self, s: Source) -> None:
+        d = SourceDesc()
+        d.space, d.energy = s.space, s.energy
+        d.point[:] = s.point
+        d.box_lo[:] = s.box_lo
+        d.box_hi[:] = s.box_hi
+        cyl = None
+        if s.cyl_xy is not None:
+            cyl = np.ascontiguousarray(s.cyl_xy, np.float64).reshape(-1)
+            d.n_cyl = cyl.size // 2
+            d.cyl_xy = cyl.ctypes.data_as(C.POINTER(C.c_double))
+        d.cyl_r, d.cyl_z0, d.cyl_z1 = s.cyl_r, s.cyl_z0, s.cyl_z1
+        d.watt_a, d.watt_b, d.mono_E = s.watt_a, s.watt_b, s.mono_E
+        self._ck(lib.mc_source_set(self._h, C.byref(d)), "mc_source_set")
+
+    def load(self, p: Problem) -> "Tracker":
+        self.upload_mesh(p.xyz, p.tet_vtx, p.tet_block, p.tet_side_bid)
+        for bid, t in p.bcs.items():
+            self.set_bc(bid, t)
+        for n in p.nuclides:
+            self.add_nuclide(n.E, n.sig_t, n.sig_s, n.awr)
+        for m in p.materials:
+            self.add_material(m.id, m.nuclides, m.densities)
+        self.block_material_map(p.blocks, p.block_materials)
+        self.set_hash_bins(p.hash_bins)
+        self.set_source(p.source)
+        return self
+
+    # -- run --------------------------------------------------------------
+    def run(self, n: int, first: int = 0, seed: int = 1, mode: int = MC_MODE_EVENT,
+            precision: int = MC_PREC_FP64, bank_size: int = 0, block_size: int = 0,
+            max_seg: int = 0, traces: bool = False, accumulate: bool = False,
+            sort_queue: bool = False, profile: bool = False, sites: np.ndarray | None = None) -> Stats:
+        if sites is not None:
+            assert sites.dtype == SITE_DTYPE and sites.size >= n and sites.flags["C_CONTIGUOUS"]
+        d = RunDesc(first, n, bank_size, seed, precision, mode, block_size, max_seg, int(traces),
+                    int(accumulate), int(sort_queue), int(profile),
+                    None if sites is None else sites.ctypes.data)
+        self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
+        return self.stats()
+
+    def sample_sites(self, n: int, first: int = 0, seed: int = 1, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.zeros(n, SITE_DTYPE)
+        self._ck(lib.mc_source_sample(self._h, first, n, seed, ptr(out)), "mc_source_sample")
+        return out
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        self._ck(lib.mc_ctx_set_stream(self._h, stream_handle), "mc_ctx_set_stream")
+
+    def sync(self) -> None:
+        self._ck(lib.mc_sync(self._h), "mc_sync")
+
+    def stats(self) -> Stats:
+        s = Stats()
+        self._ck(lib.mc_stats_get(self._h, C.byref(s)), "mc_stats_get")
+        return s
+
+    def tally(self, kind: int = MC_TALLY_BATCH, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.zeros(self.n_tet, np.float64)
+        self._ck(lib.mc_tally_download(self._h, kind, ptr(out), out.size), "mc_tally_download")
+        return out
+
+    def tally_sum(self) -> np.ndarray:
+        return self.tally(MC_TALLY_SUM)
+
+    def tally_sum_sq(self) -> np.ndarray:
+        return self.tally(MC_TALLY_SUM_SQ)
+
+    def reset_tally(self) -> None:
+        self._ck(lib.mc_tally_reset(self._h), "mc_tally_reset")
+
+    def traces(self, n: int) -> np.ndarray:
+        out = np.zeros(n, TRACE_DTYPE)
+        self._ck(lib.mc_trace_download(self._h, ptr(out), n), "mc_trace_download")
+        return out
+
+    def batches_done(self) -> int:
+        v = C.c_int64()
+        self._ck(lib.mc_batches_done(self._h, C.byref(v)), "mc_batches_done")
+        return v.value

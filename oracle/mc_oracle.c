@@ -1,0 +1,937 @@
+/*
+ * mc_oracle.c -- CPU restatement of MaCaw's particle-tracking hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GPU path and the timed CPU
+ * baseline.  The product never links or calls this file.
+ *
+ * What it restates, with the reference call sites it follows:
+ *  - source birth per history, in index order, ids 1-based
+ *      src/userobjects/OpenMCStudy.C:317-360 (OpenMC initialize_history)
+ *  - start-element location (MOOSE ClaimRays, absent), deterministic rule
+ *  - element walk (MOOSE TraceRay, absent) as a plane-based tet walk
+ *  - per segment: macroscopic XS (CollisionKernel.C:143), a fresh
+ *    distance-to-collision sample d = -ln(xi)/Sigma_t (CollisionKernel.C:150),
+ *    track-length score wgt*min(d, L) (CollisionKernel.C:153-154; the flux
+ *    score per element replaces the keff score), cross if d > L
+ *    (CollisionKernel.C:163-169), else collide at end-(L-d)*u
+ *    (CollisionKernel.C:173-182)
+ *  - collision (OpenMC event_collide, absent): nuclide, absorb/scatter,
+ *    elastic target-at-rest kinematics; scatter restarts in the same
+ *    element (CollisionKernel.C:204-205); absorption ends the history
+ *    (CollisionKernel.C:226-230); no secondaries (CollisionKernel.C:236)
+ *  - material of an element = block map id - 1 (CollisionKernel.C:110)
+ *
+ * Parity pin: the RNG (below) is checked against the seed states in
+ * test/tests/study/gold/openmc_study_rays.e.  The rest is unpinned.
+ *
+ * Build: cc -O2 -ffp-contract=off -fopenmp -fPIC -shared.
+ */
+#include "mc_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Random numbers: OpenMC 0.13 scheme.  State step of the 64-bit PCG LCG
+ * (O'Neill 2014, multiplier/increment of Knuth's MMIX), RXS-M-XS output
+ * permutation, Brown (1994) arbitrary-stride skip-ahead, stride 152917 per
+ * particle id, one stream per purpose (0 tracking, 2 source).            */
+#define PRN_MULT 6364136223846793005ULL
+#define PRN_ADD 1442695040888963407ULL
+#define PRN_STRIDE 152917ULL
+
+double oracle_prn(uint64_t* seed)
+{
+  uint64_t s = PRN_MULT * (*seed) + PRN_ADD;
+  *seed = s;
+  uint64_t w = ((s >> ((s >> 59u) + 5u)) ^ s) * 12605985483714917081ULL;
+  w = (w >> 43u) ^ w;
+  return (double)(w >> 11) * 0x1.0p-53;
+}
+
+uint64_t oracle_future_seed(uint64_t n, uint64_t seed)
+{
+  uint64_t g = PRN_MULT, c = PRN_ADD, G = 1, C = 0;
+  while (n > 0) {
+    if (n & 1ULL) {
+      G = G * g;
+      C = C * g + c;
+    }
+    c = (g + 1ULL) * c;
+    g = g * g;
+    n >>= 1;
+  }
+  return G * seed + C;
+}
+
+uint64_t oracle_init_seed(int64_t id, uint64_t master, int stream)
+{
+  return oracle_future_seed((uint64_t)id * PRN_STRIDE, master + (uint64_t)stream);
+}
+
+/* ------------------------------------------------------------------ */
+/* Natural log from the series ln(m) = 2 atanh((m-1)/(m+1)), m in
+ * [sqrt(1/2), sqrt(2)), eleven odd terms, plus e*ln2 split hi/lo.      */
+double oracle_log(double x)
+{
+  if (!(x > 0.0)) {
+    if (x == 0.0) return -INFINITY;
+    return NAN;
+  }
+  if (x == INFINITY) return x;
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  int e = (int)((b >> 52) & 0x7ffULL);
+  if (e == 0) {
+    double y = x * 18014398509481984.0; /* 2^54 */
+    memcpy(&b, &y, 8);
+    e = (int)((b >> 52) & 0x7ffULL) - 54;
+  }
+  e -= 1023;
+  b = (b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+  double m;
+  memcpy(&m, &b, 8);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
+  }
+  double f = (m - 1.0) / (m + 1.0);
+  double s = f * f;
+  double p = 0.043478260869565216;     /* 1/23 */
+  p = 0.047619047619047616 + s * p;    /* 1/21 */
+  p = 0.05263157894736842 + s * p;     /* 1/19 */
+  p = 0.058823529411764705 + s * p;    /* 1/17 */
+  p = 0.06666666666666667 + s * p;     /* 1/15 */
+  p = 0.07692307692307693 + s * p;     /* 1/13 */
+  p = 0.09090909090909091 + s * p;     /* 1/11 */
+  p = 0.1111111111111111 + s * p;      /* 1/9 */
+  p = 0.14285714285714285 + s * p;     /* 1/7 */
+  p = 0.2 + s * p;                     /* 1/5 */
+  p = 0.3333333333333333 + s * p;      /* 1/3 */
+  p = s * p;
+  double t = 2.0 * f;
+  double r = t + t * p;
+  double de = (double)e;
+  return de * 0.6931471803691238 + (r + de * 1.9082149292705877e-10);
+}
+
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int64_t n_pts;
+  double* E;
+  double* st;
+  double* ss;
+  double awr;
+  int32_t* hidx; /* n_bins+1 */
+} nuclide_t;
+
+typedef struct {
+  int32_t id;
+  int32_t n;
+  int32_t* nuc;
+  double* dens;
+} material_t;
+
+struct oracle_problem {
+  char err[512];
+  /* mesh */
+  int64_t n_vtx, n_tet;
+  double* xyz;
+  int32_t* tv;
+  int32_t* blk;
+  int32_t* side_bid; /* 4 per tet, boundary id (>=0) for boundary sides */
+  int32_t* nbr;      /* 4 per tet, -1 boundary */
+  double* planes;    /* 16 per tet: (nx,ny,nz,d) per side */
+  int32_t* tmat;     /* material index per tet (-1 none) */
+  /* locator */
+  double glo[3], gh[3];
+  int gn[3];
+  int64_t* gstart;
+  int32_t* gtets;
+  /* bcs */
+  int32_t bc_type[1024];
+  /* data */
+  int32_t n_nuc, cap_nuc;
+  nuclide_t* nucs;
+  int32_t n_mat, cap_mat;
+  material_t* mats;
+  int32_t n_map;
+  int32_t* map_blocks;
+  int32_t* map_mats;
+  int32_t n_bins;
+  double E_lo, E_hi, lE_lo, du;
+  int data_ready;
+  oracle_source src;
+  double* src_cyl;
+};
+
+static int fail(oracle_problem* p, const char* msg)
+{
+  snprintf(p->err, sizeof p->err, "%s", msg);
+  return 1;
+}
+
+oracle_problem* oracle_create(void)
+{
+  oracle_problem* p = (oracle_problem*)calloc(1, sizeof(oracle_problem));
+  p->n_bins = 8000;
+  p->src.space = 0;
+  p->src.energy = 0;
+  p->src.watt_a = 0.988e6;
+  p->src.watt_b = 2.249e-6;
+  return p;
+}
+
+static void free_mesh(oracle_problem* p)
+{
+  free(p->xyz); free(p->tv); free(p->blk); free(p->side_bid); free(p->nbr);
+  free(p->planes); free(p->tmat); free(p->gstart); free(p->gtets);
+  p->xyz = NULL; p->tv = NULL; p->blk = NULL; p->side_bid = NULL; p->nbr = NULL;
+  p->planes = NULL; p->tmat = NULL; p->gstart = NULL; p->gtets = NULL;
+}
+
+void oracle_destroy(oracle_problem* p)
+{
+  if (!p) return;
+  free_mesh(p);
+  for (int i = 0; i < p->n_nuc; ++i) {
+    free(p->nucs[i].E); free(p->nucs[i].st); free(p->nucs[i].ss); free(p->nucs[i].hidx);
+  }
+  free(p->nucs);
+  for (int i = 0; i < p->n_mat; ++i) { free(p->mats[i].nuc); free(p->mats[i].dens); }
+  free(p->mats);
+  free(p->map_blocks); free(p->map_mats); free(p->src_cyl);
+  free(p);
+}
+
+const char* oracle_error(oracle_problem* p) { return p->err; }
+
+/* ------------------------------------------------------------------ */
+/* Mesh preprocessing: face adjacency by sorted vertex triples, one
+ * canonical plane per distinct face (vertices in increasing global id),
+ * oriented outward per tet so the two sides of an interior face carry
+ * exactly negated planes.  Side f is opposite local vertex f.            */
+typedef struct { int32_t a, b, c; int64_t side; } facekey;
+
+static int cmp_face(const void* x, const void* y)
+{
+  const facekey* p = (const facekey*)x;
+  const facekey* q = (const facekey*)y;
+  if (p->a != q->a) return p->a < q->a ? -1 : 1;
+  if (p->b != q->b) return p->b < q->b ? -1 : 1;
+  if (p->c != q->c) return p->c < q->c ? -1 : 1;
+  return p->side < q->side ? -1 : (p->side > q->side ? 1 : 0);
+}
+
+static const int FACE_VTX[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+
+static void sort3(int32_t* v)
+{
+  int32_t t;
+  if (v[0] > v[1]) { t = v[0]; v[0] = v[1]; v[1] = t; }
+  if (v[1] > v[2]) { t = v[1]; v[1] = v[2]; v[2] = t; }
+  if (v[0] > v[1]) { t = v[0]; v[0] = v[1]; v[1] = t; }
+}
+
+static int build_planes(oracle_problem* p)
+{
+  for (int64_t t = 0; t < p->n_tet; ++t) {
+    for (int f = 0; f < 4; ++f) {
+      int32_t v[3] = {p->tv[4 * t + FACE_VTX[f][0]], p->tv[4 * t + FACE_VTX[f][1]],
+                      p->tv[4 * t + FACE_VTX[f][2]]};
+      sort3(v);
+      const double* A = p->xyz + 3 * (int64_t)v[0];
+      const double* B = p->xyz + 3 * (int64_t)v[1];
+      const double* C = p->xyz + 3 * (int64_t)v[2];
+      const double* O = p->xyz + 3 * (int64_t)p->tv[4 * t + f];
+      double e1x = B[0] - A[0], e1y = B[1] - A[1], e1z = B[2] - A[2];
+      double e2x = C[0] - A[0], e2y = C[1] - A[1], e2z = C[2] - A[2];
+      double nx = e1y * e2z - e1z * e2y;
+      double ny = e1z * e2x - e1x * e2z;
+      double nz = e1x * e2y - e1y * e2x;
+      double len = sqrt(nx * nx + ny * ny + nz * nz);
+      if (!(len > 0.0)) return fail(p, "degenerate tet face");
+      nx = nx / len;
+      ny = ny / len;
+      nz = nz / len;
+      double d = nx * A[0] + ny * A[1] + nz * A[2];
+      double s = nx * O[0] + ny * O[1] + nz * O[2] - d;
+      if (s == 0.0) return fail(p, "degenerate tet (zero volume)");
+      if (s > 0.0) { nx = -nx; ny = -ny; nz = -nz; d = -d; }
+      double* P = p->planes + 16 * t + 4 * f;
+      P[0] = nx; P[1] = ny; P[2] = nz; P[3] = d;
+    }
+  }
+  return 0;
+}
+
+static int build_adjacency(oracle_problem* p)
+{
+  int64_t nf = 4 * p->n_tet;
+  facekey* keys = (facekey*)malloc(sizeof(facekey) * (size_t)nf);
+  if (!keys) return fail(p, "out of memory");
+  for (int64_t t = 0; t < p->n_tet; ++t)
+    for (int f = 0; f < 4; ++f) {
+      int32_t v[3] = {p->tv[4 * t + FACE_VTX[f][0]], p->tv[4 * t + FACE_VTX[f][1]],
+                      p->tv[4 * t + FACE_VTX[f][2]]};
+      sort3(v);
+      facekey* k = keys + 4 * t + f;
+      k->a = v[0]; k->b = v[1]; k->c = v[2]; k->side = 4 * t + f;
+    }
+  qsort(keys, (size_t)nf, sizeof(facekey), cmp_face);
+  for (int64_t i = 0; i < nf; ++i) p->nbr[i] = -1;
+  int64_t i = 0;
+  while (i < nf) {
+    int64_t j = i + 1;
+    while (j < nf && keys[j].a == keys[i].a && keys[j].b == keys[i].b && keys[j].c == keys[i].c) ++j;
+    if (j - i > 2) { free(keys); return fail(p, "non-manifold face shared by more than two tets"); }
+    if (j - i == 2) {
+      p->nbr[keys[i].side] = (int32_t)(keys[i + 1].side / 4);
+      p->nbr[keys[i + 1].side] = (int32_t)(keys[i].side / 4);
+    }
+    i = j;
+  }
+  free(keys);
+  return 0;
+}
+
+static int build_locator(oracle_problem* p)
+{
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t v = 0; v < p->n_vtx; ++v)
+    for (int k = 0; k < 3; ++k) {
+      double c = p->xyz[3 * v + k];
+      if (c < lo[k]) lo[k] = c;
+      if (c > hi[k]) hi[k] = c;
+    }
+  double ext[3], vol = 1.0;
+  for (int k = 0; k < 3; ++k) {
+    ext[k] = hi[k] - lo[k];
+    if (!(ext[k] > 0.0)) ext[k] = 1.0;
+    vol *= ext[k];
+  }
+  double target = (double)p->n_tet / 2.0;
+  if (target < 1.0) target = 1.0;
+  double h = cbrt(vol / target);
+  int64_t ncell = 1;
+  for (int k = 0; k < 3; ++k) {
+    int n = (int)(ext[k] / h);
+    if (n < 1) n = 1;
+    if (n > 1024) n = 1024;
+    p->gn[k] = n;
+    p->glo[k] = lo[k];
+    p->gh[k] = ext[k] / n;
+    ncell *= n;
+  }
+  int64_t* cnt = (int64_t*)calloc((size_t)ncell + 1, sizeof(int64_t));
+  const double tol = 1e-9;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) {
+      int64_t acc = 0;
+      for (int64_t c = 0; c < ncell; ++c) { int64_t n = cnt[c]; cnt[c] = acc; acc += n; }
+      cnt[ncell] = acc;
+      p->gstart = (int64_t*)malloc(sizeof(int64_t) * (size_t)(ncell + 1));
+      memcpy(p->gstart, cnt, sizeof(int64_t) * (size_t)(ncell + 1));
+      p->gtets = (int32_t*)malloc(sizeof(int32_t) * (size_t)(acc > 0 ? acc : 1));
+    }
+    for (int64_t t = 0; t < p->n_tet; ++t) {
+      double blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (int a = 0; a < 4; ++a)
+        for (int k = 0; k < 3; ++k) {
+          double c = p->xyz[3 * (int64_t)p->tv[4 * t + a] + k];
+          if (c < blo[k]) blo[k] = c;
+          if (c > bhi[k]) bhi[k] = c;
+        }
+      int i0[3], i1[3];
+      for (int k = 0; k < 3; ++k) {
+        int a = (int)floor((blo[k] - tol - p->glo[k]) / p->gh[k]);
+        int b = (int)floor((bhi[k] + tol - p->glo[k]) / p->gh[k]);
+        if (a < 0) a = 0;
+        if (b > p->gn[k] - 1) b = p->gn[k] - 1;
+        i0[k] = a; i1[k] = b;
+      }
+      for (int z = i0[2]; z <= i1[2]; ++z)
+        for (int y = i0[1]; y <= i1[1]; ++y)
+          for (int x = i0[0]; x <= i1[0]; ++x) {
+            int64_t c = ((int64_t)z * p->gn[1] + y) * p->gn[0] + x;
+            if (pass == 0) cnt[c]++;
+            else p->gtets[cnt[c]++] = (int32_t)t;
+          }
+    }
+  }
+  free(cnt);
+  return 0;
+}
+
+int oracle_set_mesh(oracle_problem* p, int64_t n_vtx, const double* xyz, int64_t n_tet,
+                    const int32_t* tet_vtx, const int32_t* tet_block, const int32_t* tet_side_bid)
+{
+  free_mesh(p);
+  if (n_vtx < 4 || n_tet < 1) return fail(p, "empty mesh");
+  p->n_vtx = n_vtx;
+  p->n_tet = n_tet;
+  p->xyz = (double*)malloc(sizeof(double) * 3 * (size_t)n_vtx);
+  memcpy(p->xyz, xyz, sizeof(double) * 3 * (size_t)n_vtx);
+  p->tv = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)n_tet);
+  memcpy(p->tv, tet_vtx, sizeof(int32_t) * 4 * (size_t)n_tet);
+  for (int64_t i = 0; i < 4 * n_tet; ++i)
+    if (p->tv[i] < 0 || p->tv[i] >= n_vtx) return fail(p, "tet vertex index out of range");
+  p->blk = (int32_t*)malloc(sizeof(int32_t) * (size_t)n_tet);
+  memcpy(p->blk, tet_block, sizeof(int32_t) * (size_t)n_tet);
+  p->side_bid = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)n_tet);
+  for (int64_t i = 0; i < 4 * n_tet; ++i) p->side_bid[i] = tet_side_bid ? tet_side_bid[i] : -1;
+  p->nbr = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)n_tet);
+  p->planes = (double*)malloc(sizeof(double) * 16 * (size_t)n_tet);
+  p->tmat = (int32_t*)malloc(sizeof(int32_t) * (size_t)n_tet);
+  if (build_adjacency(p)) return 1;
+  if (build_planes(p)) return 1;
+  if (build_locator(p)) return 1;
+  return 0;
+}
+
+int oracle_set_bc(oracle_problem* p, int32_t bid, int32_t type)
+{
+  if (bid < 0 || bid >= 1024) return fail(p, "boundary id out of range [0,1024)");
+  if (type != 0 && type != 1) return fail(p, "bc type must be 0 (vacuum) or 1 (reflect)");
+  p->bc_type[bid] = type;
+  return 0;
+}
+
+int oracle_add_nuclide(oracle_problem* p, int64_t n_pts, const double* E, const double* sig_t,
+                       const double* sig_s, double awr)
+{
+  if (n_pts < 2) return fail(p, "nuclide grid needs at least 2 points");
+  for (int64_t i = 0; i + 1 < n_pts; ++i)
+    if (!(E[i] < E[i + 1])) return fail(p, "nuclide energy grid must be strictly increasing");
+  if (!(E[0] > 0.0)) return fail(p, "nuclide energies must be positive");
+  if (p->n_nuc == p->cap_nuc) {
+    p->cap_nuc = p->cap_nuc ? 2 * p->cap_nuc : 16;
+    p->nucs = (nuclide_t*)realloc(p->nucs, sizeof(nuclide_t) * (size_t)p->cap_nuc);
+  }
+  nuclide_t* n = p->nucs + p->n_nuc++;
+  n->n_pts = n_pts;
+  n->E = (double*)malloc(sizeof(double) * (size_t)n_pts);
+  n->st = (double*)malloc(sizeof(double) * (size_t)n_pts);
+  n->ss = (double*)malloc(sizeof(double) * (size_t)n_pts);
+  memcpy(n->E, E, sizeof(double) * (size_t)n_pts);
+  memcpy(n->st, sig_t, sizeof(double) * (size_t)n_pts);
+  memcpy(n->ss, sig_s, sizeof(double) * (size_t)n_pts);
+  n->awr = awr;
+  n->hidx = NULL;
+  p->data_ready = 0;
+  return 0;
+}
+
+int oracle_add_material(oracle_problem* p, int32_t material_id, int32_t n, const int32_t* nuclides,
+                        const double* densities)
+{
+  if (n < 1) return fail(p, "material needs at least one nuclide");
+  for (int i = 0; i < n; ++i)
+    if (nuclides[i] < 0 || nuclides[i] >= p->n_nuc) return fail(p, "material nuclide index out of range");
+  if (p->n_mat == p->cap_mat) {
+    p->cap_mat = p->cap_mat ? 2 * p->cap_mat : 16;
+    p->mats = (material_t*)realloc(p->mats, sizeof(material_t) * (size_t)p->cap_mat);
+  }
+  material_t* m = p->mats + p->n_mat++;
+  m->id = material_id;
+  m->n = n;
+  m->nuc = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  m->dens = (double*)malloc(sizeof(double) * (size_t)n);
+  memcpy(m->nuc, nuclides, sizeof(int32_t) * (size_t)n);
+  memcpy(m->dens, densities, sizeof(double) * (size_t)n);
+  return 0;
+}
+
+int oracle_block_map(oracle_problem* p, int32_t n, const int32_t* blocks, const int32_t* materials)
+{
+  free(p->map_blocks); free(p->map_mats);
+  p->n_map = n;
+  p->map_blocks = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+  p->map_mats = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+  memcpy(p->map_blocks, blocks, sizeof(int32_t) * (size_t)n);
+  memcpy(p->map_mats, materials, sizeof(int32_t) * (size_t)n);
+  return 0;
+}
+
+int oracle_set_source(oracle_problem* p, const oracle_source* s)
+{
+  p->src = *s;
+  free(p->src_cyl);
+  p->src_cyl = NULL;
+  if (s->space == 2) {
+    if (s->n_cyl < 1) return fail(p, "cylinder source needs at least one cylinder");
+    p->src_cyl = (double*)malloc(sizeof(double) * 2 * (size_t)s->n_cyl);
+    memcpy(p->src_cyl, s->cyl_xy, sizeof(double) * 2 * (size_t)s->n_cyl);
+  }
+  p->src.cyl_xy = p->src_cyl;
+  return 0;
+}
+
+int oracle_set_hash_bins(oracle_problem* p, int32_t n_bins)
+{
+  if (n_bins < 1) return fail(p, "hash bins must be >= 1");
+  p->n_bins = n_bins;
+  p->data_ready = 0;
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Energy-grid search: logarithmic hash bins over the common energy range
+ * (F. B. Brown, "New hash-based energy lookup algorithm for Monte Carlo
+ * codes", 2014; OpenMC's log grid), then bisection inside the bin.      */
+static int bucket_of(const oracle_problem* p, double lE)
+{
+  double q = (lE - p->lE_lo) / p->du;
+  if (!(q >= 0.0)) return 0;
+  if (q >= (double)p->n_bins) return p->n_bins - 1;
+  int k = (int)q;
+  if (k > p->n_bins - 1) k = p->n_bins - 1;
+  return k;
+}
+
+static int prepare_data(oracle_problem* p)
+{
+  if (p->data_ready) return 0;
+  if (p->n_nuc < 1) return fail(p, "no nuclides");
+  double lo = -INFINITY, hi = INFINITY;
+  for (int i = 0; i < p->n_nuc; ++i) {
+    if (p->nucs[i].E[0] > lo) lo = p->nucs[i].E[0];
+    if (p->nucs[i].E[p->nucs[i].n_pts - 1] < hi) hi = p->nucs[i].E[p->nucs[i].n_pts - 1];
+  }
+  if (!(hi > lo)) return fail(p, "nuclide energy ranges do not overlap");
+  p->E_lo = lo;
+  p->E_hi = hi;
+  p->lE_lo = oracle_log(lo);
+  p->du = (oracle_log(hi) - p->lE_lo) / (double)p->n_bins;
+  for (int i = 0; i < p->n_nuc; ++i) {
+    nuclide_t* n = p->nucs + i;
+    free(n->hidx);
+    n->hidx = (int32_t*)malloc(sizeof(int32_t) * (size_t)(p->n_bins + 1));
+    /* hidx[k] = (number of grid points in bins < k) - 1, at least 0 */
+    int64_t j = 0;
+    for (int k = 0; k <= p->n_bins; ++k) {
+      while (j < n->n_pts && bucket_of(p, oracle_log(n->E[j])) < k) ++j;
+      int64_t v = j - 1;
+      if (v < 0) v = 0;
+      if (v > n->n_pts - 2) v = n->n_pts - 2;
+      n->hidx[k] = (int32_t)v;
+    }
+  }
+  p->data_ready = 1;
+  return 0;
+}
+
+static int grid_index(const nuclide_t* n, int k, double E)
+{
+  int lo = n->hidx[k];
+  int hi = n->hidx[k + 1] + 1;
+  int last = (int)n->n_pts - 1;
+  if (hi > last) hi = last;
+  while (lo > 0 && E < n->E[lo]) --lo;
+  while (hi < last && E >= n->E[hi]) ++hi;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (E < n->E[mid]) hi = mid;
+    else lo = mid;
+  }
+  return lo;
+}
+
+static void micro_xs(const nuclide_t* n, int k, double E, double* st, double* ss)
+{
+  int i = grid_index(n, k, E);
+  double f = (E - n->E[i]) / (n->E[i + 1] - n->E[i]);
+  *st = n->st[i] + f * (n->st[i + 1] - n->st[i]);
+  *ss = n->ss[i] + f * (n->ss[i + 1] - n->ss[i]);
+}
+
+static double macro_total(const oracle_problem* p, int mat, double E)
+{
+  const material_t* m = p->mats + mat;
+  int k = bucket_of(p, oracle_log(E));
+  double acc = 0.0;
+  for (int j = 0; j < m->n; ++j) {
+    double st, ss;
+    micro_xs(p->nucs + m->nuc[j], k, E, &st, &ss);
+    acc = acc + m->dens[j] * st;
+  }
+  return acc;
+}
+
+int oracle_xs_index(oracle_problem* p, int32_t nuclide, double E, double* f_out)
+{
+  if (prepare_data(p)) return -1;
+  const nuclide_t* n = p->nucs + nuclide;
+  int k = bucket_of(p, oracle_log(E));
+  int i = grid_index(n, k, E);
+  if (f_out) *f_out = (E - n->E[i]) / (n->E[i + 1] - n->E[i]);
+  return i;
+}
+
+int oracle_macro_xs(oracle_problem* p, int32_t material_index, double E, double* sig_t)
+{
+  if (prepare_data(p)) return 1;
+  *sig_t = macro_total(p, material_index, E);
+  return 0;
+}
+
+int oracle_mesh_info(oracle_problem* p, const int32_t** nbr, const double** planes)
+{
+  *nbr = p->nbr;
+  *planes = p->planes;
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Start-element location (stands in for MOOSE ClaimRays): among tets whose
+ * four half-spaces contain x within 1e-9, take the lowest id whose interior
+ * the direction enters (every side with |s| <= tol has n.u < 0); if none is
+ * entered, the lowest id that contains x.                                 */
+int oracle_locate(oracle_problem* p, const double* x, const double* u)
+{
+  int ci[3];
+  for (int k = 0; k < 3; ++k) {
+    double q = (x[k] - p->glo[k]) / p->gh[k];
+    int c = (int)floor(q);
+    if (!(q >= 0.0)) c = 0;
+    if (c > p->gn[k] - 1) c = p->gn[k] - 1;
+    if (c < 0) c = 0;
+    ci[k] = c;
+  }
+  int64_t cell = ((int64_t)ci[2] * p->gn[1] + ci[1]) * p->gn[0] + ci[0];
+  const double tol = 1e-9;
+  int best_in = -1, best_any = -1;
+  for (int64_t q = p->gstart[cell]; q < p->gstart[cell + 1]; ++q) {
+    int32_t t = p->gtets[q];
+    const double* P = p->planes + 16 * (int64_t)t;
+    int inside = 1, enters = 1;
+    for (int f = 0; f < 4; ++f) {
+      const double* pl = P + 4 * f;
+      double s = pl[0] * x[0] + pl[1] * x[1] + pl[2] * x[2] - pl[3];
+      if (s > tol) { inside = 0; break; }
+      if (s >= -tol) {
+        double dn = pl[0] * u[0] + pl[1] * u[1] + pl[2] * u[2];
+        if (!(dn < 0.0)) enters = 0;
+      }
+    }
+    if (!inside) continue;
+    if (enters && (best_in < 0 || t < best_in)) best_in = t;
+    if (best_any < 0 || t < best_any) best_any = t;
+  }
+  return best_in >= 0 ? best_in : best_any;
+}
+
+/* ------------------------------------------------------------------ */
+/* Sampling helpers.  No sin/cos: a uniform azimuth is drawn as a point in
+ * the unit disk and its doubled angle (von Neumann 1951), and the Maxwell
+ * cos^2 term from a point in the unit quarter disk.                       */
+static void sample_azimuth(uint64_t* s, double* c, double* sn)
+{
+  for (;;) {
+    double a = 2.0 * oracle_prn(s) - 1.0;
+    double b = 2.0 * oracle_prn(s) - 1.0;
+    double r2 = a * a + b * b;
+    if (r2 > 0.0 && r2 <= 1.0) {
+      *c = (a * a - b * b) / r2;
+      *sn = (2.0 * a * b) / r2;
+      return;
+    }
+  }
+}
+
+static double sample_cos2_quarter(uint64_t* s)
+{
+  for (;;) {
+    double a = oracle_prn(s);
+    double b = oracle_prn(s);
+    double r2 = a * a + b * b;
+    if (r2 > 0.0 && r2 <= 1.0) return (a * a) / r2;
+  }
+}
+
+/* Watt spectrum as Maxwellian plus shift (OpenMC watt_spectrum /
+ * maxwell_spectrum formulas), redrawn outside [E_lo, E_hi). */
+static double sample_watt(uint64_t* s, double a, double b, double E_lo, double E_hi)
+{
+  for (int it = 0; it < 1000; ++it) {
+    double r1 = oracle_prn(s);
+    double r2 = oracle_prn(s);
+    double c2 = sample_cos2_quarter(s);
+    double w = -a * (oracle_log(r1) + oracle_log(r2) * c2);
+    double E = w + a * a * b / 4.0 + (2.0 * oracle_prn(s) - 1.0) * sqrt(a * a * b * w);
+    if (E < E_hi && E >= E_lo) return E;
+  }
+  return E_hi * 0.5;
+}
+
+static double pos0(double a) { return a > 0.0 ? a : 0.0; }
+
+static void rotate_dir(double* u, double mu, double cphi, double sphi)
+{
+  double u0 = u[0], v0 = u[1], w0 = u[2];
+  double a = sqrt(pos0(1.0 - mu * mu));
+  double b = sqrt(pos0(1.0 - w0 * w0));
+  if (b > 1e-10) {
+    u[0] = mu * u0 + a * (u0 * w0 * cphi - v0 * sphi) / b;
+    u[1] = mu * v0 + a * (v0 * w0 * cphi + u0 * sphi) / b;
+    u[2] = mu * w0 - a * b * cphi;
+  } else {
+    b = sqrt(1.0 - v0 * v0);
+    u[0] = mu * u0 + a * (u0 * v0 * cphi + w0 * sphi) / b;
+    u[1] = mu * v0 - a * b * cphi;
+    u[2] = mu * w0 + a * (v0 * w0 * cphi - u0 * sphi) / b;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+#define ST_LEAK 1
+#define ST_ABSORB 2
+#define ST_CUTOFF 3
+#define ST_STUCK 4
+#define ST_LOST 5
+#define ST_BADXS 6
+#define MAX_SEG 10000000
+#define MAX_ZERO_RUN 10000
+
+#define FNV_OFF 14695981039346656037ULL
+#define FNV_PRIME 1099511628211ULL
+
+static int material_of_block(const oracle_problem* p, int32_t blk)
+{
+  for (int i = 0; i < p->n_map; ++i)
+    if (p->map_blocks[i] == blk) {
+      int want = p->map_mats[i];
+      for (int m = 0; m < p->n_mat; ++m)
+        if (p->mats[m].id == want) return m;
+      return -1;
+    }
+  return -1;
+}
+
+typedef struct {
+  int64_t n_seg, n_coll, n_leak, n_absorb, n_cutoff, n_stuck, n_lost, n_badxs;
+  double leak_w;
+} lstats;
+
+static void birth(const oracle_problem* p, int64_t id, uint64_t* ssrc, double* x, double* u,
+                  double* E)
+{
+  const oracle_source* S = &p->src;
+  if (S->space == 0) {
+    x[0] = S->point[0]; x[1] = S->point[1]; x[2] = S->point[2];
+  } else if (S->space == 1) {
+    for (int k = 0; k < 3; ++k) x[k] = S->box_lo[k] + oracle_prn(ssrc) * (S->box_hi[k] - S->box_lo[k]);
+  } else {
+    int c = (int)(oracle_prn(ssrc) * (double)S->n_cyl);
+    if (c > S->n_cyl - 1) c = S->n_cyl - 1;
+    double r = S->cyl_r * sqrt(oracle_prn(ssrc));
+    double ct, st;
+    sample_azimuth(ssrc, &ct, &st);
+    x[0] = S->cyl_xy[2 * c] + r * ct;
+    x[1] = S->cyl_xy[2 * c + 1] + r * st;
+    x[2] = S->cyl_z0 + oracle_prn(ssrc) * (S->cyl_z1 - S->cyl_z0);
+  }
+  double mu = 2.0 * oracle_prn(ssrc) - 1.0;
+  double cp, sp;
+  sample_azimuth(ssrc, &cp, &sp);
+  double sm = sqrt(pos0(1.0 - mu * mu));
+  u[0] = mu;
+  u[1] = sm * cp;
+  u[2] = sm * sp;
+  if (S->energy == 1) *E = S->mono_E;
+  else *E = sample_watt(ssrc, S->watt_a, S->watt_b, p->E_lo, p->E_hi);
+  (void)id;
+}
+
+static void track(const oracle_problem* p, int64_t h, uint64_t master, double* tally,
+                  oracle_trace* tr, lstats* ls)
+{
+  int64_t id = h + 1;
+  uint64_t ssrc = oracle_init_seed(id, master, 2);
+  uint64_t strk = oracle_init_seed(id, master, 0);
+  double x[3], u[3], E, wgt = 1.0;
+  birth(p, id, &ssrc, x, u, &E);
+  uint64_t hash = FNV_OFF;
+  int status = 0, n_seg = 0, n_coll = 0, face_out = -1;
+  int elem = oracle_locate(p, x, u);
+  int cur_mat = -2;
+  double sigt = 0.0;
+  int zero_run = 0;
+  if (elem < 0) status = ST_LOST;
+  while (status == 0) {
+    if (n_seg >= MAX_SEG || zero_run >= MAX_ZERO_RUN) { status = ST_STUCK; break; }
+    int mat = p->tmat[elem];
+    if (mat < 0) { status = ST_BADXS; break; }
+    if (mat != cur_mat) {
+      sigt = macro_total(p, mat, E);
+      cur_mat = mat;
+      if (!(sigt > 0.0) || sigt != sigt) { status = ST_BADXS; break; }
+    }
+    /* exit side: smallest (d - n.x)/(n.u) over sides with n.u > 0, compared
+       by cross-multiplication, ties to the lower side index */
+    const double* P = p->planes + 16 * (int64_t)elem;
+    int bf = -1;
+    double bnum = 0.0, bden = 1.0;
+    for (int f = 0; f < 4; ++f) {
+      const double* pl = P + 4 * f;
+      double den = pl[0] * u[0] + pl[1] * u[1] + pl[2] * u[2];
+      if (den > 0.0) {
+        double num = pl[3] - (pl[0] * x[0] + pl[1] * x[1] + pl[2] * x[2]);
+        if (bf < 0 || num * bden < bnum * den) { bf = f; bnum = num; bden = den; }
+      }
+    }
+    if (bf < 0) { status = ST_STUCK; break; }
+    double L = bnum / bden;
+    if (!(L > 0.0)) L = 0.0;
+    double dist = -oracle_log(oracle_prn(&strk)) / sigt;
+    double score = (L < dist) ? L : dist;
+    tally[elem] += wgt * score;
+    ++n_seg;
+    if (L == 0.0) ++zero_run; else zero_run = 0;
+    if (dist > L) {
+      hash = (hash ^ ((uint64_t)elem * 8ULL + (uint64_t)bf)) * FNV_PRIME;
+      x[0] = x[0] + L * u[0];
+      x[1] = x[1] + L * u[1];
+      x[2] = x[2] + L * u[2];
+      int32_t nb = p->nbr[4 * (int64_t)elem + bf];
+      if (nb >= 0) { elem = nb; continue; }
+      int32_t bid = p->side_bid[4 * (int64_t)elem + bf];
+      if (bid < 0) bid = 0;
+      if (bid < 1024 && p->bc_type[bid] == 1) {
+        const double* pl = P + 4 * bf;
+        double dn = u[0] * pl[0] + u[1] * pl[1] + u[2] * pl[2];
+        double t2 = 2.0 * dn;
+        u[0] = u[0] - t2 * pl[0];
+        u[1] = u[1] - t2 * pl[1];
+        u[2] = u[2] - t2 * pl[2];
+        continue;
+      }
+      status = ST_LEAK;
+      face_out = bf;
+      ls->leak_w += wgt;
+      break;
+    }
+    /* collision inside this element */
+    hash = (hash ^ ((uint64_t)elem * 8ULL + 4ULL)) * FNV_PRIME;
+    double ex = x[0] + L * u[0], ey = x[1] + L * u[1], ez = x[2] + L * u[2];
+    double back = L - dist;
+    x[0] = ex - back * u[0];
+    x[1] = ey - back * u[1];
+    x[2] = ez - back * u[2];
+    ++n_coll;
+    zero_run = 0;
+    const material_t* m = p->mats + mat;
+    int k = bucket_of(p, oracle_log(E));
+    double cutoff = oracle_prn(&strk) * sigt;
+    double acc = 0.0, st = 0.0, ss = 0.0;
+    int pick = -1;
+    for (int j = 0; j < m->n; ++j) {
+      micro_xs(p->nucs + m->nuc[j], k, E, &st, &ss);
+      acc = acc + m->dens[j] * st;
+      if (acc >= cutoff) { pick = j; break; }
+    }
+    if (pick < 0) pick = m->n - 1; /* st/ss already hold the last nuclide */
+    double sa = st - ss;
+    if (oracle_prn(&strk) * st < sa) { status = ST_ABSORB; break; }
+    double A = p->nucs[m->nuc[pick]].awr;
+    double mu_cm = 2.0 * oracle_prn(&strk) - 1.0;
+    double q = A * A + 2.0 * A * mu_cm + 1.0;
+    double Ap1 = A + 1.0;
+    double E2 = E * q / (Ap1 * Ap1);
+    double cp, sp;
+    sample_azimuth(&strk, &cp, &sp);
+    if (!(q > 0.0) || !(E2 >= p->E_lo)) { E = E2; status = ST_CUTOFF; break; }
+    double mu_lab = (1.0 + A * mu_cm) / sqrt(q);
+    if (mu_lab > 1.0) mu_lab = 1.0;
+    if (mu_lab < -1.0) mu_lab = -1.0;
+    rotate_dir(u, mu_lab, cp, sp);
+    E = E2;
+    cur_mat = -2; /* energy changed: cross sections are recomputed */
+  }
+  hash = (hash ^ (uint64_t)(16 + status)) * FNV_PRIME;
+  ls->n_seg += n_seg;
+  ls->n_coll += n_coll;
+  switch (status) {
+    case ST_LEAK: ls->n_leak++; break;
+    case ST_ABSORB: ls->n_absorb++; break;
+    case ST_CUTOFF: ls->n_cutoff++; break;
+    case ST_STUCK: ls->n_stuck++; break;
+    case ST_LOST: ls->n_lost++; break;
+    default: ls->n_badxs++; break;
+  }
+  if (tr) {
+    tr->id = id;
+    tr->hash = hash;
+    tr->status = status;
+    tr->n_seg = n_seg;
+    tr->n_coll = n_coll;
+    tr->elem = elem;
+    tr->face = face_out;
+    tr->pad = 0;
+    tr->E = E;
+    tr->x = x[0];
+    tr->y = x[1];
+    tr->z = x[2];
+  }
+}
+
+int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n_threads,
+               double* tally, oracle_trace* traces, oracle_stats* stats)
+{
+  if (!p->planes) return fail(p, "no mesh");
+  if (prepare_data(p)) return 1;
+  if (p->n_mat < 1) return fail(p, "no materials");
+  for (int64_t t = 0; t < p->n_tet; ++t) p->tmat[t] = material_of_block(p, p->blk[t]);
+  if (n_threads < 1) n_threads = 1;
+  lstats tot;
+  memset(&tot, 0, sizeof tot);
+  int nt = n_threads;
+#ifndef _OPENMP
+  nt = 1;
+#endif
+  if (nt == 1) {
+    for (int64_t i = 0; i < n; ++i) track(p, first + i, seed, tally, traces ? traces + i : NULL, &tot);
+  } else {
+#ifdef _OPENMP
+    double** priv = (double**)calloc((size_t)nt, sizeof(double*));
+    lstats* pl = (lstats*)calloc((size_t)nt, sizeof(lstats));
+#pragma omp parallel num_threads(nt)
+    {
+      int tid = omp_get_thread_num();
+      priv[tid] = (double*)calloc((size_t)p->n_tet, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+      for (int64_t i = 0; i < n; ++i)
+        track(p, first + i, seed, priv[tid], traces ? traces + i : NULL, pl + tid);
+    }
+    for (int t = 0; t < nt; ++t) {
+      if (priv[t]) {
+        for (int64_t e = 0; e < p->n_tet; ++e) tally[e] += priv[t][e];
+        free(priv[t]);
+      }
+      tot.n_seg += pl[t].n_seg; tot.n_coll += pl[t].n_coll; tot.n_leak += pl[t].n_leak;
+      tot.n_absorb += pl[t].n_absorb; tot.n_cutoff += pl[t].n_cutoff; tot.n_stuck += pl[t].n_stuck;
+      tot.n_lost += pl[t].n_lost; tot.n_badxs += pl[t].n_badxs; tot.leak_w += pl[t].leak_w;
+    }
+    free(priv);
+    free(pl);
+#endif
+  }
+  if (stats) {
+    stats->n_hist = n;
+    stats->n_seg = tot.n_seg;
+    stats->n_coll = tot.n_coll;
+    stats->n_leak = tot.n_leak;
+    stats->n_absorb = tot.n_absorb;
+    stats->n_cutoff = tot.n_cutoff;
+    stats->n_stuck = tot.n_stuck;
+    stats->n_lost = tot.n_lost;
+    stats->n_badxs = tot.n_badxs;
+    stats->leak_weight = tot.leak_w;
+  }
+  return 0;
+}
