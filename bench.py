@@ -1,0 +1,300 @@
+#!/usr/bin/env python
+"""Throughput of the particle-tracking hot path (histories/s).
+
+Workload: the 17x17 pin-lattice fixed-source problem (2,039,184 tets, three
+materials with 15/4/3 synthetic nuclides on 20,000-point grids, uniform
+source in the fuel cylinders, Watt spectrum, vacuum boundary, FP64 element
+track-length flux tally), tracked by the FP64 event-based GPU tracker in
+batches ("steps") of 1,000,000 histories with a 1,000,000-particle bank.
+
+  value  device-timed histories/s with inputs resident in HBM (source
+         sampled on the device), CUDA events on the tracker's stream
+  e2e    the same through the C ABI with host buffers: per step the
+         1,000,000 source sites are copied from pinned host memory and the
+         accumulated element tally (SUM) is copied back
+  roofline  HBM roofline of the dominant kernel (the segment walk)
+  cpu_baseline  the CPU restatement (oracle) on the host cores, bounded sample
+
+--impl reference times the reference path's CPU implementation (the oracle
+restatement; MaCaw itself needs MOOSE/OpenMC/libMesh/MPI, absent here) on
+the same workload.  Under torchrun every rank tracks its own history range
+(weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "histories/s on 1 GB300, mixed vs plain FP64 at equal tally error; p50/p99 latency"
+HIST_PER_STEP = 1_000_000
+BANK = 1_000_000
+B_SEG_FP64 = 164   # algorithmic bytes per segment: planes 128 + neighbours 16 + material 4 + tally RMW 16
+CPU_SAMPLE = 400_000
+REF_SAMPLE = 100_000
+# DRAM bytes per segment of the advance kernel from the committed ncu
+# capture (profiles/advance_fp64_lattice.md); None until captured
+ADVANCE_DRAM_BYTES_PER_SEG = None
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def workload_config():
+    return {"workload": "lattice 17x17 pins, pitch 1.26 cm, 50 cm, 2,039,184 tets, 3 materials "
+                        "(15/4/3 nuclides x 20,000 pts), cylinder source, 1e6 histories per step",
+            "tets": 2039184, "histories_per_step": HIST_PER_STEP, "bank_size": BANK,
+            "precision": "fp64", "mode": "event",
+            "l2": "inputs larger than L2 (mesh planes 261 MB, tally 16 MB vs 129 MB L2)"}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(problem, sample, seed=1):
+    from oracle.oracle import Oracle, cpu_threads
+    threads = cpu_threads()
+    o = Oracle(problem)
+    o.run(2000, first=10**9, seed=seed, threads=threads, traces=False)  # warm caches, page in
+    _, _, st, dt = o.run(sample, first=0, seed=seed, threads=threads, traces=False)
+    return {"value": sample / dt, "unit": "histories/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} histories of the same lattice workload (C oracle, OpenMP over histories)",
+            "seconds": dt, "segments_per_history": st["n_seg"] / sample}
+
+
+def run_reference(args):
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    from macaw_gb300 import problems
+    p = problems.lattice_problem()
+    from oracle.oracle import Oracle, cpu_threads
+    threads = cpu_threads()
+    o = Oracle(p)
+    n = REF_SAMPLE
+    for w in range(args.warmup):
+        o.run(n, first=w * n, seed=1, threads=threads, traces=False)
+    t0 = time.perf_counter()
+    segs = 0
+    for k in range(args.steps):
+        _, _, st, _ = o.run(n, first=(args.warmup + k) * n, seed=1, threads=threads, traces=False)
+        segs += st["n_seg"]
+    dt = time.perf_counter() - t0
+    v = n * args.steps / dt
+    cfg = workload_config()
+    cfg["histories_per_step"] = n
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "histories/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators; the reference's meshes and ENDF data are not shipped)",
+            "config": cfg, "segments_per_s": segs / dt,
+            "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
+                             "sample": f"{n} histories per step of the lattice workload; the reference "
+                                       "(MOOSE+OpenMC) cannot be built, the oracle restates its CPU path"},
+            "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="event", choices=["event", "history"])
+    ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_MODE_EVENT, MC_MODE_HISTORY, MC_TALLY_SUM, SITE_DTYPE
+
+    mode = MC_MODE_EVENT if args.mode == "event" else MC_MODE_HISTORY
+    n = args.hist
+    p = problems.lattice_problem()
+    t = Tracker(local)
+    t.load(p)
+    stream = torch.cuda.Stream()
+    t.set_stream(stream.cuda_stream)
+    # each rank owns a disjoint range of history indices
+    base = rank * (args.warmup + 2 * args.steps + 2) * n
+
+    def step(k, **kw):
+        return t.run(n, first=base + k * n, seed=1, mode=mode, bank_size=BANK, accumulate=True, **kw)
+
+    for w in range(args.warmup):
+        step(w)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # --- device-resident timing ---
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    segs = colls = launches = 0
+    ms_adv = 0.0
+    adv_launch = 0
+    for k in range(args.steps):
+        s = step(args.warmup + k, profile=True)
+        segs += s.n_seg
+        colls += s.n_coll
+        launches += s.n_launch
+        ms_adv += s.ms_advance
+        adv_launch += s.n_advance_launch
+        if s.n_stuck or s.n_lost:
+            print(f"warning: stuck={s.n_stuck} lost={s.n_lost}", file=sys.stderr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * n * args.steps / (ms / 1e3)
+
+    # --- end to end through the C ABI with host buffers ---
+    k0 = args.warmup + args.steps
+    sites = [torch.empty(n * SITE_DTYPE.itemsize, dtype=torch.uint8).pin_memory() for _ in range(args.steps)]
+    site_np = [s.numpy().view(SITE_DTYPE) for s in sites]
+    for k in range(args.steps):
+        t.sample_sites(n, first=base + (k0 + k) * n, seed=1, out=site_np[k])
+    out = torch.empty(p.n_tet, dtype=torch.float64).pin_memory()
+    out_np = out.numpy()
+    barrier()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for k in range(args.steps):
+        t.run(n, first=base + (k0 + k) * n, seed=1, mode=mode, bank_size=BANK, accumulate=True,
+              sites=site_np[k])
+        t.tally(MC_TALLY_SUM, out=out_np)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - w0
+    if dist is not None:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": world * n * args.steps / e2e_s, "unit": "histories/s",
+           "h2d_bytes_per_step": n * SITE_DTYPE.itemsize, "d2h_bytes_per_step": p.n_tet * 8}
+
+    if rank == 0:
+        peak, peak_kind = load_peaks()
+        adv_bytes = segs * B_SEG_FP64
+        achieved = adv_bytes / (ms_adv / 1e3) / 1e9 if ms_adv > 0 else None
+        roof = {"bound": "hbm", "kernel": "k_ev_advance" if mode == MC_MODE_EVENT else "k_history",
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * segs / max(adv_launch, 1))
+                if ADVANCE_DRAM_BYTES_PER_SEG else None,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "algorithmic_bytes_per_segment": B_SEG_FP64,
+                "advance_ms_per_launch": ms_adv / max(adv_launch, 1),
+                "advance_share_of_step": ms_adv / ms if ms > 0 else None}
+        line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded generators; the reference's meshes and ENDF data are not shipped)",
+                "config": dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single"),
+                "segments_per_s": world * segs / (ms / 1e3), "segments_per_history": segs / (n * args.steps),
+                "collisions_per_history": colls / (n * args.steps),
+                "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(p, CPU_SAMPLE)
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    t.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

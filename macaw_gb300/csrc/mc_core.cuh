@@ -170,7 +170,7 @@ MC_HD double fmax0(double a) { return a > 0.0 ? a : 0.0; }
 // drawn uniformly in the unit disk (von Neumann 1951); the Maxwell cos^2
 // term is the squared cosine of the angle of a point in the unit quarter disk.
 MC_HD void sample_azimuth(uint64_t& s, double& c, double& sn) {
-  for (;;) {
+  for (int it = 0; it < 10000; ++it) {
     const double a = 2.0 * prn(s) - 1.0;
     const double b = 2.0 * prn(s) - 1.0;
     const double r2 = a * a + b * b;
@@ -180,15 +180,18 @@ MC_HD void sample_azimuth(uint64_t& s, double& c, double& sn) {
       return;
     }
   }
+  c = 1.0;  // not reached in practice: acceptance is pi/4 per try
+  sn = 0.0;
 }
 
 MC_HD double sample_cos2_quarter(uint64_t& s) {
-  for (;;) {
+  for (int it = 0; it < 10000; ++it) {
     const double a = prn(s);
     const double b = prn(s);
     const double r2 = a * a + b * b;
     if (r2 > 0.0 && r2 <= 1.0) return (a * a) / r2;
   }
+  return 0.5;
 }
 
 // Watt fission spectrum as a Maxwellian plus a shift (the form OpenMC's

@@ -632,7 +632,7 @@ int oracle_locate(oracle_problem* p, const double* x, const double* u)
  * cos^2 term from a point in the unit quarter disk.                       */
 static void sample_azimuth(uint64_t* s, double* c, double* sn)
 {
-  for (;;) {
+  for (int it = 0; it < 10000; ++it) {
     double a = 2.0 * oracle_prn(s) - 1.0;
     double b = 2.0 * oracle_prn(s) - 1.0;
     double r2 = a * a + b * b;
@@ -642,16 +642,19 @@ static void sample_azimuth(uint64_t* s, double* c, double* sn)
       return;
     }
   }
+  *c = 1.0;
+  *sn = 0.0;
 }
 
 static double sample_cos2_quarter(uint64_t* s)
 {
-  for (;;) {
+  for (int it = 0; it < 10000; ++it) {
     double a = oracle_prn(s);
     double b = oracle_prn(s);
     double r2 = a * a + b * b;
     if (r2 > 0.0 && r2 <= 1.0) return (a * a) / r2;
   }
+  return 0.5;
 }
 
 /* Watt spectrum as Maxwellian plus shift (OpenMC watt_spectrum /
