@@ -80,7 +80,7 @@ struct mc_ctx {
   DevBuf d_sites;
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
-  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero;
+  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_cm, b_cs;
   DevBuf q_xs0, q_xs1, q_adv0, q_adv1, q_coll, q_free, d_ctl;
   int64_t bank_cap = 0;
 
@@ -222,9 +222,11 @@ int ensure_bank(mc_ctx* c, int64_t cap) {
   DevBuf* d8[] = {&c->b_x, &c->b_y, &c->b_z, &c->b_u, &c->b_v, &c->b_w, &c->b_E,
                   &c->b_wgt, &c->b_sigt, &c->b_seed, &c->b_hash, &c->b_id};
   for (DevBuf* b : d8) CK(b->alloc(n * 8), "allocate particle bank");
-  DevBuf* d4[] = {&c->b_elem, &c->b_mat, &c->b_nseg, &c->b_ncoll, &c->b_zero,
+  DevBuf* d4[] = {&c->b_elem, &c->b_mat, &c->b_nseg, &c->b_ncoll, &c->b_zero, &c->b_fin,
                   &c->q_xs0, &c->q_xs1, &c->q_adv0, &c->q_adv1, &c->q_coll, &c->q_free};
   for (DevBuf* b : d4) CK(b->alloc(n * 4), "allocate particle bank");
+  CK(c->b_cm.alloc(n * 16), "allocate particle bank");
+  CK(c->b_cs.alloc(n * 32), "allocate particle bank");
   CK(c->d_ctl.alloc(sizeof(EventCtl)), "allocate event control");
   c->bank_cap = cap;
   return MC_OK;
@@ -238,6 +240,7 @@ Bank dev_bank(mc_ctx* c) {
   B.seed = c->b_seed.as<uint64_t>(); B.hash = c->b_hash.as<uint64_t>(); B.id = c->b_id.as<int64_t>();
   B.elem = c->b_elem.as<int>(); B.mat = c->b_mat.as<int>(); B.n_seg = c->b_nseg.as<int>();
   B.n_coll = c->b_ncoll.as<int>(); B.zero_run = c->b_zero.as<int>();
+  B.cm = c->b_cm.as<int4>(); B.cs = c->b_cs.as<double4_32a>(); B.fin = c->b_fin.as<int>();
   B.cap = c->bank_cap;
   return B;
 }
@@ -468,6 +471,7 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.precision = d->precision;
   a.max_seg = d->max_seg_per_advance;
   a.sites = nullptr;
+  a.n_mat = (int)c->xs.mat_ids.size();
   if (d->sites && d->n_histories > 0) {
     CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)d->n_histories)), "allocate sites");
     CK(cudaMemcpyAsync(c->d_sites.p, d->sites, sizeof(mc_site) * (size_t)d->n_histories,

@@ -20,7 +20,7 @@ namespace mc {
 struct DevMesh {
   const double4_32a* __restrict__ planes;   // 4 per tet (nx, ny, nz, d), outward
   const float4* __restrict__ planes32;  // same in float
-  const int4* __restrict__ nbr;         // neighbour per side, or -1-boundary_id
+  const int4* __restrict__ nbr;         // per side: neighbour << 2 | its side, or -1-boundary_id
   const int* __restrict__ tmat;         // material index per tet (-1: none)
   const int* __restrict__ bc_type;      // per boundary id: 0 vacuum, 1 reflect
   int n_bid;
@@ -58,7 +58,34 @@ struct Particle {
   uint64_t seed, hash;
   int64_t id;
   int elem, mat, n_seg, n_coll, status, face, zero_run;
+  int fin;  // side the particle entered its element through (-1: none)
+  // Sigma_t at the current energy for up to four materials, direct-mapped
+  // by material index (slot = mat & 3); -1 marks an empty slot.  Sigma_t is
+  // a pure function of (material, E), so a cached value is bit-identical to
+  // a fresh evaluation; every energy change empties the cache.
+  int4 cm;
+  double cs0, cs1, cs2, cs3;
 };
+
+__device__ __forceinline__ void xs_cache_clear(Particle& p) { p.cm = make_int4(-1, -1, -1, -1); }
+
+__device__ __forceinline__ bool xs_cache_get(Particle& p, int mat) {
+  switch (mat & 3) {
+    case 0: if (p.cm.x == mat) { p.sigt = p.cs0; return true; } return false;
+    case 1: if (p.cm.y == mat) { p.sigt = p.cs1; return true; } return false;
+    case 2: if (p.cm.z == mat) { p.sigt = p.cs2; return true; } return false;
+    default: if (p.cm.w == mat) { p.sigt = p.cs3; return true; } return false;
+  }
+}
+
+__device__ __forceinline__ void xs_cache_put(Particle& p, int mat, double s) {
+  switch (mat & 3) {
+    case 0: p.cm.x = mat; p.cs0 = s; break;
+    case 1: p.cm.y = mat; p.cs1 = s; break;
+    case 2: p.cm.z = mat; p.cs2 = s; break;
+    default: p.cm.w = mat; p.cs3 = s; break;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Cross sections.
@@ -158,9 +185,8 @@ __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, doub
 // Source site of history index h (OpenMCStudy::defineRays with OpenMC's
 // initialize_history, OpenMCStudy.C:317-360): position, direction, energy
 // drawn from the source stream of particle id h+1.
-__device__ __forceinline__ void sample_source(const DevXS& X, const DevSource& S, int64_t h,
+__device__ __forceinline__ void sample_source(const DevXS& X, const DevSource& S, const Skip& k,
                                               uint64_t master, mc_site& o) {
-  const Skip k = skip_ahead((uint64_t)(h + 1) * kPrnStride);
   uint64_t ss = stream_seed(k, master, kStreamSource);
   if (S.space == 0) {
     o.x = S.point[0];
@@ -193,10 +219,9 @@ __device__ __forceinline__ void sample_source(const DevXS& X, const DevSource& S
 
 // A history starts at its site: tracking stream of particle id h+1, start
 // element located (stands in for MOOSE ClaimRays).
-__device__ __forceinline__ void start(const DevMesh& M, const mc_site& o, int64_t h, uint64_t master,
-                                      Particle& p) {
+__device__ __forceinline__ void start(const DevMesh& M, const mc_site& o, int64_t h, const Skip& k,
+                                      uint64_t master, Particle& p) {
   p.id = h + 1;
-  const Skip k = skip_ahead((uint64_t)p.id * kPrnStride);
   p.seed = stream_seed(k, master, kStreamTracking);
   p.x = o.x;
   p.y = o.y;
@@ -211,9 +236,11 @@ __device__ __forceinline__ void start(const DevMesh& M, const mc_site& o, int64_
   p.n_seg = 0;
   p.n_coll = 0;
   p.face = -1;
+  p.fin = -1;
   p.zero_run = 0;
   p.mat = -2;
   p.sigt = 0.0;
+  xs_cache_clear(p);
   p.elem = locate(M, p.x, p.y, p.z, p.u, p.v, p.w);
   if (p.elem < 0) p.status = kLost;
 }
@@ -263,20 +290,24 @@ __device__ __forceinline__ void collide(const DevXS& X, Particle& p) {
   rotate_dir(p.u, p.v, p.w, mu_lab, cp, sp);
   p.E = E2;
   p.mat = -2;  // energy changed: cross sections are recomputed
+  p.fin = -1;
+  xs_cache_clear(p);
 }
 
 // ---------------------------------------------------------------------------
 // One segment of the FP64 walk.  Returns 0 when the particle crossed a face
 // (or reflected) and continues, 1 when a collision was sampled inside the
 // element (position already moved to the collision point), 2 when the
-// history ended (leak, stuck, bad XS).
+// history ended (leak, stuck, bad XS), 3 when the element's material has no
+// cached cross section and kInlineXS is false (a cross-section event is due
+// before this segment).
 //
 // The distance-to-collision test first compares -logf(xi) against
 // L*Sigma_t in float with a margin that covers float rounding and logf's
 // error bound; only when that comparison is not decisive is the FP64 log
 // evaluated.  Either way the outcome and the score (L when d > L) are the
 // values the FP64 arithmetic gives.
-template <bool kCountXS>
+template <bool kInlineXS>
 __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Particle& p,
                                             double* __restrict__ tally, float& sigt32,
                                             unsigned long long& n_xs) {
@@ -285,25 +316,34 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     return 2;
   }
   const int mat = __ldg(M.tmat + p.elem);
-  if (mat < 0) {
-    p.status = kBadXS;
-    return 2;
-  }
   if (mat != p.mat) {
-    p.sigt = macro_total(X, mat, p.E);
-    p.mat = mat;
-    sigt32 = (float)p.sigt;
-    if (kCountXS) ++n_xs;
-    if (!(p.sigt > 0.0) || p.sigt != p.sigt) {
+    if (mat < 0) {
       p.status = kBadXS;
       return 2;
     }
+    if (!xs_cache_get(p, mat)) {
+      if (!kInlineXS) return 3;
+      const double s = macro_total(X, mat, p.E);
+      ++n_xs;
+      if (!(s > 0.0) || s != s) {
+        p.status = kBadXS;
+        return 2;
+      }
+      p.sigt = s;
+      xs_cache_put(p, mat, s);
+    }
+    p.mat = mat;
+    sigt32 = (float)p.sigt;
   }
   const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
   int bf = -1;
   double bnum = 0.0, bden = 1.0;
+  // The entry side is skipped: its plane is the exact negation of the exit
+  // plane of the previous element, so n.u there is negative and the full
+  // search would reject it anyway.
 #pragma unroll
   for (int f = 0; f < 4; ++f) {
+    if (f == p.fin) continue;
     const double4_32a pl = P[f];
     const double den = pl.x * p.u + pl.y * p.v + pl.z * p.w;
     if (den > 0.0) {
@@ -345,7 +385,8 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     const int4 nb4 = M.nbr[p.elem];
     const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
     if (nb >= 0) {
-      p.elem = nb;
+      p.elem = nb >> 2;
+      p.fin = nb & 3;
       return 0;
     }
     const int bid = -1 - nb;
@@ -356,6 +397,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
       p.u = p.u - t2 * pl.x;
       p.v = p.v - t2 * pl.y;
       p.w = p.w - t2 * pl.z;
+      p.fin = -1;
       return 0;
     }
     p.status = kLeaked;

@@ -56,7 +56,7 @@ std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
                               const int32_t* tet_vtx, const int32_t* tet_block,
                               const int32_t* tet_side_bid, MeshTables& M) {
   if (n_vtx < 4 || n_tet < 1) return "empty mesh";
-  if (n_tet > (int64_t)1 << 30) return "too many tets (limit 2^30)";
+  if (n_tet > (int64_t)1 << 29) return "too many tets (limit 2^29)";
   for (int64_t i = 0; i < 4 * n_tet; ++i)
     if (tet_vtx[i] < 0 || tet_vtx[i] >= n_vtx) return "tet vertex index out of range";
   M.n_vtx = n_vtx;
@@ -83,8 +83,9 @@ std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
       ++j;
     if (j - i > 2) return "non-manifold face shared by more than two tets";
     if (j - i == 2) {
-      M.nbr[keys[i].side] = (int32_t)(keys[i + 1].side / 4);
-      M.nbr[keys[i + 1].side] = (int32_t)(keys[i].side / 4);
+      // neighbour id and the index of the shared side within the neighbour
+      M.nbr[keys[i].side] = (int32_t)((keys[i + 1].side / 4) << 2 | (keys[i + 1].side % 4));
+      M.nbr[keys[i + 1].side] = (int32_t)((keys[i].side / 4) << 2 | (keys[i].side % 4));
       has_nb[keys[i].side] = has_nb[keys[i + 1].side] = 1;
     }
     i = j;
@@ -165,16 +166,37 @@ std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
     if (!(ext[k] > 0.0)) ext[k] = 1.0;
     vol *= ext[k];
   }
-  const double h = cbrt(vol / std::max(1.0, (double)n_tet / 2.0));
+  // cells sized to the mean tet bounding-box extent along each axis (so a
+  // tet overlaps a few cells whatever its aspect ratio), capped at 2^24 cells
+  double mext[3] = {0.0, 0.0, 0.0};
+  const int64_t stride_t = std::max<int64_t>(1, n_tet / 200000);
+  int64_t n_s = 0;
+  for (int64_t t = 0; t < n_tet; t += stride_t, ++n_s)
+    for (int k = 0; k < 3; ++k) {
+      double a = INFINITY, b = -INFINITY;
+      for (int v = 0; v < 4; ++v) {
+        const double c = xyz[3 * (int64_t)tet_vtx[4 * t + v] + k];
+        a = std::min(a, c);
+        b = std::max(b, c);
+      }
+      mext[k] += b - a;
+    }
   int64_t ncell = 1;
+  double cells = 1.0;
   for (int k = 0; k < 3; ++k) {
-    int n = (int)(ext[k] / h);
-    n = std::max(1, std::min(n, 1024));
+    mext[k] = std::max(mext[k] / (double)std::max<int64_t>(n_s, 1), ext[k] * 1e-6);
+    cells *= std::max(1.0, ext[k] / mext[k]);
+  }
+  const double shrink = cells > 16777216.0 ? cbrt(cells / 16777216.0) : 1.0;
+  for (int k = 0; k < 3; ++k) {
+    int n = (int)(ext[k] / (mext[k] * shrink));
+    n = std::max(1, std::min(n, 4096));
     M.gn[k] = n;
     M.glo[k] = lo[k];
     M.gh[k] = ext[k] / n;
     ncell *= n;
   }
+  (void)vol;
   std::vector<int64_t> cnt((size_t)ncell + 1, 0);
   const double tol = kLocateTol;
   auto cell_range = [&](int64_t t, int* i0, int* i1) {

@@ -14,7 +14,8 @@ struct MeshTables {
   int64_t n_vtx = 0, n_tet = 0;
   std::vector<double> planes;   // 16 per tet: (nx, ny, nz, d) per side
   std::vector<float> planes32;  // same, rounded to float
-  std::vector<int32_t> nbr;     // 4 per tet: neighbour id, or -1-boundary_id
+  std::vector<int32_t> nbr;     // 4 per tet: neighbour id << 2 | shared side in the neighbour,
+                                // or -1-boundary_id
   std::vector<int32_t> block;   // subdomain id per tet
   // uniform-grid locator: cells hold ascending ids of tets whose bounding
   // box (grown by the locate tolerance) overlaps the cell

@@ -74,20 +74,32 @@ __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCount
   }
 }
 
-// Macroscopic XS for the particle's current element; false if unusable.
-__device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, Particle& p,
-                                          LocalCounters& L) {
+// Cross-section event: Sigma_t of the current element's material (and, when
+// the problem has at most four materials, of every material, so later
+// material changes at this energy hit the cache); false if unusable.
+__device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int n_mat,
+                                          Particle& p, LocalCounters& L) {
   const int mat = __ldg(M.tmat + p.elem);
   if (mat < 0) {
     p.status = kBadXS;
     return false;
   }
-  p.sigt = macro_total(X, mat, p.E);
-  p.mat = mat;
+  const double s = macro_total(X, mat, p.E);
   L.c[kCntXS] += 1;
-  if (!(p.sigt > 0.0) || p.sigt != p.sigt) {
+  if (!(s > 0.0) || s != s) {
     p.status = kBadXS;
     return false;
+  }
+  p.sigt = s;
+  p.mat = mat;
+  xs_cache_put(p, mat, s);
+  if (n_mat <= 4) {
+    for (int m = 0; m < n_mat; ++m) {
+      if (m == mat) continue;
+      const double o = macro_total(X, m, p.E);
+      L.c[kCntXS] += 1;
+      if (o > 0.0) xs_cache_put(p, m, o);
+    }
   }
   return true;
 }
@@ -99,6 +111,10 @@ __device__ __forceinline__ void load(const Bank& B, int s, Particle& p) {
   p.seed = B.seed[s]; p.hash = B.hash[s]; p.id = B.id[s];
   p.elem = B.elem[s]; p.mat = B.mat[s]; p.n_seg = B.n_seg[s]; p.n_coll = B.n_coll[s];
   p.zero_run = B.zero_run[s];
+  p.fin = B.fin[s];
+  p.cm = B.cm[s];
+  const double4_32a c = B.cs[s];
+  p.cs0 = c.x; p.cs1 = c.y; p.cs2 = c.z; p.cs3 = c.w;
   p.status = kAlive;
   p.face = -1;
 }
@@ -110,14 +126,20 @@ __device__ __forceinline__ void store(const Bank& B, int s, const Particle& p) {
   B.seed[s] = p.seed; B.hash[s] = p.hash; B.id[s] = p.id;
   B.elem[s] = p.elem; B.mat[s] = p.mat; B.n_seg[s] = p.n_seg; B.n_coll[s] = p.n_coll;
   B.zero_run[s] = p.zero_run;
+  B.fin[s] = p.fin;
+  B.cm[s] = p.cm;
+  double4_32a c;
+  c.x = p.cs0; c.y = p.cs1; c.z = p.cs2; c.w = p.cs3;
+  B.cs[s] = c;
 }
 
 __device__ __forceinline__ void birth(const DevMesh& M, const DevXS& X, const DevSource& S,
                                       const RunArgs& a, int64_t h, Particle& p) {
   mc_site o;
+  const Skip k = skip_ahead((uint64_t)(h + 1) * kPrnStride);
   if (a.sites) o = a.sites[h - a.first];
-  else sample_source(X, S, h, a.master, o);
-  start(M, o, h, a.master, p);
+  else sample_source(X, S, k, a.master, o);
+  start(M, o, h, k, a.master, p);
 }
 
 // Append slot to a queue with one atomic per converged group of lanes.
@@ -183,16 +205,16 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int s = Q.xs[par][i];
     Particle p;
-    p.E = B.E[s];
-    p.elem = B.elem[s];
-    p.status = kAlive;
-    if (refresh_xs(M, X, p, L)) {
+    load(B, s, p);
+    if (refresh_xs(M, X, a.n_mat, p, L)) {
       B.sigt[s] = p.sigt;
       B.mat[s] = p.mat;
+      B.cm[s] = p.cm;
+      double4_32a c;
+      c.x = p.cs0; c.y = p.cs1; c.z = p.cs2; c.w = p.cs3;
+      B.cs[s] = c;
       push(Q.adv[par], &ctl->n_adv[par], s);
     } else {
-      load(B, s, p);
-      p.status = kBadXS;
       finish(p, a, L);
       push(Q.free_slots, &ctl->n_free, s);
     }
@@ -215,11 +237,6 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     int r = 0;
     int k = 0;
     for (;;) {
-      // a new material needs a cross-section event before the next segment
-      if (p.n_seg < kMaxSegments && p.zero_run < kMaxZeroRun && __ldg(M.tmat + p.elem) != p.mat) {
-        r = 3;
-        break;
-      }
       r = segment_fp64<false>(M, X, p, a.tally, sigt32, nxs);
       if (r != 0) break;
       if (a.max_seg > 0 && ++k >= a.max_seg) {
@@ -258,6 +275,7 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
     }
     B.u[s] = p.u; B.v[s] = p.v; B.w[s] = p.w;
     B.E[s] = p.E; B.seed[s] = p.seed; B.mat[s] = p.mat;
+    B.cm[s] = p.cm; B.fin[s] = p.fin;
     push(Q.xs[nxt], &ctl->n_xs[nxt], s);
   }
   flush(L, a.counters, a.leak_w);
@@ -314,7 +332,6 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
     const int s = (i < nx) ? Q.xs[par][i] : Q.adv[par][i - nx];
     Particle p;
     load(B, s, p);
-    if (i < nx) p.mat = -2;
     float sigt32 = (float)p.sigt;
     unsigned long long nxs = 0;
     while (p.status == kAlive) {
@@ -332,7 +349,7 @@ __global__ void __launch_bounds__(256) k_sample(DevXS X, DevSource S, int64_t fi
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     mc_site o;
-    sample_source(X, S, first + i, master, o);
+    sample_source(X, S, skip_ahead((uint64_t)(first + i + 1) * kPrnStride), master, o);
     out[i] = o;
   }
 }

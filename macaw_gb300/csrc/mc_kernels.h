@@ -29,7 +29,9 @@ struct Bank {
   double *x, *y, *z, *u, *v, *w, *E, *wgt, *sigt;
   uint64_t *seed, *hash;
   int64_t* id;
-  int *elem, *mat, *n_seg, *n_coll, *zero_run;
+  int *elem, *mat, *n_seg, *n_coll, *zero_run, *fin;
+  int4* cm;            // cross-section cache keys
+  double4_32a* cs;     // cross-section cache values
   int64_t cap;
 };
 
@@ -58,6 +60,7 @@ struct RunArgs {
   unsigned long long* counters;
   double* leak_w;
   const mc_site* sites;  // device copy of caller-supplied sites, or null
+  int n_mat;
   int precision;
   int max_seg;  // event mode: segments per advance launch (<= 0: until event)
 };
