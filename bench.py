@@ -173,6 +173,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="event", choices=["event", "history"])
     ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
+    ap.add_argument("--no-mixed", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -189,7 +190,8 @@ def main():
         dist.init_process_group("nccl")
 
     from macaw_gb300 import Tracker, problems
-    from macaw_gb300._lib import MC_MODE_EVENT, MC_MODE_HISTORY, MC_TALLY_SUM, SITE_DTYPE
+    from macaw_gb300._lib import (MC_MODE_EVENT, MC_MODE_HISTORY, MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM,
+                                  SITE_DTYPE)
 
     mode = MC_MODE_EVENT if args.mode == "event" else MC_MODE_HISTORY
     n = args.hist
@@ -201,8 +203,9 @@ def main():
     # each rank owns a disjoint range of history indices
     base = rank * (args.warmup + 2 * args.steps + 2) * n
 
-    def step(k, **kw):
-        return t.run(n, first=base + k * n, seed=1, mode=mode, bank_size=BANK, accumulate=True, **kw)
+    def step(k, tr=None, precision=MC_PREC_FP64, **kw):
+        return (tr or t).run(n, first=base + k * n, seed=1, mode=mode, bank_size=BANK, accumulate=True,
+                             precision=precision, **kw)
 
     for w in range(args.warmup):
         step(w)
@@ -240,6 +243,47 @@ def main():
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
     value = world * n * args.steps / (ms / 1e3)
+    sum64 = t.tally(MC_TALLY_SUM)
+
+    # --- mixed-precision form on the same histories (second context) ---
+    mixed = None
+    if not args.no_mixed:
+        tm = Tracker(local)
+        tm.load(p)
+        tm.set_stream(stream.cuda_stream)
+        for w in range(args.warmup):
+            step(w, tr=tm, precision=MC_PREC_MIXED)
+        barrier()
+        torch.cuda.synchronize()
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        msegs = mfb = mstuck = mlost = mlaunch = 0
+        for k in range(args.steps):
+            s = step(args.warmup + k, tr=tm, precision=MC_PREC_MIXED)
+            msegs += s.n_seg
+            mfb += s.n_fallback
+            mstuck += s.n_stuck
+            mlost += s.n_lost
+            mlaunch += s.n_launch
+        m1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        mms = m0.elapsed_time(m1)
+        if dist is not None:
+            tt = torch.tensor([mms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            mms = float(tt.item())
+        summ = tm.tally(MC_TALLY_SUM)
+        tm.close()
+        nz = sum64 > 0
+        rel = np.abs(summ[nz] - sum64[nz]) / sum64[nz]
+        mixed = {"value": world * n * args.steps / (mms / 1e3), "unit": "histories/s",
+                 "ms_per_step": mms / args.steps, "speedup_vs_fp64": ms / mms,
+                 "fallback_fraction": mfb / max(msegs, 1), "stuck": int(mstuck), "lost": int(mlost),
+                 "flux_rel_diff_mean": float(rel.mean()), "flux_rel_diff_max": float(rel.max()),
+                 "flux_rel_diff_note": "element SUM tallies, mixed vs FP64 (bit-exact to the oracle), same "
+                                       f"{n * (args.warmup + args.steps)} histories, elements with a score",
+                 "gpu_launches": mlaunch}
 
     # --- end to end through the C ABI with host buffers ---
     k0 = args.warmup + args.steps
@@ -287,6 +331,8 @@ def main():
                 "segments_per_s": world * segs / (ms / 1e3), "segments_per_history": segs / (n * args.steps),
                 "collisions_per_history": colls / (n * args.steps),
                 "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+        if mixed is not None:
+            line["mixed"] = mixed
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(p, CPU_SAMPLE)
         print(json.dumps(line))

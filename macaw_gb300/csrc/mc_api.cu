@@ -444,7 +444,6 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   if (d->n_histories < 0 || d->first_history < 0) return set_err(c, MC_ERR_ARG, "negative history range");
   if (d->precision != MC_PREC_FP64 && d->precision != MC_PREC_MIXED)
     return set_err(c, MC_ERR_ARG, "unknown precision form");
-  if (d->precision == MC_PREC_MIXED) return set_err(c, MC_ERR_ARG, "mixed precision form not available");
   if (d->mode != MC_MODE_HISTORY && d->mode != MC_MODE_EVENT) return set_err(c, MC_ERR_ARG, "unknown execution form");
   if (!c->have_src) return set_err(c, MC_ERR_STATE, "no source (mc_source_set)");
   cudaSetDevice(c->device);
@@ -472,6 +471,14 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.max_seg = d->max_seg_per_advance;
   a.sites = nullptr;
   a.n_mat = (int)c->xs.mat_ids.size();
+  {
+    double dg = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double e = c->mesh.bbox_hi[k] - c->mesh.bbox_lo[k];
+      dg += e * e;
+    }
+    a.tol = (float)(1e-6 * sqrt(dg));
+  }
   if (d->sites && d->n_histories > 0) {
     CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)d->n_histories)), "allocate sites");
     CK(cudaMemcpyAsync(c->d_sites.p, d->sites, sizeof(mc_site) * (size_t)d->n_histories,

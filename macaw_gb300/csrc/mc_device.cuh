@@ -415,4 +415,168 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
   return 1;
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-precision form.  Position and direction live in float registers for
+// the walk; exits are solved on the float planes; the two nearest exit
+// distances must differ by more than tol (1e-6 of the mesh bounding-box
+// diagonal) and the nearest must not lie behind the particle by more than
+// tol, otherwise the exit is re-solved on the FP64 planes with the position
+// promoted to double (a ray passing within tol of an edge or vertex, or a
+// particle that rounding left just outside its element).  Distances to
+// collision are sampled in float; scores are accumulated in FP64.
+struct Geo32 {
+  float x, y, z, u, v, w;
+};
+
+__device__ __forceinline__ void geo_load(const Particle& p, Geo32& g) {
+  g.x = (float)p.x; g.y = (float)p.y; g.z = (float)p.z;
+  g.u = (float)p.u; g.v = (float)p.v; g.w = (float)p.w;
+}
+
+__device__ __forceinline__ void geo_store(const Geo32& g, Particle& p) {
+  p.x = g.x; p.y = g.y; p.z = g.z;
+  p.u = g.u; p.v = g.v; p.w = g.w;
+}
+
+// FP64 re-solve of the exit side for a float position/direction.
+__device__ __forceinline__ int exit_fp64(const DevMesh& M, int elem, int fin, const Geo32& g,
+                                         double& L) {
+  const double x = g.x, y = g.y, z = g.z, u = g.u, v = g.v, w = g.w;
+  const double4_32a* P = M.planes + 4 * (int64_t)elem;
+  int bf = -1;
+  double bnum = 0.0, bden = 1.0;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    if (f == fin) continue;
+    const double4_32a pl = P[f];
+    const double den = pl.x * u + pl.y * v + pl.z * w;
+    if (den > 0.0) {
+      const double num = pl.w - (pl.x * x + pl.y * y + pl.z * z);
+      if (bf < 0 || num * bden < bnum * den) {
+        bf = f;
+        bnum = num;
+        bden = den;
+      }
+    }
+  }
+  if (bf >= 0) {
+    L = bnum / bden;
+    if (!(L > 0.0)) L = 0.0;
+  }
+  return bf;
+}
+
+template <bool kInlineXS>
+__device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, Particle& p,
+                                             Geo32& g, double* __restrict__ tally, float& inv_sig,
+                                             float tol, unsigned long long& n_xs,
+                                             unsigned long long& n_fb) {
+  if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
+    p.status = kStuck;
+    return 2;
+  }
+  const int mat = __ldg(M.tmat + p.elem);
+  if (mat != p.mat) {
+    if (mat < 0) {
+      p.status = kBadXS;
+      return 2;
+    }
+    if (!xs_cache_get(p, mat)) {
+      if (!kInlineXS) return 3;
+      const double s = macro_total(X, mat, p.E);
+      ++n_xs;
+      if (!(s > 0.0) || s != s) {
+        p.status = kBadXS;
+        return 2;
+      }
+      p.sigt = s;
+      xs_cache_put(p, mat, s);
+    }
+    p.mat = mat;
+    inv_sig = (float)(1.0 / p.sigt);
+  }
+  const float4* P = M.planes32 + 4 * (int64_t)p.elem;
+  int bf = -1;
+  float t1 = 3.0e38f, t2 = 3.0e38f;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    if (f == p.fin) continue;
+    const float4 pl = __ldg(P + f);
+    const float den = fmaf(pl.x, g.u, fmaf(pl.y, g.v, pl.z * g.w));
+    if (den > 0.0f) {
+      const float num = pl.w - fmaf(pl.x, g.x, fmaf(pl.y, g.y, pl.z * g.z));
+      const float t = __fdividef(num, den);
+      if (t < t1) {
+        t2 = t1;
+        t1 = t;
+        bf = f;
+      } else if (t < t2) {
+        t2 = t;
+      }
+    }
+  }
+  float L;
+  if (bf < 0 || t2 - t1 <= tol || t1 < -tol) {
+    ++n_fb;
+    double Ld = 0.0;
+    bf = exit_fp64(M, p.elem, p.fin, g, Ld);
+    if (bf < 0) {
+      p.status = kStuck;
+      return 2;
+    }
+    L = (float)Ld;
+  } else {
+    L = fmaxf(t1, 0.0f);
+  }
+  // 32 high bits of the PCG output as the uniform deviate
+  p.seed = kPrnMult * p.seed + kPrnAdd;
+  uint64_t wv = ((p.seed >> ((p.seed >> 59u) + 5u)) ^ p.seed) * 12605985483714917081ULL;
+  wv = (wv >> 43u) ^ wv;
+  const float xi = (float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f;
+  const float dist = -__logf(xi) * inv_sig;
+  const bool cross = dist > L;
+  const float score = cross ? L : dist;
+  atomicAdd(tally + p.elem, p.wgt * (double)score);
+  ++p.n_seg;
+  if (L == 0.0f) ++p.zero_run;
+  else p.zero_run = 0;
+  if (cross) {
+    p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
+    g.x = fmaf(L, g.u, g.x);
+    g.y = fmaf(L, g.v, g.y);
+    g.z = fmaf(L, g.w, g.z);
+    const int4 nb4 = __ldg(M.nbr + p.elem);
+    const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+    if (nb >= 0) {
+      p.elem = nb >> 2;
+      p.fin = nb & 3;
+      return 0;
+    }
+    const int bid = -1 - nb;
+    if (bid < M.n_bid && M.bc_type[bid] == 1) {
+      const float4 pl = __ldg(P + bf);
+      const float t2r = 2.0f * fmaf(g.u, pl.x, fmaf(g.v, pl.y, g.w * pl.z));
+      g.u = fmaf(-t2r, pl.x, g.u);
+      g.v = fmaf(-t2r, pl.y, g.v);
+      g.w = fmaf(-t2r, pl.z, g.w);
+      const float nrm = rsqrtf(fmaf(g.u, g.u, fmaf(g.v, g.v, g.w * g.w)));
+      g.u *= nrm;
+      g.v *= nrm;
+      g.w *= nrm;
+      p.fin = -1;
+      return 0;
+    }
+    p.status = kLeaked;
+    p.face = bf;
+    return 2;
+  }
+  p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
+  g.x = fmaf(dist, g.u, g.x);
+  g.y = fmaf(dist, g.v, g.y);
+  g.z = fmaf(dist, g.w, g.z);
+  ++p.n_coll;
+  p.zero_run = 0;
+  return 1;
+}
+
 }  // namespace mc

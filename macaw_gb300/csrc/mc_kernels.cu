@@ -153,6 +153,7 @@ __device__ __forceinline__ void push(int* q, int* cnt, int slot) {
 
 // ---------------------------------------------------------------------------
 // History form.
+template <int kPrec>
 __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S, RunArgs a) {
   LocalCounters L;
   L.zero();
@@ -160,13 +161,29 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
     Particle p;
     birth(M, X, S, a, a.first + i, p);
-    float sigt32 = 0.0f;
-    unsigned long long nxs = 0;
-    while (p.status == kAlive) {
-      const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
-      if (r == 1) collide(X, p);
+    unsigned long long nxs = 0, nfb = 0;
+    if (kPrec == MC_PREC_FP64) {
+      float sigt32 = 0.0f;
+      while (p.status == kAlive) {
+        const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
+        if (r == 1) collide(X, p);
+      }
+    } else {
+      Geo32 g;
+      geo_load(p, g);
+      float inv_sig = 0.0f;
+      while (p.status == kAlive) {
+        const int r = segment_mixed<true>(M, X, p, g, a.tally, inv_sig, a.tol, nxs, nfb);
+        if (r == 1) {
+          geo_store(g, p);
+          collide(X, p);
+          geo_load(p, g);
+        }
+      }
+      geo_store(g, p);
     }
     L.c[kCntXS] += nxs;
+    L.c[kCntFallback] += nfb;
     finish(p, a, L);
   }
   flush(L, a.counters, a.leak_w);
@@ -222,38 +239,70 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
   flush(L, a.counters, a.leak_w);
 }
 
+// Take the next advance-queue entry (one atomic per converged lane group).
+__device__ __forceinline__ int take(int* head) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(head, (int)g.size());
+  return g.shfl(base, 0) + (int)g.thread_rank();
+}
+
+// Segment walk.  A lane whose particle reaches an event (collision, XS
+// miss, end of history, segment budget) hands it on and immediately takes
+// the next queued particle, so warps stay full until the queue drains
+// instead of waiting for their longest walk.
+template <int kPrec>
 __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                     EventQueues Q, EventCtl* ctl, int par) {
   LocalCounters L;
   L.zero();
   const int n = *(volatile int*)&ctl->n_adv[par];
   const int nxt = par ^ 1;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int s = Q.adv[par][i];
-    Particle p;
-    load(B, s, p);
-    float sigt32 = (float)p.sigt;
-    unsigned long long nxs = 0;
-    int r = 0;
-    int k = 0;
-    for (;;) {
-      r = segment_fp64<false>(M, X, p, a.tally, sigt32, nxs);
-      if (r != 0) break;
-      if (a.max_seg > 0 && ++k >= a.max_seg) {
-        r = 4;
-        break;
-      }
+  const int* q = Q.adv[par];
+  Particle p;
+  Geo32 g;
+  float f32 = 0.0f;  // FP64: float Sigma_t; mixed: float 1/Sigma_t
+  int s = -1, k = 0;
+  unsigned long long nxs = 0, nfb = 0;
+  {
+    const int i = take(&ctl->adv_head);
+    if (i < n) {
+      s = q[i];
+      load(B, s, p);
+      if (kPrec == MC_PREC_FP64) f32 = (float)p.sigt;
+      else { geo_load(p, g); f32 = (float)(1.0 / p.sigt); }
     }
+  }
+  while (__any_sync(0xffffffffu, s >= 0)) {
+    if (s < 0) continue;
+    int r;
+    if (kPrec == MC_PREC_FP64) r = segment_fp64<false>(M, X, p, a.tally, f32, nxs);
+    else r = segment_mixed<false>(M, X, p, g, a.tally, f32, a.tol, nxs, nfb);
+    if (r == 0) {
+      if (a.max_seg <= 0 || ++k < a.max_seg) continue;
+      r = 4;
+    }
+    if (kPrec != MC_PREC_FP64) geo_store(g, p);
     if (r == 2) {
       finish(p, a, L);
       push(Q.free_slots, &ctl->n_free, s);
-      continue;
+    } else {
+      store(B, s, p);
+      if (r == 1) push(Q.coll, &ctl->n_coll, s);
+      else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+      else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
     }
-    store(B, s, p);
-    if (r == 1) push(Q.coll, &ctl->n_coll, s);
-    else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
-    else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
+    k = 0;
+    s = -1;
+    const int i = take(&ctl->adv_head);
+    if (i < n) {
+      s = q[i];
+      load(B, s, p);
+      if (kPrec == MC_PREC_FP64) f32 = (float)p.sigt;
+      else { geo_load(p, g); f32 = (float)(1.0 / p.sigt); }
+    }
   }
+  L.c[kCntFallback] += nfb;
   flush(L, a.counters, a.leak_w);
 }
 
@@ -317,11 +366,13 @@ __global__ void k_ev_reset(EventCtl* ctl, int par, int64_t n) {
     ctl->n_xs[par] = 0;
     ctl->n_adv[par] = 0;
     ctl->n_coll = 0;
+    ctl->adv_head = 0;
   }
 }
 
 // Tail of a batch: every particle still queued runs to completion in one
 // launch, one thread per particle, with cross sections and collisions inline.
+template <int kPrec>
 __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                    EventQueues Q, EventCtl* ctl, int par) {
   LocalCounters L;
@@ -332,13 +383,29 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
     const int s = (i < nx) ? Q.xs[par][i] : Q.adv[par][i - nx];
     Particle p;
     load(B, s, p);
-    float sigt32 = (float)p.sigt;
-    unsigned long long nxs = 0;
-    while (p.status == kAlive) {
-      const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
-      if (r == 1) collide(X, p);
+    unsigned long long nxs = 0, nfb = 0;
+    if (kPrec == MC_PREC_FP64) {
+      float sigt32 = (float)p.sigt;
+      while (p.status == kAlive) {
+        const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
+        if (r == 1) collide(X, p);
+      }
+    } else {
+      Geo32 g;
+      geo_load(p, g);
+      float inv_sig = (p.mat >= 0) ? (float)(1.0 / p.sigt) : 0.0f;
+      while (p.status == kAlive) {
+        const int r = segment_mixed<true>(M, X, p, g, a.tally, inv_sig, a.tol, nxs, nfb);
+        if (r == 1) {
+          geo_store(g, p);
+          collide(X, p);
+          geo_load(p, g);
+        }
+      }
+      geo_store(g, p);
     }
     L.c[kCntXS] += nxs;
+    L.c[kCntFallback] += nfb;
     finish(p, a, L);
   }
   flush(L, a.counters, a.leak_w);
@@ -369,7 +436,8 @@ __global__ void k_accumulate(double* __restrict__ batch, double* __restrict__ su
 
 cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
                            int block, int grid, cudaStream_t st) {
-  k_history<<<grid, block, 0, st>>>(M, X, S, a);
+  if (a.precision == MC_PREC_MIXED) k_history<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, S, a);
+  else k_history<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, S, a);
   return cudaGetLastError();
 }
 
@@ -388,7 +456,8 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
                                    int* n_launch, cudaEvent_t adv0, cudaEvent_t adv1) {
   k_ev_xs<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   if (adv0) cudaEventRecord(adv0, st);
-  k_ev_advance<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.precision == MC_PREC_MIXED) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  else k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   if (adv1) cudaEventRecord(adv1, st);
   k_ev_collide<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   k_ev_refill<<<grid, block, 0, st>>>(M, X, S, a, B, Q, ctl, par);
@@ -401,7 +470,8 @@ cudaError_t launch_event_finish(const DevMesh& M, const DevXS& X, const DevSourc
                                 const RunArgs& a, const Bank& B, const EventQueues& Q,
                                 EventCtl* ctl, int par, int block, int grid, cudaStream_t st) {
   (void)S;
-  k_ev_finish<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.precision == MC_PREC_MIXED) k_ev_finish<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  else k_ev_finish<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   return cudaGetLastError();
 }
 

@@ -39,10 +39,10 @@ struct Bank {
 struct EventCtl {
   int n_xs[2], n_adv[2], n_coll;   // queue lengths, double-buffered by iteration parity
   int n_free;                       // slots freed this iteration
-  int alive;                        // particles in flight
+  int adv_head;                     // advance queue entries taken so far this iteration
   int pad;
   long long next_hist;              // next history (relative to the batch) to be born
-  long long leak_w_bits;            // unused
+  long long pad2;
 };
 
 struct EventQueues {
@@ -62,6 +62,7 @@ struct RunArgs {
   const mc_site* sites;  // device copy of caller-supplied sites, or null
   int n_mat;
   int precision;
+  float tol;    // mixed form: exit ambiguity tolerance (cm)
   int max_seg;  // event mode: segments per advance launch (<= 0: until event)
 };
 
