@@ -56,7 +56,7 @@ def workload_config():
     return {"workload": "lattice 17x17 pins, pitch 1.26 cm, 50 cm, 2,039,184 tets, 3 materials "
                         "(15/4/3 nuclides x 20,000 pts), cylinder source, 1e6 histories per step",
             "tets": 2039184, "histories_per_step": HIST_PER_STEP, "bank_size": BANK,
-            "precision": "fp64", "mode": "event",
+            "precision": "fp64", "mode": "event", "advance_refill": False,
             "l2": "inputs larger than L2 (mesh planes 261 MB, tally 16 MB vs 129 MB L2)"}
 
 
@@ -174,6 +174,7 @@ def main():
     ap.add_argument("--mode", default="event", choices=["event", "history"])
     ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--refill", type=int, default=0, help="advance lanes take further queued particles")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -205,7 +206,7 @@ def main():
 
     def step(k, tr=None, precision=MC_PREC_FP64, **kw):
         return (tr or t).run(n, first=base + k * n, seed=1, mode=mode, bank_size=BANK, accumulate=True,
-                             precision=precision, **kw)
+                             precision=precision, refill=bool(args.refill), **kw)
 
     for w in range(args.warmup):
         step(w)
@@ -298,7 +299,7 @@ def main():
     w0 = time.perf_counter()
     for k in range(args.steps):
         t.run(n, first=base + (k0 + k) * n, seed=1, mode=mode, bank_size=BANK, accumulate=True,
-              sites=site_np[k])
+              sites=site_np[k], refill=bool(args.refill))
         t.tally(MC_TALLY_SUM, out=out_np)
     torch.cuda.synchronize()
     barrier()

@@ -108,6 +108,9 @@ typedef struct {
   int32_t accumulate;      /* 1: fold this batch into SUM/SUM_SQ and clear the batch tally */
   int32_t sort_queue;      /* event mode: 1 sorts the advance queue by element */
   int32_t profile;         /* 1: time every advance launch with CUDA events (mc_stats.ms_advance) */
+  int32_t refill;          /* event mode: 1 lets an advance lane take the next queued particle when
+                              its particle reaches an event; 0 one particle per lane per launch */
+  int32_t pad;
   const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
 } mc_run_desc;
 

@@ -1,6 +1,7 @@
 """ctypes view of the C ABI declared in include/macaw_gb300.h.
 
-Loads the in-tree libmacaw_gb300.so (building it first if it is missing).
+Loads the in-tree libmacaw_gb300.so (rebuilding it first if it is missing
+or older than its sources).
 There is no fallback: if the library cannot be built or loaded, importing
 this module raises.
 """
@@ -36,7 +37,7 @@ class RunDesc(C.Structure):
                 ("seed", C.c_uint64), ("precision", C.c_int32), ("mode", C.c_int32),
                 ("block_size", C.c_int32), ("max_seg_per_advance", C.c_int32),
                 ("record_traces", C.c_int32), ("accumulate", C.c_int32), ("sort_queue", C.c_int32),
-                ("profile", C.c_int32), ("sites", C.c_void_p)]
+                ("profile", C.c_int32), ("refill", C.c_int32), ("pad", C.c_int32), ("sites", C.c_void_p)]
 
 
 class Stats(C.Structure):
@@ -90,9 +91,7 @@ SIGNATURES = {
 
 
 def _load() -> C.CDLL:
-    path = _build.LIB
-    if not path.exists():
-        _build.build()
+    path = _build.build()  # no-op when the library is newer than its sources
     lib = C.CDLL(str(path))
     for name, (args, res) in SIGNATURES.items():
         fn = getattr(lib, name)

@@ -469,6 +469,7 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.leak_w = c->d_leak_w.as<double>();
   a.precision = d->precision;
   a.max_seg = d->max_seg_per_advance;
+  a.refill = d->refill;
   a.sites = nullptr;
   a.n_mat = (int)c->xs.mat_ids.size();
   {
@@ -679,3 +680,4 @@ int mc_batches_done(mc_ctx* c, int64_t* out) {
 }
 
 }  // extern "C"
+

@@ -239,6 +239,59 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
   flush(L, a.counters, a.leak_w);
 }
 
+// Segment walk, one queued particle per thread (grid-stride over the queue).
+template <int kPrec>
+__global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, RunArgs a, Bank B,
+                                                           EventQueues Q, EventCtl* ctl, int par) {
+  LocalCounters L;
+  L.zero();
+  const int n = *(volatile int*)&ctl->n_adv[par];
+  const int nxt = par ^ 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = Q.adv[par][i];
+    Particle p;
+    load(B, s, p);
+    unsigned long long nxs = 0, nfb = 0;
+    int r = 0;
+    int k = 0;
+    if (kPrec == MC_PREC_FP64) {
+      float sigt32 = (float)p.sigt;
+      for (;;) {
+        r = segment_fp64<false>(M, X, p, a.tally, sigt32, nxs);
+        if (r != 0) break;
+        if (a.max_seg > 0 && ++k >= a.max_seg) {
+          r = 4;
+          break;
+        }
+      }
+    } else {
+      Geo32 g;
+      geo_load(p, g);
+      float inv_sig = (float)(1.0 / p.sigt);
+      for (;;) {
+        r = segment_mixed<false>(M, X, p, g, a.tally, inv_sig, a.tol, nxs, nfb);
+        if (r != 0) break;
+        if (a.max_seg > 0 && ++k >= a.max_seg) {
+          r = 4;
+          break;
+        }
+      }
+      geo_store(g, p);
+    }
+    L.c[kCntFallback] += nfb;
+    if (r == 2) {
+      finish(p, a, L);
+      push(Q.free_slots, &ctl->n_free, s);
+      continue;
+    }
+    store(B, s, p);
+    if (r == 1) push(Q.coll, &ctl->n_coll, s);
+    else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+    else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
 // Take the next advance-queue entry (one atomic per converged lane group).
 __device__ __forceinline__ int take(int* head) {
   cg::coalesced_group g = cg::coalesced_threads();
@@ -456,8 +509,13 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
                                    int* n_launch, cudaEvent_t adv0, cudaEvent_t adv1) {
   k_ev_xs<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   if (adv0) cudaEventRecord(adv0, st);
-  if (a.precision == MC_PREC_MIXED) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-  else k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.refill) {
+    if (a.precision == MC_PREC_MIXED) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  } else {
+    if (a.precision == MC_PREC_MIXED) k_ev_advance_static<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_advance_static<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  }
   if (adv1) cudaEventRecord(adv1, st);
   k_ev_collide<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   k_ev_refill<<<grid, block, 0, st>>>(M, X, S, a, B, Q, ctl, par);

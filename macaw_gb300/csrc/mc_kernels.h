@@ -64,6 +64,7 @@ struct RunArgs {
   int precision;
   float tol;    // mixed form: exit ambiguity tolerance (cm)
   int max_seg;  // event mode: segments per advance launch (<= 0: until event)
+  int refill;   // event mode: lanes take further queued particles within one launch
 };
 
 cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,

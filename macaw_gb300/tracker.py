@@ -113,11 +113,12 @@ class Tracker:
     def run(self, n: int, first: int = 0, seed: int = 1, mode: int = MC_MODE_EVENT,
             precision: int = MC_PREC_FP64, bank_size: int = 0, block_size: int = 0,
             max_seg: int = 0, traces: bool = False, accumulate: bool = False,
-            sort_queue: bool = False, profile: bool = False, sites: np.ndarray | None = None) -> Stats:
+            sort_queue: bool = False, profile: bool = False, sites: np.ndarray | None = None,
+            refill: bool = False) -> Stats:
         if sites is not None:
             assert sites.dtype == SITE_DTYPE and sites.size >= n and sites.flags["C_CONTIGUOUS"]
         d = RunDesc(first, n, bank_size, seed, precision, mode, block_size, max_seg, int(traces),
-                    int(accumulate), int(sort_queue), int(profile),
+                    int(accumulate), int(sort_queue), int(profile), int(refill), 0,
                     None if sites is None else sites.ctypes.data)
         self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
         return self.stats()
