@@ -201,6 +201,36 @@ int mc_stats_get(mc_ctx* ctx, mc_stats* out);
 /* Number of completed accumulated batches (OpenMC n_realizations). */
 int mc_batches_done(mc_ctx* ctx, int64_t* out);
 
+/* ---- batch run without device allocation ------------------------------
+ * No counterpart in the reference: MaCaw itself never allocates device
+ * memory.  mc_run obtains its particle bank, event queues and counters with
+ * cudaMalloc the first time it needs them.  Callers that cannot allow a
+ * device allocation at run time (an application whose memory pool owns the
+ * whole GPU, a serving process that budgets HBM up front, code running where
+ * an allocation would stall or fail) use mc_run_noalloc instead: it tracks
+ * the same histories in the event form, but its scratch is one fixed array
+ * of MC_NOALLOC_MAX_BANK particle slots (about 3.2 MB) compiled into the
+ * library, which every GPU that loads the library holds until the process
+ * exits.  It calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * - bank_size must be at most MC_NOALLOC_MAX_BANK (0 means the maximum);
+ *   larger values are rejected with MC_ERR_ARG.  Any number of histories
+ *   is fine: the bank is refilled as histories end.
+ * - tally: caller-owned DEVICE buffer of n_tet doubles; scores are added to
+ *   it, so clear it first.  traces: caller-owned DEVICE buffer of
+ *   n_histories records when record_traces is set, else NULL.
+ * - The mesh, tables, block map, boundary conditions and source must already
+ *   be on the device: after the last set-up call, run mc_run once (for
+ *   example with n_histories = 0).  Host source sites, accumulate and
+ *   profile are rejected (each would need memory or events).
+ * - The first call on each device looks up the array's device address
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ * - All calls on a device share the one array and it keeps the last call's
+ *   contents (the library clears what must start at zero).  Calls whose
+ *   work overlaps on the GPU race on it: run them one after another. */
+#define MC_NOALLOC_MAX_BANK 16384
+int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* desc, double* tally, mc_trace* traces);
+
 /* ---- synthetic problem generators (host only; no device needed) ------ */
 /* Cube [0,L]^3 of n^3 hexes, six Kuhn tets each; sidesets 0..5 as MOOSE's
  * GeneratedMesh (back, bottom, right, top, left, front). */

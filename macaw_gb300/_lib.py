@@ -76,6 +76,7 @@ SIGNATURES = {
     "mc_sync": ([_P], C.c_int),
     "mc_source_sample": ([_P, _I64, _I64, _U64, _P], C.c_int),
     "mc_ctx_set_stream": ([_P, _P], C.c_int),
+    "mc_run_noalloc": ([_P, C.POINTER(RunDesc), _P, _P], C.c_int),
     "mc_tally_download": ([_P, _I32, _P, _I64], C.c_int),
     "mc_tally_reset": ([_P], C.c_int),
     "mc_trace_download": ([_P, _P, _I64], C.c_int),

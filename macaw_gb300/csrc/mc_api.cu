@@ -9,6 +9,7 @@
 
 #include "../../include/macaw_gb300.h"
 #include "mc_host.h"
+#include "mc_ctx_view.h"
 #include "mc_kernels.h"
 
 using namespace mc;
@@ -681,3 +682,35 @@ int mc_batches_done(mc_ctx* c, int64_t* out) {
 
 }  // extern "C"
 
+// ===========================================================================
+// Read-only views of a context for entry points defined in other files.
+namespace mc {
+
+std::mutex& ctx_mutex(mc_ctx* c) { return c->mu; }
+
+void ctx_set_error(mc_ctx* c, const std::string& msg) { c->err = msg; }
+
+void ctx_set_stats(mc_ctx* c, const mc_stats& s) { c->last = s; }
+
+bool ctx_view(mc_ctx* c, CtxView* v) {
+  v->device = c->device;
+  v->n_sm = c->n_sm;
+  v->stream = c->stream;
+  v->n_tet = c->mesh.n_tet;
+  v->n_mat = (int)c->xs.mat_ids.size();
+  v->ready = c->have_mesh && c->have_src && !c->nucs.empty() && !c->mats.empty() && !c->xs_dirty &&
+             !c->tmat_dirty && !c->bc_dirty;
+  double dg = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const double e = c->mesh.bbox_hi[k] - c->mesh.bbox_lo[k];
+    dg += e * e;
+  }
+  v->tol = (float)(1e-6 * sqrt(dg));
+  if (!v->ready) return false;
+  v->M = dev_mesh(c);
+  v->X = dev_xs(c);
+  v->S = dev_source(c);
+  return true;
+}
+
+}  // namespace mc
