@@ -231,6 +231,19 @@ int mc_batches_done(mc_ctx* ctx, int64_t* out);
 #define MC_NOALLOC_MAX_BANK 16384
 int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* desc, double* tally, mc_trace* traces);
 
+/* ---- input-file front end ---------------------------------------------
+ * Replaces: running a MaCaw input (MooseApp::run on an .i file; src/main.C)
+ * for the tracking path.  Parses the HIT blocks [Mesh] (TetCubeMeshGenerator,
+ * TetLatticeMeshGenerator), [RayKernels] CollisionKernel, [RayBCs]
+ * KillRayBC / ReflectRayBC, [UserObjects] OpenMCStudy, OpenMCTally and
+ * SyntheticCrossSections, [AuxKernels] OpenMCTallyAux, [Executioner]
+ * Transient (num_steps = batches) and [Outputs] (csv, file_base); checks
+ * parameters as the objects' validParams do; runs every batch on the
+ * device; writes a JSON summary into report.  mc_app_check does the
+ * parsing and checks only, without a device. */
+int mc_app_run(const char* input_text, int device, const char* file_base, char* report, int64_t report_len);
+int mc_app_check(const char* input_text, char* report, int64_t report_len);
+
 /* ---- synthetic problem generators (host only; no device needed) ------ */
 /* Cube [0,L]^3 of n^3 hexes, six Kuhn tets each; sidesets 0..5 as MOOSE's
  * GeneratedMesh (back, bottom, right, top, left, front). */

@@ -77,6 +77,8 @@ SIGNATURES = {
     "mc_source_sample": ([_P, _I64, _I64, _U64, _P], C.c_int),
     "mc_ctx_set_stream": ([_P, _P], C.c_int),
     "mc_run_noalloc": ([_P, C.POINTER(RunDesc), _P, _P], C.c_int),
+    "mc_app_run": ([C.c_char_p, C.c_int, C.c_char_p, C.c_char_p, _I64], C.c_int),
+    "mc_app_check": ([C.c_char_p, C.c_char_p, _I64], C.c_int),
     "mc_tally_download": ([_P, _I32, _P, _I64], C.c_int),
     "mc_tally_reset": ([_P], C.c_int),
     "mc_trace_download": ([_P, _P, _I64], C.c_int),

@@ -1,0 +1,784 @@
+// mc_app.cpp -- input-file front end: MaCaw's HIT blocks mapped onto the C ABI.
+//
+// A MaCaw input (test/tests/study/openmc_study.i, examples/*/…i) declares
+// the tracking problem as MOOSE objects: a CollisionKernel in
+// [RayKernels], ReflectRayBC/KillRayBC in [RayBCs], an OpenMCStudy and
+// OpenMCTally in [UserObjects], an OpenMCTallyAux in [AuxKernels], and a
+// Transient executioner whose steps are the batches (OpenMCStudy.C:199-203).
+// This file parses that block syntax (a subset of HIT: nested [name] ... []
+// blocks, key = value, quoted lists, # comments, and [a/b] path headers),
+// builds the registered objects by their `type`, checks their parameters
+// the way their validParams/constructors do, and drives one context through
+// the batches.  OpenMC's XML inputs are replaced by the synthetic-data and
+// source parameters listed with each object below.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <chrono>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/macaw_gb300.h"
+
+namespace {
+
+struct InputError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+// ---------------------------------------------------------------------------
+// HIT subset parser.
+struct Block {
+  std::string name, path;
+  std::map<std::string, std::string> params;
+  std::vector<std::string> order;  // parameter insertion order
+  std::vector<Block> children;
+  Block* child(const std::string& n) {
+    for (auto& c : children)
+      if (c.name == n) return &c;
+    return nullptr;
+  }
+};
+
+std::string trim(const std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+  return a == std::string::npos ? "" : s.substr(a, b - a + 1);
+}
+
+std::string strip_comment(const std::string& line) {
+  bool q1 = false, q2 = false;
+  for (size_t i = 0; i < line.size(); ++i) {
+    const char c = line[i];
+    if (c == '\'' && !q2) q1 = !q1;
+    else if (c == '"' && !q1) q2 = !q2;
+    else if (c == '#' && !q1 && !q2) return line.substr(0, i);
+  }
+  return line;
+}
+
+std::string unquote(const std::string& v) {
+  std::string t = trim(v);
+  if (t.size() >= 2 && ((t.front() == '\'' && t.back() == '\'') || (t.front() == '"' && t.back() == '"')))
+    return t.substr(1, t.size() - 2);
+  return t;
+}
+
+Block parse_hit(const std::string& text) {
+  Block root;
+  root.name = "";
+  std::vector<Block*> stack{&root};
+  std::vector<int> depth_of;  // how many path components each open header pushed
+  std::istringstream in(text);
+  std::string raw;
+  int lineno = 0;
+  std::string pending_key, pending_val;
+  bool in_quote = false;
+  char quote = 0;
+  while (std::getline(in, raw)) {
+    ++lineno;
+    std::string line = in_quote ? raw : trim(strip_comment(raw));
+    if (in_quote) {  // continuation of a multi-line quoted value
+      pending_val += " " + trim(raw);
+      if (raw.find(quote) != std::string::npos) {
+        in_quote = false;
+        stack.back()->params[pending_key] = unquote(trim(pending_val));
+        stack.back()->order.push_back(pending_key);
+      }
+      continue;
+    }
+    if (line.empty()) continue;
+    if (line.front() == '[') {
+      const size_t close = line.find(']');
+      if (close == std::string::npos)
+        throw InputError("line " + std::to_string(lineno) + ": unterminated block header");
+      std::string hdr = trim(line.substr(1, close - 1));
+      if (hdr.empty() || hdr == "../" || hdr == "..") {
+        if (depth_of.empty()) throw InputError("line " + std::to_string(lineno) + ": unmatched []");
+        for (int k = depth_of.back(); k > 0; --k) stack.pop_back();
+        depth_of.pop_back();
+        continue;
+      }
+      if (hdr.rfind("./", 0) == 0) hdr = hdr.substr(2);
+      int pushed = 0;
+      size_t pos = 0;
+      while (pos <= hdr.size()) {
+        size_t slash = hdr.find('/', pos);
+        std::string part = hdr.substr(pos, slash == std::string::npos ? std::string::npos : slash - pos);
+        if (!part.empty()) {
+          Block* parent = stack.back();
+          Block* c = parent->child(part);
+          if (!c) {
+            Block nb;
+            nb.name = part;
+            nb.path = parent->path.empty() ? part : parent->path + "/" + part;
+            parent->children.push_back(nb);
+            c = &parent->children.back();
+          }
+          stack.push_back(c);
+          ++pushed;
+        }
+        if (slash == std::string::npos) break;
+        pos = slash + 1;
+      }
+      depth_of.push_back(pushed);
+      // text after the header on the same line ([block] type = X ... [])
+      std::string rest = trim(line.substr(close + 1));
+      if (!rest.empty()) throw InputError("line " + std::to_string(lineno) + ": put parameters on their own lines");
+      continue;
+    }
+    const size_t eq = line.find('=');
+    if (eq == std::string::npos) throw InputError("line " + std::to_string(lineno) + ": expected key = value");
+    const std::string key = trim(line.substr(0, eq));
+    std::string val = trim(line.substr(eq + 1));
+    if (stack.size() == 1) throw InputError("line " + std::to_string(lineno) + ": parameter outside a block");
+    if (!val.empty() && (val.front() == '\'' || val.front() == '"')) {
+      const char q = val.front();
+      if (val.size() == 1 || val.find(q, 1) == std::string::npos) {
+        in_quote = true;
+        quote = q;
+        pending_key = key;
+        pending_val = val;
+        continue;
+      }
+    }
+    stack.back()->params[key] = unquote(val);
+    stack.back()->order.push_back(key);
+  }
+  if (in_quote) throw InputError("unterminated quoted value for '" + pending_key + "'");
+  if (!depth_of.empty()) throw InputError("unterminated block (missing [])");
+  return root;
+}
+
+// ---------------------------------------------------------------------------
+// Parameters with the checks validParams would make.
+struct Params {
+  const Block* b;
+  std::map<std::string, bool> used;
+  explicit Params(const Block* blk) : b(blk) {}
+  bool has(const std::string& k) const { return b->params.count(k) > 0; }
+  std::string raw(const std::string& k) {
+    used[k] = true;
+    return b->params.at(k);
+  }
+  [[noreturn]] void error(const std::string& k, const std::string& msg) const {
+    throw InputError(b->path + "/" + k + ": " + msg);
+  }
+  std::string str(const std::string& k, const std::string& def = "\x01") {
+    if (!has(k)) {
+      if (def == "\x01") error(k, "missing required parameter");
+      return def;
+    }
+    return raw(k);
+  }
+  double real(const std::string& k, double def = NAN, bool required = false) {
+    if (!has(k)) {
+      if (required) error(k, "missing required parameter");
+      return def;
+    }
+    const std::string v = raw(k);
+    char* end = nullptr;
+    const double x = strtod(v.c_str(), &end);
+    if (end == v.c_str() || *end) error(k, "expected a number, got '" + v + "'");
+    return x;
+  }
+  long long integer(const std::string& k, long long def = 0, bool required = false) {
+    if (!has(k)) {
+      if (required) error(k, "missing required parameter");
+      return def;
+    }
+    const std::string v = raw(k);
+    char* end = nullptr;
+    const double x = strtod(v.c_str(), &end);
+    if (end == v.c_str() || *end || x != floor(x)) error(k, "expected an integer, got '" + v + "'");
+    return (long long)x;
+  }
+  bool boolean(const std::string& k, bool def) {
+    if (!has(k)) return def;
+    const std::string v = raw(k);
+    if (v == "true" || v == "1") return true;
+    if (v == "false" || v == "0") return false;
+    error(k, "expected true or false");
+  }
+  std::vector<std::string> list(const std::string& k, bool required = false) {
+    std::vector<std::string> out;
+    if (!has(k)) {
+      if (required) error(k, "missing required parameter");
+      return out;
+    }
+    std::istringstream s(raw(k));
+    std::string w;
+    while (s >> w) out.push_back(w);
+    return out;
+  }
+  std::vector<double> reals(const std::string& k, bool required = false) {
+    std::vector<double> out;
+    for (auto& w : list(k, required)) {
+      char* end = nullptr;
+      const double x = strtod(w.c_str(), &end);
+      if (end == w.c_str() || *end) error(k, "expected numbers, got '" + w + "'");
+      out.push_back(x);
+    }
+    return out;
+  }
+  std::vector<int> ints(const std::string& k, bool required = false) {
+    std::vector<int> out;
+    for (double x : reals(k, required)) {
+      if (x != floor(x)) error(k, "expected integers");
+      out.push_back((int)x);
+    }
+    return out;
+  }
+  std::string choice(const std::string& k, const std::vector<std::string>& opts, const std::string& def) {
+    std::string v = has(k) ? raw(k) : def;
+    for (auto& o : opts)
+      if (o == v) return v;
+    std::string all;
+    for (auto& o : opts) all += (all.empty() ? "" : " ") + o;
+    error(k, "'" + v + "' is not one of: " + all);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// The problem being assembled.
+struct Problem {
+  // mesh
+  std::vector<double> xyz;
+  std::vector<int32_t> tv, blk, bid;
+  int64_t n_vtx = 0, n_tet = 0;
+  std::vector<double> cyl_xy;  // pin centres for a cylinder source (lattice meshes)
+  double cyl_r = 0.0, height = 0.0, lattice_pitch = 0.0;
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  // boundaries: id -> type
+  std::map<int, int> bcs;
+  // block map
+  std::vector<int32_t> blocks, materials;
+  bool have_kernel = false;
+  // data
+  struct Nuc {
+    std::vector<double> E, st, ss;
+    double awr;
+  };
+  std::vector<Nuc> nucs;
+  struct Mat {
+    int id;
+    std::vector<int32_t> nuc;
+    std::vector<double> dens;
+  };
+  std::vector<Mat> mats;
+  // study
+  int64_t particles = 0, bank_size = 0;
+  uint64_t seed = 1;
+  int precision = MC_PREC_FP64, mode = MC_MODE_EVENT;
+  mc_source_desc src{};
+  bool have_study = false, verbose = false;
+  // tallies
+  struct Tally {
+    int id;
+    std::string filter;  // cell | universe
+  };
+  std::vector<Tally> tallies;
+  struct Aux {
+    std::string name, variable, granularity;
+    int tally_id;
+  };
+  std::vector<Aux> aux;
+  int64_t batches = 1;
+  std::string file_base;
+  bool csv = false;
+};
+
+const std::map<std::string, int> kSideNames = {{"back", 0}, {"bottom", 1}, {"right", 2},
+                                                 {"top", 3},  {"left", 4},   {"front", 5}};
+
+using Factory = std::function<void(Params&, Problem&)>;
+
+// --- [Mesh] generators ------------------------------------------------------
+void tet_cube_mesh(Params& p, Problem& P) {
+  const int n = (int)p.integer("n", 20);
+  const double L = p.real("length", 20.0);
+  if (n < 1) p.error("n", "must be positive");
+  if (!(L > 0)) p.error("length", "must be positive");
+  if (mc_gen_cube_sizes(n, &P.n_vtx, &P.n_tet)) p.error("n", "invalid size");
+  P.xyz.resize(3 * P.n_vtx);
+  P.tv.resize(4 * P.n_tet);
+  P.blk.resize(P.n_tet);
+  P.bid.resize(4 * P.n_tet);
+  mc_gen_cube(n, L, P.xyz.data(), P.tv.data(), P.blk.data(), P.bid.data());
+  const int block_id = (int)p.integer("block_id", 0);
+  for (auto& b : P.blk) b = block_id;
+  for (int k = 0; k < 3; ++k) {
+    P.lo[k] = 0.0;
+    P.hi[k] = L;
+  }
+}
+
+void tet_lattice_mesh(Params& p, Problem& P) {
+  const int nx = (int)p.integer("nx", 17), ny = (int)p.integer("ny", 17), nz = (int)p.integer("nz", 21);
+  const int n_sec = (int)p.integer("sectors", 16), n_fr = (int)p.integer("fuel_rings", 2);
+  const double pitch = p.real("pitch", 1.26), height = p.real("height", 50.0);
+  const double r_fuel = p.real("fuel_radius", 0.41), r_clad = p.real("clad_radius", 0.475);
+  if (mc_gen_lattice_sizes(nx, ny, nz, n_sec, n_fr, &P.n_vtx, &P.n_tet))
+    p.error("sectors", "invalid lattice (nx, ny, nz >= 1, sectors a multiple of 8, fuel_rings >= 1)");
+  P.xyz.resize(3 * P.n_vtx);
+  P.tv.resize(4 * P.n_tet);
+  P.blk.resize(P.n_tet);
+  P.bid.resize(4 * P.n_tet);
+  if (mc_gen_lattice(nx, ny, nz, n_sec, n_fr, pitch, height, r_fuel, r_clad, P.xyz.data(), P.tv.data(),
+                     P.blk.data(), P.bid.data()))
+    p.error("pitch", "invalid lattice geometry (need pitch > 2 clad_radius > 2 fuel_radius > 0)");
+  P.cyl_xy.clear();
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      P.cyl_xy.push_back((i + 0.5) * pitch);
+      P.cyl_xy.push_back((j + 0.5) * pitch);
+    }
+  P.cyl_r = r_fuel;
+  P.height = height;
+  P.lattice_pitch = pitch;
+  P.lo[0] = P.lo[1] = P.lo[2] = 0.0;
+  P.hi[0] = nx * pitch;
+  P.hi[1] = ny * pitch;
+  P.hi[2] = height;
+}
+
+// --- [RayKernels] -------------------------------------------------------------
+// CollisionKernel parameters (src/raykernels/CollisionKernel.C:24-76).
+void collision_kernel(Params& p, Problem& P) {
+  p.str("temperature");  // required coupled variable; synthetic tables carry no temperature
+  const auto blocks = p.ints("blocks", true);
+  const auto mats = p.ints("materials", true);
+  if (blocks.size() != mats.size())
+    p.error("blocks", "The blocks parameter must be the same size as the materials parameter.");
+  p.real("z_coord", 0.0);
+  P.verbose = p.boolean("verbose", false) || P.verbose;
+  P.blocks.assign(blocks.begin(), blocks.end());
+  P.materials.assign(mats.begin(), mats.end());
+  P.have_kernel = true;
+}
+
+// --- [RayBCs] -----------------------------------------------------------------
+void ray_bc(Params& p, Problem& P, int type) {
+  for (auto& b : p.list("boundary", true)) {
+    auto it = kSideNames.find(b);
+    int id;
+    if (it != kSideNames.end()) id = it->second;
+    else {
+      char* end = nullptr;
+      id = (int)strtol(b.c_str(), &end, 10);
+      if (end == b.c_str() || *end || id < 0) p.error("boundary", "unknown boundary '" + b + "'");
+    }
+    P.bcs[id] = type;
+  }
+}
+
+// --- [UserObjects] ------------------------------------------------------------
+// Synthetic nuclear data in place of OpenMC's materials.xml + HDF5 library.
+void synthetic_xs(Params& p, Problem& P) {
+  const auto ids = p.ints("material_ids", true);
+  const auto counts = p.ints("nuclides_per_material", true);
+  if (ids.size() != counts.size())
+    p.error("material_ids", "must have as many entries as nuclides_per_material");
+  const uint64_t seed = (uint64_t)p.integer("seed", 20240611);
+  const int n_pts = (int)p.integer("n_points", 10000);
+  const int n_peaks = (int)p.integer("n_peaks", 20);
+  const double e_min = p.real("energy_min", 1e-5), e_max = p.real("energy_max", 2e7);
+  const double d_lo = p.real("density_min", 1e-4), d_hi = p.real("density_max", 5e-2);
+  int k = 0;
+  for (size_t m = 0; m < ids.size(); ++m) {
+    Problem::Mat mat;
+    mat.id = ids[m];
+    if (counts[m] < 1) p.error("nuclides_per_material", "must be positive");
+    mat.dens.resize(counts[m]);
+    if (mc_gen_densities(seed, (int)m, counts[m], d_lo, d_hi, mat.dens.data()))
+      p.error("density_min", "invalid density range");
+    for (int j = 0; j < counts[m]; ++j, ++k) {
+      Problem::Nuc n;
+      n.E.resize(n_pts);
+      n.st.resize(n_pts);
+      n.ss.resize(n_pts);
+      if (mc_gen_nuclide(seed, k, n_pts, e_min, e_max, n_peaks, n.E.data(), n.st.data(), n.ss.data(), &n.awr))
+        p.error("n_points", "invalid nuclide table parameters");
+      mat.nuc.push_back((int32_t)P.nucs.size());
+      P.nucs.push_back(std::move(n));
+    }
+    P.mats.push_back(std::move(mat));
+  }
+}
+
+// OpenMCStudy (src/userobjects/OpenMCStudy.C:49-76) plus the fixed-source
+// settings OpenMC would read from settings.xml.
+void openmc_study(Params& p, Problem& P) {
+  p.boolean("suppress_openmc_output", true);
+  p.boolean("has_internal_surface_tallies", false);
+  P.verbose = p.boolean("verbose", true) && P.verbose;
+  for (const char* k : {"execute_on", "always_cache_traces", "segments_on_cache_traces", "data_on_cache_traces",
+                        "aux_data_on_cache_traces"})
+    if (p.has(k)) p.raw(k);
+  P.particles = p.integer("particles", 0, true);
+  if (P.particles < 1) p.error("particles", "must be positive");
+  P.bank_size = p.integer("bank_size", 0);
+  P.seed = (uint64_t)p.integer("seed", 1);
+  P.precision = p.choice("precision", {"fp64", "mixed"}, "fp64") == "mixed" ? MC_PREC_MIXED : MC_PREC_FP64;
+  P.mode = p.choice("mode", {"event", "history"}, "event") == "history" ? MC_MODE_HISTORY : MC_MODE_EVENT;
+  if (p.has("batches")) P.batches = p.integer("batches", 1);
+  mc_source_desc& s = P.src;
+  const std::string space = p.choice("source_space", {"point", "box", "cylinders"}, "point");
+  if (space == "point") {
+    s.space = MC_SRC_POINT;
+    auto pt = p.reals("source_point");
+    if (pt.empty()) {
+      for (int k = 0; k < 3; ++k) s.point[k] = 0.5 * (P.lo[k] + P.hi[k]);
+    } else {
+      if (pt.size() != 3) p.error("source_point", "needs three coordinates");
+      for (int k = 0; k < 3; ++k) s.point[k] = pt[k];
+    }
+  } else if (space == "box") {
+    s.space = MC_SRC_BOX;
+    auto b = p.reals("source_box", true);
+    if (b.size() != 6) p.error("source_box", "needs xmin ymin zmin xmax ymax zmax");
+    for (int k = 0; k < 3; ++k) {
+      s.box_lo[k] = b[k];
+      s.box_hi[k] = b[3 + k];
+    }
+  } else {
+    s.space = MC_SRC_CYLINDERS;
+    if (P.cyl_xy.empty()) p.error("source_space", "cylinder sources need a TetLatticeMeshGenerator mesh");
+    s.n_cyl = (int32_t)(P.cyl_xy.size() / 2);
+    s.cyl_r = p.real("source_radius", P.cyl_r);
+    s.cyl_z0 = 0.0;
+    s.cyl_z1 = P.height;
+  }
+  const std::string en = p.choice("source_energy", {"watt", "mono"}, "watt");
+  if (en == "watt") {
+    s.energy = MC_SRC_WATT;
+    auto w = p.reals("watt_parameters");
+    s.watt_a = w.size() > 0 ? w[0] : 0.988e6;
+    s.watt_b = w.size() > 1 ? w[1] : 2.249e-6;
+  } else {
+    s.energy = MC_SRC_MONO;
+    s.mono_E = p.real("source_energy_value", 0.0, true);
+  }
+  P.have_study = true;
+}
+
+// OpenMCTally (src/userobjects/OpenMCTally.C:30-101): the GPU path scores the
+// element track-length flux, so the estimator must be TRACKLENGTH and the
+// score flux; the filter selects cell (element) or universe (block) bins.
+void openmc_tally(Params& p, Problem& P) {
+  Problem::Tally t;
+  t.id = (int)p.integer("id", 0, true);
+  if (p.choice("particle_type", {"neutron", "photon", "electron", "positron"}, "neutron") != "neutron")
+    p.error("particle_type", "Only neutrons are currently supported.");
+  if (p.choice("estimator", {"ANALOG", "TRACKLENGTH", "COLLISION"}, "TRACKLENGTH") != "TRACKLENGTH")
+    p.error("estimator", "Only the tracklength estimator is available on the GPU path");
+  for (auto& s : p.list("scores", true))
+    if (s != "flux") p.error("scores", "Only the flux score is available on the GPU path");
+  auto f = p.list("filters", true);
+  if (f.size() != 1 || (f[0] != "cell" && f[0] != "universe"))
+    p.error("filters", "Use one of the filters 'cell' or 'universe'");
+  t.filter = f[0];
+  if (p.has("execute_on")) p.raw("execute_on");
+  for (auto& o : P.tallies)
+    if (o.id == t.id) p.error("id", "duplicate tally id");
+  P.tallies.push_back(t);
+}
+
+// --- [AuxKernels] -------------------------------------------------------------
+// OpenMCTallyAux (src/auxkernels/OpenMCTallyAux.C:26-68).
+void openmc_tally_aux(Params& p, Problem& P) {
+  Problem::Aux a;
+  a.tally_id = (int)p.integer("tally_id", 0, true);
+  a.granularity = p.choice("granularity", {"global", "universe", "cell"}, "cell");
+  if (a.granularity == "global") p.error("granularity", "Global Tally retrieving currently not supported");
+  if (p.str("score") != "flux") p.error("score", "The specified score does not exist in given tally");
+  p.choice("estimator", {"ANALOG", "TRACKLENGTH", "COLLISION"}, "COLLISION");
+  p.choice("particle_type", {"neutron", "photon", "electron", "positron"}, "neutron");
+  a.variable = p.str("variable");
+  if (p.has("execute_on")) p.raw("execute_on");
+  a.name = p.b->name;
+  P.aux.push_back(a);
+}
+
+std::map<std::string, Factory>& registry() {
+  static std::map<std::string, Factory> r = {
+      {"TetCubeMeshGenerator", tet_cube_mesh},
+      {"TetLatticeMeshGenerator", tet_lattice_mesh},
+      {"CollisionKernel", collision_kernel},
+      {"KillRayBC", [](Params& p, Problem& P) { ray_bc(p, P, MC_BC_VACUUM); }},
+      {"ReflectRayBC", [](Params& p, Problem& P) { ray_bc(p, P, MC_BC_REFLECT); }},
+      {"SyntheticCrossSections", synthetic_xs},
+      {"OpenMCStudy", openmc_study},
+      {"OpenMCTally", openmc_tally},
+      {"OpenMCTallyAux", openmc_tally_aux},
+  };
+  return r;
+}
+
+void build_object(const Block& b, Problem& P, const char* section) {
+  auto it = b.params.find("type");
+  if (it == b.params.end()) {
+    // a grouping block: build its children
+    for (auto& c : b.children) build_object(c, P, section);
+    return;
+  }
+  auto f = registry().find(it->second);
+  if (f == registry().end())
+    throw InputError(b.path + "/type: unknown object type '" + it->second + "' in [" + section + "]");
+  Params p(&b);
+  p.used["type"] = true;
+  f->second(p, P);
+  for (auto& k : b.order)
+    if (!p.used.count(k))
+      throw InputError(b.path + "/" + k + ": unused parameter for " + it->second);
+}
+
+// [UserObjects] must see the mesh and data in a fixed order: data and
+// tallies first, then the study (which may derive its source from the mesh).
+void build_user_objects(const Block& uo, Problem& P) {
+  std::vector<std::string> active;
+  bool restrict = false;
+  auto act = uo.params.find("active");
+  if (act != uo.params.end()) {
+    restrict = true;
+    std::istringstream s(act->second);
+    std::string w;
+    while (s >> w) active.push_back(w);
+  }
+  auto is_active = [&](const std::string& n) {
+    if (!restrict) return true;
+    for (auto& a : active)
+      if (a == n) return true;
+    return false;
+  };
+  std::vector<const Block*> later;
+  for (auto& c : uo.children) {
+    if (!is_active(c.name)) continue;
+    auto t = c.params.find("type");
+    if (t != c.params.end() && t->second == "OpenMCStudy") later.push_back(&c);
+    else build_object(c, P, "UserObjects");
+  }
+  for (auto* c : later) build_object(*c, P, "UserObjects");
+}
+
+int check(mc_ctx* ctx, int rc, const char* what) {
+  if (rc) throw std::runtime_error(std::string(what) + ": " + (ctx ? mc_last_error(ctx) : "error"));
+  return rc;
+}
+
+}  // namespace
+
+// Runs a whole input: setup, `batches` batches, readback of every
+// OpenMCTallyAux variable.  Writes a JSON summary into report (truncated to
+// report_len) and, when [Outputs] csv = true, <file_base>_<variable>.csv.
+extern "C" int mc_app_run(const char* input_text, int device, const char* file_base, char* report,
+                          int64_t report_len) {
+  auto put = [&](const std::string& s) {
+    if (report && report_len > 0) {
+      const size_t n = std::min<size_t>(s.size(), (size_t)report_len - 1);
+      memcpy(report, s.data(), n);
+      report[n] = 0;
+    }
+  };
+  if (!input_text) {
+    put("{\"error\": \"null input\"}");
+    return MC_ERR_ARG;
+  }
+  mc_ctx* ctx = nullptr;
+  try {
+    Block root = parse_hit(input_text);
+    Problem P;
+    P.file_base = file_base ? file_base : "";
+    Block* mesh = root.child("Mesh");
+    if (!mesh) throw InputError("[Mesh]: missing");
+    build_object(*mesh, P, "Mesh");
+    if (P.n_tet == 0) throw InputError("[Mesh]: no mesh generator produced a mesh");
+    for (const char* ignored : {"Problem", "Variables", "AuxVariables", "Postprocessors", "VectorPostprocessors"})
+      (void)ignored;
+    if (Block* rk = root.child("RayKernels")) build_object(*rk, P, "RayKernels");
+    if (!P.have_kernel) throw InputError("[RayKernels]: a CollisionKernel is required");
+    if (Block* rb = root.child("RayBCs")) build_object(*rb, P, "RayBCs");
+    Block* uo = root.child("UserObjects");
+    if (!uo) throw InputError("[UserObjects]: missing");
+    build_user_objects(*uo, P);
+    if (!P.have_study) throw InputError("[UserObjects]: an OpenMCStudy is required");
+    if (P.mats.empty()) throw InputError("[UserObjects]: a SyntheticCrossSections object is required");
+    if (Block* ak = root.child("AuxKernels")) build_object(*ak, P, "AuxKernels");
+    if (Block* ex = root.child("Executioner")) {
+      Params p(ex);
+      if (p.has("type") && p.raw("type") != "Transient")
+        p.error("type", "Only a Transient executioner is supported (one step per batch)");
+      if (p.has("num_steps")) P.batches = p.integer("num_steps", 1);
+    }
+    if (P.batches < 1) throw InputError("[Executioner]/num_steps: must be positive");
+    if (Block* out = root.child("Outputs")) {
+      Params p(out);
+      P.csv = p.boolean("csv", false);
+      if (p.has("file_base")) P.file_base = p.raw("file_base");
+    }
+    for (auto& a : P.aux) {
+      bool found = false;
+      for (auto& t : P.tallies)
+        if (t.id == a.tally_id) {
+          found = true;
+          if (a.granularity == "universe" && t.filter != "universe")
+            throw InputError("AuxKernels/" + a.name + ": Tally does not have a universe filter");
+          if (a.granularity == "cell" && t.filter != "cell")
+            throw InputError("AuxKernels/" + a.name + ": Specified tally does not contain a cell filter");
+        }
+      if (!found) throw InputError("AuxKernels/" + a.name + "/tally_id: no OpenMCTally with id " +
+                                   std::to_string(a.tally_id));
+    }
+
+    // ---- device setup (OpenMCStudy constructor + initialSetup) ----
+    check(nullptr, mc_ctx_create(device, &ctx), "mc_ctx_create");
+    check(ctx, mc_mesh_upload(ctx, P.n_vtx, P.xyz.data(), P.n_tet, P.tv.data(), P.blk.data(), P.bid.data()),
+          "mesh");
+    for (auto& b : P.bcs) check(ctx, mc_bc_set(ctx, b.first, b.second), "RayBCs");
+    for (auto& n : P.nucs)
+      check(ctx, mc_nuclide_add(ctx, (int64_t)n.E.size(), n.E.data(), n.st.data(), n.ss.data(), n.awr, nullptr),
+            "nuclide");
+    for (auto& m : P.mats)
+      check(ctx, mc_material_add(ctx, m.id, (int32_t)m.nuc.size(), m.nuc.data(), m.dens.data()), "material");
+    check(ctx, mc_block_material_map(ctx, (int32_t)P.blocks.size(), P.blocks.data(), P.materials.data()),
+          "CollisionKernel");
+    if (P.src.space == MC_SRC_CYLINDERS) P.src.cyl_xy = P.cyl_xy.data();
+    check(ctx, mc_source_set(ctx, &P.src), "OpenMCStudy source");
+
+    // ---- batches (Transient steps) ----
+    const auto t0 = std::chrono::steady_clock::now();
+    mc_stats tot{};
+    for (int64_t b = 0; b < P.batches; ++b) {
+      mc_run_desc d{};
+      d.first_history = b * P.particles;
+      d.n_histories = P.particles;
+      d.bank_size = P.bank_size;
+      d.seed = P.seed;
+      d.precision = P.precision;
+      d.mode = P.mode;
+      d.accumulate = 1;
+      check(ctx, mc_run(ctx, &d), "batch");
+      mc_stats s;
+      mc_stats_get(ctx, &s);
+      tot.n_hist += s.n_hist;
+      tot.n_seg += s.n_seg;
+      tot.n_coll += s.n_coll;
+      tot.n_leak += s.n_leak;
+      tot.n_absorb += s.n_absorb;
+      tot.n_stuck += s.n_stuck;
+      tot.n_lost += s.n_lost;
+      tot.leak_weight += s.leak_weight;
+    }
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+
+    // ---- AuxKernel readback ----
+    std::vector<double> sum((size_t)P.n_tet), sq((size_t)P.n_tet);
+    check(ctx, mc_tally_download(ctx, MC_TALLY_SUM, sum.data(), P.n_tet), "tally");
+    check(ctx, mc_tally_download(ctx, MC_TALLY_SUM_SQ, sq.data(), P.n_tet), "tally");
+    std::ostringstream js;
+    js.precision(17);
+    js << "{\"histories\": " << tot.n_hist << ", \"segments\": " << tot.n_seg << ", \"collisions\": " << tot.n_coll
+       << ", \"leaked\": " << tot.n_leak << ", \"absorbed\": " << tot.n_absorb << ", \"stuck\": " << tot.n_stuck
+       << ", \"lost\": " << tot.n_lost << ", \"batches\": " << P.batches << ", \"seconds\": " << secs
+       << ", \"neutrons_per_s\": " << (secs > 0 ? tot.n_hist / secs : 0.0) << ", \"aux\": {";
+    bool first = true;
+    for (auto& a : P.aux) {
+      std::vector<double> val((size_t)P.n_tet);
+      if (a.granularity == "cell") {
+        val = sum;
+      } else {
+        std::map<int, double> per_block;
+        for (int64_t t = 0; t < P.n_tet; ++t) per_block[P.blk[t]] += sum[t];
+        for (int64_t t = 0; t < P.n_tet; ++t) val[t] = per_block[P.blk[t]];
+      }
+      double total = 0.0;
+      for (double v : val) total += v;
+      js << (first ? "" : ", ") << "\"" << a.variable << "\": {\"sum\": " << total << "}";
+      first = false;
+      if (P.csv && !P.file_base.empty()) {
+        std::ofstream f(P.file_base + "_" + a.variable + ".csv");
+        if (!f) throw std::runtime_error("cannot write " + P.file_base + "_" + a.variable + ".csv");
+        f.precision(17);
+        f << "elem,block," << a.variable << ",rel_err\n";
+        const double nb = (double)P.batches;
+        for (int64_t t = 0; t < P.n_tet; ++t) {
+          double re = 0.0;
+          if (a.granularity == "cell" && sum[t] > 0 && nb > 1) {
+            const double mean = sum[t] / nb;
+            const double var = (sq[t] / nb - mean * mean) / (nb - 1);
+            re = var > 0 ? sqrt(var) / mean : 0.0;
+          }
+          f << t << "," << P.blk[t] << "," << val[t] / nb << "," << re << "\n";
+        }
+      }
+    }
+    js << "}}";
+    put(js.str());
+    mc_ctx_destroy(ctx);
+    return MC_OK;
+  } catch (const InputError& e) {
+    if (ctx) mc_ctx_destroy(ctx);
+    put(std::string("{\"error\": \"") + e.what() + "\"}");
+    return MC_ERR_ARG;
+  } catch (const std::exception& e) {
+    if (ctx) mc_ctx_destroy(ctx);
+    put(std::string("{\"error\": \"") + e.what() + "\"}");
+    return MC_ERR_STATE;
+  }
+}
+
+// Parses and checks an input without touching a device (used to validate
+// inputs on hosts without a GPU): the same object construction and
+// parameter checks as mc_app_run, returning a JSON summary of the problem.
+extern "C" int mc_app_check(const char* input_text, char* report, int64_t report_len) {
+  auto put = [&](const std::string& s) {
+    if (report && report_len > 0) {
+      const size_t n = std::min<size_t>(s.size(), (size_t)report_len - 1);
+      memcpy(report, s.data(), n);
+      report[n] = 0;
+    }
+  };
+  if (!input_text) return MC_ERR_ARG;
+  try {
+    Block root = parse_hit(input_text);
+    Problem P;
+    Block* mesh = root.child("Mesh");
+    if (!mesh) throw InputError("[Mesh]: missing");
+    build_object(*mesh, P, "Mesh");
+    if (Block* rk = root.child("RayKernels")) build_object(*rk, P, "RayKernels");
+    if (!P.have_kernel) throw InputError("[RayKernels]: a CollisionKernel is required");
+    if (Block* rb = root.child("RayBCs")) build_object(*rb, P, "RayBCs");
+    Block* uo = root.child("UserObjects");
+    if (!uo) throw InputError("[UserObjects]: missing");
+    build_user_objects(*uo, P);
+    if (!P.have_study) throw InputError("[UserObjects]: an OpenMCStudy is required");
+    if (Block* ak = root.child("AuxKernels")) build_object(*ak, P, "AuxKernels");
+    if (Block* ex = root.child("Executioner")) {
+      Params p(ex);
+      if (p.has("type") && p.raw("type") != "Transient")
+        p.error("type", "Only a Transient executioner is supported (one step per batch)");
+      if (p.has("num_steps")) P.batches = p.integer("num_steps", 1);
+    }
+    std::ostringstream js;
+    js << "{\"tets\": " << P.n_tet << ", \"vertices\": " << P.n_vtx << ", \"nuclides\": " << P.nucs.size()
+       << ", \"materials\": " << P.mats.size() << ", \"particles\": " << P.particles << ", \"batches\": "
+       << P.batches << ", \"reflective\": " << [&] {
+            int n = 0;
+            for (auto& b : P.bcs) n += b.second == MC_BC_REFLECT;
+            return n;
+          }()
+       << ", \"tallies\": " << P.tallies.size() << ", \"aux\": " << P.aux.size() << ", \"precision\": \""
+       << (P.precision == MC_PREC_MIXED ? "mixed" : "fp64") << "\"}";
+    put(js.str());
+    return MC_OK;
+  } catch (const std::exception& e) {
+    put(std::string("{\"error\": \"") + e.what() + "\"}");
+    return MC_ERR_ARG;
+  }
+}

@@ -416,6 +416,155 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
 }
 
 // ---------------------------------------------------------------------------
+// FP64 segment with a float-certified exit side.  Exit distances are first
+// solved on the float planes with the float position; each float distance
+// t32 carries a bound e on |t32 - t| derived from the float rounding of the
+// planes, the position and every operation (constant 12 * 2^-24 covers the
+// input roundings and the fused dot products, see below).  When the float
+// intervals [t32-e, t32+e] of the nearest candidate and every other
+// candidate are disjoint, and every side's n.u sign is certain, the FP64
+// search of segment_fp64 would pick the same side, so only that side is
+// evaluated in FP64; otherwise this falls back to segment_fp64's full
+// search.  The distance-to-collision pre-test uses the float interval for L
+// and a float upper bound for xi.  Results are bit-identical to
+// segment_fp64.
+//
+// Error bounds (u = 2^-24): planes32 and the float position/direction are
+// roundings of the FP64 values (relative u each); num32 = d - (nx*x + ny*y
+// + nz*z) through two fmaf and one product and a subtraction: |num32 - num|
+// <= u (2|d| + 6 sum|n_i x_i|)(1+u) <= 12u (|d| + |x|_1) since |n_i| <= 1;
+// likewise |den32 - den| <= 12u |u|_1; t32 = num32/den32 rounded (0.5 ulp):
+// |t - t32| <= (E_num + |t32| E_den)/(den32 - E_den) + 4.8e-7 |t32|, padded
+// by 0.1%.
+template <bool kInlineXS>
+__device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, Particle& p,
+                                             const float uf, const float vf, const float wf,
+                                             double* __restrict__ tally, float& sigt32,
+                                             unsigned long long& n_xs) {
+  if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
+    p.status = kStuck;
+    return 2;
+  }
+  const int mat = __ldg(M.tmat + p.elem);
+  if (mat != p.mat) {
+    if (mat < 0) {
+      p.status = kBadXS;
+      return 2;
+    }
+    if (!xs_cache_get(p, mat)) {
+      if (!kInlineXS) return 3;
+      const double s = macro_total(X, mat, p.E);
+      ++n_xs;
+      if (!(s > 0.0) || s != s) {
+        p.status = kBadXS;
+        return 2;
+      }
+      p.sigt = s;
+      xs_cache_put(p, mat, s);
+    }
+    p.mat = mat;
+    sigt32 = (float)p.sigt;
+  }
+  const float xf = (float)p.x, yf = (float)p.y, zf = (float)p.z;
+  const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
+  const float Eden = 7.2e-7f * (fabsf(uf) + fabsf(vf) + fabsf(wf));
+  const float4* P32 = M.planes32 + 4 * (int64_t)p.elem;
+  bool sure = true;
+  int bf = -1;
+  float tb = 3.0e38f, eb = 0.0f, lo_other = 3.0e38f;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    if (f == p.fin) continue;
+    const float4 pl = __ldg(P32 + f);
+    const float den = fmaf(pl.x, uf, fmaf(pl.y, vf, pl.z * wf));
+    if (fabsf(den) <= Eden) sure = false;
+    if (den > Eden) {
+      const float num = pl.w - fmaf(pl.x, xf, fmaf(pl.y, yf, pl.z * zf));
+      const float En = 7.2e-7f * (fabsf(pl.w) + xa);
+      const float t = num / den;
+      const float e = ((En + fabsf(t) * Eden) / (den - Eden) + 4.8e-7f * fabsf(t)) * 1.001f + 1e-30f;
+      if (t < tb) {
+        if (bf >= 0) lo_other = fminf(lo_other, tb - eb);
+        bf = f;
+        tb = t;
+        eb = e;
+      } else {
+        lo_other = fminf(lo_other, t - e);
+      }
+    }
+  }
+  if (!sure || bf < 0 || !(tb + eb < lo_other)) {
+    const int r = segment_fp64<kInlineXS>(M, X, p, tally, sigt32, n_xs);
+    return (r == 0 && p.fin < 0) ? 5 : r;  // a reflection changed the direction
+  }
+  const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
+  const double4_32a plb = P[bf];
+  const double bden = plb.x * p.u + plb.y * p.v + plb.z * p.w;
+  const double bnum = plb.w - (plb.x * p.x + plb.y * p.y + plb.z * p.z);
+  double L = bnum / bden;
+  if (!(L > 0.0)) L = 0.0;
+  // one draw per segment: advance the state once, derive both forms
+  p.seed = kPrnMult * p.seed + kPrnAdd;
+  uint64_t wv = ((p.seed >> ((p.seed >> 59u) + 5u)) ^ p.seed) * 12605985483714917081ULL;
+  wv = (wv >> 43u) ^ wv;
+  // xi = (wv >> 11) 2^-53 < (hi32 + 1) 2^-32 <= xhi; -logf(xhi) is a lower
+  // bound of -ln(xi) up to logf's 1-ulp error
+  const float xhi = fmaf((float)(uint32_t)(wv >> 32), 2.3283064365386963e-10f, 2.3283064365386963e-10f) *
+                    1.00000024f;
+  const float lf = -logf(xhi) * 0.99999976f - 1e-7f;
+  const float thr = fmaxf(tb + eb, 0.0f) * sigt32;
+  bool cross;
+  double dist = 0.0;
+  if (lf > thr * 1.00001f + 1e-6f) {
+    cross = true;
+  } else {
+    const double xi = (double)(wv >> 11) * 0x1.0p-53;
+    dist = -mc::log64(xi) / p.sigt;
+    cross = dist > L;
+  }
+  const double score = cross ? L : dist;
+  atomicAdd(tally + p.elem, p.wgt == 1.0 ? score : p.wgt * score);
+  ++p.n_seg;
+  if (L == 0.0) ++p.zero_run;
+  else p.zero_run = 0;
+  if (cross) {
+    p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
+    p.x = p.x + L * p.u;
+    p.y = p.y + L * p.v;
+    p.z = p.z + L * p.w;
+    const int4 nb4 = __ldg(M.nbr + p.elem);
+    const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+    if (nb >= 0) {
+      p.elem = nb >> 2;
+      p.fin = nb & 3;
+      return 0;
+    }
+    const int bid = -1 - nb;
+    if (bid < M.n_bid && M.bc_type[bid] == 1) {
+      const double dn = p.u * plb.x + p.v * plb.y + p.w * plb.z;
+      const double t2 = 2.0 * dn;
+      p.u = p.u - t2 * plb.x;
+      p.v = p.v - t2 * plb.y;
+      p.w = p.w - t2 * plb.z;
+      p.fin = -1;
+      return 5;  // reflected: the caller refreshes its float direction
+    }
+    p.status = kLeaked;
+    p.face = bf;
+    return 2;
+  }
+  p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
+  const double ex = p.x + L * p.u, ey = p.y + L * p.v, ez = p.z + L * p.w;
+  const double back = L - dist;
+  p.x = ex - back * p.u;
+  p.y = ey - back * p.v;
+  p.z = ez - back * p.w;
+  ++p.n_coll;
+  p.zero_run = 0;
+  return 1;
+}
+
+// ---------------------------------------------------------------------------
 // Mixed-precision form.  Position and direction live in float registers for
 // the walk; exits are solved on the float planes; the two nearest exit
 // distances must differ by more than tol (1e-6 of the mesh bounding-box

@@ -164,9 +164,15 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
     unsigned long long nxs = 0, nfb = 0;
     if (kPrec == MC_PREC_FP64) {
       float sigt32 = 0.0f;
+      float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
+        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, a.tally, sigt32, nxs);
         if (r == 1) collide(X, p);
+        if (r == 1 || r == 5) {
+          uf = (float)p.u;
+          vf = (float)p.v;
+          wf = (float)p.w;
+        }
       }
     } else {
       Geo32 g;
@@ -256,8 +262,15 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
     int k = 0;
     if (kPrec == MC_PREC_FP64) {
       float sigt32 = (float)p.sigt;
+      float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       for (;;) {
-        r = segment_fp64<false>(M, X, p, a.tally, sigt32, nxs);
+        r = segment_fp64g<false>(M, X, p, uf, vf, wf, a.tally, sigt32, nxs);
+        if (r == 5) {
+          uf = (float)p.u;
+          vf = (float)p.v;
+          wf = (float)p.w;
+          r = 0;
+        }
         if (r != 0) break;
         if (a.max_seg > 0 && ++k >= a.max_seg) {
           r = 4;
@@ -322,15 +335,24 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     if (i < n) {
       s = q[i];
       load(B, s, p);
-      if (kPrec == MC_PREC_FP64) f32 = (float)p.sigt;
-      else { geo_load(p, g); f32 = (float)(1.0 / p.sigt); }
+      geo_load(p, g);
+      f32 = (kPrec == MC_PREC_FP64) ? (float)p.sigt : (float)(1.0 / p.sigt);
     }
   }
   while (__any_sync(0xffffffffu, s >= 0)) {
     if (s < 0) continue;
     int r;
-    if (kPrec == MC_PREC_FP64) r = segment_fp64<false>(M, X, p, a.tally, f32, nxs);
-    else r = segment_mixed<false>(M, X, p, g, a.tally, f32, a.tol, nxs, nfb);
+    if (kPrec == MC_PREC_FP64) {
+      r = segment_fp64g<false>(M, X, p, g.u, g.v, g.w, a.tally, f32, nxs);
+      if (r == 5) {
+        g.u = (float)p.u;
+        g.v = (float)p.v;
+        g.w = (float)p.w;
+        r = 0;
+      }
+    } else {
+      r = segment_mixed<false>(M, X, p, g, a.tally, f32, a.tol, nxs, nfb);
+    }
     if (r == 0) {
       if (a.max_seg <= 0 || ++k < a.max_seg) continue;
       r = 4;
@@ -351,8 +373,8 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     if (i < n) {
       s = q[i];
       load(B, s, p);
-      if (kPrec == MC_PREC_FP64) f32 = (float)p.sigt;
-      else { geo_load(p, g); f32 = (float)(1.0 / p.sigt); }
+      geo_load(p, g);
+      f32 = (kPrec == MC_PREC_FP64) ? (float)p.sigt : (float)(1.0 / p.sigt);
     }
   }
   L.c[kCntFallback] += nfb;
@@ -439,9 +461,15 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
     unsigned long long nxs = 0, nfb = 0;
     if (kPrec == MC_PREC_FP64) {
       float sigt32 = (float)p.sigt;
+      float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64<true>(M, X, p, a.tally, sigt32, nxs);
+        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, a.tally, sigt32, nxs);
         if (r == 1) collide(X, p);
+        if (r == 1 || r == 5) {
+          uf = (float)p.u;
+          vf = (float)p.v;
+          wf = (float)p.w;
+        }
       }
     } else {
       Geo32 g;
