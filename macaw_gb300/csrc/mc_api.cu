@@ -72,7 +72,7 @@ struct mc_ctx {
 
   // device copies
   DevBuf d_planes, d_planes32, d_nbr, d_tmat, d_bc, d_gstart, d_gtets;
-  DevBuf d_pts, d_nuc_off, d_nuc_n, d_hidx, d_awr, d_mat_off, d_mat_nuc, d_mat_dens;
+  DevBuf d_gE, d_goff, d_gn, d_ghidx, d_nuc_grid, d_nuc_off, d_sig, d_awr, d_mat_off, d_mat_nuc, d_mat_dens;
   DevBuf d_cyl;
   DevBuf d_tally, d_sum, d_sumsq;
   DevBuf d_counters, d_leak_w;
@@ -122,10 +122,13 @@ int ensure_device_tables(mc_ctx* c) {
   if (c->xs_dirty) {
     std::string m = build_xs_tables(c->nucs, c->mats, c->n_bins, c->xs);
     if (!m.empty()) return set_err(c, MC_ERR_ARG, m);
-    CK(upload(c->d_pts, c->xs.pts, c->stream), "upload xs points");
+    CK(upload(c->d_gE, c->xs.gE, c->stream), "upload xs grids");
+    CK(upload(c->d_goff, c->xs.g_off, c->stream), "upload xs grids");
+    CK(upload(c->d_gn, c->xs.g_n, c->stream), "upload xs grids");
+    CK(upload(c->d_ghidx, c->xs.ghidx, c->stream), "upload xs hash index");
+    CK(upload(c->d_nuc_grid, c->xs.nuc_grid, c->stream), "upload xs grid map");
     CK(upload(c->d_nuc_off, c->xs.nuc_off, c->stream), "upload xs offsets");
-    CK(upload(c->d_nuc_n, c->xs.nuc_n, c->stream), "upload xs sizes");
-    CK(upload(c->d_hidx, c->xs.hidx, c->stream), "upload xs hash index");
+    CK(upload(c->d_sig, c->xs.sig, c->stream), "upload xs values");
     CK(upload(c->d_awr, c->xs.awr, c->stream), "upload awr");
     CK(upload(c->d_mat_off, c->xs.mat_off, c->stream), "upload materials");
     CK(upload(c->d_mat_nuc, c->xs.mat_nuc, c->stream), "upload materials");
@@ -180,15 +183,19 @@ DevMesh dev_mesh(mc_ctx* c) {
 
 DevXS dev_xs(mc_ctx* c) {
   DevXS X;
-  X.pts = c->d_pts.as<double4_32a>();
+  X.gE = c->d_gE.as<double>();
+  X.g_off = c->d_goff.as<int64_t>();
+  X.g_n = c->d_gn.as<int>();
+  X.ghidx = c->d_ghidx.as<int>();
+  X.nuc_grid = c->d_nuc_grid.as<int>();
   X.nuc_off = c->d_nuc_off.as<int64_t>();
-  X.nuc_n = c->d_nuc_n.as<int>();
-  X.hidx = c->d_hidx.as<int>();
+  X.sig = c->d_sig.as<double2>();
   X.awr = c->d_awr.as<double>();
   X.mat_off = c->d_mat_off.as<int>();
   X.mat_nuc = c->d_mat_nuc.as<int>();
   X.mat_dens = c->d_mat_dens.as<double>();
-  X.n_nuc = (int)c->xs.nuc_n.size();
+  X.n_nuc = (int)c->xs.nuc_grid.size();
+  X.n_grid = (int)c->xs.g_n.size();
   X.n_bins = c->xs.n_bins;
   X.E_lo = c->xs.E_lo;
   X.E_hi = c->xs.E_hi;

@@ -32,15 +32,18 @@ struct DevMesh {
 };
 
 struct DevXS {
-  const double4_32a* __restrict__ pts;      // (E, sigma_t, sigma_s, 0) per point
-  const int64_t* __restrict__ nuc_off;
-  const int* __restrict__ nuc_n;
-  const int* __restrict__ hidx;         // (n_bins+1) x n_nuc, bin-major
+  const double* __restrict__ gE;        // energies of the distinct grids
+  const int64_t* __restrict__ g_off;
+  const int* __restrict__ g_n;
+  const int* __restrict__ ghidx;        // (n_bins+1) x n_grid, bin-major
+  const int* __restrict__ nuc_grid;
+  const int64_t* __restrict__ nuc_off;  // into sig
+  const double2* __restrict__ sig;      // (sigma_t, sigma_s) per point
   const double* __restrict__ awr;
   const int* __restrict__ mat_off;
   const int* __restrict__ mat_nuc;
   const double* __restrict__ mat_dens;
-  int n_nuc, n_bins;
+  int n_nuc, n_grid, n_bins;
   double E_lo, E_hi, lE_lo, du;
 };
 
@@ -98,53 +101,74 @@ __device__ __forceinline__ int xs_bucket(const DevXS& X, double lE) {
   return k;
 }
 
-// Bisection inside the hash bin, guarded so a bin estimate that is off by
-// rounding still ends on the right interval.
-__device__ __forceinline__ int xs_index(const DevXS& X, int nuc, int k, double E) {
-  const double4_32a* P = X.pts + X.nuc_off[nuc];
-  int lo = __ldg(X.hidx + (size_t)k * X.n_nuc + nuc);
-  int hi = __ldg(X.hidx + (size_t)(k + 1) * X.n_nuc + nuc) + 1;
-  const int last = X.nuc_n[nuc] - 1;
+// Bisection inside the hash bin of grid g, guarded so a bin estimate that is
+// off by rounding still ends on the right interval; returns the interval
+// index i (E_i <= E < E_i+1) and the interpolation fraction.
+__device__ __forceinline__ void grid_locate(const DevXS& X, int g, int k, double E, int& i, double& f) {
+  const double* G = X.gE + __ldg(X.g_off + g);
+  int lo = __ldg(X.ghidx + (size_t)k * X.n_grid + g);
+  int hi = __ldg(X.ghidx + (size_t)(k + 1) * X.n_grid + g) + 1;
+  const int last = __ldg(X.g_n + g) - 1;
   if (hi > last) hi = last;
-  while (lo > 0 && E < __ldg(&P[lo].x)) --lo;
-  while (hi < last && E >= __ldg(&P[hi].x)) ++hi;
+  while (lo > 0 && E < __ldg(G + lo)) --lo;
+  while (hi < last && E >= __ldg(G + hi)) ++hi;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
-    if (E < __ldg(&P[mid].x)) hi = mid;
+    if (E < __ldg(G + mid)) hi = mid;
     else lo = mid;
   }
-  return lo;
+  i = lo;
+  const double e0 = __ldg(G + lo), e1 = __ldg(G + lo + 1);
+  f = (E - e0) / (e1 - e0);
 }
 
-__device__ __forceinline__ void micro_xs(const DevXS& X, int nuc, int k, double E, double& st,
-                                         double& ss) {
-  const double4_32a* P = X.pts + X.nuc_off[nuc];
-  const int i = xs_index(X, nuc, k, E);
-  const double4_32a a = P[i];
-  const double4_32a b = P[i + 1];
-  const double f = (E - a.x) / (b.x - a.x);
-  st = a.y + f * (b.y - a.y);
-  ss = a.z + f * (b.z - a.z);
+// Lookups of several nuclides at one energy: nuclides on the grid located
+// last reuse its interval and fraction (identical grids give identical
+// values, so this is bit-identical to a search per nuclide).
+struct GridCursor {
+  int g = -1, i = 0;
+  double f = 0.0;
+};
+
+__device__ __forceinline__ void micro_xs(const DevXS& X, int nuc, int k, double E, GridCursor& c,
+                                         double& st, double& ss) {
+  const int g = __ldg(X.nuc_grid + nuc);
+  if (g != c.g) {
+    grid_locate(X, g, k, E, c.i, c.f);
+    c.g = g;
+  }
+  const double2* S = X.sig + __ldg(X.nuc_off + nuc) + c.i;
+  const double2 a = __ldg(S), b = __ldg(S + 1);
+  st = a.x + c.f * (b.x - a.x);
+  ss = a.y + c.f * (b.y - a.y);
 }
 
 // Sigma_t = sum_i N_i sigma_t,i(E), in material order (OpenMC
 // Material::calculate_xs, called through event_calculate_xs).
-__device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E) {
-  const int k = xs_bucket(X, mc::log64(E));
+__device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E, int k) {
   double acc = 0.0;
+  GridCursor c;
   const int j1 = __ldg(X.mat_off + mat + 1);
   for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
     double st, ss;
-    micro_xs(X, __ldg(X.mat_nuc + j), k, E, st, ss);
+    micro_xs(X, __ldg(X.mat_nuc + j), k, E, c, st, ss);
     acc = acc + __ldg(X.mat_dens + j) * st;
   }
   return acc;
 }
 
+__device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E) {
+  return macro_total(X, mat, E, xs_bucket(X, mc::log64(E)));
+}
+
 // ---------------------------------------------------------------------------
 // Start element (stands in for MOOSE ClaimRays): lowest-id tet containing x
 // (all four half-spaces within kLocateTol) whose interior the direction
-// enters; else the lowest-id containing tet; else -1.
+// enters; else the lowest-id containing tet; else -1.  Cell lists are in
+// ascending tet id, so the first entered tet found is the answer.  Each
+// candidate is first tested on the float planes: it is skipped only when a
+// side proves x outside by more than the float error bound (same 12 * 2^-24
+// bound as the float exit test), which the FP64 test would reject too.
 __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, double z, double u,
                                       double v, double w) {
   const double xs[3] = {x, y, z};
@@ -158,9 +182,24 @@ __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, doub
     ci[k] = c;
   }
   const int64_t cell = ((int64_t)ci[2] * M.gn[1] + ci[1]) * M.gn[0] + ci[0];
-  int best_in = -1, best_any = -1;
-  for (int64_t q = M.gstart[cell]; q < M.gstart[cell + 1]; ++q) {
-    const int t = M.gtets[q];
+  const float xf = (float)x, yf = (float)y, zf = (float)z;
+  const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
+  int best_any = -1;
+  const int64_t q1 = M.gstart[cell + 1];
+  for (int64_t q = M.gstart[cell]; q < q1; ++q) {
+    const int t = __ldg(M.gtets + q);
+    const float4* P32 = M.planes32 + 4 * (int64_t)t;
+    bool out = false;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const float4 pl = __ldg(P32 + f);
+      const float s32 = fmaf(pl.x, xf, fmaf(pl.y, yf, pl.z * zf)) - pl.w;
+      if (s32 > 1e-9f + 7.3e-7f * (fabsf(pl.w) + xa)) {
+        out = true;
+        break;
+      }
+    }
+    if (out) continue;
     bool inside = true, enters = true;
     for (int f = 0; f < 4; ++f) {
       const double4_32a pl = M.planes[4 * (int64_t)t + f];
@@ -175,10 +214,10 @@ __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, doub
       }
     }
     if (!inside) continue;
-    if (enters && (best_in < 0 || t < best_in)) best_in = t;
-    if (best_any < 0 || t < best_any) best_any = t;
+    if (enters) return t;
+    if (best_any < 0) best_any = t;
   }
-  return best_in >= 0 ? best_in : best_any;
+  return best_any;
 }
 
 // ---------------------------------------------------------------------------
@@ -258,8 +297,9 @@ __device__ __forceinline__ void collide(const DevXS& X, Particle& p) {
   double acc = 0.0, st = 0.0, ss = 0.0;
   const int j0 = __ldg(X.mat_off + mat), j1 = __ldg(X.mat_off + mat + 1);
   int pick = -1;
+  GridCursor gc;
   for (int j = j0; j < j1; ++j) {
-    micro_xs(X, __ldg(X.mat_nuc + j), k, p.E, st, ss);
+    micro_xs(X, __ldg(X.mat_nuc + j), k, p.E, gc, st, ss);
     acc = acc + __ldg(X.mat_dens + j) * st;
     if (acc >= cutoff) {
       pick = j;

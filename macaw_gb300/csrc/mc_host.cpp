@@ -181,15 +181,40 @@ std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
       }
       mext[k] += b - a;
     }
+  for (int k = 0; k < 3; ++k) mext[k] = std::max(mext[k] / (double)std::max<int64_t>(n_s, 1), ext[k] * 1e-6);
+  // finest cell scale (relative to the mean extent) whose list entries stay
+  // within 12 per tet and whose cell count stays within 2^25
   int64_t ncell = 1;
-  double cells = 1.0;
-  for (int k = 0; k < 3; ++k) {
-    mext[k] = std::max(mext[k] / (double)std::max<int64_t>(n_s, 1), ext[k] * 1e-6);
-    cells *= std::max(1.0, ext[k] / mext[k]);
+  double scale = 1.0;
+  for (double sc : {0.35, 0.5, 0.7, 1.0}) {
+    double cells = 1.0, h[3];
+    for (int k = 0; k < 3; ++k) {
+      h[k] = ext[k] / std::max(1.0, std::min(4096.0, floor(ext[k] / (mext[k] * sc))));
+      cells *= ext[k] / h[k];
+    }
+    double per = 0.0;
+    int64_t ns = 0;
+    for (int64_t t = 0; t < n_tet; t += stride_t, ++ns) {
+      double c = 1.0;
+      for (int k = 0; k < 3; ++k) {
+        double a = INFINITY, b = -INFINITY;
+        for (int vv = 0; vv < 4; ++vv) {
+          const double x = xyz[3 * (int64_t)tet_vtx[4 * t + vv] + k];
+          a = std::min(a, x);
+          b = std::max(b, x);
+        }
+        c *= floor((b - lo[k]) / h[k]) - floor((a - lo[k]) / h[k]) + 1.0;
+      }
+      per += c;
+    }
+    per /= (double)std::max<int64_t>(ns, 1);
+    if ((per <= 12.0 && cells <= 33554432.0) || sc == 1.0) {
+      scale = sc;
+      break;
+    }
   }
-  const double shrink = cells > 16777216.0 ? cbrt(cells / 16777216.0) : 1.0;
   for (int k = 0; k < 3; ++k) {
-    int n = (int)(ext[k] / (mext[k] * shrink));
+    int n = (int)floor(ext[k] / (mext[k] * scale));
     n = std::max(1, std::min(n, 4096));
     M.gn[k] = n;
     M.glo[k] = lo[k];
@@ -264,34 +289,47 @@ std::string build_xs_tables(const std::vector<Nuclide>& nucs, const std::vector<
   X.lE_lo = mc::log64(lo);
   X.du = (mc::log64(hi) - X.lE_lo) / (double)n_bins;
   const int64_t nn = (int64_t)nucs.size();
+  X.nuc_grid.assign(nn, -1);
   X.nuc_off.resize(nn);
-  X.nuc_n.resize(nn);
   X.awr.resize(nn);
-  int64_t tot = 0;
-  for (int64_t i = 0; i < nn; ++i) {
-    X.nuc_off[i] = tot;
-    X.nuc_n[i] = (int32_t)nucs[i].E.size();
-    X.awr[i] = nucs[i].awr;
-    tot += (int64_t)nucs[i].E.size();
-  }
-  X.pts.assign((size_t)(4 * tot), 0.0);
-  X.hidx.assign((size_t)(n_bins + 1) * nn, 0);
+  X.gE.clear();
+  X.g_off.clear();
+  X.g_n.clear();
+  X.sig.clear();
+  std::vector<int64_t> rep;  // a nuclide holding each grid
   for (int64_t i = 0; i < nn; ++i) {
     const Nuclide& n = nucs[i];
-    const int64_t np = (int64_t)n.E.size();
-    for (int64_t j = 0; j < np; ++j) {
-      double* P = &X.pts[4 * (X.nuc_off[i] + j)];
-      P[0] = n.E[j];
-      P[1] = n.st[j];
-      P[2] = n.ss[j];
-      P[3] = 0.0;
+    int g = -1;
+    for (size_t r = 0; r < rep.size() && g < 0; ++r) {
+      const Nuclide& o = nucs[rep[r]];
+      if (o.E.size() == n.E.size() && std::equal(o.E.begin(), o.E.end(), n.E.begin())) g = (int)r;
     }
-    // hidx[k] = (number of grid points in bins < k) - 1, clamped to [0, n-2]
+    if (g < 0) {
+      g = (int)rep.size();
+      rep.push_back(i);
+      X.g_off.push_back((int64_t)X.gE.size());
+      X.g_n.push_back((int32_t)n.E.size());
+      X.gE.insert(X.gE.end(), n.E.begin(), n.E.end());
+    }
+    X.nuc_grid[i] = g;
+    X.awr[i] = n.awr;
+    X.nuc_off[i] = (int64_t)X.sig.size() / 2;
+    for (size_t j = 0; j < n.E.size(); ++j) {
+      X.sig.push_back(n.st[j]);
+      X.sig.push_back(n.ss[j]);
+    }
+  }
+  const int64_t ng = (int64_t)rep.size();
+  X.ghidx.assign((size_t)(n_bins + 1) * ng, 0);
+  for (int64_t g = 0; g < ng; ++g) {
+    const double* E = X.gE.data() + X.g_off[g];
+    const int64_t np = X.g_n[g];
+    // ghidx[k] = (number of grid points in bins < k) - 1, clamped to [0, n-2]
     int64_t j = 0;
     for (int k = 0; k <= n_bins; ++k) {
-      while (j < np && bucket_of(X, mc::log64(n.E[j])) < k) ++j;
+      while (j < np && bucket_of(X, mc::log64(E[j])) < k) ++j;
       int64_t v = std::max<int64_t>(0, std::min<int64_t>(j - 1, np - 2));
-      X.hidx[(size_t)k * nn + i] = (int32_t)v;
+      X.ghidx[(size_t)k * ng + g] = (int32_t)v;
     }
   }
   X.mat_off.assign(mats.size() + 1, 0);

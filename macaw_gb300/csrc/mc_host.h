@@ -42,12 +42,17 @@ struct Material {
   std::vector<double> dens;
 };
 
-// Flattened cross-section tables in the layouts the kernels read.
+// Flattened cross-section tables in the layouts the kernels read.  Nuclides
+// whose energy grids are identical share one stored grid (and so one hash
+// search and one interpolation fraction per lookup).
 struct XSTables {
-  std::vector<double> pts;      // 4 per point: (E, sigma_t, sigma_s, 0), nuclides concatenated
-  std::vector<int64_t> nuc_off; // first point of each nuclide
-  std::vector<int32_t> nuc_n;   // points per nuclide
-  std::vector<int32_t> hidx;    // (n_bins+1) x n_nuc, bin-major
+  std::vector<double> gE;       // energies of the distinct grids, concatenated
+  std::vector<int64_t> g_off;   // first point of each grid
+  std::vector<int32_t> g_n;     // points per grid
+  std::vector<int32_t> ghidx;   // (n_bins+1) x n_grid, bin-major
+  std::vector<int32_t> nuc_grid;  // grid of each nuclide
+  std::vector<int64_t> nuc_off;   // first (sigma_t, sigma_s) pair of each nuclide
+  std::vector<double> sig;        // 2 per point: (sigma_t, sigma_s), nuclides concatenated
   std::vector<double> awr;
   std::vector<int32_t> mat_off; // n_mat+1
   std::vector<int32_t> mat_nuc;

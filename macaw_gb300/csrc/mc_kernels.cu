@@ -84,7 +84,8 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
     p.status = kBadXS;
     return false;
   }
-  const double s = macro_total(X, mat, p.E);
+  const int k = xs_bucket(X, mc::log64(p.E));
+  const double s = macro_total(X, mat, p.E, k);
   L.c[kCntXS] += 1;
   if (!(s > 0.0) || s != s) {
     p.status = kBadXS;
@@ -96,7 +97,7 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
   if (n_mat <= 4) {
     for (int m = 0; m < n_mat; ++m) {
       if (m == mat) continue;
-      const double o = macro_total(X, m, p.E);
+      const double o = macro_total(X, m, p.E, k);
       L.c[kCntXS] += 1;
       if (o > 0.0) xs_cache_put(p, m, o);
     }
