@@ -81,7 +81,7 @@ struct mc_ctx {
   DevBuf d_sites;
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
-  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_cm, b_cs;
+  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_cm, b_cs, b_cinv;
   DevBuf q_xs0, q_xs1, q_adv0, q_adv1, q_coll, q_free, d_ctl;
   int64_t bank_cap = 0;
 
@@ -235,6 +235,7 @@ int ensure_bank(mc_ctx* c, int64_t cap) {
   for (DevBuf* b : d4) CK(b->alloc(n * 4), "allocate particle bank");
   CK(c->b_cm.alloc(n * 16), "allocate particle bank");
   CK(c->b_cs.alloc(n * 32), "allocate particle bank");
+  CK(c->b_cinv.alloc(n * 16), "allocate particle bank");
   CK(c->d_ctl.alloc(sizeof(EventCtl)), "allocate event control");
   c->bank_cap = cap;
   return MC_OK;
@@ -249,6 +250,7 @@ Bank dev_bank(mc_ctx* c) {
   B.elem = c->b_elem.as<int>(); B.mat = c->b_mat.as<int>(); B.n_seg = c->b_nseg.as<int>();
   B.n_coll = c->b_ncoll.as<int>(); B.zero_run = c->b_zero.as<int>();
   B.cm = c->b_cm.as<int4>(); B.cs = c->b_cs.as<double4_32a>(); B.fin = c->b_fin.as<int>();
+  B.cinv = c->b_cinv.as<float4>();
   B.cap = c->bank_cap;
   return B;
 }

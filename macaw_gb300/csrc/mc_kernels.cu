@@ -237,6 +237,10 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
       double4_32a c;
       c.x = p.cs0; c.y = p.cs1; c.z = p.cs2; c.w = p.cs3;
       B.cs[s] = c;
+      if (a.precision == MC_PREC_MIXED) {
+        B.cinv[s] = make_float4(p.cm.x >= 0 ? (float)(1.0 / p.cs0) : 0.0f, p.cm.y >= 0 ? (float)(1.0 / p.cs1) : 0.0f,
+                                p.cm.z >= 0 ? (float)(1.0 / p.cs2) : 0.0f, p.cm.w >= 0 ? (float)(1.0 / p.cs3) : 0.0f);
+      }
       push(Q.adv[par], &ctl->n_adv[par], s);
     } else {
       finish(p, a, L);
@@ -376,6 +380,177 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
       load(B, s, p);
       geo_load(p, g);
       f32 = (kPrec == MC_PREC_FP64) ? (float)p.sigt : (float)(1.0 / p.sigt);
+    }
+  }
+  L.c[kCntFallback] += nfb;
+  flush(L, a.counters, a.leak_w);
+}
+
+// Mixed-precision segment walk with a compact state: float position and
+// direction, float 1/Sigma_t for the cached materials, 64-bit RNG state and
+// trace hash.  Only the bank fields the walk reads or changes move; the
+// rest of a particle is touched only when its history ends here.  Same
+// arithmetic as segment_mixed.
+__global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B, EventQueues Q,
+                                                             EventCtl* ctl, int par) {
+  LocalCounters L;
+  L.zero();
+  const int n = *(volatile int*)&ctl->n_adv[par];
+  const int nxt = par ^ 1;
+  const float tol = a.tol;
+  unsigned long long nfb = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = Q.adv[par][i];
+    float x = (float)B.x[s], y = (float)B.y[s], z = (float)B.z[s];
+    float u = (float)B.u[s], v = (float)B.v[s], w = (float)B.w[s];
+    int elem = B.elem[s], fin = B.fin[s], mat = B.mat[s], n_seg = B.n_seg[s], zrun = B.zero_run[s];
+    uint64_t seed = B.seed[s], hash = B.hash[s];
+    const double wgt = B.wgt[s];
+    const int4 cm = B.cm[s];
+    const float4 ci = B.cinv[s];
+    int slot = -1;  // cache slot whose Sigma_t is current, if the walk changed material
+    float inv_sig = (float)(1.0 / B.sigt[s]);
+    int r = 0, face = -1;
+    int k = 0;
+    for (;;) {
+      if (n_seg >= kMaxSegments || zrun >= kMaxZeroRun) {
+        r = 2;
+        face = -2;  // stuck
+        break;
+      }
+      const int m = __ldg(M.tmat + elem);
+      if (m != mat) {
+        const int sl = m & 3;
+        const int key = sl == 0 ? cm.x : sl == 1 ? cm.y : sl == 2 ? cm.z : cm.w;
+        if (m < 0 || key != m) {
+          r = (m < 0) ? 2 : 3;
+          if (m < 0) face = -3;  // no material: bad cross section
+          break;
+        }
+        mat = m;
+        slot = sl;
+        inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
+      }
+      const float4* P = M.planes32 + 4 * (int64_t)elem;
+      int bf = -1;
+      float t1 = 3.0e38f, t2 = 3.0e38f;
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        if (f == fin) continue;
+        const float4 pl = __ldg(P + f);
+        const float den = fmaf(pl.x, u, fmaf(pl.y, v, pl.z * w));
+        if (den > 0.0f) {
+          const float num = pl.w - fmaf(pl.x, x, fmaf(pl.y, y, pl.z * z));
+          const float t = __fdividef(num, den);
+          if (t < t1) {
+            t2 = t1;
+            t1 = t;
+            bf = f;
+          } else if (t < t2) {
+            t2 = t;
+          }
+        }
+      }
+      float Ls;
+      if (bf < 0 || t2 - t1 <= tol || t1 < -tol) {
+        ++nfb;
+        Geo32 g{x, y, z, u, v, w};
+        double Ld = 0.0;
+        bf = exit_fp64(M, elem, fin, g, Ld);
+        if (bf < 0) {
+          r = 2;
+          face = -2;
+          break;
+        }
+        Ls = (float)Ld;
+      } else {
+        Ls = fmaxf(t1, 0.0f);
+      }
+      seed = kPrnMult * seed + kPrnAdd;
+      uint64_t wv = ((seed >> ((seed >> 59u) + 5u)) ^ seed) * 12605985483714917081ULL;
+      wv = (wv >> 43u) ^ wv;
+      const float xi = (float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f;
+      const float dist = -__logf(xi) * inv_sig;
+      const bool cross = dist > Ls;
+      const float score = cross ? Ls : dist;
+      atomicAdd(a.tally + elem, wgt == 1.0 ? (double)score : wgt * (double)score);
+      ++n_seg;
+      if (Ls == 0.0f) ++zrun;
+      else zrun = 0;
+      if (!cross) {
+        hash = fnv(hash, (uint64_t)elem * 8ULL + 4ULL);
+        x = fmaf(dist, u, x);
+        y = fmaf(dist, v, y);
+        z = fmaf(dist, w, z);
+        zrun = 0;
+        r = 1;
+        break;
+      }
+      hash = fnv(hash, (uint64_t)elem * 8ULL + (uint64_t)bf);
+      x = fmaf(Ls, u, x);
+      y = fmaf(Ls, v, y);
+      z = fmaf(Ls, w, z);
+      const int4 nb4 = __ldg(M.nbr + elem);
+      const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+      if (nb >= 0) {
+        elem = nb >> 2;
+        fin = nb & 3;
+      } else {
+        const int bid = -1 - nb;
+        if (bid < M.n_bid && M.bc_type[bid] == 1) {
+          const float4 pl = __ldg(P + bf);
+          const float t2r = 2.0f * fmaf(u, pl.x, fmaf(v, pl.y, w * pl.z));
+          u = fmaf(-t2r, pl.x, u);
+          v = fmaf(-t2r, pl.y, v);
+          w = fmaf(-t2r, pl.z, w);
+          const float nrm = rsqrtf(fmaf(u, u, fmaf(v, v, w * w)));
+          u *= nrm;
+          v *= nrm;
+          w *= nrm;
+          fin = -1;
+        } else {
+          r = 2;
+          face = bf;  // leaked through side bf
+          break;
+        }
+      }
+      if (a.max_seg > 0 && ++k >= a.max_seg) {
+        r = 4;
+        break;
+      }
+    }
+    if (r == 2) {
+      Particle p;
+      load(B, s, p);
+      p.x = x; p.y = y; p.z = z;
+      p.u = u; p.v = v; p.w = w;
+      p.elem = elem; p.fin = fin; p.mat = mat; p.n_seg = n_seg; p.zero_run = zrun;
+      p.seed = seed; p.hash = hash;
+      if (face >= 0) {
+        p.status = kLeaked;
+        p.face = face;
+      } else {
+        p.status = face == -3 ? kBadXS : kStuck;
+      }
+      finish(p, a, L);
+      push(Q.free_slots, &ctl->n_free, s);
+      continue;
+    }
+    B.x[s] = x; B.y[s] = y; B.z[s] = z;
+    B.u[s] = u; B.v[s] = v; B.w[s] = w;
+    B.elem[s] = elem; B.fin[s] = fin; B.mat[s] = mat; B.n_seg[s] = n_seg; B.zero_run[s] = zrun;
+    B.seed[s] = seed; B.hash[s] = hash;
+    if (slot >= 0) {
+      const double4_32a c = B.cs[s];
+      B.sigt[s] = slot == 0 ? c.x : slot == 1 ? c.y : slot == 2 ? c.z : c.w;
+    }
+    if (r == 1) {
+      B.n_coll[s] = B.n_coll[s] + 1;
+      push(Q.coll, &ctl->n_coll, s);
+    } else if (r == 3) {
+      push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+    } else {
+      push(Q.adv[nxt], &ctl->n_adv[nxt], s);
     }
   }
   L.c[kCntFallback] += nfb;
@@ -542,7 +717,7 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
     if (a.precision == MC_PREC_MIXED) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   } else {
-    if (a.precision == MC_PREC_MIXED) k_ev_advance_static<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    if (a.precision == MC_PREC_MIXED) k_ev_advance_mixed<<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
     else k_ev_advance_static<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   }
   if (adv1) cudaEventRecord(adv1, st);

@@ -32,6 +32,7 @@ struct Bank {
   int *elem, *mat, *n_seg, *n_coll, *zero_run, *fin;
   int4* cm;            // cross-section cache keys
   double4_32a* cs;     // cross-section cache values
+  float4* cinv;        // float 1/Sigma_t of the cached values (mixed-precision walk)
   int64_t cap;
 };
 

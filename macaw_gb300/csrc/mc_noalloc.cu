@@ -26,12 +26,13 @@ constexpr size_t kAlign = 256;
 constexpr size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 // Per particle slot: 12 eight-byte fields, 6 four-byte fields, the XS cache
-// (16 + 32 bytes) and 6 four-byte queue entries.
+// (16 + 32 bytes), its float inverses (16 bytes) and 6 four-byte queue
+// entries.
 constexpr size_t kSlotArrays8 = 12, kSlotArrays4 = 6 + 6;
 constexpr size_t kScratchBytes =
     kSlotArrays8 * align_up(8 * (size_t)MC_NOALLOC_MAX_BANK) +
     kSlotArrays4 * align_up(4 * (size_t)MC_NOALLOC_MAX_BANK) +
-    align_up(16 * (size_t)MC_NOALLOC_MAX_BANK) + align_up(32 * (size_t)MC_NOALLOC_MAX_BANK) +
+    2 * align_up(16 * (size_t)MC_NOALLOC_MAX_BANK) + align_up(32 * (size_t)MC_NOALLOC_MAX_BANK) +
     align_up(sizeof(EventCtl)) + align_up(sizeof(unsigned long long) * kNumCounters) +
     align_up(sizeof(double));
 
@@ -125,6 +126,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   B.n_coll = cv.take<int>(n); B.zero_run = cv.take<int>(n); B.fin = cv.take<int>(n);
   B.cm = cv.take<int4>(n);
   B.cs = cv.take<double4_32a>(n);
+  B.cinv = cv.take<float4>(n);
   B.cap = cap;
   EventQueues Q;
   Q.xs[0] = cv.take<int>(n); Q.xs[1] = cv.take<int>(n);
