@@ -110,8 +110,10 @@ typedef struct {
   int32_t profile;         /* 1: time every advance launch with CUDA events (mc_stats.ms_advance) */
   int32_t refill;          /* event mode: 1 lets an advance lane take the next queued particle when
                               its particle reaches an event; 0 one particle per lane per launch */
-  int32_t pad;
+  int32_t n_batches;       /* > 1: consecutive batches of batch_sizes histories run through one
+                              pipeline, each folded into SUM/SUM_SQ when it drains (needs accumulate) */
   const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
+  const int64_t* batch_sizes; /* HOST array of n_batches sizes adding up to n_histories */
 } mc_run_desc;
 
 /* Per-history outcome: element sequence hash, counts, end state. */

@@ -79,6 +79,9 @@ struct mc_ctx {
   DevBuf d_traces;
   int64_t trace_n = 0;
   DevBuf d_sites;
+  DevBuf d_tally2, d_batch_end;
+  bool tally2_clear = false;
+  long long h_limit = 0;
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
   DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_cm, b_cs, b_cinv;
@@ -504,12 +507,64 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   const int grid = std::max(1, c->n_sm * per_sm);
   int n_launch = 0, n_adv = 0;
   float ms_adv = 0.0f;
+  // batches run through one pipeline: batch b scores into tally[b & 1] and
+  // is folded into SUM/SUM_SQ (normalised by its size) once its last
+  // particle ends; births of batch b+2 wait until then
+  const int nb = d->n_batches > 1 ? d->n_batches : 1;
+  std::vector<int64_t> bend((size_t)nb);
+  if (nb > 1) {
+    if (!d->batch_sizes) return set_err(c, MC_ERR_ARG, "n_batches > 1 needs batch_sizes");
+    if (!d->accumulate) return set_err(c, MC_ERR_ARG, "pipelined batches need accumulate = 1");
+    int64_t acc = 0;
+    for (int b = 0; b < nb; ++b) {
+      if (d->batch_sizes[b] < 1) return set_err(c, MC_ERR_ARG, "batch sizes must be positive");
+      acc += d->batch_sizes[b];
+      bend[b] = acc;
+    }
+    if (acc != d->n_histories) return set_err(c, MC_ERR_ARG, "batch sizes must add up to n_histories");
+    CK(upload(c->d_batch_end, bend, c->stream), "upload batch ends");
+    CK(c->d_tally2.alloc(sizeof(double) * (size_t)c->mesh.n_tet), "allocate batch tally");
+    if (!c->tally2_clear) {
+      CK(cudaMemsetAsync(c->d_tally2.p, 0, c->d_tally2.bytes, c->stream), "clear batch tally");
+      c->tally2_clear = true;
+    }
+    a.tally2 = c->d_tally2.as<double>();
+    a.batch_end = c->d_batch_end.as<int64_t>();
+  } else {
+    bend[0] = d->n_histories;
+    a.tally2 = a.tally;
+    a.batch_end = nullptr;
+  }
+  a.n_batches = nb;
+  a.live = nullptr;
+  auto fold = [&](int b) -> int {
+    const int64_t size = bend[b] - (b ? bend[b - 1] : 0);
+    CK(launch_accumulate((b & 1) ? a.tally2 : a.tally, c->d_sum.as<double>(), c->d_sumsq.as<double>(),
+                         c->mesh.n_tet, size > 0 ? 1.0 / (double)size : 0.0, c->stream),
+       "launch accumulate");
+    c->batches += 1;
+    return MC_OK;
+  };
   CK(cudaEventRecord(c->ev0, c->stream), "event");
+  int folded = 0;
   if (d->n_histories > 0) {
     if (d->mode == MC_MODE_HISTORY) {
-      CK(launch_history(M, X, S, a, block, grid, c->stream), "launch history kernel");
-      n_launch = 1;
-      n_adv = 1;
+      for (int b = 0; b < nb; ++b) {
+        RunArgs ab = a;
+        ab.first = a.first + (b ? bend[b - 1] : 0);
+        ab.n = bend[b] - (b ? bend[b - 1] : 0);
+        ab.n_batches = 1;
+        ab.tally2 = ab.tally;
+        ab.traces = a.traces ? a.traces + (ab.first - a.first) : nullptr;
+        CK(launch_history(M, X, S, ab, block, grid, c->stream), "launch history kernel");
+        ++n_launch;
+        if (nb > 1) {
+          rc = fold(b);
+          if (rc) return rc;
+          ++folded;
+        }
+      }
+      n_adv = n_launch;
     } else {
       int64_t cap = d->bank_size > 0 ? std::min(d->bank_size, d->n_histories) : d->n_histories;
       cap = std::max<int64_t>(cap, 1);
@@ -519,9 +574,12 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       const Bank B = dev_bank(c);
       const EventQueues Q = dev_queues(c);
       EventCtl* ctl = c->d_ctl.as<EventCtl>();
-      CK(launch_event_init(M, X, S, a, B, Q, ctl, block, grid, c->stream), "launch event init");
+      if (nb > 1) a.live = ctl->live;
+      int64_t limit = nb > 1 ? bend[std::min(1, nb - 1)] : d->n_histories;
+      CK(launch_event_init(M, X, S, a, B, Q, ctl, block, grid, c->stream, limit), "launch event init");
       n_launch = 1;
       int par = 0;
+      int oldest = 0;
       EventCtl h;
       const int kGroup = 4;
       const int64_t tail = std::max<int64_t>(4096, cap / 64);
@@ -544,8 +602,27 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
         }
         CK(cudaMemcpyAsync(&h, ctl, sizeof(EventCtl), cudaMemcpyDeviceToHost, c->stream), "read event control");
         CK(cudaStreamSynchronize(c->stream), "event loop");
+        if (nb > 1) {
+          // retire drained batches, then let the next batch be born
+          bool moved = false;
+          while (oldest < nb && h.next_hist >= bend[oldest] && h.live[oldest & 1] == 0) {
+            rc = fold(oldest);
+            if (rc) return rc;
+            ++oldest;
+            ++folded;
+            moved = true;
+          }
+          if (moved && oldest < nb) {
+            c->h_limit = bend[std::min(oldest + 1, nb - 1)];
+            CK(cudaMemcpyAsync(&ctl->birth_limit, &c->h_limit, sizeof(long long), cudaMemcpyHostToDevice,
+                               c->stream),
+               "raise birth limit");
+            CK(cudaStreamSynchronize(c->stream), "raise birth limit");
+          }
+          if (oldest >= nb) break;
+        }
         const int64_t inflight = (int64_t)h.n_xs[par] + h.n_adv[par];
-        if (inflight == 0 && h.next_hist >= a.n) break;
+        if (nb == 1 && inflight == 0 && h.next_hist >= a.n) break;
         if (h.next_hist >= a.n && inflight <= tail) {
           CK(launch_event_finish(M, X, S, a, B, Q, ctl, par, block, grid, c->stream), "launch event finish");
           ++n_launch;
@@ -557,11 +634,15 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   }
   CK(cudaEventRecord(c->ev1, c->stream), "event");
   if (d->accumulate) {
-    const double inv_w = d->n_histories > 0 ? 1.0 / (double)d->n_histories : 0.0;
-    CK(launch_accumulate(c->d_tally.as<double>(), c->d_sum.as<double>(), c->d_sumsq.as<double>(),
-                         c->mesh.n_tet, inv_w, c->stream),
-       "launch accumulate");
-    c->batches += 1;
+    if (nb == 1) {
+      rc = fold(0);
+      if (rc) return rc;
+    } else {
+      for (int b = folded; b < nb; ++b) {
+        rc = fold(b);
+        if (rc) return rc;
+      }
+    }
   }
   unsigned long long cnt[kNumCounters];
   double leak_w = 0.0;

@@ -62,6 +62,7 @@ struct Particle {
   int64_t id;
   int elem, mat, n_seg, n_coll, status, face, zero_run;
   int fin;  // side the particle entered its element through (-1: none)
+  int tag;  // parity of the particle's batch (selects its batch tally)
   // Sigma_t at the current energy for up to four materials, direct-mapped
   // by material index (slot = mat & 3); -1 marks an empty slot.  Sigma_t is
   // a pure function of (material, E), so a cached value is bit-identical to

@@ -42,8 +42,12 @@ __device__ __forceinline__ void flush(LocalCounters& L, unsigned long long* g, d
   if ((threadIdx.x & 31) == 0 && w != 0.0) atomicAdd(leak_w, w);
 }
 
+// Batch tally a particle scores into.
+__device__ __forceinline__ double* tally_of(const RunArgs& a, int tag) { return tag ? a.tally2 : a.tally; }
+
 // End of a history: closing hash word, counters, optional trace record.
 __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCounters& L) {
+  if (a.live) atomicAdd(a.live + p.tag, -1);
   p.hash = fnv(p.hash, (uint64_t)(16 + p.status));
   L.c[kCntSeg] += (unsigned long long)p.n_seg;
   L.c[kCntColl] += (unsigned long long)p.n_coll;
@@ -113,6 +117,7 @@ __device__ __forceinline__ void load(const Bank& B, int s, Particle& p) {
   p.elem = B.elem[s]; p.mat = B.mat[s]; p.n_seg = B.n_seg[s]; p.n_coll = B.n_coll[s];
   p.zero_run = B.zero_run[s];
   p.fin = B.fin[s];
+  p.tag = B.tag[s];
   p.cm = B.cm[s];
   const double4_32a c = B.cs[s];
   p.cs0 = c.x; p.cs1 = c.y; p.cs2 = c.z; p.cs3 = c.w;
@@ -128,6 +133,7 @@ __device__ __forceinline__ void store(const Bank& B, int s, const Particle& p) {
   B.elem[s] = p.elem; B.mat[s] = p.mat; B.n_seg[s] = p.n_seg; B.n_coll[s] = p.n_coll;
   B.zero_run[s] = p.zero_run;
   B.fin[s] = p.fin;
+  B.tag[s] = p.tag;
   B.cm[s] = p.cm;
   double4_32a c;
   c.x = p.cs0; c.y = p.cs1; c.z = p.cs2; c.w = p.cs3;
@@ -141,6 +147,19 @@ __device__ __forceinline__ void birth(const DevMesh& M, const DevXS& X, const De
   if (a.sites) o = a.sites[h - a.first];
   else sample_source(X, S, k, a.master, o);
   start(M, o, h, k, a.master, p);
+  int b = 0;
+  if (a.n_batches > 1) {
+    const int64_t r = h - a.first;
+    int lo = 0, hi = a.n_batches - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (r < a.batch_end[mid]) hi = mid;
+      else lo = mid + 1;
+    }
+    b = lo;
+  }
+  p.tag = b & 1;
+  if (a.live) atomicAdd(a.live + p.tag, 1);
 }
 
 // Append slot to a queue with one atomic per converged group of lanes.
@@ -150,6 +169,28 @@ __device__ __forceinline__ void push(int* q, int* cnt, int slot) {
   if (g.thread_rank() == 0) base = atomicAdd(cnt, (int)g.size());
   base = g.shfl(base, 0);
   q[base + g.thread_rank()] = slot;
+}
+
+// Return a slot to the free ring (slots of ended histories wait there until
+// births are allowed).
+__device__ __forceinline__ void push_free(const EventQueues& Q, EventCtl* ctl, int slot, int64_t cap) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(&ctl->free_tail, (unsigned long long)g.size());
+  base = g.shfl(base, 0);
+  Q.free_slots[(base + g.thread_rank()) % (unsigned long long)cap] = slot;
+}
+
+// Births allowed in this iteration: free slots available, histories left
+// below the birth limit.
+__device__ __forceinline__ long long births_now(const EventCtl* ctl, int64_t n) {
+  const long long base = *(volatile const long long*)&ctl->next_hist;
+  const long long lim0 = *(volatile const long long*)&ctl->birth_limit;
+  const long long lim = lim0 < n ? lim0 : n;
+  const long long avail = (long long)(*(volatile const unsigned long long*)&ctl->free_tail -
+                                      *(volatile const unsigned long long*)&ctl->free_head);
+  const long long left = lim - base;
+  return left < avail ? (left > 0 ? left : 0) : avail;
 }
 
 // ---------------------------------------------------------------------------
@@ -167,7 +208,7 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
       float sigt32 = 0.0f;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, a.tally, sigt32, nxs);
+        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
         if (r == 1) collide(X, p);
         if (r == 1 || r == 5) {
           uf = (float)p.u;
@@ -180,7 +221,7 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
       geo_load(p, g);
       float inv_sig = 0.0f;
       while (p.status == kAlive) {
-        const int r = segment_mixed<true>(M, X, p, g, a.tally, inv_sig, a.tol, nxs, nfb);
+        const int r = segment_mixed<true>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
         if (r == 1) {
           geo_store(g, p);
           collide(X, p);
@@ -201,23 +242,27 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
 
 // Births of histories [0, min(n, cap)) into slots of the same index.
 __global__ void __launch_bounds__(256) k_ev_init(DevMesh M, DevXS X, DevSource S, RunArgs a,
-                                                 Bank B, EventQueues Q, EventCtl* ctl) {
+                                                 Bank B, EventQueues Q, EventCtl* ctl, int64_t limit) {
   LocalCounters L;
   L.zero();
-  const int64_t m = a.n < B.cap ? a.n : B.cap;
+  int64_t m = a.n < B.cap ? a.n : B.cap;
+  if (limit < m) m = limit;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
     Particle p;
     birth(M, X, S, a, a.first + i, p);
     if (p.status != kAlive) {
       finish(p, a, L);
-      push(Q.free_slots, &ctl->n_free, (int)i);
+      push_free(Q, ctl, (int)i, B.cap);
       continue;
     }
     store(B, (int)i, p);
     push(Q.xs[0], &ctl->n_xs[0], (int)i);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->next_hist = m;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->next_hist = m;
+    ctl->birth_limit = limit;
+  }
   flush(L, a.counters, a.leak_w);
 }
 
@@ -244,7 +289,7 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
       push(Q.adv[par], &ctl->n_adv[par], s);
     } else {
       finish(p, a, L);
-      push(Q.free_slots, &ctl->n_free, s);
+      push_free(Q, ctl, s, B.cap);
     }
   }
   flush(L, a.counters, a.leak_w);
@@ -269,7 +314,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       for (;;) {
-        r = segment_fp64g<false>(M, X, p, uf, vf, wf, a.tally, sigt32, nxs);
+        r = segment_fp64g<false>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
         if (r == 5) {
           uf = (float)p.u;
           vf = (float)p.v;
@@ -287,7 +332,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       geo_load(p, g);
       float inv_sig = (float)(1.0 / p.sigt);
       for (;;) {
-        r = segment_mixed<false>(M, X, p, g, a.tally, inv_sig, a.tol, nxs, nfb);
+        r = segment_mixed<false>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
         if (r != 0) break;
         if (a.max_seg > 0 && ++k >= a.max_seg) {
           r = 4;
@@ -299,7 +344,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
     L.c[kCntFallback] += nfb;
     if (r == 2) {
       finish(p, a, L);
-      push(Q.free_slots, &ctl->n_free, s);
+      push_free(Q, ctl, s, B.cap);
       continue;
     }
     store(B, s, p);
@@ -348,7 +393,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     if (s < 0) continue;
     int r;
     if (kPrec == MC_PREC_FP64) {
-      r = segment_fp64g<false>(M, X, p, g.u, g.v, g.w, a.tally, f32, nxs);
+      r = segment_fp64g<false>(M, X, p, g.u, g.v, g.w, tally_of(a, p.tag), f32, nxs);
       if (r == 5) {
         g.u = (float)p.u;
         g.v = (float)p.v;
@@ -356,7 +401,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
         r = 0;
       }
     } else {
-      r = segment_mixed<false>(M, X, p, g, a.tally, f32, a.tol, nxs, nfb);
+      r = segment_mixed<false>(M, X, p, g, tally_of(a, p.tag), f32, a.tol, nxs, nfb);
     }
     if (r == 0) {
       if (a.max_seg <= 0 || ++k < a.max_seg) continue;
@@ -365,7 +410,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     if (kPrec != MC_PREC_FP64) geo_store(g, p);
     if (r == 2) {
       finish(p, a, L);
-      push(Q.free_slots, &ctl->n_free, s);
+      push_free(Q, ctl, s, B.cap);
     } else {
       store(B, s, p);
       if (r == 1) push(Q.coll, &ctl->n_coll, s);
@@ -406,6 +451,7 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
     int elem = B.elem[s], fin = B.fin[s], mat = B.mat[s], n_seg = B.n_seg[s], zrun = B.zero_run[s];
     uint64_t seed = B.seed[s], hash = B.hash[s];
     const double wgt = B.wgt[s];
+    double* const tal = tally_of(a, B.tag[s]);
     const int4 cm = B.cm[s];
     const float4 ci = B.cinv[s];
     int slot = -1;  // cache slot whose Sigma_t is current, if the walk changed material
@@ -473,7 +519,7 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
       const float dist = -__logf(xi) * inv_sig;
       const bool cross = dist > Ls;
       const float score = cross ? Ls : dist;
-      atomicAdd(a.tally + elem, wgt == 1.0 ? (double)score : wgt * (double)score);
+      atomicAdd(tal + elem, wgt == 1.0 ? (double)score : wgt * (double)score);
       ++n_seg;
       if (Ls == 0.0f) ++zrun;
       else zrun = 0;
@@ -533,7 +579,7 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
         p.status = face == -3 ? kBadXS : kStuck;
       }
       finish(p, a, L);
-      push(Q.free_slots, &ctl->n_free, s);
+      push_free(Q, ctl, s, B.cap);
       continue;
     }
     B.x[s] = x; B.y[s] = y; B.z[s] = z;
@@ -570,7 +616,7 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
     collide(X, p);
     if (p.status != kAlive) {
       finish(p, a, L);
-      push(Q.free_slots, &ctl->n_free, s);
+      push_free(Q, ctl, s, B.cap);
       continue;
     }
     B.u[s] = p.u; B.v[s] = p.v; B.w[s] = p.w;
@@ -581,24 +627,23 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
   flush(L, a.counters, a.leak_w);
 }
 
-// New histories into the slots freed this iteration: free slot i takes
-// history next_hist + i while histories remain.
+// New histories into free slots: the i-th free slot of the ring takes
+// history next_hist + i, as far as histories below the birth limit remain.
 __global__ void __launch_bounds__(256) k_ev_refill(DevMesh M, DevXS X, DevSource S, RunArgs a,
                                                    Bank B, EventQueues Q, EventCtl* ctl, int par) {
   LocalCounters L;
   L.zero();
-  const int nf = *(volatile int*)&ctl->n_free;
   const long long base = *(volatile long long*)&ctl->next_hist;
-  const long long left = a.n - base;
-  const int n = (int)(left < (long long)nf ? (left > 0 ? left : 0) : nf);
+  const unsigned long long head = *(volatile unsigned long long*)&ctl->free_head;
+  const long long n = births_now(ctl, a.n);
   const int nxt = par ^ 1;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int s = Q.free_slots[i];
+  for (long long i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = Q.free_slots[(head + (unsigned long long)i) % (unsigned long long)B.cap];
     Particle p;
     birth(M, X, S, a, a.first + base + i, p);
     if (p.status != kAlive) {
       finish(p, a, L);
-      continue;  // slot stays empty for the rest of the batch
+      continue;  // slot stays empty for the rest of the run
     }
     store(B, s, p);
     push(Q.xs[nxt], &ctl->n_xs[nxt], s);
@@ -606,14 +651,13 @@ __global__ void __launch_bounds__(256) k_ev_refill(DevMesh M, DevXS X, DevSource
   flush(L, a.counters, a.leak_w);
 }
 
-// End of an iteration: consumed queues emptied, births committed.  Free
-// slots never outlive an iteration: either all were refilled, or every
-// remaining history was born and the spare slots are not needed again.
+// End of an iteration: consumed queues emptied, births committed (the same
+// count the refill computed: no slot is freed between the two launches).
 __global__ void k_ev_reset(EventCtl* ctl, int par, int64_t n) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    long long nh = ctl->next_hist + (long long)ctl->n_free;
-    ctl->next_hist = nh < n ? nh : n;
-    ctl->n_free = 0;
+    const long long b = births_now(ctl, n);
+    ctl->next_hist += b;
+    ctl->free_head += (unsigned long long)b;
     ctl->n_xs[par] = 0;
     ctl->n_adv[par] = 0;
     ctl->n_coll = 0;
@@ -639,7 +683,7 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, a.tally, sigt32, nxs);
+        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
         if (r == 1) collide(X, p);
         if (r == 1 || r == 5) {
           uf = (float)p.u;
@@ -652,7 +696,7 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       geo_load(p, g);
       float inv_sig = (p.mat >= 0) ? (float)(1.0 / p.sigt) : 0.0f;
       while (p.status == kAlive) {
-        const int r = segment_mixed<true>(M, X, p, g, a.tally, inv_sig, a.tol, nxs, nfb);
+        const int r = segment_mixed<true>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
         if (r == 1) {
           geo_store(g, p);
           collide(X, p);
@@ -700,10 +744,10 @@ cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S,
 
 cudaError_t launch_event_init(const DevMesh& M, const DevXS& X, const DevSource& S,
                               const RunArgs& a, const Bank& B, const EventQueues& Q,
-                              EventCtl* ctl, int block, int grid, cudaStream_t st) {
+                              EventCtl* ctl, int block, int grid, cudaStream_t st, int64_t birth_limit) {
   cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(EventCtl), st);
   if (e != cudaSuccess) return e;
-  k_ev_init<<<grid, block, 0, st>>>(M, X, S, a, B, Q, ctl);
+  k_ev_init<<<grid, block, 0, st>>>(M, X, S, a, B, Q, ctl, birth_limit);
   return cudaGetLastError();
 }
 

@@ -29,7 +29,7 @@ struct Bank {
   double *x, *y, *z, *u, *v, *w, *E, *wgt, *sigt;
   uint64_t *seed, *hash;
   int64_t* id;
-  int *elem, *mat, *n_seg, *n_coll, *zero_run, *fin;
+  int *elem, *mat, *n_seg, *n_coll, *zero_run, *fin, *tag;
   int4* cm;            // cross-section cache keys
   double4_32a* cs;     // cross-section cache values
   float4* cinv;        // float 1/Sigma_t of the cached values (mixed-precision walk)
@@ -39,24 +39,28 @@ struct Bank {
 // Event-loop control block (device memory).
 struct EventCtl {
   int n_xs[2], n_adv[2], n_coll;   // queue lengths, double-buffered by iteration parity
-  int n_free;                       // slots freed this iteration
   int adv_head;                     // advance queue entries taken so far this iteration
-  int pad;
-  long long next_hist;              // next history (relative to the batch) to be born
-  long long pad2;
+  unsigned long long free_head, free_tail;  // ring of free bank slots (monotonic counters)
+  long long next_hist;              // next history (relative to the run) to be born
+  long long birth_limit;            // histories at or past this index wait (pipelined batches)
+  int live[2];                      // particles in flight per batch parity
 };
 
 struct EventQueues {
   int* xs[2];
   int* adv[2];
   int* coll;
-  int* free_slots;
+  int* free_slots;  // ring of bank-capacity entries
 };
 
 struct RunArgs {
   int64_t first, n;
   uint64_t master;
-  double* tally;
+  double* tally;                // scores of even batches
+  double* tally2;               // scores of odd batches (== tally for a single batch)
+  const int64_t* batch_end;     // device: end of each batch (relative index), or null
+  int n_batches;
+  int* live;                    // event mode: in-flight counters per batch parity, or null
   mc_trace* traces;
   unsigned long long* counters;
   double* leak_w;
@@ -75,7 +79,7 @@ cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S,
 // device-side queue lengths), so the launch shapes never depend on counts.
 cudaError_t launch_event_init(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
                               const Bank& B, const EventQueues& Q, EventCtl* ctl, int block,
-                              int grid, cudaStream_t st);
+                              int grid, cudaStream_t st, int64_t birth_limit);
 cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSource& S,
                                    const RunArgs& a, const Bank& B, const EventQueues& Q,
                                    EventCtl* ctl, int parity, int block, int grid,

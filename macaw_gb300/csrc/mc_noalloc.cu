@@ -148,6 +148,10 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.n = d->n_histories;
   a.master = d->seed;
   a.tally = tally;
+  a.tally2 = tally;
+  a.batch_end = nullptr;
+  a.n_batches = 1;
+  a.live = nullptr;
   a.traces = d->record_traces ? traces : nullptr;
   a.counters = counters;
   a.leak_w = leak_w;
@@ -160,7 +164,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   const int grid = std::max(1, v.n_sm * (2048 / block));
   int n_launch = 0;
   if (d->n_histories > 0) {
-    e = launch_event_init(v.M, v.X, v.S, a, B, Q, ctl, block, grid, st);
+    e = launch_event_init(v.M, v.X, v.S, a, B, Q, ctl, block, grid, st, a.n);
     if (e != cudaSuccess) return fail(MC_ERR_CUDA, std::string("event init: ") + cudaGetErrorString(e));
     n_launch = 1;
     int par = 0;

@@ -1,0 +1,77 @@
+"""Batches of uneven size run through one event pipeline.
+
+Batch b scores into its own tally (two alternate) and is folded into
+SUM/SUM_SQ, normalised by its size, when its last particle ends; the next
+batch's births fill the bank meanwhile.  The result must equal one mc_run
+per batch: SUM and SUM_SQ within 1e-12, per-history traces bit for bit.
+"""
+import numpy as np
+import pytest
+
+from macaw_gb300 import Tracker, problems
+from macaw_gb300._lib import (MC_MODE_EVENT, MC_MODE_HISTORY, MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM,
+                              MC_TALLY_SUM_SQ)
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [3000, 5000, 1000, 7000, 2500]
+
+
+def close(a, b, rtol=1e-12):
+    nz = b != 0
+    return np.all(a[~nz] == 0) and np.all(np.abs(a[nz] - b[nz]) <= rtol * np.abs(b[nz]))
+
+
+@pytest.fixture(scope="module")
+def cube():
+    return problems.cube_problem(n=10, L=10.0, n_nuc=5, n_pts=3000)
+
+
+@pytest.fixture(scope="module")
+def separate(cube):
+    with Tracker(0) as t:
+        t.load(cube)
+        first = 0
+        trs = []
+        for s in SIZES:
+            t.run(s, first=first, seed=5, mode=MC_MODE_EVENT, accumulate=True, traces=True)
+            trs.append(t.traces(s))
+            first += s
+        return t.tally(MC_TALLY_SUM), t.tally(MC_TALLY_SUM_SQ), np.concatenate(trs)
+
+
+@pytest.mark.parametrize("mode,bank", [(MC_MODE_EVENT, 2048), (MC_MODE_EVENT, 40000), (MC_MODE_HISTORY, 0)])
+def test_pipelined_batches_equal_separate_runs(cube, separate, mode, bank):
+    s_ref, sq_ref, tr_ref = separate
+    n = sum(SIZES)
+    with Tracker(0) as t:
+        t.load(cube)
+        st = t.run(n, seed=5, mode=mode, bank_size=bank, accumulate=True, traces=True, batch_sizes=SIZES)
+        assert st.n_hist == n
+        assert t.batches_done() == len(SIZES)
+        tr = t.traces(n)
+        for f in ("hash", "status", "n_seg", "n_coll", "elem", "face"):
+            assert np.array_equal(tr[f], tr_ref[f]), f
+        assert close(t.tally(MC_TALLY_SUM), s_ref)
+        assert close(t.tally(MC_TALLY_SUM_SQ), sq_ref)
+        assert np.all(t.tally() == 0)
+
+
+def test_pipelined_mixed_batches_keep_every_particle(cube):
+    n = sum(SIZES)
+    with Tracker(0) as t:
+        t.load(cube)
+        st = t.run(n, seed=5, mode=MC_MODE_EVENT, precision=MC_PREC_MIXED, bank_size=4096,
+                   max_seg=64, accumulate=True, batch_sizes=SIZES)
+        assert st.n_hist == n and st.n_stuck == 0 and st.n_lost == 0
+        assert t.batches_done() == len(SIZES)
+
+
+def test_batch_arguments_are_checked(cube):
+    from macaw_gb300 import MCError
+    with Tracker(0) as t:
+        t.load(cube)
+        with pytest.raises(MCError, match="add up"):
+            t.run(100, accumulate=True, batch_sizes=[40, 50])
+        with pytest.raises(MCError, match="accumulate"):
+            t.run(90, accumulate=False, batch_sizes=[40, 50])
