@@ -56,7 +56,7 @@ def workload_config():
     return {"workload": "lattice 17x17 pins, pitch 1.26 cm, 50 cm, 2,039,184 tets, 3 materials "
                         "(15/4/3 nuclides x 20,000 pts), cylinder source, 1e6 histories per step",
             "tets": 2039184, "histories_per_step": HIST_PER_STEP, "bank_size": BANK,
-            "precision": "fp64", "mode": "event", "advance_refill": False,
+            "precision": "fp64", "mode": "event",
             "l2": "inputs larger than L2 (mesh planes 261 MB, tally 16 MB vs 129 MB L2)"}
 
 
@@ -171,10 +171,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="event", choices=["event", "history"])
-    ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
     ap.add_argument("--no-mixed", action="store_true")
-    ap.add_argument("--refill", type=int, default=0, help="advance lanes take further queued particles")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (fixed parameters)")
+    ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -191,115 +190,94 @@ def main():
         dist.init_process_group("nccl")
 
     from macaw_gb300 import Tracker, problems
-    from macaw_gb300._lib import (MC_MODE_EVENT, MC_MODE_HISTORY, MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM,
-                                  SITE_DTYPE)
+    from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM, SITE_DTYPE
 
-    mode = MC_MODE_EVENT if args.mode == "event" else MC_MODE_HISTORY
-    n = args.hist
+    n, K, W = args.hist, args.steps, args.warmup
     p = problems.lattice_problem()
-    t = Tracker(local)
-    t.load(p)
     stream = torch.cuda.Stream()
-    t.set_stream(stream.cuda_stream)
-    # each rank owns a disjoint range of history indices
-    base = rank * (args.warmup + 2 * args.steps + 2) * n
-
-    def step(k, tr=None, precision=MC_PREC_FP64, **kw):
-        return (tr or t).run(n, first=base + k * n, seed=1, mode=mode, bank_size=BANK, accumulate=True,
-                             precision=precision, refill=bool(args.refill), **kw)
-
-    for w in range(args.warmup):
-        step(w)
+    # each rank owns a disjoint range of history indices (weak scaling)
+    base = rank * (W + 2 * K + 2) * n
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    # --- device-resident timing ---
+    def tracker():
+        t = Tracker(local)
+        t.load(p)
+        t.set_stream(stream.cuda_stream)
+        return t
+
+    def tune(t, precision):
+        fixed = {"bank_size": BANK, "block_size": 256, "max_seg": 64, "sort_queue": 0, "refill": False}
+        if args.no_tune:
+            return fixed, None
+        params, rate = t.autotune(trial=min(n, 300_000), first=base + (W + 2 * K + 1) * n, bank_size=BANK,
+                                  precision=precision, block_size=256, max_seg=64)
+        return params, rate
+
+    def timed(t, precision, params, first_step, steps, profile):
+        """steps batches of n histories through one pipelined call; device ms."""
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = t.run(n * steps, first=base + first_step * n, seed=1, precision=precision, accumulate=True,
+                   batch_sizes=[n] * steps, profile=profile, **params)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            tt = torch.tensor([ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms, st
+
+    # --- FP64 (the configuration the metric is quoted on) ---
+    t = tracker()
+    params64, tune64 = tune(t, MC_PREC_FP64)
+    timed(t, MC_PREC_FP64, params64, 0, W, False)
     clocks = ClockSampler(local)
-    barrier()
-    torch.cuda.synchronize()
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    segs = colls = launches = 0
-    ms_adv = 0.0
-    adv_launch = 0
-    for k in range(args.steps):
-        s = step(args.warmup + k, profile=True)
-        segs += s.n_seg
-        colls += s.n_coll
-        launches += s.n_launch
-        ms_adv += s.ms_advance
-        adv_launch += s.n_advance_launch
-        if s.n_stuck or s.n_lost:
-            print(f"warning: stuck={s.n_stuck} lost={s.n_lost}", file=sys.stderr)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
+    ms, st = timed(t, MC_PREC_FP64, params64, W, K, True)
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * n * args.steps / (ms / 1e3)
+    value = world * n * K / (ms / 1e3)
     sum64 = t.tally(MC_TALLY_SUM)
 
-    # --- mixed-precision form on the same histories (second context) ---
+    # --- mixed-precision form on the same histories ---
     mixed = None
     if not args.no_mixed:
-        tm = Tracker(local)
-        tm.load(p)
-        tm.set_stream(stream.cuda_stream)
-        for w in range(args.warmup):
-            step(w, tr=tm, precision=MC_PREC_MIXED)
-        barrier()
-        torch.cuda.synchronize()
-        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        m0.record(stream)
-        msegs = mfb = mstuck = mlost = mlaunch = 0
-        for k in range(args.steps):
-            s = step(args.warmup + k, tr=tm, precision=MC_PREC_MIXED)
-            msegs += s.n_seg
-            mfb += s.n_fallback
-            mstuck += s.n_stuck
-            mlost += s.n_lost
-            mlaunch += s.n_launch
-        m1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        mms = m0.elapsed_time(m1)
-        if dist is not None:
-            tt = torch.tensor([mms], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            mms = float(tt.item())
+        tm = tracker()
+        paramsm, tunem = tune(tm, MC_PREC_MIXED)
+        timed(tm, MC_PREC_MIXED, paramsm, 0, W, False)
+        mms, mst = timed(tm, MC_PREC_MIXED, paramsm, W, K, False)
         summ = tm.tally(MC_TALLY_SUM)
         tm.close()
         nz = sum64 > 0
         rel = np.abs(summ[nz] - sum64[nz]) / sum64[nz]
-        mixed = {"value": world * n * args.steps / (mms / 1e3), "unit": "histories/s",
-                 "ms_per_step": mms / args.steps, "speedup_vs_fp64": ms / mms,
-                 "fallback_fraction": mfb / max(msegs, 1), "stuck": int(mstuck), "lost": int(mlost),
+        mixed = {"value": world * n * K / (mms / 1e3), "unit": "histories/s", "ms_per_step": mms / K,
+                 "speedup_vs_fp64": ms / mms, "fallback_fraction": mst.n_fallback / max(mst.n_seg, 1),
+                 "stuck": int(mst.n_stuck), "lost": int(mst.n_lost),
                  "flux_rel_diff_mean": float(rel.mean()), "flux_rel_diff_max": float(rel.max()),
                  "flux_rel_diff_note": "element SUM tallies, mixed vs FP64 (bit-exact to the oracle), same "
-                                       f"{n * (args.warmup + args.steps)} histories, elements with a score",
-                 "gpu_launches": mlaunch}
+                                       f"{n * (W + K)} histories, elements with a score",
+                 "tuned": paramsm, "gpu_launches": int(mst.n_launch)}
 
-    # --- end to end through the C ABI with host buffers ---
-    k0 = args.warmup + args.steps
-    sites = [torch.empty(n * SITE_DTYPE.itemsize, dtype=torch.uint8).pin_memory() for _ in range(args.steps)]
-    site_np = [s.numpy().view(SITE_DTYPE) for s in sites]
-    for k in range(args.steps):
+    # --- end to end through the C ABI with host buffers, one call per step ---
+    k0 = W + K
+    sites = [torch.empty(n * SITE_DTYPE.itemsize, dtype=torch.uint8).pin_memory() for _ in range(K)]
+    site_np = [x.numpy().view(SITE_DTYPE) for x in sites]
+    for k in range(K):
         t.sample_sites(n, first=base + (k0 + k) * n, seed=1, out=site_np[k])
     out = torch.empty(p.n_tet, dtype=torch.float64).pin_memory()
     out_np = out.numpy()
     barrier()
     torch.cuda.synchronize()
     w0 = time.perf_counter()
-    for k in range(args.steps):
-        t.run(n, first=base + (k0 + k) * n, seed=1, mode=mode, bank_size=BANK, accumulate=True,
-              sites=site_np[k], refill=bool(args.refill))
+    for k in range(K):
+        t.run(n, first=base + (k0 + k) * n, seed=1, precision=MC_PREC_FP64, accumulate=True,
+              sites=site_np[k], **params64)
         t.tally(MC_TALLY_SUM, out=out_np)
     torch.cuda.synchronize()
     barrier()
@@ -308,30 +286,35 @@ def main():
         tt = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e2e_s = float(tt.item())
-    e2e = {"value": world * n * args.steps / e2e_s, "unit": "histories/s",
-           "h2d_bytes_per_step": n * SITE_DTYPE.itemsize, "d2h_bytes_per_step": p.n_tet * 8}
+    e2e = {"value": world * n * K / e2e_s, "unit": "histories/s",
+           "h2d_bytes_per_step": n * SITE_DTYPE.itemsize, "d2h_bytes_per_step": p.n_tet * 8,
+           "note": "one mc_run per step (1e6 host sites copied in, SUM tally copied out)"}
 
     if rank == 0:
         peak, peak_kind = load_peaks()
+        segs = st.n_seg
         adv_bytes = segs * B_SEG_FP64
-        achieved = adv_bytes / (ms_adv / 1e3) / 1e9 if ms_adv > 0 else None
-        roof = {"bound": "hbm", "kernel": "k_ev_advance" if mode == MC_MODE_EVENT else "k_history",
+        achieved = adv_bytes / (st.ms_advance / 1e3) / 1e9 if st.ms_advance > 0 else None
+        roof = {"bound": "hbm", "kernel": "k_ev_advance_static<FP64>",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * segs / max(adv_launch, 1))
+                "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * segs / max(st.n_advance_launch, 1))
                 if ADVANCE_DRAM_BYTES_PER_SEG else None,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes_per_segment": B_SEG_FP64,
-                "advance_ms_per_launch": ms_adv / max(adv_launch, 1),
-                "advance_share_of_step": ms_adv / ms if ms > 0 else None}
-        line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "advance_ms_per_launch": st.ms_advance / max(st.n_advance_launch, 1),
+                "advance_share_of_step": st.ms_advance / ms if ms > 0 else None,
+                "note": "the FP64 walk is bound by GB300's FP64 pipe, not HBM (see profiles/)"}
+        cfg = dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single",
+                   pipelined_batches=K, tuned=params64)
+        line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": K,
+                "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded generators; the reference's meshes and ENDF data are not shipped)",
-                "config": dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single"),
-                "segments_per_s": world * segs / (ms / 1e3), "segments_per_history": segs / (n * args.steps),
-                "collisions_per_history": colls / (n * args.steps),
-                "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+                "config": cfg, "segments_per_s": world * segs / (ms / 1e3), "segments_per_history": segs / (n * K),
+                "collisions_per_history": st.n_coll / (n * K),
+                "stuck": int(st.n_stuck), "lost": int(st.n_lost),
+                "roofline": roof, "e2e": e2e, "gpu_launches": int(st.n_launch), "clocks": clk}
         if mixed is not None:
             line["mixed"] = mixed
         if world == 1 and not args.no_cpu_baseline:

@@ -106,7 +106,8 @@ typedef struct {
   int32_t max_seg_per_advance; /* event mode: segments per advance launch; 0 = until event */
   int32_t record_traces;   /* 1: fill one mc_trace per history */
   int32_t accumulate;      /* 1: fold this batch into SUM/SUM_SQ and clear the batch tally */
-  int32_t sort_queue;      /* event mode: 1 sorts the advance queue by element */
+  int32_t sort_queue;      /* event mode: 0 off; s > 0 orders the advance queue by element id >> (s-1)
+                              (coarsened to at most 65536 buckets) before each walk launch */
   int32_t profile;         /* 1: time every advance launch with CUDA events (mc_stats.ms_advance) */
   int32_t refill;          /* event mode: 1 lets an advance lane take the next queued particle when
                               its particle reaches an event; 0 one particle per lane per launch */
@@ -192,12 +193,23 @@ int mc_source_sample(mc_ctx* ctx, int64_t first, int64_t n, uint64_t seed, mc_si
 /* Work of this context goes to the given cudaStream_t (NULL: the context's
  * own stream). */
 int mc_ctx_set_stream(mc_ctx* ctx, void* stream);
+/* Autotuner (no counterpart in the reference, whose MPI/thread layout is set
+ * by hand on the command line): picks segments per walk launch, threads per
+ * block, advance-queue ordering, bank size and lane refill of the event form
+ * that give the most histories/s on trial batches of trial_histories
+ * (>= 1024) histories of this context's problem, starting from *base;
+ * writes *base with those fields replaced to *best and the rate reached to
+ * *best_rate.  Trial scores go to the batch tally, which is cleared. */
+int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_histories, mc_run_desc* best,
+                double* best_rate);
 
 /* ---- results --------------------------------------------------------- */
 /* Replaces: OpenMCTallyAux::computeValue element readback
  * (src/auxkernels/OpenMCTallyAux.C:187-205), for the element flux tally. */
 int mc_tally_download(mc_ctx* ctx, int32_t kind, double* out, int64_t n);
 int mc_tally_reset(mc_ctx* ctx);
+/* Clears one tally (MC_TALLY_BATCH, MC_TALLY_SUM or MC_TALLY_SUM_SQ). */
+int mc_tally_clear(mc_ctx* ctx, int32_t kind);
 int mc_trace_download(mc_ctx* ctx, mc_trace* out, int64_t n);
 int mc_stats_get(mc_ctx* ctx, mc_stats* out);
 /* Number of completed accumulated batches (OpenMC n_realizations). */

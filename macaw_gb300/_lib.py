@@ -82,6 +82,8 @@ SIGNATURES = {
     "mc_app_check": ([C.c_char_p, C.c_char_p, _I64], C.c_int),
     "mc_tally_download": ([_P, _I32, _P, _I64], C.c_int),
     "mc_tally_reset": ([_P], C.c_int),
+    "mc_tally_clear": ([_P, _I32], C.c_int),
+    "mc_autotune": ([_P, C.POINTER(RunDesc), _I64, C.POINTER(RunDesc), C.POINTER(_D)], C.c_int),
     "mc_trace_download": ([_P, _P, _I64], C.c_int),
     "mc_stats_get": ([_P, C.POINTER(Stats)], C.c_int),
     "mc_batches_done": ([_P, C.POINTER(_I64)], C.c_int),

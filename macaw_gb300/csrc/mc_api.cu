@@ -80,11 +80,12 @@ struct mc_ctx {
   int64_t trace_n = 0;
   DevBuf d_sites;
   DevBuf d_tally2, d_batch_end;
+  DevBuf d_sort_tmp, d_sort_cnt;
   bool tally2_clear = false;
   long long h_limit = 0;
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
-  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_cm, b_cs, b_cinv;
+  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_tag, b_cm, b_cs, b_cinv;
   DevBuf q_xs0, q_xs1, q_adv0, q_adv1, q_coll, q_free, d_ctl;
   int64_t bank_cap = 0;
 
@@ -166,7 +167,7 @@ int ensure_device_tables(mc_ctx* c) {
 }
 
 DevMesh dev_mesh(mc_ctx* c) {
-  DevMesh M;
+  DevMesh M{};
   M.planes = c->d_planes.as<double4_32a>();
   M.planes32 = c->d_planes32.as<float4>();
   M.nbr = c->d_nbr.as<int4>();
@@ -185,7 +186,7 @@ DevMesh dev_mesh(mc_ctx* c) {
 }
 
 DevXS dev_xs(mc_ctx* c) {
-  DevXS X;
+  DevXS X{};
   X.gE = c->d_gE.as<double>();
   X.g_off = c->d_goff.as<int64_t>();
   X.g_n = c->d_gn.as<int>();
@@ -208,7 +209,7 @@ DevXS dev_xs(mc_ctx* c) {
 }
 
 DevSource dev_source(mc_ctx* c) {
-  DevSource S;
+  DevSource S{};
   S.space = c->src.space;
   S.energy = c->src.energy;
   for (int k = 0; k < 3; ++k) {
@@ -233,7 +234,7 @@ int ensure_bank(mc_ctx* c, int64_t cap) {
   DevBuf* d8[] = {&c->b_x, &c->b_y, &c->b_z, &c->b_u, &c->b_v, &c->b_w, &c->b_E,
                   &c->b_wgt, &c->b_sigt, &c->b_seed, &c->b_hash, &c->b_id};
   for (DevBuf* b : d8) CK(b->alloc(n * 8), "allocate particle bank");
-  DevBuf* d4[] = {&c->b_elem, &c->b_mat, &c->b_nseg, &c->b_ncoll, &c->b_zero, &c->b_fin,
+  DevBuf* d4[] = {&c->b_elem, &c->b_mat, &c->b_nseg, &c->b_ncoll, &c->b_zero, &c->b_fin, &c->b_tag,
                   &c->q_xs0, &c->q_xs1, &c->q_adv0, &c->q_adv1, &c->q_coll, &c->q_free};
   for (DevBuf* b : d4) CK(b->alloc(n * 4), "allocate particle bank");
   CK(c->b_cm.alloc(n * 16), "allocate particle bank");
@@ -245,7 +246,7 @@ int ensure_bank(mc_ctx* c, int64_t cap) {
 }
 
 Bank dev_bank(mc_ctx* c) {
-  Bank B;
+  Bank B{};
   B.x = c->b_x.as<double>(); B.y = c->b_y.as<double>(); B.z = c->b_z.as<double>();
   B.u = c->b_u.as<double>(); B.v = c->b_v.as<double>(); B.w = c->b_w.as<double>();
   B.E = c->b_E.as<double>(); B.wgt = c->b_wgt.as<double>(); B.sigt = c->b_sigt.as<double>();
@@ -254,12 +255,13 @@ Bank dev_bank(mc_ctx* c) {
   B.n_coll = c->b_ncoll.as<int>(); B.zero_run = c->b_zero.as<int>();
   B.cm = c->b_cm.as<int4>(); B.cs = c->b_cs.as<double4_32a>(); B.fin = c->b_fin.as<int>();
   B.cinv = c->b_cinv.as<float4>();
+  B.tag = c->b_tag.as<int>();
   B.cap = c->bank_cap;
   return B;
 }
 
 EventQueues dev_queues(mc_ctx* c) {
-  EventQueues Q;
+  EventQueues Q{};
   Q.xs[0] = c->q_xs0.as<int>();
   Q.xs[1] = c->q_xs1.as<int>();
   Q.adv[0] = c->q_adv0.as<int>();
@@ -472,7 +474,7 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   }
   CK(cudaMemsetAsync(c->d_counters.p, 0, c->d_counters.bytes, c->stream), "clear counters");
   CK(cudaMemsetAsync(c->d_leak_w.p, 0, sizeof(double), c->stream), "clear counters");
-  RunArgs a;
+  RunArgs a{};
   a.first = d->first_history;
   a.n = d->n_histories;
   a.master = d->seed;
@@ -483,6 +485,18 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.precision = d->precision;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.sort_shift = -1;
+  a.sort_buckets = 0;
+  a.sort_tmp = nullptr;
+  a.sort_cnt = nullptr;
+  if (d->sort_queue > 0 && d->mode == MC_MODE_EVENT) {
+    // key = elem >> shift with at most 65536 buckets
+    int shift = d->sort_queue - 1;
+    while ((c->mesh.n_tet >> shift) >= 65536) ++shift;
+    a.sort_shift = shift;
+    a.sort_buckets = (int)(c->mesh.n_tet >> shift) + 1;
+    CK(c->d_sort_cnt.alloc(sizeof(int) * (size_t)(a.sort_buckets + 1)), "allocate sort counters");
+  }
   a.sites = nullptr;
   a.n_mat = (int)c->xs.mat_ids.size();
   {
@@ -572,9 +586,15 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       rc = ensure_bank(c, std::max(cap, c->bank_cap));
       if (rc) return rc;
       const Bank B = dev_bank(c);
+      if (!bank_complete(B)) return set_err(c, MC_ERR_STATE, "internal: particle bank incomplete");
       const EventQueues Q = dev_queues(c);
       EventCtl* ctl = c->d_ctl.as<EventCtl>();
       if (nb > 1) a.live = ctl->live;
+      if (a.sort_shift >= 0) {
+        CK(c->d_sort_tmp.alloc(std::max(c->d_sort_tmp.bytes, sizeof(int) * (size_t)c->bank_cap)), "allocate sort");
+        a.sort_tmp = c->d_sort_tmp.as<int>();
+        a.sort_cnt = c->d_sort_cnt.as<int>();
+      }
       int64_t limit = nb > 1 ? bend[std::min(1, nb - 1)] : d->n_histories;
       CK(launch_event_init(M, X, S, a, B, Q, ctl, block, grid, c->stream, limit), "launch event init");
       n_launch = 1;
@@ -742,6 +762,19 @@ int mc_tally_reset(mc_ctx* c) {
   CK(cudaMemsetAsync(c->d_sumsq.p, 0, c->d_sumsq.bytes, c->stream), "clear tally");
   CK(cudaStreamSynchronize(c->stream), "clear tally");
   c->batches = 0;
+  return MC_OK;
+}
+
+int mc_tally_clear(mc_ctx* c, int32_t kind) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh");
+  DevBuf* b = kind == MC_TALLY_BATCH ? &c->d_tally : kind == MC_TALLY_SUM ? &c->d_sum
+              : kind == MC_TALLY_SUM_SQ ? &c->d_sumsq : nullptr;
+  if (!b) return set_err(c, MC_ERR_ARG, "unknown tally kind");
+  cudaSetDevice(c->device);
+  CK(cudaMemsetAsync(b->p, 0, b->bytes, c->stream), "clear tally");
+  CK(cudaStreamSynchronize(c->stream), "clear tally");
   return MC_OK;
 }
 

@@ -722,6 +722,52 @@ __global__ void __launch_bounds__(256) k_sample(DevXS X, DevSource S, int64_t fi
   }
 }
 
+// Counting sort of the advance queue by a coarse element key, so the warps
+// of the walk start in nearby elements (better L1/L2 reuse of tet records).
+__global__ void k_sort_copy(const int* __restrict__ q, int* __restrict__ tmp, const EventCtl* ctl, int par) {
+  const int n = *(volatile const int*)&ctl->n_adv[par];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) tmp[i] = q[i];
+}
+
+__global__ void k_sort_count(const int* __restrict__ tmp, const int* __restrict__ elem, int* cnt, int shift,
+                             const EventCtl* ctl, int par) {
+  const int n = *(volatile const int*)&ctl->n_adv[par];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(cnt + (elem[tmp[i]] >> shift), 1);
+}
+
+// Exclusive scan of nb counters in one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_sort_scan(int* cnt, int nb) {
+  __shared__ int part[1024];
+  const int per = (nb + 1023) / 1024;
+  const int b0 = threadIdx.x * per;
+  int sum = 0;
+  for (int i = b0; i < b0 + per && i < nb; ++i) sum += cnt[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int i = b0; i < b0 + per && i < nb; ++i) {
+    const int c = cnt[i];
+    cnt[i] = run;
+    run += c;
+  }
+}
+
+__global__ void k_sort_scatter(const int* __restrict__ tmp, const int* __restrict__ elem, int* cnt, int* q,
+                               int shift, const EventCtl* ctl, int par) {
+  const int n = *(volatile const int*)&ctl->n_adv[par];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = tmp[i];
+    q[atomicAdd(cnt + (elem[s] >> shift), 1)] = s;
+  }
+}
+
 __global__ void k_accumulate(double* __restrict__ batch, double* __restrict__ sum,
                              double* __restrict__ sumsq, int64_t n, double inv_w) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -756,6 +802,14 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
                                    EventCtl* ctl, int par, int block, int grid, cudaStream_t st,
                                    int* n_launch, cudaEvent_t adv0, cudaEvent_t adv1) {
   k_ev_xs<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.sort_shift >= 0) {
+    cudaMemsetAsync(a.sort_cnt, 0, sizeof(int) * (size_t)(a.sort_buckets + 1), st);
+    k_sort_copy<<<grid, block, 0, st>>>(Q.adv[par], a.sort_tmp, ctl, par);
+    k_sort_count<<<grid, block, 0, st>>>(a.sort_tmp, B.elem, a.sort_cnt, a.sort_shift, ctl, par);
+    k_sort_scan<<<1, 1024, 0, st>>>(a.sort_cnt, a.sort_buckets);
+    k_sort_scatter<<<grid, block, 0, st>>>(a.sort_tmp, B.elem, a.sort_cnt, Q.adv[par], a.sort_shift, ctl, par);
+    if (n_launch) *n_launch += 4;
+  }
   if (adv0) cudaEventRecord(adv0, st);
   if (a.refill) {
     if (a.precision == MC_PREC_MIXED) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);

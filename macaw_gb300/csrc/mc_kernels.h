@@ -36,6 +36,16 @@ struct Bank {
   int64_t cap;
 };
 
+// True when every array of the bank is set (checked on the host before any
+// launch that uses the bank).
+inline bool bank_complete(const Bank& B) {
+  const void* p[] = {B.x, B.y, B.z, B.u, B.v, B.w, B.E, B.wgt, B.sigt, B.seed, B.hash, B.id, B.elem,
+                     B.mat, B.n_seg, B.n_coll, B.zero_run, B.fin, B.tag, B.cm, B.cs, B.cinv};
+  for (const void* q : p)
+    if (!q) return false;
+  return B.cap > 0;
+}
+
 // Event-loop control block (device memory).
 struct EventCtl {
   int n_xs[2], n_adv[2], n_coll;   // queue lengths, double-buffered by iteration parity
@@ -70,6 +80,10 @@ struct RunArgs {
   float tol;    // mixed form: exit ambiguity tolerance (cm)
   int max_seg;  // event mode: segments per advance launch (<= 0: until event)
   int refill;   // event mode: lanes take further queued particles within one launch
+  int sort_shift;    // event mode: advance queue ordered by elem >> sort_shift (-1: unordered)
+  int sort_buckets;  // (n_tet >> sort_shift) + 1
+  int* sort_tmp;     // bank-capacity scratch for the ordering
+  int* sort_cnt;     // sort_buckets + 1 counters
 };
 
 cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,

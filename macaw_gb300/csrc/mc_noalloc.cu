@@ -25,10 +25,10 @@ using namespace mc;
 constexpr size_t kAlign = 256;
 constexpr size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
-// Per particle slot: 12 eight-byte fields, 6 four-byte fields, the XS cache
+// Per particle slot: 12 eight-byte fields, 7 four-byte fields, the XS cache
 // (16 + 32 bytes), its float inverses (16 bytes) and 6 four-byte queue
 // entries.
-constexpr size_t kSlotArrays8 = 12, kSlotArrays4 = 6 + 6;
+constexpr size_t kSlotArrays8 = 12, kSlotArrays4 = 7 + 6;
 constexpr size_t kScratchBytes =
     kSlotArrays8 * align_up(8 * (size_t)MC_NOALLOC_MAX_BANK) +
     kSlotArrays4 * align_up(4 * (size_t)MC_NOALLOC_MAX_BANK) +
@@ -117,18 +117,20 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
 
   Carve cv{(unsigned char*)base};
   const size_t n = (size_t)cap;
-  Bank B;
+  Bank B{};
   B.x = cv.take<double>(n); B.y = cv.take<double>(n); B.z = cv.take<double>(n);
   B.u = cv.take<double>(n); B.v = cv.take<double>(n); B.w = cv.take<double>(n);
   B.E = cv.take<double>(n); B.wgt = cv.take<double>(n); B.sigt = cv.take<double>(n);
   B.seed = cv.take<uint64_t>(n); B.hash = cv.take<uint64_t>(n); B.id = cv.take<int64_t>(n);
   B.elem = cv.take<int>(n); B.mat = cv.take<int>(n); B.n_seg = cv.take<int>(n);
   B.n_coll = cv.take<int>(n); B.zero_run = cv.take<int>(n); B.fin = cv.take<int>(n);
+  B.tag = cv.take<int>(n);
   B.cm = cv.take<int4>(n);
   B.cs = cv.take<double4_32a>(n);
   B.cinv = cv.take<float4>(n);
   B.cap = cap;
-  EventQueues Q;
+  if (!bank_complete(B)) return fail(MC_ERR_STATE, "internal: particle bank incomplete");
+  EventQueues Q{};
   Q.xs[0] = cv.take<int>(n); Q.xs[1] = cv.take<int>(n);
   Q.adv[0] = cv.take<int>(n); Q.adv[1] = cv.take<int>(n);
   Q.coll = cv.take<int>(n); Q.free_slots = cv.take<int>(n);
@@ -143,7 +145,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   if (e == cudaSuccess) e = cudaMemsetAsync(leak_w, 0, sizeof(double), st);
   if (e != cudaSuccess) return fail(MC_ERR_CUDA, std::string("clear scratch: ") + cudaGetErrorString(e));
 
-  RunArgs a;
+  RunArgs a{};
   a.first = d->first_history;
   a.n = d->n_histories;
   a.master = d->seed;
@@ -161,6 +163,10 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.tol = v.tol;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.sort_shift = -1;  // ordering needs scratch beyond the fixed array
+  a.sort_buckets = 0;
+  a.sort_tmp = nullptr;
+  a.sort_cnt = nullptr;
   const int grid = std::max(1, v.n_sm * (2048 / block));
   int n_launch = 0;
   if (d->n_histories > 0) {

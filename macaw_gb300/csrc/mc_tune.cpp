@@ -1,0 +1,98 @@
+// mc_tune.cpp -- autotuner for the event form's execution parameters.
+//
+// Bank size, block shape, segments per walk launch, the advance-queue
+// ordering granularity and lane refill all move throughput, and their best
+// values depend on the mesh, the cross sections and the precision form.
+// mc_autotune measures them on short trial batches of the context's own
+// problem (device time from the CUDA events inside mc_run) by coordinate
+// descent: each parameter in turn over its candidate values, the others held
+// at their best so far, two passes.  The trial batches score into the batch
+// tally, which is cleared afterwards; SUM/SUM_SQ are not touched.
+#include <algorithm>
+#include <vector>
+
+#include "../../include/macaw_gb300.h"
+
+namespace {
+
+double measure(mc_ctx* ctx, const mc_run_desc& d, int reps) {
+  double best = 0.0;
+  for (int r = 0; r < reps; ++r) {
+    if (mc_run(ctx, &d) != MC_OK) return -1.0;
+    mc_stats s;
+    mc_stats_get(ctx, &s);
+    if (s.ms_total > 0.0) best = std::max(best, (double)d.n_histories / (s.ms_total * 1e-3));
+  }
+  return best;
+}
+
+}  // namespace
+
+extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_histories, mc_run_desc* best,
+                           double* best_rate) {
+  if (!ctx || !base || !best || trial_histories < 1024) return MC_ERR_ARG;
+  mc_run_desc cur = *base;
+  cur.n_histories = trial_histories;
+  cur.mode = MC_MODE_EVENT;
+  cur.accumulate = 0;
+  cur.record_traces = 0;
+  cur.profile = 0;
+  cur.sites = nullptr;
+  cur.n_batches = 0;
+  cur.batch_sizes = nullptr;
+  if (cur.bank_size <= 0 || cur.bank_size > trial_histories) cur.bank_size = trial_histories;
+  if (cur.block_size <= 0) cur.block_size = 256;
+  if (cur.max_seg_per_advance < 0) cur.max_seg_per_advance = 0;
+  double rate = measure(ctx, cur, 2);
+  if (rate < 0.0) return MC_ERR_STATE;
+
+  struct Knob {
+    int kind;
+    std::vector<int64_t> values;
+  };
+  const int64_t t = trial_histories;
+  std::vector<Knob> knobs = {
+      {0, {0, 16, 32, 64, 128}},                                   // segments per walk launch
+      {1, {64, 128, 256}},                                         // threads per block
+      {2, {0, 1, 5, 9, 13}},                                       // queue ordering granularity
+      {3, {std::max<int64_t>(16384, t / 4), std::max<int64_t>(16384, t / 2), t}},  // bank
+      {4, {0, 1}},                                                 // lane refill
+  };
+  auto apply = [](mc_run_desc& d, int kind, int64_t v) {
+    switch (kind) {
+      case 0: d.max_seg_per_advance = (int32_t)v; break;
+      case 1: d.block_size = (int32_t)v; break;
+      case 2: d.sort_queue = (int32_t)v; break;
+      case 3: d.bank_size = v; break;
+      default: d.refill = (int32_t)v; break;
+    }
+  };
+  for (int pass = 0; pass < 2; ++pass) {
+    for (const Knob& k : knobs) {
+      mc_run_desc keep = cur;
+      for (int64_t v : k.values) {
+        mc_run_desc trial = keep;
+        apply(trial, k.kind, v);
+        const double r = measure(ctx, trial, 2);
+        if (r > rate) {
+          rate = r;
+          cur = trial;
+        }
+      }
+    }
+  }
+  mc_tally_clear(ctx, MC_TALLY_BATCH);
+  *best = *base;
+  best->mode = MC_MODE_EVENT;
+  best->max_seg_per_advance = cur.max_seg_per_advance;
+  best->block_size = cur.block_size;
+  best->sort_queue = cur.sort_queue;
+  best->refill = cur.refill;
+  // the largest trial bank winning means "as large as the batch allows":
+  // keep the caller's bank when it is larger than the trial
+  int64_t bank = cur.bank_size;
+  if (bank >= t && base->bank_size > t) bank = base->bank_size;
+  best->bank_size = bank;
+  if (best_rate) *best_rate = rate;
+  return MC_OK;
+}

@@ -126,6 +126,18 @@ class Tracker:
         self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
         return self.stats()
 
+    def autotune(self, trial: int = 200_000, **base) -> tuple[dict, float]:
+        """Best event-form parameters on trial batches; returns (params, histories/s)."""
+        d = RunDesc(base.get("first", 0), trial, base.get("bank_size", 0), base.get("seed", 1),
+                    base.get("precision", MC_PREC_FP64), MC_MODE_EVENT, base.get("block_size", 0),
+                    base.get("max_seg", 0), 0, 0, base.get("sort_queue", 0), 0, base.get("refill", 0), 0,
+                    None, None)
+        out = RunDesc()
+        rate = C.c_double()
+        self._ck(lib.mc_autotune(self._h, C.byref(d), trial, C.byref(out), C.byref(rate)), "mc_autotune")
+        return ({"bank_size": out.bank_size, "block_size": out.block_size, "max_seg": out.max_seg_per_advance,
+                 "sort_queue": out.sort_queue, "refill": bool(out.refill)}, rate.value)
+
     def sample_sites(self, n: int, first: int = 0, seed: int = 1, out: np.ndarray | None = None) -> np.ndarray:
         if out is None:
             out = np.zeros(n, SITE_DTYPE)
