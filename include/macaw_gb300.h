@@ -113,6 +113,9 @@ typedef struct {
                               its particle reaches an event; 0 one particle per lane per launch */
   int32_t n_batches;       /* > 1: consecutive batches of batch_sizes histories run through one
                               pipeline, each folded into SUM/SUM_SQ when it drains (needs accumulate) */
+  int32_t graph;           /* event mode: 1 captures a cycle of event iterations once as a CUDA
+                              graph and replays it (ignored with profile) */
+  int32_t pad;
   const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
   const int64_t* batch_sizes; /* HOST array of n_batches sizes adding up to n_histories */
 } mc_run_desc;

@@ -536,24 +536,40 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       bend[b] = acc;
     }
     if (acc != d->n_histories) return set_err(c, MC_ERR_ARG, "batch sizes must add up to n_histories");
-    CK(upload(c->d_batch_end, bend, c->stream), "upload batch ends");
+    std::vector<DevRequest> rq((size_t)nb);
+    for (int b = 0; b < nb; ++b) {
+      DevRequest& q = rq[b];
+      q = DevRequest{};
+      q.start = b ? bend[b - 1] : 0;
+      q.end = bend[b];
+      q.first_id = a.first + q.start;
+      q.seed = d->seed;
+      q.slot = b & 1;
+      q.has_src = 0;
+    }
+    CK(upload(c->d_batch_end, rq, c->stream), "upload batch table");
     CK(c->d_tally2.alloc(sizeof(double) * (size_t)c->mesh.n_tet), "allocate batch tally");
     if (!c->tally2_clear) {
       CK(cudaMemsetAsync(c->d_tally2.p, 0, c->d_tally2.bytes, c->stream), "clear batch tally");
       c->tally2_clear = true;
     }
     a.tally2 = c->d_tally2.as<double>();
-    a.batch_end = c->d_batch_end.as<int64_t>();
+    a.req = c->d_batch_end.as<DevRequest>();
+    a.n_req = nb;
   } else {
     bend[0] = d->n_histories;
     a.tally2 = a.tally;
-    a.batch_end = nullptr;
+    a.req = nullptr;
+    a.n_req = 0;
   }
-  a.n_batches = nb;
+  a.n_tet = c->mesh.n_tet;
   a.live = nullptr;
+  // history-form batches all score into slot 0 (one runs at a time);
+  // event-form batches alternate between slots 0 and 1
   auto fold = [&](int b) -> int {
     const int64_t size = bend[b] - (b ? bend[b - 1] : 0);
-    CK(launch_accumulate((b & 1) ? a.tally2 : a.tally, c->d_sum.as<double>(), c->d_sumsq.as<double>(),
+    double* buf = (d->mode == MC_MODE_EVENT && (b & 1)) ? a.tally2 : a.tally;
+    CK(launch_accumulate(buf, c->d_sum.as<double>(), c->d_sumsq.as<double>(),
                          c->mesh.n_tet, size > 0 ? 1.0 / (double)size : 0.0, c->stream),
        "launch accumulate");
     c->batches += 1;
@@ -567,7 +583,8 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
         RunArgs ab = a;
         ab.first = a.first + (b ? bend[b - 1] : 0);
         ab.n = bend[b] - (b ? bend[b - 1] : 0);
-        ab.n_batches = 1;
+        ab.req = nullptr;
+        ab.n_req = 0;
         ab.tally2 = ab.tally;
         ab.traces = a.traces ? a.traces + (ab.first - a.first) : nullptr;
         CK(launch_history(M, X, S, ab, block, grid, c->stream), "launch history kernel");
@@ -603,8 +620,37 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       EventCtl h;
       const int kGroup = 4;
       const int64_t tail = std::max<int64_t>(4096, cap / 64);
+      // a graph replays one group of iterations (parity 0,1,0,1: the group
+      // always starts at parity 0), captured on first use
+      const bool use_graph = d->graph && !d->profile;
+      cudaGraphExec_t gexec = nullptr;
+      struct GraphGuard {
+        cudaGraphExec_t* e;
+        ~GraphGuard() {
+          if (*e) cudaGraphExecDestroy(*e);
+        }
+      } gguard{&gexec};
+      if (use_graph) {
+        int nl = 0;
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin graph capture");
+        cudaError_t ce = cudaSuccess;
+        for (int gi = 0; gi < kGroup && ce == cudaSuccess; ++gi)
+          ce = launch_event_iteration(M, X, S, a, B, Q, ctl, gi & 1, block, grid, c->stream, &nl);
+        const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+        if (ce != cudaSuccess) return cuda_err(c, ce, "capture event iterations");
+        if (ee != cudaSuccess) return cuda_err(c, ee, "end graph capture");
+        ce = cudaGraphInstantiate(&gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return cuda_err(c, ce, "instantiate event graph");
+      }
       for (int64_t it = 0;; ++it) {
-        for (int gi = 0; gi < kGroup; ++gi) {
+        if (use_graph) {
+          CK(cudaGraphLaunch(gexec, c->stream), "launch event graph");
+          n_launch += kGroup * (5 + (a.sort_shift >= 0 ? 4 : 0));
+          n_adv += kGroup;
+        }
+        for (int gi = 0; gi < kGroup && !use_graph; ++gi) {
           cudaEvent_t e0 = nullptr, e1 = nullptr;
           if (d->profile) {
             while (c->prof_ev.size() < (size_t)(2 * n_adv + 2)) {

@@ -43,7 +43,9 @@ __device__ __forceinline__ void flush(LocalCounters& L, unsigned long long* g, d
 }
 
 // Batch tally a particle scores into.
-__device__ __forceinline__ double* tally_of(const RunArgs& a, int tag) { return tag ? a.tally2 : a.tally; }
+__device__ __forceinline__ double* tally_of(const RunArgs& a, int tag) {
+  return tag ? a.tally2 + (int64_t)(tag - 1) * a.n_tet : a.tally;
+}
 
 // End of a history: closing hash word, counters, optional trace record.
 __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCounters& L) {
@@ -142,23 +144,31 @@ __device__ __forceinline__ void store(const Bank& B, int s, const Particle& p) {
 
 __device__ __forceinline__ void birth(const DevMesh& M, const DevXS& X, const DevSource& S,
                                       const RunArgs& a, int64_t h, Particle& p) {
-  mc_site o;
-  const Skip k = skip_ahead((uint64_t)(h + 1) * kPrnStride);
-  if (a.sites) o = a.sites[h - a.first];
-  else sample_source(X, S, k, a.master, o);
-  start(M, o, h, k, a.master, p);
-  int b = 0;
-  if (a.n_batches > 1) {
+  // which batch / request of the birth sequence this history belongs to
+  int64_t id = h + 1;
+  uint64_t master = a.master;
+  int tag = 0;
+  const DevSource* src = &S;
+  if (a.req) {
     const int64_t r = h - a.first;
-    int lo = 0, hi = a.n_batches - 1;
+    int lo = 0, hi = a.n_req - 1;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (r < a.batch_end[mid]) hi = mid;
+      if (r < a.req[mid].end) hi = mid;
       else lo = mid + 1;
     }
-    b = lo;
+    const DevRequest& q = a.req[lo];
+    id = q.first_id + (r - q.start) + 1;
+    master = q.seed;
+    tag = q.slot;
+    if (q.has_src) src = &q.src;
   }
-  p.tag = b & 1;
+  mc_site o;
+  const Skip k = skip_ahead((uint64_t)id * kPrnStride);
+  if (a.sites) o = a.sites[h - a.first];
+  else sample_source(X, *src, k, master, o);
+  start(M, o, id - 1, k, master, p);
+  p.tag = tag;
   if (a.live) atomicAdd(a.live + p.tag, 1);
 }
 

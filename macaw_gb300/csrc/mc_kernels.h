@@ -63,14 +63,29 @@ struct EventQueues {
   int* free_slots;  // ring of bank-capacity entries
 };
 
+// One entry of the birth sequence: a batch of a pipelined run, or a serving
+// request.  Histories [start, end) of the sequence are its histories
+// 0..end-start-1, with particle ids first_id+1... and master seed `seed`,
+// born from `src` (or the context source) and scored into tally `slot`.
+struct DevRequest {
+  int64_t start, end;
+  int64_t first_id;
+  uint64_t seed;
+  int slot;
+  int has_src;
+  DevSource src;
+};
+
 struct RunArgs {
   int64_t first, n;
   uint64_t master;
   double* tally;                // scores of even batches
-  double* tally2;               // scores of odd batches (== tally for a single batch)
-  const int64_t* batch_end;     // device: end of each batch (relative index), or null
-  int n_batches;
-  int* live;                    // event mode: in-flight counters per batch parity, or null
+  double* tally2;               // tally slot 1 (== tally for a single batch); slots k >= 1 are
+                                // tally2 + (k-1)*n_tet
+  int64_t n_tet;
+  const DevRequest* req;        // device: birth-sequence entries sorted by start, or null
+  int n_req;
+  int* live;                    // event mode: in-flight counters per tally slot, or null
   mc_trace* traces;
   unsigned long long* counters;
   double* leak_w;

@@ -151,8 +151,9 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.master = d->seed;
   a.tally = tally;
   a.tally2 = tally;
-  a.batch_end = nullptr;
-  a.n_batches = 1;
+  a.req = nullptr;
+  a.n_req = 0;
+  a.n_tet = v.n_tet;
   a.live = nullptr;
   a.traces = d->record_traces ? traces : nullptr;
   a.counters = counters;

@@ -1,7 +1,7 @@
 // mc_tune.cpp -- autotuner for the event form's execution parameters.
 //
 // Bank size, block shape, segments per walk launch, the advance-queue
-// ordering granularity and lane refill all move throughput, and their best
+// ordering granularity, lane refill and CUDA-graph replay all move throughput, and their best
 // values depend on the mesh, the cross sections and the precision form.
 // mc_autotune measures them on short trial batches of the context's own
 // problem (device time from the CUDA events inside mc_run) by coordinate
@@ -57,6 +57,7 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       {2, {0, 1, 5, 9, 13}},                                       // queue ordering granularity
       {3, {std::max<int64_t>(16384, t / 4), std::max<int64_t>(16384, t / 2), t}},  // bank
       {4, {0, 1}},                                                 // lane refill
+      {5, {0, 1}},                                                 // CUDA-graph event cycles
   };
   auto apply = [](mc_run_desc& d, int kind, int64_t v) {
     switch (kind) {
@@ -64,7 +65,8 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       case 1: d.block_size = (int32_t)v; break;
       case 2: d.sort_queue = (int32_t)v; break;
       case 3: d.bank_size = v; break;
-      default: d.refill = (int32_t)v; break;
+      case 4: d.refill = (int32_t)v; break;
+      default: d.graph = (int32_t)v; break;
     }
   };
   for (int pass = 0; pass < 2; ++pass) {
@@ -88,6 +90,7 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
   best->block_size = cur.block_size;
   best->sort_queue = cur.sort_queue;
   best->refill = cur.refill;
+  best->graph = cur.graph;
   // the largest trial bank winning means "as large as the batch allows":
   // keep the caller's bank when it is larger than the trial
   int64_t bank = cur.bank_size;

@@ -33,7 +33,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_struct_layouts_match_header_sizes():
     assert C.sizeof(_lib.SourceDesc) == 4 + 4 + 9 * 8 + 4 + 4 + 8 + 6 * 8
-    assert C.sizeof(_lib.RunDesc) == 4 * 8 + 10 * 4 + 8 + 8
+    assert C.sizeof(_lib.RunDesc) == 4 * 8 + 12 * 4 + 8 + 8
     assert _lib.TRACE_DTYPE.itemsize == 8 + 8 + 6 * 4 + 4 * 8
 
 

@@ -57,6 +57,28 @@ def test_pipelined_batches_equal_separate_runs(cube, separate, mode, bank):
         assert np.all(t.tally() == 0)
 
 
+def test_graph_replayed_event_cycles_are_bit_exact(cube, separate):
+    s_ref, sq_ref, tr_ref = separate
+    n = sum(SIZES)
+    with Tracker(0) as t:
+        t.load(cube)
+        t.run(n, seed=5, mode=MC_MODE_EVENT, bank_size=3000, max_seg=8, sort_queue=5, graph=True,
+              accumulate=True, traces=True, batch_sizes=SIZES)
+        tr = t.traces(n)
+        for f in ("hash", "status", "n_seg", "n_coll", "elem", "face"):
+            assert np.array_equal(tr[f], tr_ref[f]), f
+        assert close(t.tally(MC_TALLY_SUM), s_ref)
+
+
+def test_autotune_returns_usable_parameters(cube):
+    with Tracker(0) as t:
+        t.load(cube)
+        params, rate = t.autotune(trial=20000, bank_size=8192)
+        assert rate > 0
+        st = t.run(5000, seed=5, accumulate=True, **params)
+        assert st.n_hist == 5000 and st.n_stuck == 0
+
+
 def test_pipelined_mixed_batches_keep_every_particle(cube):
     n = sum(SIZES)
     with Tracker(0) as t:

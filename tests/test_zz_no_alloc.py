@@ -23,7 +23,7 @@ RTOL = 1e-12
 
 
 def _desc(first, n, bank, traces):
-    return RunDesc(first, n, bank, 7, MC_PREC_FP64, MC_MODE_EVENT, 0, 0, int(traces), 0, 0, 0, 0, 0, None, None)
+    return RunDesc(first, n, bank, 7, MC_PREC_FP64, MC_MODE_EVENT, 0, 0, int(traces), 0, 0, 0, 0, 0, 0, 0, None, None)
 
 
 def test_noalloc_matches_mc_run_twice_in_a_row():
