@@ -248,6 +248,36 @@ int mc_batches_done(mc_ctx* ctx, int64_t* out);
 #define MC_NOALLOC_MAX_BANK 16384
 int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* desc, double* tally, mc_trace* traces);
 
+/* ---- serving: continuous batching of fixed-source requests ------------
+ * No counterpart in the reference (MaCaw runs one input file per process).
+ * A context with its mesh and cross sections resident takes requests as
+ * they arrive.  Each admitted request gets a tally slot (n_tet doubles) and
+ * its histories join the shared particle bank, born as slots free up, so
+ * requests overlap on the device without draining between them.  Request
+ * particle ids are 1..n_histories under the request's seed: a request's
+ * result does not depend on what else is in flight.  While serving is open,
+ * mc_run in the event form is rejected on this context. */
+typedef struct {
+  int64_t n_histories;
+  uint64_t seed;
+  mc_source_desc source;  /* point or box space; Watt or mono energy */
+} mc_request;
+/* max_slots requests in flight (tally memory max_slots*n_tet*8 bytes),
+ * bank_size particles in flight, precision MC_PREC_*, max_seg segments per
+ * walk launch (0: until an event). */
+int mc_serve_open(mc_ctx* ctx, int32_t max_slots, int64_t bank_size, int32_t precision, int32_t max_seg);
+int mc_serve_submit(mc_ctx* ctx, const mc_request* req, int64_t* ticket);
+/* Admits queued requests into free slots and launches `iterations` event
+ * iterations (asynchronous). */
+int mc_serve_step(mc_ctx* ctx, int32_t iterations);
+/* Waits for launched work; retires finished requests, writing up to
+ * capacity tickets into done and their count into n_done. */
+int mc_serve_poll(mc_ctx* ctx, int64_t* done, int32_t capacity, int32_t* n_done);
+/* FP64 element track-length tally (sum of wgt*length) of a finished request. */
+int mc_serve_result(mc_ctx* ctx, int64_t ticket, double* tally, int64_t n_tet);
+int mc_serve_status(mc_ctx* ctx, int32_t* queued, int32_t* active, int32_t* free_slots);
+int mc_serve_close(mc_ctx* ctx);
+
 /* ---- input-file front end ---------------------------------------------
  * Replaces: running a MaCaw input (MooseApp::run on an .i file; src/main.C)
  * for the tracking path.  Parses the HIT blocks [Mesh] (TetCubeMeshGenerator,

@@ -41,6 +41,10 @@ class RunDesc(C.Structure):
                 ("pad", C.c_int32), ("sites", C.c_void_p), ("batch_sizes", C.c_void_p)]
 
 
+class Request(C.Structure):
+    _fields_ = [("n_histories", C.c_int64), ("seed", C.c_uint64), ("source", SourceDesc)]
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("n_hist", "n_seg", "n_coll", "n_leak", "n_absorb", "n_cutoff",
                                         "n_stuck", "n_lost", "n_badxs", "n_fallback", "n_xs", "n_launch")] + \
@@ -77,6 +81,13 @@ SIGNATURES = {
     "mc_sync": ([_P], C.c_int),
     "mc_source_sample": ([_P, _I64, _I64, _U64, _P], C.c_int),
     "mc_ctx_set_stream": ([_P, _P], C.c_int),
+    "mc_serve_open": ([_P, _I32, _I64, _I32, _I32], C.c_int),
+    "mc_serve_submit": ([_P, C.POINTER(Request), C.POINTER(_I64)], C.c_int),
+    "mc_serve_step": ([_P, _I32], C.c_int),
+    "mc_serve_poll": ([_P, _P, _I32, C.POINTER(_I32)], C.c_int),
+    "mc_serve_result": ([_P, _I64, _P, _I64], C.c_int),
+    "mc_serve_status": ([_P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)], C.c_int),
+    "mc_serve_close": ([_P], C.c_int),
     "mc_run_noalloc": ([_P, C.POINTER(RunDesc), _P, _P], C.c_int),
     "mc_app_run": ([C.c_char_p, C.c_int, C.c_char_p, C.c_char_p, _I64], C.c_int),
     "mc_app_check": ([C.c_char_p, C.c_char_p, _I64], C.c_int),

@@ -91,6 +91,7 @@ struct mc_ctx {
 
   int64_t batches = 0;
   mc_stats last{};
+  bool serving = false;  // the event state belongs to an open serving session
 };
 
 namespace {
@@ -461,6 +462,8 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
     return set_err(c, MC_ERR_ARG, "unknown precision form");
   if (d->mode != MC_MODE_HISTORY && d->mode != MC_MODE_EVENT) return set_err(c, MC_ERR_ARG, "unknown execution form");
   if (!c->have_src) return set_err(c, MC_ERR_STATE, "no source (mc_source_set)");
+  if (c->serving && d->mode == MC_MODE_EVENT)
+    return set_err(c, MC_ERR_STATE, "a serving session holds this context's event state (mc_serve_close)");
   cudaSetDevice(c->device);
   int rc = ensure_device_tables(c);
   if (rc) return rc;
@@ -867,19 +870,45 @@ bool ctx_view(mc_ctx* c, CtxView* v) {
   v->stream = c->stream;
   v->n_tet = c->mesh.n_tet;
   v->n_mat = (int)c->xs.mat_ids.size();
-  v->ready = c->have_mesh && c->have_src && !c->nucs.empty() && !c->mats.empty() && !c->xs_dirty &&
-             !c->tmat_dirty && !c->bc_dirty;
+  const bool tables = c->have_mesh && !c->nucs.empty() && !c->mats.empty() && !c->xs_dirty && !c->tmat_dirty &&
+                      !c->bc_dirty;
+  v->ready = tables && c->have_src;
   double dg = 0.0;
   for (int k = 0; k < 3; ++k) {
     const double e = c->mesh.bbox_hi[k] - c->mesh.bbox_lo[k];
     dg += e * e;
   }
   v->tol = (float)(1e-6 * sqrt(dg));
-  if (!v->ready) return false;
+  if (!tables) return false;
   v->M = dev_mesh(c);
   v->X = dev_xs(c);
   v->S = dev_source(c);
-  return true;
+  return v->ready;
 }
+
+void ctx_set_serving(mc_ctx* c, bool on) { c->serving = on; }
+
+}  // namespace mc
+
+namespace mc {
+
+int ctx_prepare(mc_ctx* c) {
+  cudaSetDevice(c->device);
+  return ensure_device_tables(c);
+}
+
+int ctx_event_state(mc_ctx* c, int64_t cap, CtxEvent* out) {
+  int rc = ensure_bank(c, std::max(cap, c->bank_cap));
+  if (rc) return rc;
+  out->B = dev_bank(c);
+  if (!bank_complete(out->B)) return set_err(c, MC_ERR_STATE, "internal: particle bank incomplete");
+  out->Q = dev_queues(c);
+  out->ctl = c->d_ctl.as<EventCtl>();
+  out->counters = c->d_counters.as<unsigned long long>();
+  out->leak_w = c->d_leak_w.as<double>();
+  return MC_OK;
+}
+
+int ctx_fail(mc_ctx* c, int code, const std::string& msg) { return set_err(c, code, msg); }
 
 }  // namespace mc

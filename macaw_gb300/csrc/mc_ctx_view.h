@@ -7,6 +7,7 @@
 
 #include "../../include/macaw_gb300.h"
 #include "mc_device.cuh"
+#include "mc_kernels.h"
 
 namespace mc {
 
@@ -16,6 +17,7 @@ struct CtxView {
   int64_t n_tet = 0;
   float tol = 0.0f;
   bool ready = false;  // mesh, tables, block map, BCs and source resident on the device
+                       // (M, X and S are filled whenever the tables are resident)
   DevMesh M;
   DevXS X;
   DevSource S;
@@ -26,5 +28,19 @@ void ctx_set_error(mc_ctx* c, const std::string& msg);
 void ctx_set_stats(mc_ctx* c, const mc_stats& s);
 // Fills v; false (with v->ready false) when the device tables are not resident.
 bool ctx_view(mc_ctx* c, CtxView* v);
+
+// Device event state of a context (bank of at least cap slots, queues,
+// control block, counters), allocated on first use.
+struct CtxEvent {
+  Bank B;
+  EventQueues Q;
+  EventCtl* ctl;
+  unsigned long long* counters;
+  double* leak_w;
+};
+int ctx_prepare(mc_ctx* c);  // puts mesh, tables, block map, BCs on the device
+int ctx_event_state(mc_ctx* c, int64_t cap, CtxEvent* out);
+int ctx_fail(mc_ctx* c, int code, const std::string& msg);
+void ctx_set_serving(mc_ctx* c, bool on);
 
 }  // namespace mc
