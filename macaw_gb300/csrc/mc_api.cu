@@ -71,7 +71,7 @@ struct mc_ctx {
   bool have_src = false;
 
   // device copies
-  DevBuf d_planes, d_planes32, d_nbr, d_tmat, d_bc, d_gstart, d_gtets;
+  DevBuf d_planes, d_tet, d_tmat, d_bc, d_gstart, d_gtets;
   DevBuf d_gE, d_goff, d_gn, d_ghidx, d_nuc_grid, d_nuc_off, d_sig, d_awr, d_mat_off, d_mat_nuc, d_mat_dens;
   DevBuf d_cyl;
   DevBuf d_tally, d_sum, d_sumsq;
@@ -158,6 +158,25 @@ int ensure_device_tables(mc_ctx* c) {
         }
     }
     CK(upload(c->d_tmat, tmat, c->stream), "upload element materials");
+    // packed float record per tet: planes, and neighbour entries flagged
+    // where the material changes across the side
+    std::vector<Tet32> rec((size_t)c->mesh.n_tet);
+    for (int64_t t = 0; t < c->mesh.n_tet; ++t) {
+      Tet32& r = rec[t];
+      const float* q = &c->mesh.planes32[16 * t];
+      r.p[0] = make_float4(q[0], q[1], q[2], q[3]);
+      r.p[1] = make_float4(q[4], q[5], q[6], q[7]);
+      r.p[2] = make_float4(q[8], q[9], q[10], q[11]);
+      r.p[3] = make_float4(q[12], q[13], q[14], q[15]);
+      int e[4];
+      for (int f = 0; f < 4; ++f) {
+        e[f] = c->mesh.nbr[4 * t + f];
+        if (e[f] >= 0 && tmat[(size_t)(e[f] >> 2)] != tmat[t]) e[f] |= kMatChange;
+      }
+      r.nbr = make_int4(e[0], e[1], e[2], e[3]);
+    }
+    CK(upload(c->d_tet, rec, c->stream), "upload tet records");
+    CK(cudaStreamSynchronize(c->stream), "upload tet records");
     c->tmat_dirty = false;
   }
   if (c->bc_dirty) {
@@ -170,8 +189,7 @@ int ensure_device_tables(mc_ctx* c) {
 DevMesh dev_mesh(mc_ctx* c) {
   DevMesh M{};
   M.planes = c->d_planes.as<double4_32a>();
-  M.planes32 = c->d_planes32.as<float4>();
-  M.nbr = c->d_nbr.as<int4>();
+  M.tet = c->d_tet.as<Tet32>();
   M.tmat = c->d_tmat.as<int>();
   M.bc_type = c->d_bc.as<int>();
   M.n_bid = (int)c->bc_type.size();
@@ -340,8 +358,7 @@ int mc_mesh_upload(mc_ctx* c, int64_t n_vtx, const double* xyz, int64_t n_tet,
   cudaSetDevice(c->device);
   c->mesh = std::move(M);
   CK(upload(c->d_planes, c->mesh.planes, c->stream), "upload planes");
-  CK(upload(c->d_planes32, c->mesh.planes32, c->stream), "upload planes");
-  CK(upload(c->d_nbr, c->mesh.nbr, c->stream), "upload neighbours");
+
   CK(upload(c->d_gstart, c->mesh.gstart, c->stream), "upload locator");
   CK(upload(c->d_gtets, c->mesh.gtets, c->stream), "upload locator");
   CK(c->d_tally.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");

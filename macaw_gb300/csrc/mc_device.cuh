@@ -17,10 +17,24 @@
 
 namespace mc {
 
+// Per-tet record of the float walk: the four outward face planes rounded to
+// float and the neighbour entries, 80 bytes (three 32-byte sectors).  An
+// interior entry is neighbour << 2 | the shared side's index in the
+// neighbour, with kMatChange set when the neighbour's material differs; a
+// boundary entry is -1-boundary_id.
+struct __align__(16) Tet32 {
+  float4 p[4];
+  int4 nbr;
+};
+constexpr int kMatChange = 1 << 30;
+
+__device__ __forceinline__ int side_entry(const int4& n, int f) {
+  return f == 0 ? n.x : f == 1 ? n.y : f == 2 ? n.z : n.w;
+}
+
 struct DevMesh {
   const double4_32a* __restrict__ planes;   // 4 per tet (nx, ny, nz, d), outward
-  const float4* __restrict__ planes32;  // same in float
-  const int4* __restrict__ nbr;         // per side: neighbour << 2 | its side, or -1-boundary_id
+  const Tet32* __restrict__ tet;        // float planes + neighbour entries
   const int* __restrict__ tmat;         // material index per tet (-1: none)
   const int* __restrict__ bc_type;      // per boundary id: 0 vacuum, 1 reflect
   int n_bid;
@@ -189,7 +203,7 @@ __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, doub
   const int64_t q1 = M.gstart[cell + 1];
   for (int64_t q = M.gstart[cell]; q < q1; ++q) {
     const int t = __ldg(M.gtets + q);
-    const float4* P32 = M.planes32 + 4 * (int64_t)t;
+    const float4* P32 = M.tet[t].p;
     bool out = false;
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -356,8 +370,10 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     p.status = kStuck;
     return 2;
   }
-  const int mat = __ldg(M.tmat + p.elem);
-  if (mat != p.mat) {
+  // the material is looked up only when it may have changed: after birth,
+  // a collision, or a crossing through a side flagged kMatChange
+  if (p.mat < 0) {
+    const int mat = __ldg(M.tmat + p.elem);
     if (mat < 0) {
       p.status = kBadXS;
       return 2;
@@ -423,10 +439,10 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     p.x = p.x + L * p.u;
     p.y = p.y + L * p.v;
     p.z = p.z + L * p.w;
-    const int4 nb4 = M.nbr[p.elem];
-    const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+    const int nb = side_entry(M.tet[p.elem].nbr, bf);
     if (nb >= 0) {
-      p.elem = nb >> 2;
+      if (nb & kMatChange) p.mat = -2;
+      p.elem = (nb & (kMatChange - 1)) >> 2;
       p.fin = nb & 3;
       return 0;
     }
@@ -470,7 +486,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
 // and a float upper bound for xi.  Results are bit-identical to
 // segment_fp64.
 //
-// Error bounds (u = 2^-24): planes32 and the float position/direction are
+// Error bounds (u = 2^-24): the float planes and position/direction are
 // roundings of the FP64 values (relative u each); num32 = d - (nx*x + ny*y
 // + nz*z) through two fmaf and one product and a subtraction: |num32 - num|
 // <= u (2|d| + 6 sum|n_i x_i|)(1+u) <= 12u (|d| + |x|_1) since |n_i| <= 1;
@@ -486,8 +502,10 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     p.status = kStuck;
     return 2;
   }
-  const int mat = __ldg(M.tmat + p.elem);
-  if (mat != p.mat) {
+  // the material is looked up only when it may have changed: after birth,
+  // a collision, or a crossing through a side flagged kMatChange
+  if (p.mat < 0) {
+    const int mat = __ldg(M.tmat + p.elem);
     if (mat < 0) {
       p.status = kBadXS;
       return 2;
@@ -509,7 +527,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   const float xf = (float)p.x, yf = (float)p.y, zf = (float)p.z;
   const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
   const float Eden = 7.2e-7f * (fabsf(uf) + fabsf(vf) + fabsf(wf));
-  const float4* P32 = M.planes32 + 4 * (int64_t)p.elem;
+  const float4* P32 = M.tet[p.elem].p;
   bool sure = true;
   int bf = -1;
   float tb = 3.0e38f, eb = 0.0f, lo_other = 3.0e38f;
@@ -573,10 +591,10 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     p.x = p.x + L * p.u;
     p.y = p.y + L * p.v;
     p.z = p.z + L * p.w;
-    const int4 nb4 = __ldg(M.nbr + p.elem);
-    const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+    const int nb = side_entry(M.tet[p.elem].nbr, bf);
     if (nb >= 0) {
-      p.elem = nb >> 2;
+      if (nb & kMatChange) p.mat = -2;
+      p.elem = (nb & (kMatChange - 1)) >> 2;
       p.fin = nb & 3;
       return 0;
     }
@@ -665,8 +683,10 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
     p.status = kStuck;
     return 2;
   }
-  const int mat = __ldg(M.tmat + p.elem);
-  if (mat != p.mat) {
+  // the material is looked up only when it may have changed: after birth,
+  // a collision, or a crossing through a side flagged kMatChange
+  if (p.mat < 0) {
+    const int mat = __ldg(M.tmat + p.elem);
     if (mat < 0) {
       p.status = kBadXS;
       return 2;
@@ -685,7 +705,7 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
     p.mat = mat;
     inv_sig = (float)(1.0 / p.sigt);
   }
-  const float4* P = M.planes32 + 4 * (int64_t)p.elem;
+  const float4* P = M.tet[p.elem].p;
   int bf = -1;
   float t1 = 3.0e38f, t2 = 3.0e38f;
 #pragma unroll
@@ -735,10 +755,10 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
     g.x = fmaf(L, g.u, g.x);
     g.y = fmaf(L, g.v, g.y);
     g.z = fmaf(L, g.w, g.z);
-    const int4 nb4 = __ldg(M.nbr + p.elem);
-    const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+    const int nb = side_entry(M.tet[p.elem].nbr, bf);
     if (nb >= 0) {
-      p.elem = nb >> 2;
+      if (nb & kMatChange) p.mat = -2;
+      p.elem = (nb & (kMatChange - 1)) >> 2;
       p.fin = nb & 3;
       return 0;
     }

@@ -56,7 +56,7 @@ std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
                               const int32_t* tet_vtx, const int32_t* tet_block,
                               const int32_t* tet_side_bid, MeshTables& M) {
   if (n_vtx < 4 || n_tet < 1) return "empty mesh";
-  if (n_tet > (int64_t)1 << 29) return "too many tets (limit 2^29)";
+  if (n_tet > (int64_t)1 << 28) return "too many tets (limit 2^28)";
   for (int64_t i = 0; i < 4 * n_tet; ++i)
     if (tet_vtx[i] < 0 || tet_vtx[i] >= n_vtx) return "tet vertex index out of range";
   M.n_vtx = n_vtx;

@@ -474,8 +474,8 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
         face = -2;  // stuck
         break;
       }
-      const int m = __ldg(M.tmat + elem);
-      if (m != mat) {
+      if (mat < 0) {  // after a side flagged kMatChange
+        const int m = __ldg(M.tmat + elem);
         const int sl = m & 3;
         const int key = sl == 0 ? cm.x : sl == 1 ? cm.y : sl == 2 ? cm.z : cm.w;
         if (m < 0 || key != m) {
@@ -487,7 +487,8 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
         slot = sl;
         inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
       }
-      const float4* P = M.planes32 + 4 * (int64_t)elem;
+      const Tet32& T = M.tet[elem];
+      const float4* P = T.p;
       int bf = -1;
       float t1 = 3.0e38f, t2 = 3.0e38f;
 #pragma unroll
@@ -546,10 +547,10 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
       x = fmaf(Ls, u, x);
       y = fmaf(Ls, v, y);
       z = fmaf(Ls, w, z);
-      const int4 nb4 = __ldg(M.nbr + elem);
-      const int nb = (bf == 0) ? nb4.x : (bf == 1) ? nb4.y : (bf == 2) ? nb4.z : nb4.w;
+      const int nb = side_entry(T.nbr, bf);
       if (nb >= 0) {
-        elem = nb >> 2;
+        if (nb & kMatChange) mat = -2;
+        elem = (nb & (kMatChange - 1)) >> 2;
         fin = nb & 3;
       } else {
         const int bid = -1 - nb;
