@@ -305,6 +305,19 @@ int mc_gen_lattice_sizes(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int3
 int mc_gen_lattice(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int32_t n_fuel_rings,
                    double pitch, double height, double r_fuel, double r_clad, double* xyz,
                    int32_t* tet_vtx, int32_t* tet_block, int32_t* tet_side_bid);
+/* Cylindrical core: 193 assemblies of pins x pins pin cells on a 15 x 15
+ * assembly grid (rows of 7, 11, 13, 13, 15 x7, 13, 13, 11, 7) centred on the
+ * z axis, plus whole reflector cells whose corners lie inside radius; nz
+ * axial layers over [0, height].  Blocks: fuel 1..193 (one per assembly),
+ * clad 194, moderator 195, reflector 196..200 (five 72-degree sectors).
+ * The square grid of cells extends past the assemblies far enough to reach
+ * the radius.  Sidesets: bottom 0, top 5, radial staircase 6.  pin_xy
+ * (optional, 2*n_pins) receives the pin-cell centres. */
+int mc_gen_core_sizes(int32_t pins, int32_t nz, int32_t n_sec, int32_t n_fuel_rings, double pitch, double radius,
+                      int64_t* n_vtx, int64_t* n_tet, int64_t* n_pins);
+int mc_gen_core(int32_t pins, int32_t nz, int32_t n_sec, int32_t n_fuel_rings, double pitch, double height,
+                double r_fuel, double r_clad, double radius, double* xyz, int32_t* tet_vtx, int32_t* tet_block,
+                int32_t* tet_side_bid, double* pin_xy);
 /* Synthetic nuclide: n_pts log-uniform energies in [E_min, E_max] eV,
  * sigma_t = a/sqrt(E) + n_peaks Lorentzians, sigma_s = f_s*sigma_t,
  * awr; all drawn from (seed, index). */

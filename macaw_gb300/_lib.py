@@ -102,6 +102,8 @@ SIGNATURES = {
     "mc_gen_cube": ([_I32, _D, _P, _P, _P, _P], C.c_int),
     "mc_gen_lattice_sizes": ([_I32, _I32, _I32, _I32, _I32, C.POINTER(_I64), C.POINTER(_I64)], C.c_int),
     "mc_gen_lattice": ([_I32, _I32, _I32, _I32, _I32, _D, _D, _D, _D, _P, _P, _P, _P], C.c_int),
+    "mc_gen_core_sizes": ([_I32, _I32, _I32, _I32, _D, _D, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)], C.c_int),
+    "mc_gen_core": ([_I32, _I32, _I32, _I32, _D, _D, _D, _D, _D, _P, _P, _P, _P, _P], C.c_int),
     "mc_gen_nuclide": ([_U64, _I32, _I64, _D, _D, _I32, _P, _P, _P, C.POINTER(_D)], C.c_int),
     "mc_gen_densities": ([_U64, _I32, _I32, _D, _D, _P], C.c_int),
 }

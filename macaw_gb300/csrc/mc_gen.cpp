@@ -124,9 +124,20 @@ struct Lattice2D {
   std::vector<int32_t> tri_block;
 };
 
-int lattice2d(int nx, int ny, int n_sec, int n_fr, double pitch, double r_fuel, double r_clad,
-              Lattice2D& G) {
-  if (nx < 1 || ny < 1 || n_sec < 8 || n_sec % 8 != 0 || n_fr < 1) return MC_ERR_ARG;
+// Cell kinds of the 2-D mesh.
+enum CellKind { kPinCell = 0, kFillCell = 1 };
+
+// Cells of a square grid (pitch p, origin x0/y0), each a pin cell (fuel /
+// clad / moderator blocks) or a fill cell (a fan from the centre to the
+// same square points, so fill and pin cells conform).
+struct CellSpec {
+  int ci, cj, kind;
+  int32_t fuel, clad, mod, fill;
+};
+
+int cells2d(const std::vector<CellSpec>& cells, int nx, int ny, double x0, double y0, int n_sec, int n_fr,
+            double pitch, double r_fuel, double r_clad, Lattice2D& G) {
+  if (n_sec < 8 || n_sec % 8 != 0 || n_fr < 1) return MC_ERR_ARG;
   if (!(r_fuel > 0.0) || !(r_clad > r_fuel) || !(pitch > 2.0 * r_clad)) return MC_ERR_ARG;
   const double twopi = 6.283185307179586;
   const int q = n_sec / 8;
@@ -189,12 +200,13 @@ int lattice2d(int nx, int ny, int n_sec, int n_fr, double pitch, double r_fuel, 
   const double h = pitch * 0.5;
   const int n_rings = n_fr + 1;  // fuel rings + clad ring
   std::vector<int32_t> ring((size_t)n_rings * n_sec), sq(n_sec);
-  for (int cj = 0; cj < ny; ++cj)
-    for (int ci = 0; ci < nx; ++ci) {
-      const double X0 = ci * pitch, X1 = (ci + 1) * pitch, Y0 = cj * pitch, Y1 = (cj + 1) * pitch;
+  for (const CellSpec& cell : cells) {
+      const int ci = cell.ci, cj = cell.cj;
+      const double X0 = x0 + ci * pitch, X1 = x0 + (ci + 1) * pitch, Y0 = y0 + cj * pitch,
+                   Y1 = y0 + (cj + 1) * pitch;
       const double cx = (X0 + X1) * 0.5, cy = (Y0 + Y1) * 0.5;
       const int32_t ctr = add_pt(cx, cy, false, 0, 0, 0, 0);
-      for (int r = 0; r < n_rings; ++r) {
+      for (int r = 0; r < n_rings && cell.kind == kPinCell; ++r) {
         const double rad = (r < n_fr) ? r_fuel * (r + 1) / n_fr : r_clad;
         for (int k = 0; k < n_sec; ++k) ring[(size_t)r * n_sec + k] = add_pt(cx + rad * cs[k], cy + rad * sn[k], false, 0, 0, 0, 0);
       }
@@ -212,22 +224,92 @@ int lattice2d(int nx, int ny, int n_sec, int n_fr, double pitch, double r_fuel, 
         const int fy0 = (y == Y0 && cj == 0), fy1 = (y == Y1 && cj == ny - 1);
         sq[k] = add_pt(x, y, true, fx0, fx1, fy0, fy1);
       }
+      if (cell.kind == kFillCell) {
+        for (int k = 0; k < n_sec; ++k) tri(ctr, sq[k], sq[(k + 1) % n_sec], cell.fill);
+        continue;
+      }
       for (int k = 0; k < n_sec; ++k) {
         const int k1 = (k + 1) % n_sec;
-        tri(ctr, ring[k], ring[k1], 1);
+        tri(ctr, ring[k], ring[k1], cell.fuel);
         for (int r = 0; r + 1 < n_rings; ++r) {
           const int32_t a = ring[(size_t)r * n_sec + k], b = ring[(size_t)r * n_sec + k1];
           const int32_t c = ring[(size_t)(r + 1) * n_sec + k1], d = ring[(size_t)(r + 1) * n_sec + k];
-          const int32_t blk = (r + 1 < n_fr) ? 1 : 2;
+          const int32_t blk = (r + 1 < n_fr) ? cell.fuel : cell.clad;
           tri(a, b, c, blk);
           tri(a, c, d, blk);
         }
         const int32_t a = ring[(size_t)(n_rings - 1) * n_sec + k], b = ring[(size_t)(n_rings - 1) * n_sec + k1];
-        tri(a, b, sq[k1], 3);
-        tri(a, sq[k1], sq[k], 3);
+        tri(a, b, sq[k1], cell.mod);
+        tri(a, sq[k1], sq[k], cell.mod);
       }
     }
   return MC_OK;
+}
+
+int lattice2d(int nx, int ny, int n_sec, int n_fr, double pitch, double r_fuel, double r_clad, Lattice2D& G) {
+  if (nx < 1 || ny < 1) return MC_ERR_ARG;
+  std::vector<CellSpec> cells;
+  for (int cj = 0; cj < ny; ++cj)
+    for (int ci = 0; ci < nx; ++ci) cells.push_back(CellSpec{ci, cj, kPinCell, 1, 2, 3, 0});
+  return cells2d(cells, nx, ny, 0.0, 0.0, n_sec, n_fr, pitch, r_fuel, r_clad, G);
+}
+
+// Core map of 193 assemblies: rows of 7, 11, 13, 13, 15 (x7), 13, 13, 11, 7
+// centred on a 15x15 assembly grid.
+const int kCoreRows[15] = {7, 11, 13, 13, 15, 15, 15, 15, 15, 15, 15, 13, 13, 11, 7};
+
+int core2d(int pins, int n_sec, int n_fr, double pitch, double r_fuel, double r_clad, double radius, Lattice2D& G,
+           std::vector<double>* pin_xy) {
+  if (pins < 1 || !(radius > 0.0) || !(pitch > 0.0)) return MC_ERR_ARG;
+  const int na = 15;
+  // margin of reflector cells around the assembly square, out to the radius
+  const double half_core = 0.5 * na * pins * pitch;
+  const int m = radius > half_core ? (int)ceil((radius - half_core) / pitch) : 0;
+  const int n = na * pins + 2 * m;
+  if ((int64_t)n * n > ((int64_t)1 << 26)) return MC_ERR_ARG;
+  const double x0 = -0.5 * n * pitch;
+  std::vector<int> assembly((size_t)na * na, -1);
+  int a = 0;
+  for (int r = 0; r < na; ++r) {
+    const int w = kCoreRows[r], c0 = (na - w) / 2;
+    for (int c = c0; c < c0 + w; ++c) assembly[(size_t)r * na + c] = a++;
+  }
+  std::vector<CellSpec> cells;
+  for (int cj = 0; cj < n; ++cj)
+    for (int ci = 0; ci < n; ++ci) {
+      const int ai = ci - m, aj = cj - m;
+      const int as = (ai >= 0 && aj >= 0 && ai < na * pins && aj < na * pins)
+                         ? assembly[(size_t)(aj / pins) * na + ai / pins]
+                         : -1;
+      const double cx = x0 + (ci + 0.5) * pitch, cy = x0 + (cj + 0.5) * pitch;
+      if (as >= 0) {
+        cells.push_back(CellSpec{ci, cj, kPinCell, 1 + as, 194, 195, 0});
+        if (pin_xy) {
+          pin_xy->push_back(cx);
+          pin_xy->push_back(cy);
+        }
+        continue;
+      }
+      // reflector: whole cells inside the radius, five 72-degree sectors
+      bool inside = true;
+      for (int k = 0; k < 4; ++k) {
+        const double px = x0 + (ci + (k & 1)) * pitch, py = x0 + (cj + (k >> 1)) * pitch;
+        if (px * px + py * py > radius * radius) inside = false;
+      }
+      if (!inside) continue;
+      // sector from the cell centre's quadrant and slope (no atan): 0..4
+      double ang = 0.0;  // a monotone stand-in for angle / (pi/2), in [0, 4)
+      const double ax = fabs(cx), ay = fabs(cy);
+      const double t = ax >= ay ? (ax > 0.0 ? ay / ax : 0.0) * 0.5 : 1.0 - (ay > 0.0 ? ax / ay : 0.0) * 0.5;
+      if (cx >= 0 && cy >= 0) ang = t;
+      else if (cx < 0 && cy >= 0) ang = 2.0 - t;
+      else if (cx < 0) ang = 2.0 + t;
+      else ang = 4.0 - t;
+      int sector = (int)(ang * 5.0 / 4.0);
+      if (sector > 4) sector = 4;
+      cells.push_back(CellSpec{ci, cj, kFillCell, 0, 0, 0, 196 + sector});
+    }
+  return cells2d(cells, n, n, x0, x0, n_sec, n_fr, pitch, r_fuel, r_clad, G);
 }
 
 }  // namespace
@@ -243,14 +325,15 @@ extern "C" int mc_gen_lattice_sizes(int32_t nx, int32_t ny, int32_t nz, int32_t 
   return MC_OK;
 }
 
-extern "C" int mc_gen_lattice(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int32_t n_fr,
-                              double pitch, double height, double r_fuel, double r_clad,
-                              double* xyz, int32_t* tet_vtx, int32_t* tet_block,
-                              int32_t* tet_side_bid) {
-  Lattice2D G;
-  if (nz < 1 || !(height > 0.0)) return MC_ERR_ARG;
-  int rc = lattice2d(nx, ny, n_sec, n_fr, pitch, r_fuel, r_clad, G);
-  if (rc) return rc;
+namespace {
+
+// Extrudes the 2-D mesh into nz layers of prisms over [0, height], three
+// conforming tets per prism; sidesets from the box-side flags of the 2-D
+// points and the bottom/top layers (back = 0, front = 5).  With radial_id
+// >= 0 the x/y box sides are not used: every face off the two z planes gets
+// radial_id (only faces without a neighbour ever read it).
+void extrude(const Lattice2D& G, int nz, double height, double* xyz, int32_t* tet_vtx, int32_t* tet_block,
+             int32_t* tet_side_bid, int radial_id = -1) {
   const int64_t n2 = (int64_t)G.x.size();
   for (int l = 0; l <= nz; ++l) {
     const double z = (l == nz) ? height : height * l / nz;
@@ -288,11 +371,57 @@ extern "C" int mc_gen_lattice(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec,
               if (lay != 0) lo_hit[2] = 0;
               if (lay != nz) hi_hit[2] = 0;
             }
-            tet_side_bid[4 * t + fc] = box_side_id(lo_hit, hi_hit);
+            if (radial_id >= 0) {
+              lo_hit[0] = lo_hit[1] = hi_hit[0] = hi_hit[1] = 0;
+              const int id = box_side_id(lo_hit, hi_hit);
+              tet_side_bid[4 * t + fc] = id >= 0 ? id : radial_id;
+            } else {
+              tet_side_bid[4 * t + fc] = box_side_id(lo_hit, hi_hit);
+            }
           }
         }
       }
     }
+}
+
+}  // namespace
+
+extern "C" int mc_gen_lattice(int32_t nx, int32_t ny, int32_t nz, int32_t n_sec, int32_t n_fr,
+                              double pitch, double height, double r_fuel, double r_clad,
+                              double* xyz, int32_t* tet_vtx, int32_t* tet_block,
+                              int32_t* tet_side_bid) {
+  Lattice2D G;
+  if (nz < 1 || !(height > 0.0)) return MC_ERR_ARG;
+  int rc = lattice2d(nx, ny, n_sec, n_fr, pitch, r_fuel, r_clad, G);
+  if (rc) return rc;
+  extrude(G, nz, height, xyz, tet_vtx, tet_block, tet_side_bid);
+  return MC_OK;
+}
+
+extern "C" int mc_gen_core_sizes(int32_t pins, int32_t nz, int32_t n_sec, int32_t n_fr, double pitch,
+                                 double radius, int64_t* n_vtx, int64_t* n_tet, int64_t* n_pins) {
+  Lattice2D G;
+  std::vector<double> xy;
+  if (nz < 1) return MC_ERR_ARG;
+  int rc = core2d(pins, n_sec, n_fr, pitch, 0.41 * pitch / 1.26, 0.475 * pitch / 1.26, radius, G, &xy);
+  if (rc) return rc;
+  *n_vtx = (int64_t)G.x.size() * (nz + 1);
+  *n_tet = (int64_t)G.tri_block.size() * nz * 3;
+  *n_pins = (int64_t)xy.size() / 2;
+  if ((int64_t)G.x.size() * (nz + 1) > ((int64_t)1 << 31) - 1) return MC_ERR_ARG;
+  return MC_OK;
+}
+
+extern "C" int mc_gen_core(int32_t pins, int32_t nz, int32_t n_sec, int32_t n_fr, double pitch, double height,
+                           double r_fuel, double r_clad, double radius, double* xyz, int32_t* tet_vtx,
+                           int32_t* tet_block, int32_t* tet_side_bid, double* pin_xy) {
+  Lattice2D G;
+  std::vector<double> xy;
+  if (nz < 1 || !(height > 0.0)) return MC_ERR_ARG;
+  int rc = core2d(pins, n_sec, n_fr, pitch, r_fuel, r_clad, radius, G, &xy);
+  if (rc) return rc;
+  extrude(G, nz, height, xyz, tet_vtx, tet_block, tet_side_bid, 6);
+  if (pin_xy) std::copy(xy.begin(), xy.end(), pin_xy);
   return MC_OK;
 }
 

@@ -11,6 +11,12 @@ cube_problem     -- 20 cm cube, 20^3 hexes x 6 tets (48,000 tets), one
 lattice_problem  -- 17x17 pin cells, pitch 1.26 cm, 50 cm tall, fuel/clad/
                     moderator rings (15/4/3 nuclides, 20,000-point grids),
                     about 2.0M tets, uniform source in the fuel cylinders.
+core_problem     -- cylindrical core, radius 180 cm, 400 cm tall: 193
+                    assemblies of 17x17 pin cells plus a reflector of whole
+                    cells, 6 axial layers (about 41M tets); 200 materials of
+                    5-40 nuclides drawn from a pool of 300 (30,000-point
+                    grids, up to 60 peaks); uniform source in every fuel
+                    cylinder.
 """
 from __future__ import annotations
 
@@ -111,6 +117,29 @@ def lattice_mesh(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fu
     return xyz, tv, blk, bid
 
 
+def core_mesh(pins: int = 17, nz: int = 6, n_sec: int = 8, n_fuel_rings: int = 1, pitch: float = 1.26,
+              height: float = 400.0, r_fuel: float = 0.41, r_clad: float = 0.475, radius: float = 180.0):
+    nv, nt, npn = C.c_int64(), C.c_int64(), C.c_int64()
+    _check(lib.mc_gen_core_sizes(pins, nz, n_sec, n_fuel_rings, pitch, radius, C.byref(nv), C.byref(nt),
+                                 C.byref(npn)), "mc_gen_core_sizes")
+    xyz = np.zeros((nv.value, 3), np.float64)
+    tv = np.zeros((nt.value, 4), np.int32)
+    blk = np.zeros(nt.value, np.int32)
+    bid = np.zeros((nt.value, 4), np.int32)
+    pins_xy = np.zeros((npn.value, 2), np.float64)
+    _check(lib.mc_gen_core(pins, nz, n_sec, n_fuel_rings, pitch, height, r_fuel, r_clad, radius, ptr(xyz), ptr(tv),
+                           ptr(blk), ptr(bid), ptr(pins_xy)), "mc_gen_core")
+    return xyz, tv, blk, bid, pins_xy
+
+
+def _splitmix(x: int) -> int:
+    """splitmix64 finaliser (integer-only, identical on every host)."""
+    x = (x + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return x ^ (x >> 31)
+
+
 def make_nuclide(seed: int, index: int, n_pts: int, n_peaks: int = 20,
                  E_min: float = E_MIN, E_max: float = E_MAX) -> Nuclide:
     E = np.zeros(n_pts)
@@ -162,3 +191,33 @@ def lattice_problem(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n
     return Problem(f"lattice{nx}x{ny}x{nz}", xyz, tv, blk, bid, nucs, mats,
                    np.array([1, 2, 3], np.int32), np.array([1, 2, 3], np.int32), src,
                    {b: MC_BC_VACUUM for b in range(6)})
+
+
+def core_problem(pins: int = 17, nz: int = 6, n_sec: int = 8, n_fuel_rings: int = 1, pitch: float = 1.26,
+                 height: float = 400.0, radius: float = 180.0, n_pool: int = 300, n_pts: int = 30000,
+                 max_peaks: int = 60, nuclides_per_material=(5, 40), seed: int = 20240611) -> Problem:
+    """Cylindrical core (about 41M tets at the defaults).  Blocks 1..193 are
+    the fuel of each assembly, 194 clad, 195 moderator, 196..200 reflector
+    sectors; block b maps to material b.  Material b holds a count drawn
+    uniformly from `nuclides_per_material` of distinct nuclides out of a
+    pool of `n_pool`; nuclide k has 1 + (k mod max_peaks) resonance peaks.
+    Vacuum on every sideset (bottom 0, top 5, radial 6)."""
+    xyz, tv, blk, bid, pins_xy = core_mesh(pins, nz, n_sec, n_fuel_rings, pitch, height, radius=radius)
+    nucs = [make_nuclide(seed, k, n_pts, 1 + k % max_peaks) for k in range(n_pool)]
+    lo, hi = nuclides_per_material
+    mats = []
+    for b in range(1, 201):
+        h = _splitmix(seed * 1000003 + b)
+        cnt = min(lo + h % (hi - lo + 1), n_pool)
+        chosen, j = [], 0
+        while len(chosen) < cnt:
+            k = _splitmix(h + 7919 * j) % n_pool
+            j += 1
+            if k not in chosen:
+                chosen.append(k)
+        mats.append(Material(b, np.array(sorted(chosen), np.int32), make_densities(seed, 1000 + b, cnt)))
+    blocks = np.arange(1, 201, dtype=np.int32)
+    src = Source(space=MC_SRC_CYLINDERS, cyl_xy=np.ascontiguousarray(pins_xy), cyl_r=0.41 * pitch / 1.26,
+                 cyl_z0=0.0, cyl_z1=height)
+    return Problem(f"core{pins}x{nz}", xyz, tv, blk, bid, nucs, mats, blocks, blocks.copy(), src,
+                   {b: MC_BC_VACUUM for b in range(7)})

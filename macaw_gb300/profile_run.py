@@ -1,0 +1,42 @@
+"""Runs the lattice workload once for profiling (ncu, nsys).
+
+  python -m macaw_gb300.profile_run --precision fp64 --hist 1000000 --batches 2
+
+One untimed batch (so the first launches of every kernel are warm), then
+`--batches` batches of `--hist` histories through one pipelined call, with
+fixed execution parameters (the autotuner's choices on this workload unless
+overridden).  Prints the run's statistics as JSON.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+from . import Tracker, problems
+from ._lib import MC_PREC_FP64, MC_PREC_MIXED
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--hist", type=int, default=1_000_000)
+    ap.add_argument("--batches", type=int, default=2)
+    ap.add_argument("--pins", type=int, default=17, help="pin cells per lattice side")
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--max-seg", type=int, default=64)
+    ap.add_argument("--sort", type=int, default=9)
+    args = ap.parse_args()
+    prec = MC_PREC_MIXED if args.precision == "mixed" else MC_PREC_FP64
+    block = args.block or (64 if prec == MC_PREC_MIXED else 128)
+    p = problems.lattice_problem(nx=args.pins, ny=args.pins)
+    n = args.hist
+    with Tracker(0) as t:
+        t.load(p)
+        kw = dict(bank_size=n, block_size=block, max_seg=args.max_seg, sort_queue=args.sort, precision=prec)
+        t.run(n, first=0, seed=1, accumulate=True, **kw)
+        st = t.run(n * args.batches, first=n, seed=1, accumulate=True, batch_sizes=[n] * args.batches, **kw)
+        print(json.dumps(st.as_dict()))
+
+
+if __name__ == "__main__":
+    main()
