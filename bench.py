@@ -15,6 +15,19 @@ batches ("steps") of 1,000,000 histories with a 1,000,000-particle bank.
   roofline  HBM roofline of the dominant kernel (the segment walk)
   cpu_baseline  the CPU restatement (oracle) on the host cores, bounded sample
 
+Two more workloads print their own JSON line (not the default run):
+  --workload core   the batched large-mesh form: cylindrical core, radius
+                    180 cm, 400 cm, 41,283,792 tets, 200 materials of 5-40
+                    nuclides (30,000-point grids); 1e8 histories in 64
+                    batches of log-uniform size (1e5-5e6, rescaled) through
+                    one pipelined, graph-replayed, autotuned call, mixed and
+                    FP64 on the same histories
+  --workload serve  the serving form: a Poisson stream (50 requests/s) over
+                    8 preloaded meshes of 10k-2M tets, continuous batching
+                    with the mixed tracker and FP64 per-request tallies,
+                    p50/p99 latency and throughput beside a one-request-at-
+                    a-time FP64 loop on the same arrival trace
+
 --impl reference times the reference path's CPU implementation (the oracle
 restatement; MaCaw itself needs MOOSE/OpenMC/libMesh/MPI, absent here) on
 the same workload.  Under torchrun every rank tracks its own history range
@@ -38,6 +51,7 @@ METRIC = "histories/s on 1 GB300, mixed vs plain FP64 at equal tally error; p50/
 HIST_PER_STEP = 1_000_000
 BANK = 1_000_000
 B_SEG_FP64 = 164   # algorithmic bytes per segment: planes 128 + neighbours 16 + material 4 + tally RMW 16
+B_SEG_MIXED = 100  # float planes 64 + neighbours 16 + material 4 + tally RMW 16
 CPU_SAMPLE = 400_000
 REF_SAMPLE = 100_000
 # DRAM bytes per segment of the advance kernel from the committed ncu
@@ -164,6 +178,115 @@ def run_reference(args):
     return 0
 
 
+def core_batch_sizes(total=100_000_000, n=64, lo=1e5, hi=5e6, seed=64):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    s = np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+    s = np.floor(s * (total / s.sum())).astype(np.int64)
+    s[-1] += total - s.sum()
+    return s
+
+
+def run_core(args):
+    """Batched large-mesh form (one JSON line)."""
+    import numpy as np
+    import torch
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    p = problems.core_problem()
+    sizes = core_batch_sizes(args.core_histories)
+    stream = torch.cuda.Stream()
+    bank = 2_000_000
+    out = {"metric": "histories/s, batched large-mesh form", "unit": "histories/s", "n_gpus": 1,
+           "higher_is_better": True, "dtype": "f32+f64",
+           "data": "synthetic (seeded generators)",
+           "config": {"workload": f"core R=180 cm H=400 cm, {p.n_tet} tets, 200 materials x 5-40 nuclides x "
+                                  f"30,000 pts; {int(sizes.sum())} histories in {sizes.size} batches "
+                                  f"({int(sizes.min())}..{int(sizes.max())})", "tets": p.n_tet,
+                      "bank_size": bank, "l2": "inputs larger than L2 (mesh tables about 10 GB)"}}
+    res = {}
+    for name, prec in (("mixed", MC_PREC_MIXED), ("fp64", MC_PREC_FP64)):
+        t = Tracker(0)
+        t.load(p)
+        t.set_stream(stream.cuda_stream)
+        if name == "mixed":
+            out["setup_s"] = time.perf_counter() - t0
+        params, rate = t.autotune(trial=1_000_000, first=10**10, bank_size=bank, precision=prec,
+                                  block_size=256, max_seg=64)
+        params["graph"] = True if name == "mixed" else params["graph"]
+        t.run(int(sizes[:3].sum()), first=2 * 10**10, seed=1, precision=prec, accumulate=True,
+              batch_sizes=sizes[:3], **params)  # warm-up
+        t.reset_tally()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = t.run(int(sizes.sum()), first=0, seed=1, precision=prec, accumulate=True, batch_sizes=sizes,
+                   **params)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[name] = {"value": int(sizes.sum()) / (ms / 1e3), "ms": ms, "tuned": params,
+                     "segments_per_s": st.n_seg / (ms / 1e3), "segments_per_history": st.n_seg / sizes.sum(),
+                     "xs_per_history": st.n_xs / sizes.sum(), "stuck": int(st.n_stuck), "lost": int(st.n_lost),
+                     "fallback_fraction": st.n_fallback / max(st.n_seg, 1), "gpu_launches": int(st.n_launch),
+                     "batches_done": t.batches_done()}
+        res[name]["sum"] = t.tally(MC_TALLY_SUM)
+        t.close()
+    a, b = res["mixed"].pop("sum"), res["fp64"].pop("sum")
+    nz = b > 0
+    rel = np.abs(a[nz] - b[nz]) / b[nz]
+    out.update({"value": res["mixed"]["value"], "mixed": res["mixed"], "fp64": res["fp64"],
+                "speedup_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+                "flux_rel_diff_mean": float(rel.mean()), "flux_rel_diff_max": float(rel.max()),
+                "flux_rel_diff_note": "SUM tallies, mixed vs FP64 on the same histories, elements with a score"})
+    print(json.dumps(out))
+    return 0
+
+
+def serve_problems():
+    from macaw_gb300 import problems
+    cubes = [(12, 12.0), (20, 20.0), (40, 40.0), (60, 60.0)]
+    lats = [(5, 5, 10, 20.0), (9, 9, 15, 30.0), (13, 13, 20, 40.0), (17, 17, 21, 50.0)]
+    ps = [problems.cube_problem(n=n, L=L, seed=1000 + i) for i, (n, L) in enumerate(cubes)]
+    ps += [problems.lattice_problem(nx=a, ny=b, nz=c, height=h, seed=2000 + i) for i, (a, b, c, h) in enumerate(lats)]
+    return ps
+
+
+def run_serve(args):
+    """Serving form (one JSON line)."""
+    import torch
+    from macaw_gb300 import Tracker
+    from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED
+    from macaw_gb300.serve import Server, poisson_jobs, run_one_at_a_time, run_stream
+    torch.cuda.set_device(0)
+    ps = serve_problems()
+    jobs = poisson_jobs(ps, rate=50.0, duration=args.serve_seconds, seed=7, hist_range=(1e4, 1e6))
+    srv = Server(ps, precision=MC_PREC_MIXED, hbm_budget=96 << 30, bank=1 << 20, max_slots=8)
+    warm = poisson_jobs(ps, rate=50.0, duration=1.0, seed=8, hist_range=(1e4, 1e5))
+    run_stream(srv, warm)
+    rep = run_stream(srv, jobs)
+    slots = list(srv.slots)
+    srv.close()
+    trackers = [Tracker(0).load(p) for p in ps]
+    run_one_at_a_time(trackers, warm[:8], precision=MC_PREC_FP64)
+    base = run_one_at_a_time(trackers, jobs, precision=MC_PREC_FP64)
+    for t in trackers:
+        t.close()
+    out = {"metric": "serving: histories/s and p50/p99 request latency", "unit": "histories/s",
+           "value": rep["histories_per_s"], "n_gpus": 1, "higher_is_better": True, "dtype": "f32+f64",
+           "data": "synthetic (seeded generators and arrival trace)",
+           "config": {"workload": f"Poisson 50 requests/s for {args.serve_seconds} s over 8 meshes "
+                                  f"({', '.join(str(p.n_tet) for p in ps)} tets), point sources, Watt energies, "
+                                  "log-uniform 1e4..1e6 histories", "slots_per_mesh": slots,
+                      "requests": rep["requests"], "histories": rep["histories"]},
+           "serving": rep, "one_at_a_time_fp64": base,
+           "p50_speedup": base["p50_ms"] / rep["p50_ms"], "p99_speedup": base["p99_ms"] / rep["p99_ms"]}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -174,10 +297,17 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (fixed parameters)")
     ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
+    ap.add_argument("--workload", default="lattice", choices=["lattice", "core", "serve"])
+    ap.add_argument("--core-histories", type=int, default=100_000_000)
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "core":
+        return run_core(args)
+    if args.workload == "serve":
+        return run_serve(args)
 
     import numpy as np
     import torch
@@ -209,11 +339,13 @@ def main():
         return t
 
     def tune(t, precision):
-        fixed = {"bank_size": BANK, "block_size": 256, "max_seg": 64, "sort_queue": 0, "refill": False}
+        fixed = {"bank_size": BANK, "block_size": 128, "max_seg": 64 if precision == MC_PREC_FP64 else 128,
+                 "sort_queue": 9, "refill": False, "graph": True}
         if args.no_tune:
             return fixed, None
-        params, rate = t.autotune(trial=min(n, 300_000), first=base + (W + 2 * K + 1) * n, bank_size=BANK,
-                                  precision=precision, block_size=256, max_seg=64)
+        # trials: four pipelined batches of n/2 histories
+        params, rate = t.autotune(trial=2 * n, first=base + (W + 2 * K + 1) * n, bank_size=BANK,
+                                  precision=precision, block_size=128, max_seg=64, sort_queue=9)
         return params, rate
 
     def timed(t, precision, params, first_step, steps, profile):
@@ -253,6 +385,8 @@ def main():
         timed(tm, MC_PREC_MIXED, paramsm, 0, W, False)
         mms, mst = timed(tm, MC_PREC_MIXED, paramsm, W, K, False)
         summ = tm.tally(MC_TALLY_SUM)
+        # one more batch with the walk launches timed, for the walk's roofline
+        _, pst = timed(tm, MC_PREC_MIXED, paramsm, W + K, 1, True)
         tm.close()
         nz = sum64 > 0
         rel = np.abs(summ[nz] - sum64[nz]) / sum64[nz]
@@ -263,6 +397,14 @@ def main():
                  "flux_rel_diff_note": "element SUM tallies, mixed vs FP64 (bit-exact to the oracle), same "
                                        f"{n * (W + K)} histories, elements with a score",
                  "tuned": paramsm, "gpu_launches": int(mst.n_launch)}
+        if pst.ms_advance > 0:
+            mach = pst.n_seg_advance * B_SEG_MIXED / (pst.ms_advance / 1e3) / 1e9
+            mixed["roofline"] = {"bound": "hbm", "kernel": "k_ev_advance<MIXED>" if paramsm.get("refill")
+                                 else "k_ev_advance_mixed", "achieved": mach, "unit": "GB/s",
+                                 "algorithmic_bytes_per_segment": B_SEG_MIXED,
+                                 "advance_ms_per_launch": pst.ms_advance / max(pst.n_advance_launch, 1),
+                                 "segments_per_launch": pst.n_seg_advance / max(pst.n_advance_launch, 1),
+                                 "sample": f"one extra profiled batch of {n} histories"}
 
     # --- end to end through the C ABI with host buffers, one call per step ---
     k0 = W + K
@@ -293,13 +435,16 @@ def main():
     if rank == 0:
         peak, peak_kind = load_peaks()
         segs = st.n_seg
-        adv_bytes = segs * B_SEG_FP64
+        walk = st.n_seg_advance  # segments inside the timed walk launches (the rest: tail kernel)
+        adv_bytes = walk * B_SEG_FP64
         achieved = adv_bytes / (st.ms_advance / 1e3) / 1e9 if st.ms_advance > 0 else None
-        roof = {"bound": "hbm", "kernel": "k_ev_advance_static<FP64>",
+        roof = {"bound": "hbm", "kernel": "k_ev_advance<FP64>" if params64.get("refill")
+                else "k_ev_advance_static<FP64>",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * segs / max(st.n_advance_launch, 1))
+                "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * walk / max(st.n_advance_launch, 1))
                 if ADVANCE_DRAM_BYTES_PER_SEG else None,
+                "segments_per_launch": walk / max(st.n_advance_launch, 1),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes_per_segment": B_SEG_FP64,
                 "advance_ms_per_launch": st.ms_advance / max(st.n_advance_launch, 1),
@@ -307,6 +452,9 @@ def main():
                 "note": "the FP64 walk is bound by GB300's FP64 pipe, not HBM (see profiles/)"}
         cfg = dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single",
                    pipelined_batches=K, tuned=params64)
+        if mixed is not None and "roofline" in mixed:
+            mixed["roofline"]["peak"] = peak
+            mixed["roofline"]["frac"] = mixed["roofline"]["achieved"] / peak
         line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64",

@@ -115,7 +115,8 @@ typedef struct {
                               pipeline, each folded into SUM/SUM_SQ when it drains (needs accumulate) */
   int32_t graph;           /* event mode: 1 captures a cycle of event iterations once as a CUDA
                               graph and replays it (ignored with profile) */
-  int32_t pad;
+  int32_t walk_plain;      /* mixed event walk: 0 requests each next element's record one step ahead
+                              (fewer resident warps), 1 at the top of its step */
   const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
   const int64_t* batch_sizes; /* HOST array of n_batches sizes adding up to n_histories */
 } mc_run_desc;
@@ -143,6 +144,7 @@ typedef struct {
   double ms_total;      /* device time of the last mc_run (CUDA events) */
   double ms_advance;    /* device time in the segment-walk kernels */
   int64_t n_advance_launch;
+  int64_t n_seg_advance; /* segments walked inside the segment-walk kernels (the rest: tail kernel) */
 } mc_stats;
 
 /* ---- context --------------------------------------------------------- */

@@ -38,7 +38,7 @@ class RunDesc(C.Structure):
                 ("block_size", C.c_int32), ("max_seg_per_advance", C.c_int32),
                 ("record_traces", C.c_int32), ("accumulate", C.c_int32), ("sort_queue", C.c_int32),
                 ("profile", C.c_int32), ("refill", C.c_int32), ("n_batches", C.c_int32), ("graph", C.c_int32),
-                ("pad", C.c_int32), ("sites", C.c_void_p), ("batch_sizes", C.c_void_p)]
+                ("walk_plain", C.c_int32), ("sites", C.c_void_p), ("batch_sizes", C.c_void_p)]
 
 
 class Request(C.Structure):
@@ -49,7 +49,7 @@ class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("n_hist", "n_seg", "n_coll", "n_leak", "n_absorb", "n_cutoff",
                                         "n_stuck", "n_lost", "n_badxs", "n_fallback", "n_xs", "n_launch")] + \
                [("leak_weight", C.c_double), ("ms_total", C.c_double), ("ms_advance", C.c_double),
-                ("n_advance_launch", C.c_int64)]
+                ("n_advance_launch", C.c_int64), ("n_seg_advance", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -79,9 +79,11 @@ struct mc_ctx {
   DevBuf d_traces;
   int64_t trace_n = 0;
   DevBuf d_sites;
-  DevBuf d_tally2, d_batch_end;
+  DevBuf d_tally2, d_batch_end, d_live;
+  DevBuf d_accum_save;  // SUM and SUM_SQ kept aside while the autotuner runs pipelined trials
+  int64_t batches_save = 0;
   DevBuf d_sort_tmp, d_sort_cnt;
-  bool tally2_clear = false;
+  bool tally2_clear = false;  // d_tally2 is all zeros between runs
   long long h_limit = 0;
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
@@ -197,6 +199,7 @@ DevMesh dev_mesh(mc_ctx* c) {
   for (int k = 0; k < 3; ++k) {
     M.glo[k] = c->mesh.glo[k];
     M.gh[k] = c->mesh.gh[k];
+    M.ginv[k] = 1.0 / c->mesh.gh[k];
     M.gn[k] = c->mesh.gn[k];
   }
   M.gstart = c->d_gstart.as<int64_t>();
@@ -505,6 +508,7 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.precision = d->precision;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.walk_plain = d->walk_plain;
   a.sort_shift = -1;
   a.sort_buckets = 0;
   a.sort_tmp = nullptr;
@@ -541,10 +545,12 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   const int grid = std::max(1, c->n_sm * per_sm);
   int n_launch = 0, n_adv = 0;
   float ms_adv = 0.0f;
-  // batches run through one pipeline: batch b scores into tally[b & 1] and
-  // is folded into SUM/SUM_SQ (normalised by its size) once its last
-  // particle ends; births of batch b+2 wait until then
+  // batches run through one pipeline: batch b scores into tally slot
+  // b % slots and is folded into SUM/SUM_SQ (normalised by its size) once
+  // its last particle ends; births of batch b+slots wait until then, so the
+  // long walks of one batch overlap the bulk of the next slots-1 batches
   const int nb = d->n_batches > 1 ? d->n_batches : 1;
+  const int slots = std::min(nb, kPipeSlots);
   std::vector<int64_t> bend((size_t)nb);
   if (nb > 1) {
     if (!d->batch_sizes) return set_err(c, MC_ERR_ARG, "n_batches > 1 needs batch_sizes");
@@ -564,11 +570,15 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       q.end = bend[b];
       q.first_id = a.first + q.start;
       q.seed = d->seed;
-      q.slot = b & 1;
+      q.slot = b % slots;
       q.has_src = 0;
     }
     CK(upload(c->d_batch_end, rq, c->stream), "upload batch table");
-    CK(c->d_tally2.alloc(sizeof(double) * (size_t)c->mesh.n_tet), "allocate batch tally");
+    const size_t need = sizeof(double) * (size_t)c->mesh.n_tet * (size_t)(slots - 1);
+    if (c->d_tally2.bytes < need) {
+      CK(c->d_tally2.alloc(need), "allocate batch tallies");
+      c->tally2_clear = false;
+    }
     if (!c->tally2_clear) {
       CK(cudaMemsetAsync(c->d_tally2.p, 0, c->d_tally2.bytes, c->stream), "clear batch tally");
       c->tally2_clear = true;
@@ -585,10 +595,11 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.n_tet = c->mesh.n_tet;
   a.live = nullptr;
   // history-form batches all score into slot 0 (one runs at a time);
-  // event-form batches alternate between slots 0 and 1
+  // event-form batch b scores into slot b % slots
   auto fold = [&](int b) -> int {
     const int64_t size = bend[b] - (b ? bend[b - 1] : 0);
-    double* buf = (d->mode == MC_MODE_EVENT && (b & 1)) ? a.tally2 : a.tally;
+    const int sl = (d->mode == MC_MODE_EVENT) ? b % slots : 0;
+    double* buf = sl ? a.tally2 + (int64_t)(sl - 1) * c->mesh.n_tet : a.tally;
     CK(launch_accumulate(buf, c->d_sum.as<double>(), c->d_sumsq.as<double>(),
                          c->mesh.n_tet, size > 0 ? 1.0 / (double)size : 0.0, c->stream),
        "launch accumulate");
@@ -626,13 +637,18 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       if (!bank_complete(B)) return set_err(c, MC_ERR_STATE, "internal: particle bank incomplete");
       const EventQueues Q = dev_queues(c);
       EventCtl* ctl = c->d_ctl.as<EventCtl>();
-      if (nb > 1) a.live = ctl->live;
+      int h_live[kPipeSlots] = {0};
+      if (nb > 1) {
+        if (c->d_live.bytes < sizeof(int) * kPipeSlots) CK(c->d_live.alloc(sizeof(int) * kPipeSlots), "allocate live");
+        CK(cudaMemsetAsync(c->d_live.p, 0, sizeof(int) * kPipeSlots, c->stream), "clear live");
+        a.live = c->d_live.as<int>();
+      }
       if (a.sort_shift >= 0) {
         CK(c->d_sort_tmp.alloc(std::max(c->d_sort_tmp.bytes, sizeof(int) * (size_t)c->bank_cap)), "allocate sort");
         a.sort_tmp = c->d_sort_tmp.as<int>();
         a.sort_cnt = c->d_sort_cnt.as<int>();
       }
-      int64_t limit = nb > 1 ? bend[std::min(1, nb - 1)] : d->n_histories;
+      int64_t limit = nb > 1 ? bend[slots - 1] : d->n_histories;
       CK(launch_event_init(M, X, S, a, B, Q, ctl, block, grid, c->stream, limit), "launch event init");
       n_launch = 1;
       int par = 0;
@@ -687,11 +703,14 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
           par ^= 1;
         }
         CK(cudaMemcpyAsync(&h, ctl, sizeof(EventCtl), cudaMemcpyDeviceToHost, c->stream), "read event control");
+        if (nb > 1)
+          CK(cudaMemcpyAsync(h_live, a.live, sizeof(int) * slots, cudaMemcpyDeviceToHost, c->stream),
+             "read live counters");
         CK(cudaStreamSynchronize(c->stream), "event loop");
         if (nb > 1) {
-          // retire drained batches, then let the next batch be born
+          // retire drained batches, then let the next batches be born
           bool moved = false;
-          while (oldest < nb && h.next_hist >= bend[oldest] && h.live[oldest & 1] == 0) {
+          while (oldest < nb && h.next_hist >= bend[oldest] && h_live[oldest % slots] == 0) {
             rc = fold(oldest);
             if (rc) return rc;
             ++oldest;
@@ -699,7 +718,7 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
             moved = true;
           }
           if (moved && oldest < nb) {
-            c->h_limit = bend[std::min(oldest + 1, nb - 1)];
+            c->h_limit = bend[std::min(oldest + slots - 1, nb - 1)];
             CK(cudaMemcpyAsync(&ctl->birth_limit, &c->h_limit, sizeof(long long), cudaMemcpyHostToDevice,
                                c->stream),
                "raise birth limit");
@@ -763,6 +782,7 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   s.ms_total = ms;
   s.ms_advance = ms_adv;
   s.n_advance_launch = n_adv;
+  s.n_seg_advance = (int64_t)cnt[kCntSegWalk];
   if (s.n_hist != d->n_histories)
     return set_err(c, MC_ERR_DEVICE, "device finished " + std::to_string(s.n_hist) + " of " +
                                          std::to_string(d->n_histories) + " histories");
@@ -927,5 +947,31 @@ int ctx_event_state(mc_ctx* c, int64_t cap, CtxEvent* out) {
 }
 
 int ctx_fail(mc_ctx* c, int code, const std::string& msg) { return set_err(c, code, msg); }
+
+// Copies SUM and SUM_SQ (and the batch count) aside (restore = 0) or back
+// (restore = 1), so that trial runs which fold batches leave no trace.
+int accum_snapshot(mc_ctx* c, int restore) {
+  std::lock_guard<std::mutex> lock(c->mu);
+  if (!c->d_sum.p || !c->d_sumsq.p) return MC_OK;  // nothing accumulated yet
+  const size_t n = c->d_sum.bytes;
+  cudaError_t e = cudaSuccess;
+  if (!restore) {
+    if (c->d_accum_save.bytes != 2 * n) e = c->d_accum_save.alloc(2 * n);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->d_accum_save.p, c->d_sum.p, n, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((char*)c->d_accum_save.p + n, c->d_sumsq.p, n, cudaMemcpyDeviceToDevice, c->stream);
+    c->batches_save = c->batches;
+  } else {
+    if (c->d_accum_save.bytes != 2 * n) return set_err(c, MC_ERR_STATE, "no saved accumulators");
+    e = cudaMemcpyAsync(c->d_sum.p, c->d_accum_save.p, n, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->d_sumsq.p, (char*)c->d_accum_save.p + n, n, cudaMemcpyDeviceToDevice, c->stream);
+    c->batches = c->batches_save;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return set_err(c, MC_ERR_CUDA, std::string("accumulator snapshot: ") + cudaGetErrorString(e));
+  return MC_OK;
+}
 
 }  // namespace mc

@@ -28,6 +28,35 @@ struct __align__(16) Tet32 {
 };
 constexpr int kMatChange = 1 << 30;
 
+// float <-> double by integer operations, for the mixed-precision walk: on
+// this GPU a conversion instruction issues on the narrow FP64 pipe, an
+// integer operation on the full-rate ALU.  widen() is exact for every
+// normal float (zero and subnormals give a signed zero); narrow() rounds to
+// nearest even like a conversion for results in the normal float range and
+// gives a signed zero below it (|x| < 2^-126) -- positions, directions and
+// cross sections never leave that range except through zero.
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+  if (e == 0u) return __longlong_as_double((long long)sign);
+  return __longlong_as_double(
+      (long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29)));
+}
+
+__device__ __forceinline__ float narrow(double d) {
+  const uint64_t b = (uint64_t)__double_as_longlong(d);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ffu) - 896;
+  if (e <= 0) return __uint_as_float(sign);
+  const uint64_t m = b & 0xfffffffffffffull;
+  const uint32_t lo = (uint32_t)(m & 0x1fffffffu);  // 29 dropped bits
+  uint32_t r = ((uint32_t)e << 23) + (uint32_t)(m >> 29);
+  if (lo > 0x10000000u || (lo == 0x10000000u && (r & 1u))) ++r;  // may carry into the exponent
+  if (e >= 255) r = 0x7f800000u;
+  return __uint_as_float(sign | r);
+}
+
 __device__ __forceinline__ int side_entry(const int4& n, int f) {
   return f == 0 ? n.x : f == 1 ? n.y : f == 2 ? n.z : n.w;
 }
@@ -39,7 +68,7 @@ struct DevMesh {
   const int* __restrict__ bc_type;      // per boundary id: 0 vacuum, 1 reflect
   int n_bid;
   int64_t n_tet;
-  double glo[3], gh[3];
+  double glo[3], gh[3], ginv[3];  // locator origin, cell size, 1 / cell size
   int gn[3];
   const int64_t* __restrict__ gstart;
   const int* __restrict__ gtets;
@@ -189,7 +218,10 @@ __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, doub
   const double xs[3] = {x, y, z};
   int ci[3];
   for (int k = 0; k < 3; ++k) {
-    const double q = (xs[k] - M.glo[k]) / M.gh[k];
+    // a multiplication instead of a division: the cell lists are padded by
+    // kLocateTol, far above the few-ulp difference, so any point near a
+    // cell boundary is listed in both cells and the result is the same
+    const double q = (xs[k] - M.glo[k]) * M.ginv[k];
     int c = (int)floor(q);
     if (!(q >= 0.0)) c = 0;
     if (c > M.gn[k] - 1) c = M.gn[k] - 1;
@@ -204,17 +236,23 @@ __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, doub
   for (int64_t q = M.gstart[cell]; q < q1; ++q) {
     const int t = __ldg(M.gtets + q);
     const float4* P32 = M.tet[t].p;
-    bool out = false;
+    bool out = false, in = true;
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
       const float4 pl = __ldg(P32 + f);
       const float s32 = fmaf(pl.x, xf, fmaf(pl.y, yf, pl.z * zf)) - pl.w;
-      if (s32 > 1e-9f + 7.3e-7f * (fabsf(pl.w) + xa)) {
+      const float m = 1e-9f + 7.3e-7f * (fabsf(pl.w) + xa);
+      if (s32 > m) {
         out = true;
         break;
       }
+      if (!(s32 < -m)) in = false;
     }
     if (out) continue;
+    // strictly inside by more than the float error and kLocateTol on every
+    // side: the FP64 test below would find it inside and entered, and no
+    // other tet of a conforming mesh can contain the point
+    if (in) return t;
     bool inside = true, enters = true;
     for (int f = 0; f < 4; ++f) {
       const double4_32a pl = M.planes[4 * (int64_t)t + f];
@@ -268,6 +306,95 @@ __device__ __forceinline__ void sample_source(const DevXS& X, const DevSource& S
   o.v = sm * cp;
   o.w = sm * sp;
   o.E = (S.energy == 1) ? S.mono_E : sample_watt(ss, S.watt_a, S.watt_b, X.E_lo, X.E_hi);
+  o.wgt = 1.0;
+}
+
+// Source site in float arithmetic for the mixed-precision form: the same
+// source stream and the same sequence of draws as sample_source, each draw
+// reduced to its 24 high bits, with float sqrt/log; the site is widened to
+// double exactly.  Energies are accepted in [E_lo, E_hi) of the double
+// grid bounds.
+__device__ __forceinline__ float prn32(uint64_t& s) {
+  s = kPrnMult * s + kPrnAdd;
+  uint64_t w = ((s >> ((s >> 59u) + 5u)) ^ s) * 12605985483714917081ULL;
+  w = (w >> 43u) ^ w;
+  return (float)(uint32_t)(w >> 40) * 0x1.0p-24f;
+}
+
+__device__ __forceinline__ void azimuth32(uint64_t& s, float& c, float& sn) {
+  for (int it = 0; it < 10000; ++it) {
+    const float a = 2.0f * prn32(s) - 1.0f;
+    const float b = 2.0f * prn32(s) - 1.0f;
+    const float r2 = fmaf(a, a, b * b);
+    if (r2 > 0.0f && r2 <= 1.0f) {
+      const float inv = 1.0f / r2;
+      c = (a - b) * (a + b) * inv;
+      sn = 2.0f * a * b * inv;
+      return;
+    }
+  }
+  c = 1.0f;
+  sn = 0.0f;
+}
+
+__device__ __forceinline__ double watt32(uint64_t& s, float a, float b, double E_lo, double E_hi) {
+  const float ab4 = a * a * b * 0.25f, a2b = a * a * b;
+  for (int it = 0; it < 1000; ++it) {
+    const float r1 = prn32(s);
+    const float r2 = prn32(s);
+    float c2 = 0.5f;
+    for (int j = 0; j < 10000; ++j) {
+      const float p = prn32(s), q = prn32(s);
+      const float rr = fmaf(p, p, q * q);
+      if (rr > 0.0f && rr <= 1.0f) {
+        c2 = p * p / rr;
+        break;
+      }
+    }
+    const float w = -a * (logf(r1) + logf(r2) * c2);
+    const float E = w + ab4 + (2.0f * prn32(s) - 1.0f) * sqrtf(a2b * w);
+    if (E > 0.0f && E < 3.0e38f) {
+      const double Ed = widen(E);
+      if (Ed < E_hi && Ed >= E_lo) return Ed;
+    }
+  }
+  return E_hi * 0.5;
+}
+
+__device__ __forceinline__ void sample_source32(const DevXS& X, const DevSource& S, const Skip& k,
+                                                uint64_t master, mc_site& o) {
+  uint64_t ss = stream_seed(k, master, kStreamSource);
+  float x, y, z;
+  if (S.space == 0) {
+    x = narrow(S.point[0]);
+    y = narrow(S.point[1]);
+    z = narrow(S.point[2]);
+  } else if (S.space == 1) {
+    x = fmaf(prn32(ss), narrow(S.box_hi[0]) - narrow(S.box_lo[0]), narrow(S.box_lo[0]));
+    y = fmaf(prn32(ss), narrow(S.box_hi[1]) - narrow(S.box_lo[1]), narrow(S.box_lo[1]));
+    z = fmaf(prn32(ss), narrow(S.box_hi[2]) - narrow(S.box_lo[2]), narrow(S.box_lo[2]));
+  } else {
+    int c = (int)(prn32(ss) * (float)S.n_cyl);
+    if (c > S.n_cyl - 1) c = S.n_cyl - 1;
+    const float r = narrow(S.cyl_r) * sqrtf(prn32(ss));
+    float ct, st;
+    azimuth32(ss, ct, st);
+    x = fmaf(r, ct, narrow(__ldg(S.cyl_xy + 2 * c)));
+    y = fmaf(r, st, narrow(__ldg(S.cyl_xy + 2 * c + 1)));
+    const float z0 = narrow(S.cyl_z0);
+    z = fmaf(prn32(ss), narrow(S.cyl_z1) - z0, z0);
+  }
+  const float mu = 2.0f * prn32(ss) - 1.0f;
+  float cp, sp;
+  azimuth32(ss, cp, sp);
+  const float sm = sqrtf(fmaxf(0.0f, (1.0f - mu) * (1.0f + mu)));
+  o.x = widen(x);
+  o.y = widen(y);
+  o.z = widen(z);
+  o.u = widen(mu);
+  o.v = widen(sm * cp);
+  o.w = widen(sm * sp);
+  o.E = (S.energy == 1) ? S.mono_E : watt32(ss, narrow(S.watt_a), narrow(S.watt_b), X.E_lo, X.E_hi);
   o.wgt = 1.0;
 }
 
@@ -528,6 +655,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
   const float Eden = 7.2e-7f * (fabsf(uf) + fabsf(vf) + fabsf(wf));
   const float4* P32 = M.tet[p.elem].p;
+  const int4 nb4 = __ldg(&M.tet[p.elem].nbr);  // issued with the plane loads
   bool sure = true;
   int bf = -1;
   float tb = 3.0e38f, eb = 0.0f, lo_other = 3.0e38f;
@@ -591,7 +719,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     p.x = p.x + L * p.u;
     p.y = p.y + L * p.v;
     p.z = p.z + L * p.w;
-    const int nb = side_entry(M.tet[p.elem].nbr, bf);
+    const int nb = side_entry(nb4, bf);
     if (nb >= 0) {
       if (nb & kMatChange) p.mat = -2;
       p.elem = (nb & (kMatChange - 1)) >> 2;

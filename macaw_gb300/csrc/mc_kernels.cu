@@ -18,28 +18,41 @@ namespace mc {
 
 namespace {
 
+// Event counters of one launch, accumulated in shared memory (one set per
+// block) so that no thread carries them in registers through its walk.
+// Declared by MC_COUNTERS at the top of a kernel, which every thread of the
+// block executes; flush() is reached by every thread at the end.
 struct LocalCounters {
-  unsigned long long c[kNumCounters];
-  double leak_w;
-  __device__ void zero() {
-#pragma unroll
-    for (int i = 0; i < kNumCounters; ++i) c[i] = 0;
-    leak_w = 0.0;
+  unsigned long long* c;
+  double* leak_w;
+  __device__ __forceinline__ void add(int k, unsigned long long v) {
+    if (v) atomicAdd(c + k, v);
   }
+  __device__ __forceinline__ void add_leak(double w) { atomicAdd(leak_w, w); }
 };
 
+#define MC_COUNTERS(L)                                          \
+  __shared__ unsigned long long L##_c[kNumCounters];            \
+  __shared__ double L##_w;                                      \
+  LocalCounters L{L##_c, &L##_w};                               \
+  for (int i_ = threadIdx.x; i_ < kNumCounters; i_ += blockDim.x) L##_c[i_] = 0; \
+  if (threadIdx.x == 0) L##_w = 0.0;                            \
+  __syncthreads()
+
 __device__ __forceinline__ void flush(LocalCounters& L, unsigned long long* g, double* leak_w) {
-#pragma unroll
-  for (int i = 0; i < kNumCounters; ++i) {
-    unsigned long long v = L.c[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v) atomicAdd(g + i, v);
-  }
-  double w = L.leak_w;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-  if ((threadIdx.x & 31) == 0 && w != 0.0) atomicAdd(leak_w, w);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kNumCounters; i += blockDim.x)
+    if (L.c[i]) atomicAdd(g + i, L.c[i]);
+  if (threadIdx.x == 0 && *L.leak_w != 0.0) atomicAdd(leak_w, *L.leak_w);
+}
+
+// In-flight counter of a tally slot, one atomic per group of converged
+// lanes with the same slot (births and deaths come in warp-wide bursts on
+// a handful of addresses).
+__device__ __forceinline__ void live_add(int* live, int tag, int v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  cg::coalesced_group same = cg::labeled_partition(g, tag);
+  if (same.thread_rank() == 0) atomicAdd(live + tag, v * (int)same.size());
 }
 
 // Batch tally a particle scores into.
@@ -49,18 +62,18 @@ __device__ __forceinline__ double* tally_of(const RunArgs& a, int tag) {
 
 // End of a history: closing hash word, counters, optional trace record.
 __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCounters& L) {
-  if (a.live) atomicAdd(a.live + p.tag, -1);
+  if (a.live) live_add(a.live, p.tag, -1);
   p.hash = fnv(p.hash, (uint64_t)(16 + p.status));
-  L.c[kCntSeg] += (unsigned long long)p.n_seg;
-  L.c[kCntColl] += (unsigned long long)p.n_coll;
-  L.c[kCntHist] += 1;
+  L.add(kCntSeg, (unsigned long long)p.n_seg);
+  L.add(kCntColl, (unsigned long long)p.n_coll);
+  L.add(kCntHist, 1);
   switch (p.status) {
-    case kLeaked: L.c[kCntLeak] += 1; L.leak_w += p.wgt; break;
-    case kAbsorbed: L.c[kCntAbsorb] += 1; break;
-    case kCutoff: L.c[kCntCutoff] += 1; break;
-    case kStuck: L.c[kCntStuck] += 1; break;
-    case kLost: L.c[kCntLost] += 1; break;
-    default: L.c[kCntBadXS] += 1; break;
+    case kLeaked: L.add(kCntLeak, 1); L.add_leak(p.wgt); break;
+    case kAbsorbed: L.add(kCntAbsorb, 1); break;
+    case kCutoff: L.add(kCntCutoff, 1); break;
+    case kStuck: L.add(kCntStuck, 1); break;
+    case kLost: L.add(kCntLost, 1); break;
+    default: L.add(kCntBadXS, 1); break;
   }
   if (a.traces) {
     mc_trace t;
@@ -92,7 +105,7 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
   }
   const int k = xs_bucket(X, mc::log64(p.E));
   const double s = macro_total(X, mat, p.E, k);
-  L.c[kCntXS] += 1;
+  L.add(kCntXS, 1);
   if (!(s > 0.0) || s != s) {
     p.status = kBadXS;
     return false;
@@ -104,7 +117,7 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
     for (int m = 0; m < n_mat; ++m) {
       if (m == mat) continue;
       const double o = macro_total(X, m, p.E, k);
-      L.c[kCntXS] += 1;
+      L.add(kCntXS, 1);
       if (o > 0.0) xs_cache_put(p, m, o);
     }
   }
@@ -166,10 +179,11 @@ __device__ __forceinline__ void birth(const DevMesh& M, const DevXS& X, const De
   mc_site o;
   const Skip k = skip_ahead((uint64_t)id * kPrnStride);
   if (a.sites) o = a.sites[h - a.first];
+  else if (a.precision == MC_PREC_MIXED) sample_source32(X, *src, k, master, o);
   else sample_source(X, *src, k, master, o);
   start(M, o, id - 1, k, master, p);
   p.tag = tag;
-  if (a.live) atomicAdd(a.live + p.tag, 1);
+  if (a.live) live_add(a.live, p.tag, 1);
 }
 
 // Append slot to a queue with one atomic per converged group of lanes.
@@ -207,8 +221,7 @@ __device__ __forceinline__ long long births_now(const EventCtl* ctl, int64_t n) 
 // History form.
 template <int kPrec>
 __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S, RunArgs a) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
     Particle p;
@@ -240,8 +253,8 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
       }
       geo_store(g, p);
     }
-    L.c[kCntXS] += nxs;
-    L.c[kCntFallback] += nfb;
+    L.add(kCntXS, nxs);
+    L.add(kCntFallback, nfb);
     finish(p, a, L);
   }
   flush(L, a.counters, a.leak_w);
@@ -253,8 +266,7 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
 // Births of histories [0, min(n, cap)) into slots of the same index.
 __global__ void __launch_bounds__(256) k_ev_init(DevMesh M, DevXS X, DevSource S, RunArgs a,
                                                  Bank B, EventQueues Q, EventCtl* ctl, int64_t limit) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   int64_t m = a.n < B.cap ? a.n : B.cap;
   if (limit < m) m = limit;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -278,8 +290,7 @@ __global__ void __launch_bounds__(256) k_ev_init(DevMesh M, DevXS X, DevSource S
 
 __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                EventQueues Q, EventCtl* ctl, int par) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_xs[par];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int s = Q.xs[par][i];
@@ -305,18 +316,31 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
   flush(L, a.counters, a.leak_w);
 }
 
-// Segment walk, one queued particle per thread (grid-stride over the queue).
+// Next 32 advance-queue entries for the calling warp (all 32 lanes call it
+// together).  Warps take chunks as they finish, so a warp whose particles
+// walk far never holds up queue entries a faster warp could take.
+__device__ __forceinline__ int take_chunk(int* head) {
+  int base = 0;
+  if ((threadIdx.x & 31) == 0) base = atomicAdd(head, 32);
+  return __shfl_sync(0xffffffffu, base, 0);
+}
+
+// Segment walk, one queued particle per lane, queue entries taken by warp
+// chunks.
 template <int kPrec>
 __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                            EventQueues Q, EventCtl* ctl, int par) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_adv[par];
   const int nxt = par ^ 1;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (;;) {
+    const int i = take_chunk(&ctl->adv_head) + (int)(threadIdx.x & 31);
+    if (__shfl_sync(0xffffffffu, i, 0) >= n) break;
+    if (i >= n) continue;
     const int s = Q.adv[par][i];
     Particle p;
     load(B, s, p);
+    const int seg0 = p.n_seg;
     unsigned long long nxs = 0, nfb = 0;
     int r = 0;
     int k = 0;
@@ -351,7 +375,8 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       }
       geo_store(g, p);
     }
-    L.c[kCntFallback] += nfb;
+    L.add(kCntFallback, nfb);
+    L.add(kCntSegWalk, (unsigned long long)(p.n_seg - seg0));
     if (r == 2) {
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
@@ -380,21 +405,21 @@ __device__ __forceinline__ int take(int* head) {
 template <int kPrec>
 __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                     EventQueues Q, EventCtl* ctl, int par) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_adv[par];
   const int nxt = par ^ 1;
   const int* q = Q.adv[par];
   Particle p;
   Geo32 g;
   float f32 = 0.0f;  // FP64: float Sigma_t; mixed: float 1/Sigma_t
-  int s = -1, k = 0;
-  unsigned long long nxs = 0, nfb = 0;
+  int s = -1, k = 0, seg0 = 0;
+  unsigned long long nxs = 0, nfb = 0, nwalk = 0;
   {
     const int i = take(&ctl->adv_head);
     if (i < n) {
       s = q[i];
       load(B, s, p);
+      seg0 = p.n_seg;
       geo_load(p, g);
       f32 = (kPrec == MC_PREC_FP64) ? (float)p.sigt : (float)(1.0 / p.sigt);
     }
@@ -418,6 +443,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
       r = 4;
     }
     if (kPrec != MC_PREC_FP64) geo_store(g, p);
+    nwalk += (unsigned long long)(p.n_seg - seg0);
     if (r == 2) {
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
@@ -433,11 +459,13 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     if (i < n) {
       s = q[i];
       load(B, s, p);
+      seg0 = p.n_seg;
       geo_load(p, g);
       f32 = (kPrec == MC_PREC_FP64) ? (float)p.sigt : (float)(1.0 / p.sigt);
     }
   }
-  L.c[kCntFallback] += nfb;
+  L.add(kCntFallback, nfb);
+  L.add(kCntSegWalk, nwalk);
   flush(L, a.counters, a.leak_w);
 }
 
@@ -446,36 +474,79 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
 // trace hash.  Only the bank fields the walk reads or changes move; the
 // rest of a particle is touched only when its history ends here.  Same
 // arithmetic as segment_mixed.
-__global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B, EventQueues Q,
-                                                             EventCtl* ctl, int par) {
-  LocalCounters L;
-  L.zero();
+template <bool kAhead>
+__global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B,
+                                                                         EventQueues Q, EventCtl* ctl, int par) {
+  MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_adv[par];
   const int nxt = par ^ 1;
   const float tol = a.tol;
-  unsigned long long nfb = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const bool hashing = a.traces != nullptr;  // the event hash is only reported in traces
+  for (;;) {
+    const int i = take_chunk(&ctl->adv_head) + (int)(threadIdx.x & 31);
+    if (__shfl_sync(0xffffffffu, i, 0) >= n) break;
+    if (i >= n) continue;
     const int s = Q.adv[par][i];
-    float x = (float)B.x[s], y = (float)B.y[s], z = (float)B.z[s];
-    float u = (float)B.u[s], v = (float)B.v[s], w = (float)B.w[s];
+    float x = narrow(B.x[s]), y = narrow(B.y[s]), z = narrow(B.z[s]);
+    float u = narrow(B.u[s]), v = narrow(B.v[s]), w = narrow(B.w[s]);
     int elem = B.elem[s], fin = B.fin[s], mat = B.mat[s], n_seg = B.n_seg[s], zrun = B.zero_run[s];
+    const int seg0 = n_seg;
     uint64_t seed = B.seed[s], hash = B.hash[s];
     const double wgt = B.wgt[s];
+    const bool unit_w = __double_as_longlong(wgt) == __double_as_longlong(1.0);
     double* const tal = tally_of(a, B.tag[s]);
     const int4 cm = B.cm[s];
     const float4 ci = B.cinv[s];
     int slot = -1;  // cache slot whose Sigma_t is current, if the walk changed material
-    float inv_sig = (float)(1.0 / B.sigt[s]);
+    // the cached float 1/Sigma_t of the current material (set below when mat < 0)
+    float inv_sig = 0.0f;
+    if (mat >= 0) {
+      const int sl = mat & 3;
+      inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
+    }
     int r = 0, face = -1;
     int k = 0;
+    // kAhead: the record of the element being walked is loaded one step
+    // ahead -- at each crossing the neighbour's planes, entries and (after a
+    // flagged side) material are requested before that segment's tally,
+    // hash and position update, so the loads are in flight while those run
+    // (more registers: 24 resident warps per SM instead of 32).  Otherwise
+    // the record is loaded at the top of each step.
+    float4 P0, P1, P2, P3;
+    int4 nb4;
+    int mnext = 0;  // material of elem, valid while mat < 0
+    if (kAhead) {
+      const Tet32* T = M.tet + elem;
+      P0 = __ldg(&T->p[0]);
+      P1 = __ldg(&T->p[1]);
+      P2 = __ldg(&T->p[2]);
+      P3 = __ldg(&T->p[3]);
+      nb4 = __ldg(&T->nbr);
+      if (mat < 0) mnext = __ldg(M.tmat + elem);
+    }
     for (;;) {
       if (n_seg >= kMaxSegments || zrun >= kMaxZeroRun) {
         r = 2;
         face = -2;  // stuck
         break;
       }
+      // this segment's draw depends on no load: with kAhead it is formed
+      // while they land, committed to the RNG state only when the segment
+      // is scored (without, it is formed after the exit search, which keeps
+      // fewer registers live across the loads)
+      const uint64_t seed_n = kPrnMult * seed + kPrnAdd;
+      auto draw = [&]() {
+        uint64_t wv = ((seed_n >> ((seed_n >> 59u) + 5u)) ^ seed_n) * 12605985483714917081ULL;
+        wv = (wv >> 43u) ^ wv;
+        return -__logf((float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f);
+      };
+      float lnxi = kAhead ? draw() : 0.0f;
+      if (!kAhead) {
+        nb4 = __ldg(&M.tet[elem].nbr);
+        if (mat < 0) mnext = __ldg(M.tmat + elem);
+      }
       if (mat < 0) {  // after a side flagged kMatChange
-        const int m = __ldg(M.tmat + elem);
+        const int m = mnext;
         const int sl = m & 3;
         const int key = sl == 0 ? cm.x : sl == 1 ? cm.y : sl == 2 ? cm.z : cm.w;
         if (m < 0 || key != m) {
@@ -487,14 +558,11 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
         slot = sl;
         inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
       }
-      const Tet32& T = M.tet[elem];
-      const float4* P = T.p;
       int bf = -1;
       float t1 = 3.0e38f, t2 = 3.0e38f;
-#pragma unroll
-      for (int f = 0; f < 4; ++f) {
-        if (f == fin) continue;
-        const float4 pl = __ldg(P + f);
+      auto side = [&](const float4& held, int f) {
+        if (f == fin) return;
+        const float4 pl = kAhead ? held : __ldg(&M.tet[elem].p[f]);  // plain: the three planes needed
         const float den = fmaf(pl.x, u, fmaf(pl.y, v, pl.z * w));
         if (den > 0.0f) {
           const float num = pl.w - fmaf(pl.x, x, fmaf(pl.y, y, pl.z * z));
@@ -507,10 +575,14 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
             t2 = t;
           }
         }
-      }
+      };
+      side(P0, 0);
+      side(P1, 1);
+      side(P2, 2);
+      side(P3, 3);
       float Ls;
       if (bf < 0 || t2 - t1 <= tol || t1 < -tol) {
-        ++nfb;
+        L.add(kCntFallback, 1);
         Geo32 g{x, y, z, u, v, w};
         double Ld = 0.0;
         bf = exit_fp64(M, elem, fin, g, Ld);
@@ -523,19 +595,28 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
       } else {
         Ls = fmaxf(t1, 0.0f);
       }
-      seed = kPrnMult * seed + kPrnAdd;
-      uint64_t wv = ((seed >> ((seed >> 59u) + 5u)) ^ seed) * 12605985483714917081ULL;
-      wv = (wv >> 43u) ^ wv;
-      const float xi = (float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f;
-      const float dist = -__logf(xi) * inv_sig;
+      seed = seed_n;
+      if (!kAhead) lnxi = draw();
+      const float dist = lnxi * inv_sig;
       const bool cross = dist > Ls;
+      const int nb = side_entry(nb4, bf);
+      const int next = (nb & (kMatChange - 1)) >> 2;
+      if (kAhead && cross && nb >= 0) {
+        const Tet32* T = M.tet + next;
+        P0 = __ldg(&T->p[0]);
+        P1 = __ldg(&T->p[1]);
+        P2 = __ldg(&T->p[2]);
+        P3 = __ldg(&T->p[3]);
+        nb4 = __ldg(&T->nbr);
+        if (nb & kMatChange) mnext = __ldg(M.tmat + next);
+      }
       const float score = cross ? Ls : dist;
-      atomicAdd(tal + elem, wgt == 1.0 ? (double)score : wgt * (double)score);
+      atomicAdd(tal + elem, unit_w ? widen(score) : wgt * widen(score));
       ++n_seg;
       if (Ls == 0.0f) ++zrun;
       else zrun = 0;
       if (!cross) {
-        hash = fnv(hash, (uint64_t)elem * 8ULL + 4ULL);
+        if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + 4ULL);
         x = fmaf(dist, u, x);
         y = fmaf(dist, v, y);
         z = fmaf(dist, w, z);
@@ -543,23 +624,24 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
         r = 1;
         break;
       }
-      hash = fnv(hash, (uint64_t)elem * 8ULL + (uint64_t)bf);
+      if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + (uint64_t)bf);
       x = fmaf(Ls, u, x);
       y = fmaf(Ls, v, y);
       z = fmaf(Ls, w, z);
-      const int nb = side_entry(T.nbr, bf);
       if (nb >= 0) {
         if (nb & kMatChange) mat = -2;
-        elem = (nb & (kMatChange - 1)) >> 2;
+        elem = next;
         fin = nb & 3;
       } else {
         const int bid = -1 - nb;
         if (bid < M.n_bid && M.bc_type[bid] == 1) {
-          const float4 pl = __ldg(P + bf);
-          const float t2r = 2.0f * fmaf(u, pl.x, fmaf(v, pl.y, w * pl.z));
-          u = fmaf(-t2r, pl.x, u);
-          v = fmaf(-t2r, pl.y, v);
-          w = fmaf(-t2r, pl.z, w);
+          // no load is issued for a boundary side: P0..P3 are still this element's
+          const float4 pb = !kAhead ? __ldg(&M.tet[elem].p[bf])
+                            : bf == 0 ? P0 : bf == 1 ? P1 : bf == 2 ? P2 : P3;
+          const float t2r = 2.0f * fmaf(u, pb.x, fmaf(v, pb.y, w * pb.z));
+          u = fmaf(-t2r, pb.x, u);
+          v = fmaf(-t2r, pb.y, v);
+          w = fmaf(-t2r, pb.z, w);
           const float nrm = rsqrtf(fmaf(u, u, fmaf(v, v, w * w)));
           u *= nrm;
           v *= nrm;
@@ -576,11 +658,12 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
         break;
       }
     }
+    L.add(kCntSegWalk, (unsigned long long)(n_seg - seg0));
     if (r == 2) {
       Particle p;
       load(B, s, p);
-      p.x = x; p.y = y; p.z = z;
-      p.u = u; p.v = v; p.w = w;
+      p.x = widen(x); p.y = widen(y); p.z = widen(z);
+      p.u = widen(u); p.v = widen(v); p.w = widen(w);
       p.elem = elem; p.fin = fin; p.mat = mat; p.n_seg = n_seg; p.zero_run = zrun;
       p.seed = seed; p.hash = hash;
       if (face >= 0) {
@@ -593,8 +676,8 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
       push_free(Q, ctl, s, B.cap);
       continue;
     }
-    B.x[s] = x; B.y[s] = y; B.z[s] = z;
-    B.u[s] = u; B.v[s] = v; B.w[s] = w;
+    B.x[s] = widen(x); B.y[s] = widen(y); B.z[s] = widen(z);
+    B.u[s] = widen(u); B.v[s] = widen(v); B.w[s] = widen(w);
     B.elem[s] = elem; B.fin[s] = fin; B.mat[s] = mat; B.n_seg[s] = n_seg; B.zero_run[s] = zrun;
     B.seed[s] = seed; B.hash[s] = hash;
     if (slot >= 0) {
@@ -610,14 +693,12 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
       push(Q.adv[nxt], &ctl->n_adv[nxt], s);
     }
   }
-  L.c[kCntFallback] += nfb;
   flush(L, a.counters, a.leak_w);
 }
 
 __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                     EventQueues Q, EventCtl* ctl, int par) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_coll;
   const int nxt = par ^ 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -642,8 +723,7 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
 // history next_hist + i, as far as histories below the birth limit remain.
 __global__ void __launch_bounds__(256) k_ev_refill(DevMesh M, DevXS X, DevSource S, RunArgs a,
                                                    Bank B, EventQueues Q, EventCtl* ctl, int par) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   const long long base = *(volatile long long*)&ctl->next_hist;
   const unsigned long long head = *(volatile unsigned long long*)&ctl->free_head;
   const long long n = births_now(ctl, a.n);
@@ -681,8 +761,7 @@ __global__ void k_ev_reset(EventCtl* ctl, int par, int64_t n) {
 template <int kPrec>
 __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                    EventQueues Q, EventCtl* ctl, int par) {
-  LocalCounters L;
-  L.zero();
+  MC_COUNTERS(L);
   const int nx = *(volatile int*)&ctl->n_xs[par];
   const int na = *(volatile int*)&ctl->n_adv[par];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx + na; i += gridDim.x * blockDim.x) {
@@ -716,8 +795,8 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       }
       geo_store(g, p);
     }
-    L.c[kCntXS] += nxs;
-    L.c[kCntFallback] += nfb;
+    L.add(kCntXS, nxs);
+    L.add(kCntFallback, nfb);
     finish(p, a, L);
   }
   flush(L, a.counters, a.leak_w);
@@ -826,7 +905,10 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
     if (a.precision == MC_PREC_MIXED) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   } else {
-    if (a.precision == MC_PREC_MIXED) k_ev_advance_mixed<<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
+    if (a.precision == MC_PREC_MIXED) {
+      if (a.walk_plain) k_ev_advance_mixed<false><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
+      else k_ev_advance_mixed<true><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
+    }
     else k_ev_advance_static<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   }
   if (adv1) cudaEventRecord(adv1, st);

@@ -9,6 +9,9 @@
 namespace mc {
 
 // Device counters, one 64-bit slot each.
+// Batches of one pipelined mc_run in flight at once (one tally slot each).
+constexpr int kPipeSlots = 8;
+
 enum Counter : int {
   kCntSeg = 0,
   kCntColl,
@@ -21,6 +24,7 @@ enum Counter : int {
   kCntXS,
   kCntFallback,
   kCntHist,
+  kCntSegWalk,  // segments walked by the advance kernels
   kNumCounters
 };
 
@@ -53,7 +57,7 @@ struct EventCtl {
   unsigned long long free_head, free_tail;  // ring of free bank slots (monotonic counters)
   long long next_hist;              // next history (relative to the run) to be born
   long long birth_limit;            // histories at or past this index wait (pipelined batches)
-  int live[2];                      // particles in flight per batch parity
+  int live[2];                      // unused (per-slot counters live in RunArgs::live)
 };
 
 struct EventQueues {
@@ -86,6 +90,7 @@ struct RunArgs {
   const DevRequest* req;        // device: birth-sequence entries sorted by start, or null
   int n_req;
   int* live;                    // event mode: in-flight counters per tally slot, or null
+  int walk_plain;               // mixed walk: 1 loads each element's record at the top of its step
   mc_trace* traces;
   unsigned long long* counters;
   double* leak_w;

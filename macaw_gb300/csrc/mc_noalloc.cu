@@ -164,6 +164,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.tol = v.tol;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.walk_plain = d->walk_plain;
   a.sort_shift = -1;  // ordering needs scratch beyond the fixed array
   a.sort_buckets = 0;
   a.sort_tmp = nullptr;
@@ -206,6 +207,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   mc_stats s{};
   s.n_hist = (int64_t)cnt[kCntHist];
   s.n_seg = (int64_t)cnt[kCntSeg];
+  s.n_seg_advance = (int64_t)cnt[kCntSegWalk];
   s.n_coll = (int64_t)cnt[kCntColl];
   s.n_leak = (int64_t)cnt[kCntLeak];
   s.n_absorb = (int64_t)cnt[kCntAbsorb];

@@ -1,17 +1,25 @@
 // mc_tune.cpp -- autotuner for the event form's execution parameters.
 //
 // Bank size, block shape, segments per walk launch, the advance-queue
-// ordering granularity, lane refill and CUDA-graph replay all move throughput, and their best
+// ordering granularity, lane refill, CUDA-graph replay and the mixed walk's
+// load placement all move throughput, and their best
 // values depend on the mesh, the cross sections and the precision form.
-// mc_autotune measures them on short trial batches of the context's own
-// problem (device time from the CUDA events inside mc_run) by coordinate
-// descent: each parameter in turn over its candidate values, the others held
-// at their best so far, two passes.  The trial batches score into the batch
-// tally, which is cleared afterwards; SUM/SUM_SQ are not touched.
+// mc_autotune measures them on trial runs of the context's own problem
+// (device time from the CUDA events inside mc_run) by coordinate descent:
+// each parameter in turn over its candidate values, the others held at
+// their best so far, two passes.  A trial is four pipelined batches of a
+// quarter of the trial size each, the way production runs stream batches
+// through the bank, so that the tail of one batch overlaps the next as it
+// will in use.  SUM/SUM_SQ and the batch count are set aside before the
+// trials and put back after them; the batch tally is left cleared.
 #include <algorithm>
 #include <vector>
 
 #include "../../include/macaw_gb300.h"
+
+namespace mc {
+int accum_snapshot(mc_ctx* c, int restore);
+}
 
 namespace {
 
@@ -31,18 +39,28 @@ double measure(mc_ctx* ctx, const mc_run_desc& d, int reps) {
 extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_histories, mc_run_desc* best,
                            double* best_rate) {
   if (!ctx || !base || !best || trial_histories < 1024) return MC_ERR_ARG;
+  const int64_t quarter = trial_histories / 4;
+  const int64_t sizes[4] = {quarter, quarter, quarter, trial_histories - 3 * quarter};
   mc_run_desc cur = *base;
   cur.n_histories = trial_histories;
   cur.mode = MC_MODE_EVENT;
-  cur.accumulate = 0;
+  cur.accumulate = 1;
   cur.record_traces = 0;
   cur.profile = 0;
   cur.sites = nullptr;
-  cur.n_batches = 0;
-  cur.batch_sizes = nullptr;
+  cur.n_batches = 4;
+  cur.batch_sizes = sizes;
   if (cur.bank_size <= 0 || cur.bank_size > trial_histories) cur.bank_size = trial_histories;
   if (cur.block_size <= 0) cur.block_size = 256;
   if (cur.max_seg_per_advance < 0) cur.max_seg_per_advance = 0;
+  if (mc::accum_snapshot(ctx, 0) != MC_OK) return MC_ERR_STATE;
+  struct Restore {
+    mc_ctx* c;
+    ~Restore() {
+      mc::accum_snapshot(c, 1);
+      mc_tally_clear(c, MC_TALLY_BATCH);
+    }
+  } restore{ctx};
   double rate = measure(ctx, cur, 2);
   if (rate < 0.0) return MC_ERR_STATE;
 
@@ -52,12 +70,14 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
   };
   const int64_t t = trial_histories;
   std::vector<Knob> knobs = {
-      {0, {0, 16, 32, 64, 128}},                                   // segments per walk launch
+      {0, {0, 16, 32, 64, 128, 256}},                              // segments per walk launch
       {1, {64, 128, 256}},                                         // threads per block
       {2, {0, 1, 5, 9, 13}},                                       // queue ordering granularity
-      {3, {std::max<int64_t>(16384, t / 4), std::max<int64_t>(16384, t / 2), t}},  // bank
+      {3, {std::max<int64_t>(16384, t / 8), std::max<int64_t>(16384, t / 4), std::max<int64_t>(16384, t / 2)}},
+      // (bank sizes only when the caller left the bank open)
       {4, {0, 1}},                                                 // lane refill
       {5, {0, 1}},                                                 // CUDA-graph event cycles
+      {6, {0, 1}},                                                 // mixed walk: loads ahead / plain
   };
   auto apply = [](mc_run_desc& d, int kind, int64_t v) {
     switch (kind) {
@@ -66,11 +86,13 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       case 2: d.sort_queue = (int32_t)v; break;
       case 3: d.bank_size = v; break;
       case 4: d.refill = (int32_t)v; break;
-      default: d.graph = (int32_t)v; break;
+      case 5: d.graph = (int32_t)v; break;
+      default: d.walk_plain = (int32_t)v; break;
     }
   };
   for (int pass = 0; pass < 2; ++pass) {
     for (const Knob& k : knobs) {
+      if (k.kind == 3 && base->bank_size > 0) continue;
       mc_run_desc keep = cur;
       for (int64_t v : k.values) {
         mc_run_desc trial = keep;
@@ -83,7 +105,6 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       }
     }
   }
-  mc_tally_clear(ctx, MC_TALLY_BATCH);
   *best = *base;
   best->mode = MC_MODE_EVENT;
   best->max_seg_per_advance = cur.max_seg_per_advance;
@@ -91,11 +112,8 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
   best->sort_queue = cur.sort_queue;
   best->refill = cur.refill;
   best->graph = cur.graph;
-  // the largest trial bank winning means "as large as the batch allows":
-  // keep the caller's bank when it is larger than the trial
-  int64_t bank = cur.bank_size;
-  if (bank >= t && base->bank_size > t) bank = base->bank_size;
-  best->bank_size = bank;
+  best->walk_plain = cur.walk_plain;
+  best->bank_size = base->bank_size > 0 ? base->bank_size : cur.bank_size;
   if (best_rate) *best_rate = rate;
   return MC_OK;
 }

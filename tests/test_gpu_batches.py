@@ -1,8 +1,8 @@
 """Batches of uneven size run through one event pipeline.
 
-Batch b scores into its own tally (two alternate) and is folded into
-SUM/SUM_SQ, normalised by its size, when its last particle ends; the next
-batch's births fill the bank meanwhile.  The result must equal one mc_run
+Batch b scores into tally slot b mod 8 (up to eight batches in flight) and
+is folded into SUM/SUM_SQ, normalised by its size, when its last particle
+ends; the next batches' births fill the bank meanwhile.  The result must equal one mc_run
 per batch: SUM and SUM_SQ within 1e-12, per-history traces bit for bit.
 """
 import numpy as np
@@ -15,6 +15,8 @@ from macaw_gb300._lib import (MC_MODE_EVENT, MC_MODE_HISTORY, MC_PREC_FP64, MC_P
 pytestmark = pytest.mark.gpu
 
 SIZES = [3000, 5000, 1000, 7000, 2500]
+# more batches than tally slots: slots are reused once their batch drained
+SIZES_LONG = [900, 1500, 400, 2200, 700, 1300, 300, 1800, 1000, 600, 2500, 800]
 
 
 def close(a, b, rtol=1e-12):
@@ -27,17 +29,37 @@ def cube():
     return problems.cube_problem(n=10, L=10.0, n_nuc=5, n_pts=3000)
 
 
-@pytest.fixture(scope="module")
-def separate(cube):
+def _separate(cube, sizes):
     with Tracker(0) as t:
         t.load(cube)
         first = 0
         trs = []
-        for s in SIZES:
+        for s in sizes:
             t.run(s, first=first, seed=5, mode=MC_MODE_EVENT, accumulate=True, traces=True)
             trs.append(t.traces(s))
             first += s
         return t.tally(MC_TALLY_SUM), t.tally(MC_TALLY_SUM_SQ), np.concatenate(trs)
+
+
+@pytest.fixture(scope="module")
+def separate(cube):
+    return _separate(cube, SIZES)
+
+
+@pytest.mark.parametrize("bank", [1024, 6000])
+def test_more_batches_than_tally_slots(cube, bank):
+    s_ref, sq_ref, tr_ref = _separate(cube, SIZES_LONG)
+    n = sum(SIZES_LONG)
+    with Tracker(0) as t:
+        t.load(cube)
+        st = t.run(n, seed=5, bank_size=bank, accumulate=True, traces=True, batch_sizes=SIZES_LONG)
+        assert st.n_hist == n and t.batches_done() == len(SIZES_LONG)
+        tr = t.traces(n)
+        for f in ("hash", "status", "n_seg", "n_coll", "elem", "face"):
+            assert np.array_equal(tr[f], tr_ref[f]), f
+        assert close(t.tally(MC_TALLY_SUM), s_ref)
+        assert close(t.tally(MC_TALLY_SUM_SQ), sq_ref)
+        assert np.all(t.tally() == 0)
 
 
 @pytest.mark.parametrize("mode,bank", [(MC_MODE_EVENT, 2048), (MC_MODE_EVENT, 40000), (MC_MODE_HISTORY, 0)])
@@ -73,8 +95,14 @@ def test_graph_replayed_event_cycles_are_bit_exact(cube, separate):
 def test_autotune_returns_usable_parameters(cube):
     with Tracker(0) as t:
         t.load(cube)
-        params, rate = t.autotune(trial=20000, bank_size=8192)
-        assert rate > 0
+        t.run(3000, seed=9, accumulate=True)
+        s0, q0, b0 = t.tally(MC_TALLY_SUM), t.tally(MC_TALLY_SUM_SQ), t.batches_done()
+        for prec in (MC_PREC_FP64, MC_PREC_MIXED):
+            params, rate = t.autotune(trial=20000, bank_size=8192, precision=prec)
+            assert rate > 0
+        # the pipelined trials leave the accumulators and the batch count as they were
+        assert np.array_equal(t.tally(MC_TALLY_SUM), s0) and np.array_equal(t.tally(MC_TALLY_SUM_SQ), q0)
+        assert t.batches_done() == b0 and np.all(t.tally() == 0)
         st = t.run(5000, seed=5, accumulate=True, **params)
         assert st.n_hist == 5000 and st.n_stuck == 0
 
