@@ -1,4 +1,4 @@
-"""Runs the lattice workload once for profiling (ncu, nsys).
+"""Runs the lattice (or core) workload once for profiling (ncu).
 
   python -m macaw_gb300.profile_run --precision fp64 --hist 1000000 --batches 2
 
@@ -23,16 +23,19 @@ def main() -> None:
     ap.add_argument("--batches", type=int, default=2)
     ap.add_argument("--pins", type=int, default=17, help="pin cells per lattice side")
     ap.add_argument("--block", type=int, default=0)
-    ap.add_argument("--max-seg", type=int, default=64)
+    ap.add_argument("--max-seg", type=int, default=0, help="0: 128 for mixed, 64 for fp64")
     ap.add_argument("--sort", type=int, default=9)
+    ap.add_argument("--workload", choices=["lattice", "core"], default="lattice")
     args = ap.parse_args()
     prec = MC_PREC_MIXED if args.precision == "mixed" else MC_PREC_FP64
     block = args.block or (64 if prec == MC_PREC_MIXED else 128)
-    p = problems.lattice_problem(nx=args.pins, ny=args.pins)
+    max_seg = args.max_seg or (128 if prec == MC_PREC_MIXED else 64)
+    p = problems.lattice_problem(nx=args.pins, ny=args.pins) if args.workload == "lattice" \
+        else problems.core_problem()
     n = args.hist
     with Tracker(0) as t:
         t.load(p)
-        kw = dict(bank_size=n, block_size=block, max_seg=args.max_seg, sort_queue=args.sort, precision=prec)
+        kw = dict(bank_size=n, block_size=block, max_seg=max_seg, sort_queue=args.sort, precision=prec)
         t.run(n, first=0, seed=1, accumulate=True, **kw)
         st = t.run(n * args.batches, first=n, seed=1, accumulate=True, batch_sizes=[n] * args.batches, **kw)
         print(json.dumps(st.as_dict()))
