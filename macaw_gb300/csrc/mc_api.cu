@@ -71,7 +71,7 @@ struct mc_ctx {
   bool have_src = false;
 
   // device copies
-  DevBuf d_planes, d_tet, d_tmat, d_bc, d_gstart, d_gtets;
+  DevBuf d_planes, d_tet, d_tmat, d_bc, d_gstart, d_gtets, d_gseed;
   DevBuf d_gE, d_goff, d_gn, d_ghidx, d_nuc_grid, d_nuc_off, d_sig, d_awr, d_mat_off, d_mat_nuc, d_mat_dens;
   DevBuf d_cyl;
   DevBuf d_tally, d_sum, d_sumsq;
@@ -204,6 +204,7 @@ DevMesh dev_mesh(mc_ctx* c) {
   }
   M.gstart = c->d_gstart.as<int64_t>();
   M.gtets = c->d_gtets.as<int>();
+  M.gseed = c->d_gseed.as<int>();
   return M;
 }
 
@@ -364,6 +365,7 @@ int mc_mesh_upload(mc_ctx* c, int64_t n_vtx, const double* xyz, int64_t n_tet,
 
   CK(upload(c->d_gstart, c->mesh.gstart, c->stream), "upload locator");
   CK(upload(c->d_gtets, c->mesh.gtets, c->stream), "upload locator");
+  CK(upload(c->d_gseed, c->mesh.gseed, c->stream), "upload locator");
   CK(c->d_tally.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
   CK(c->d_sum.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
   CK(c->d_sumsq.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");

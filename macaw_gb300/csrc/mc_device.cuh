@@ -72,6 +72,7 @@ struct DevMesh {
   int gn[3];
   const int64_t* __restrict__ gstart;
   const int* __restrict__ gtets;
+  const int* __restrict__ gseed;  // per cell: a tet containing its centre, or -1
 };
 
 struct DevXS {
@@ -148,7 +149,7 @@ __device__ __forceinline__ int xs_bucket(const DevXS& X, double lE) {
 // Bisection inside the hash bin of grid g, guarded so a bin estimate that is
 // off by rounding still ends on the right interval; returns the interval
 // index i (E_i <= E < E_i+1) and the interpolation fraction.
-__device__ __forceinline__ void grid_locate(const DevXS& X, int g, int k, double E, int& i, double& f) {
+__device__ __forceinline__ int grid_index(const DevXS& X, int g, int k, double E) {
   const double* G = X.gE + __ldg(X.g_off + g);
   int lo = __ldg(X.ghidx + (size_t)k * X.n_grid + g);
   int hi = __ldg(X.ghidx + (size_t)(k + 1) * X.n_grid + g) + 1;
@@ -161,8 +162,13 @@ __device__ __forceinline__ void grid_locate(const DevXS& X, int g, int k, double
     if (E < __ldg(G + mid)) hi = mid;
     else lo = mid;
   }
-  i = lo;
-  const double e0 = __ldg(G + lo), e1 = __ldg(G + lo + 1);
+  return lo;
+}
+
+__device__ __forceinline__ void grid_locate(const DevXS& X, int g, int k, double E, int& i, double& f) {
+  const double* G = X.gE + __ldg(X.g_off + g);
+  i = grid_index(X, g, k, E);
+  const double e0 = __ldg(G + i), e1 = __ldg(G + i + 1);
   f = (E - e0) / (e1 - e0);
 }
 
@@ -205,6 +211,40 @@ __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E)
   return macro_total(X, mat, E, xs_bucket(X, mc::log64(E)));
 }
 
+// Mixed-precision Sigma_t: the hash bin from a float log (grid_locate's
+// guards correct a bin that rounding moved by one), the grid interval
+// located in FP64 on the double grid, so the bracketing points are the
+// FP64 ones; the fraction, the interpolation and the sum over nuclides in
+// float.
+__device__ __forceinline__ int xs_bucket32(const DevXS& X, double E) {
+  const float q = (__logf(narrow(E)) - narrow(X.lE_lo)) / narrow(X.du);
+  if (!(q >= 0.0f)) return 0;
+  const int k = (int)q;
+  return k > X.n_bins - 1 ? X.n_bins - 1 : k;
+}
+
+__device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E, int k) {
+  float acc = 0.0f;
+  int gc = -1, i = 0;
+  float f = 0.0f;
+  const int j1 = __ldg(X.mat_off + mat + 1);
+  for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
+    const int nuc = __ldg(X.mat_nuc + j);
+    const int g = __ldg(X.nuc_grid + nuc);
+    if (g != gc) {
+      const double* G = X.gE + __ldg(X.g_off + g);
+      i = grid_index(X, g, k, E);
+      const double e0 = __ldg(G + i);
+      f = narrow(E - e0) / narrow(__ldg(G + i + 1) - e0);
+      gc = g;
+    }
+    const double2* S = X.sig + __ldg(X.nuc_off + nuc) + i;
+    const float a = narrow(__ldg(&S[0].x)), b = narrow(__ldg(&S[1].x));
+    acc = fmaf(narrow(__ldg(X.mat_dens + j)), fmaf(f, b - a, a), acc);
+  }
+  return acc;
+}
+
 // ---------------------------------------------------------------------------
 // Start element (stands in for MOOSE ClaimRays): lowest-id tet containing x
 // (all four half-spaces within kLocateTol) whose interior the direction
@@ -231,6 +271,45 @@ __device__ __forceinline__ int locate(const DevMesh& M, double x, double y, doub
   const int64_t cell = ((int64_t)ci[2] * M.gn[1] + ci[1]) * M.gn[0] + ci[0];
   const float xf = (float)x, yf = (float)y, zf = (float)z;
   const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
+  // Fast path: walk from the cell's seed tet (which holds the cell centre c)
+  // along the segment c -> x, one neighbour per step, on the float planes.
+  // The walk only proposes a tet: it is returned when x is strictly inside
+  // it by more than the float error bound and kLocateTol on every side --
+  // then it is the one tet the FP64 rule below would return.  A walk that
+  // meets the boundary, stalls or ends near a side falls back to the list.
+  if (M.gseed) {
+    int t = __ldg(M.gseed + cell);
+    const float cx = (float)(M.glo[0] + (ci[0] + 0.5) * M.gh[0]);
+    const float cy = (float)(M.glo[1] + (ci[1] + 0.5) * M.gh[1]);
+    const float cz = (float)(M.glo[2] + (ci[2] + 0.5) * M.gh[2]);
+    const float dx = xf - cx, dy = yf - cy, dz = zf - cz;
+    for (int step = 0; step < 32 && t >= 0; ++step) {
+      const Tet32* T = M.tet + t;
+      const float4 pl[4] = {__ldg(&T->p[0]), __ldg(&T->p[1]), __ldg(&T->p[2]), __ldg(&T->p[3])};
+      const int4 nb4 = __ldg(&T->nbr);
+      bool in = true;
+      int bf = -1;
+      float tb = 3.0e38f;
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const float s32 = fmaf(pl[f].x, xf, fmaf(pl[f].y, yf, pl[f].z * zf)) - pl[f].w;
+        if (!(s32 < -(1e-9f + 7.3e-7f * (fabsf(pl[f].w) + xa)))) in = false;
+        const float den = fmaf(pl[f].x, dx, fmaf(pl[f].y, dy, pl[f].z * dz));
+        if (den > 0.0f) {
+          const float tt = (pl[f].w - fmaf(pl[f].x, cx, fmaf(pl[f].y, cy, pl[f].z * cz))) / den;
+          if (tt < tb) {
+            tb = tt;
+            bf = f;
+          }
+        }
+      }
+      if (in) return t;
+      if (bf < 0) break;
+      const int nb = side_entry(nb4, bf);
+      if (nb < 0) break;
+      t = (nb & (kMatChange - 1)) >> 2;
+    }
+  }
   int best_any = -1;
   const int64_t q1 = M.gstart[cell + 1];
   for (int64_t q = M.gstart[cell]; q < q1; ++q) {
@@ -821,7 +900,7 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
     }
     if (!xs_cache_get(p, mat)) {
       if (!kInlineXS) return 3;
-      const double s = macro_total(X, mat, p.E);
+      const double s = widen(macro_total32(X, mat, p.E, xs_bucket32(X, p.E)));
       ++n_xs;
       if (!(s > 0.0) || s != s) {
         p.status = kBadXS;

@@ -258,6 +258,28 @@ std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
         for (int x = i0[0]; x <= i1[0]; ++x)
           M.gtets[fill[((int64_t)z * M.gn[1] + y) * M.gn[0] + x]++] = (int32_t)t;
   }
+  // walk seeds: the first listed tet that contains the cell centre (within
+  // the locate tolerance), found on the FP64 planes
+  M.gseed.assign((size_t)ncell, -1);
+  parallel_for(ncell, [&](int64_t c) {
+    {
+      const int64_t ix = c % M.gn[0], iy = (c / M.gn[0]) % M.gn[1], iz = c / ((int64_t)M.gn[0] * M.gn[1]);
+      const double p[3] = {M.glo[0] + (ix + 0.5) * M.gh[0], M.glo[1] + (iy + 0.5) * M.gh[1],
+                           M.glo[2] + (iz + 0.5) * M.gh[2]};
+      for (int64_t q = M.gstart[c]; q < M.gstart[c + 1]; ++q) {
+        const int32_t t = M.gtets[q];
+        bool in = true;
+        for (int f = 0; f < 4 && in; ++f) {
+          const double* pl = &M.planes[16 * (size_t)t + 4 * f];
+          if (pl[0] * p[0] + pl[1] * p[1] + pl[2] * p[2] - pl[3] > tol) in = false;
+        }
+        if (in) {
+          M.gseed[c] = t;
+          break;
+        }
+      }
+    }
+  });
   return "";
 }
 

@@ -23,6 +23,9 @@ struct MeshTables {
   int32_t gn[3] = {1, 1, 1};
   std::vector<int64_t> gstart;
   std::vector<int32_t> gtets;
+  // per cell: a tet containing the cell's centre (-1: none), where a
+  // locate's walk to the point starts
+  std::vector<int32_t> gseed;
   double bbox_lo[3] = {0, 0, 0}, bbox_hi[3] = {0, 0, 0};
 };
 

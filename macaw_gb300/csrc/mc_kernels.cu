@@ -96,15 +96,16 @@ __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCount
 // Cross-section event: Sigma_t of the current element's material (and, when
 // the problem has at most four materials, of every material, so later
 // material changes at this energy hit the cache); false if unusable.
-__device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int n_mat,
+// f32: the mixed-precision form's float interpolation (macro_total32).
+__device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int n_mat, bool f32,
                                           Particle& p, LocalCounters& L) {
   const int mat = __ldg(M.tmat + p.elem);
   if (mat < 0) {
     p.status = kBadXS;
     return false;
   }
-  const int k = xs_bucket(X, mc::log64(p.E));
-  const double s = macro_total(X, mat, p.E, k);
+  const int k = f32 ? xs_bucket32(X, p.E) : xs_bucket(X, mc::log64(p.E));
+  const double s = f32 ? widen(macro_total32(X, mat, p.E, k)) : macro_total(X, mat, p.E, k);
   L.add(kCntXS, 1);
   if (!(s > 0.0) || s != s) {
     p.status = kBadXS;
@@ -116,7 +117,7 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
   if (n_mat <= 4) {
     for (int m = 0; m < n_mat; ++m) {
       if (m == mat) continue;
-      const double o = macro_total(X, m, p.E, k);
+      const double o = f32 ? widen(macro_total32(X, m, p.E, k)) : macro_total(X, m, p.E, k);
       L.add(kCntXS, 1);
       if (o > 0.0) xs_cache_put(p, m, o);
     }
@@ -296,7 +297,7 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
     const int s = Q.xs[par][i];
     Particle p;
     load(B, s, p);
-    if (refresh_xs(M, X, a.n_mat, p, L)) {
+    if (refresh_xs(M, X, a.n_mat, a.precision == MC_PREC_MIXED, p, L)) {
       B.sigt[s] = p.sigt;
       B.mat[s] = p.mat;
       B.cm[s] = p.cm;

@@ -5,7 +5,8 @@
 One untimed batch (so the first launches of every kernel are warm), then
 `--batches` batches of `--hist` histories through one pipelined call, with
 fixed execution parameters (the autotuner's choices on this workload unless
-overridden).  Prints the run's statistics as JSON.
+overridden).  Prints the pipelined run's statistics as JSON, with the
+untimed batch's under "warm".
 """
 from __future__ import annotations
 
@@ -36,9 +37,9 @@ def main() -> None:
     with Tracker(0) as t:
         t.load(p)
         kw = dict(bank_size=n, block_size=block, max_seg=max_seg, sort_queue=args.sort, precision=prec)
-        t.run(n, first=0, seed=1, accumulate=True, **kw)
+        warm = t.run(n, first=0, seed=1, accumulate=True, **kw).as_dict()
         st = t.run(n * args.batches, first=n, seed=1, accumulate=True, batch_sizes=[n] * args.batches, **kw)
-        print(json.dumps(st.as_dict()))
+        print(json.dumps(dict(st.as_dict(), warm=warm)))
 
 
 if __name__ == "__main__":
