@@ -54,9 +54,11 @@ B_SEG_FP64 = 164   # algorithmic bytes per segment: planes 128 + neighbours 16 +
 B_SEG_MIXED = 100  # float planes 64 + neighbours 16 + material 4 + tally RMW 16
 CPU_SAMPLE = 400_000
 REF_SAMPLE = 100_000
-# DRAM bytes per segment of the advance kernel from the committed ncu
-# capture (profiles/advance_fp64_lattice.md); None until captured
-ADVANCE_DRAM_BYTES_PER_SEG = None
+# DRAM bytes per walked segment of the walk kernels, from ncu captures of
+# every walk launch of a 2 x 2e5-history lattice run (profiles/walk_*_lattice.md);
+# traffic per launch = this x the launch's segments
+ADVANCE_DRAM_BYTES_PER_SEG = 208.4
+MIXED_DRAM_BYTES_PER_SEG = 71.8
 
 
 def env_int(name, default):
@@ -404,6 +406,7 @@ def main():
                                  "algorithmic_bytes_per_segment": B_SEG_MIXED,
                                  "advance_ms_per_launch": pst.ms_advance / max(pst.n_advance_launch, 1),
                                  "segments_per_launch": pst.n_seg_advance / max(pst.n_advance_launch, 1),
+                                 "traffic": MIXED_DRAM_BYTES_PER_SEG * pst.n_seg_advance / max(pst.n_advance_launch, 1),
                                  "sample": f"one extra profiled batch of {n} histories"}
 
     # --- end to end through the C ABI with host buffers, one call per step ---
@@ -449,6 +452,8 @@ def main():
                 "algorithmic_bytes_per_segment": B_SEG_FP64,
                 "advance_ms_per_launch": st.ms_advance / max(st.n_advance_launch, 1),
                 "advance_share_of_step": st.ms_advance / ms if ms > 0 else None,
+                "traffic_source": "ncu DRAM bytes per walked segment (profiles/walk_fp64_lattice.md) x segments "
+                                  "per launch",
                 "note": "the FP64 walk is bound by GB300's FP64 pipe, not HBM (see profiles/)"}
         cfg = dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single",
                    pipelined_batches=K, tuned=params64)

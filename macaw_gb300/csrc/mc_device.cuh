@@ -107,32 +107,40 @@ struct Particle {
   int elem, mat, n_seg, n_coll, status, face, zero_run;
   int fin;  // side the particle entered its element through (-1: none)
   int tag;  // parity of the particle's batch (selects its batch tally)
-  // Sigma_t at the current energy for up to four materials, direct-mapped
-  // by material index (slot = mat & 3); -1 marks an empty slot.  Sigma_t is
-  // a pure function of (material, E), so a cached value is bit-identical to
-  // a fresh evaluation; every energy change empties the cache.
+  // Sigma_t at the current energy for up to four materials, most recently
+  // inserted first (an insert shifts the others down one slot and drops the
+  // last); -1 marks an empty slot.  Sigma_t is a pure function of
+  // (material, E), so a cached value is bit-identical to a fresh
+  // evaluation whatever the slot order; every energy change empties the
+  // cache.
   int4 cm;
   double cs0, cs1, cs2, cs3;
 };
 
 __device__ __forceinline__ void xs_cache_clear(Particle& p) { p.cm = make_int4(-1, -1, -1, -1); }
 
+// Slot of material mat in a cache key set, or -1.
+__device__ __forceinline__ int xs_cache_slot(const int4& cm, int mat) {
+  return cm.x == mat ? 0 : cm.y == mat ? 1 : cm.z == mat ? 2 : cm.w == mat ? 3 : -1;
+}
+
 __device__ __forceinline__ bool xs_cache_get(Particle& p, int mat) {
-  switch (mat & 3) {
-    case 0: if (p.cm.x == mat) { p.sigt = p.cs0; return true; } return false;
-    case 1: if (p.cm.y == mat) { p.sigt = p.cs1; return true; } return false;
-    case 2: if (p.cm.z == mat) { p.sigt = p.cs2; return true; } return false;
-    default: if (p.cm.w == mat) { p.sigt = p.cs3; return true; } return false;
+  switch (xs_cache_slot(p.cm, mat)) {
+    case 0: p.sigt = p.cs0; return true;
+    case 1: p.sigt = p.cs1; return true;
+    case 2: p.sigt = p.cs2; return true;
+    case 3: p.sigt = p.cs3; return true;
+    default: return false;
   }
 }
 
+// Insert on a miss (mat is not cached).
 __device__ __forceinline__ void xs_cache_put(Particle& p, int mat, double s) {
-  switch (mat & 3) {
-    case 0: p.cm.x = mat; p.cs0 = s; break;
-    case 1: p.cm.y = mat; p.cs1 = s; break;
-    case 2: p.cm.z = mat; p.cs2 = s; break;
-    default: p.cm.w = mat; p.cs3 = s; break;
-  }
+  p.cm = make_int4(mat, p.cm.x, p.cm.y, p.cm.z);
+  p.cs3 = p.cs2;
+  p.cs2 = p.cs1;
+  p.cs1 = p.cs0;
+  p.cs0 = s;
 }
 
 // ---------------------------------------------------------------------------
@@ -568,6 +576,31 @@ __device__ __forceinline__ void collide(const DevXS& X, Particle& p) {
 // error bound; only when that comparison is not decisive is the FP64 log
 // evaluated.  Either way the outcome and the score (L when d > L) are the
 // values the FP64 arithmetic gives.
+// L2 prefetch of the walk records (and, for the FP64 form, the FP64
+// planes) of the neighbours of the element just entered: used by the tail
+// kernel, where a few long histories walk alone and each step would
+// otherwise wait a full DRAM round trip for a record nobody else touches.
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+template <bool kFP64>
+__device__ __forceinline__ void prefetch_neighbours(const DevMesh& M, const int4& nb4, int fin) {
+  const int e[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    if (f == fin || e[f] < 0) continue;
+    const int t = (e[f] & (kMatChange - 1)) >> 2;
+    const char* r = (const char*)(M.tet + t);
+    prefetch_l2(r);
+    prefetch_l2(r + 64);
+    if (kFP64) {
+      prefetch_l2(M.planes + 4 * (int64_t)t);
+      prefetch_l2(M.planes + 4 * (int64_t)t + 2);
+    }
+  }
+}
+
 template <bool kInlineXS>
 __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Particle& p,
                                             double* __restrict__ tally, float& sigt32,
@@ -699,7 +732,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
 // likewise |den32 - den| <= 12u |u|_1; t32 = num32/den32 rounded (0.5 ulp):
 // |t - t32| <= (E_num + |t32| E_den)/(den32 - E_den) + 4.8e-7 |t32|, padded
 // by 0.1%.
-template <bool kInlineXS>
+template <bool kInlineXS, bool kPrefetch = false>
 __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, Particle& p,
                                              const float uf, const float vf, const float wf,
                                              double* __restrict__ tally, float& sigt32,
@@ -735,6 +768,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   const float Eden = 7.2e-7f * (fabsf(uf) + fabsf(vf) + fabsf(wf));
   const float4* P32 = M.tet[p.elem].p;
   const int4 nb4 = __ldg(&M.tet[p.elem].nbr);  // issued with the plane loads
+  if (kPrefetch) prefetch_neighbours<true>(M, nb4, p.fin);
   bool sure = true;
   int bf = -1;
   float tb = 3.0e38f, eb = 0.0f, lo_other = 3.0e38f;
@@ -881,7 +915,7 @@ __device__ __forceinline__ int exit_fp64(const DevMesh& M, int elem, int fin, co
   return bf;
 }
 
-template <bool kInlineXS>
+template <bool kInlineXS, bool kPrefetch = false>
 __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, Particle& p,
                                              Geo32& g, double* __restrict__ tally, float& inv_sig,
                                              float tol, unsigned long long& n_xs,
@@ -913,6 +947,8 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
     inv_sig = (float)(1.0 / p.sigt);
   }
   const float4* P = M.tet[p.elem].p;
+  const int4 nb4 = __ldg(&M.tet[p.elem].nbr);  // issued with the plane loads
+  if (kPrefetch) prefetch_neighbours<false>(M, nb4, p.fin);
   int bf = -1;
   float t1 = 3.0e38f, t2 = 3.0e38f;
 #pragma unroll
@@ -962,7 +998,7 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
     g.x = fmaf(L, g.u, g.x);
     g.y = fmaf(L, g.v, g.y);
     g.z = fmaf(L, g.w, g.z);
-    const int nb = side_entry(M.tet[p.elem].nbr, bf);
+    const int nb = side_entry(nb4, bf);
     if (nb >= 0) {
       if (nb & kMatChange) p.mat = -2;
       p.elem = (nb & (kMatChange - 1)) >> 2;

@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMes
     // the cached float 1/Sigma_t of the current material (set below when mat < 0)
     float inv_sig = 0.0f;
     if (mat >= 0) {
-      const int sl = mat & 3;
+      const int sl = xs_cache_slot(cm, mat);
       inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
     }
     int r = 0, face = -1;
@@ -548,9 +548,8 @@ __global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMes
       }
       if (mat < 0) {  // after a side flagged kMatChange
         const int m = mnext;
-        const int sl = m & 3;
-        const int key = sl == 0 ? cm.x : sl == 1 ? cm.y : sl == 2 ? cm.z : cm.w;
-        if (m < 0 || key != m) {
+        const int sl = m < 0 ? -1 : xs_cache_slot(cm, m);
+        if (sl < 0) {
           r = (m < 0) ? 2 : 3;
           if (m < 0) face = -3;  // no material: bad cross section
           break;
@@ -774,7 +773,7 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
+        const int r = segment_fp64g<true, true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
         if (r == 1) collide(X, p);
         if (r == 1 || r == 5) {
           uf = (float)p.u;
@@ -787,7 +786,7 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       geo_load(p, g);
       float inv_sig = (p.mat >= 0) ? (float)(1.0 / p.sigt) : 0.0f;
       while (p.status == kAlive) {
-        const int r = segment_mixed<true>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
+        const int r = segment_mixed<true, true>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
         if (r == 1) {
           geo_store(g, p);
           collide(X, p);
