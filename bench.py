@@ -389,7 +389,6 @@ def main():
         summ = tm.tally(MC_TALLY_SUM)
         # one more batch with the walk launches timed, for the walk's roofline
         _, pst = timed(tm, MC_PREC_MIXED, paramsm, W + K, 1, True)
-        tm.close()
         nz = sum64 > 0
         rel = np.abs(summ[nz] - sum64[nz]) / sum64[nz]
         mixed = {"value": world * n * K / (mms / 1e3), "unit": "histories/s", "ms_per_step": mms / K,
@@ -431,6 +430,25 @@ def main():
         tt = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e2e_s = float(tt.item())
+    if mixed is not None:
+        # the same end-to-end loop in the mixed form (same host sites)
+        barrier()
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for k in range(K):
+            tm.run(n, first=base + (k0 + k) * n, seed=1, precision=MC_PREC_MIXED, accumulate=True,
+                   sites=site_np[k], **paramsm)
+            tm.tally(MC_TALLY_SUM, out=out_np)
+        torch.cuda.synchronize()
+        barrier()
+        m_s = time.perf_counter() - w0
+        if dist is not None:
+            tt = torch.tensor([m_s], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            m_s = float(tt.item())
+        mixed["e2e"] = {"value": world * n * K / m_s, "unit": "histories/s",
+                        "h2d_bytes_per_step": n * SITE_DTYPE.itemsize, "d2h_bytes_per_step": p.n_tet * 8}
+        tm.close()
     e2e = {"value": world * n * K / e2e_s, "unit": "histories/s",
            "h2d_bytes_per_step": n * SITE_DTYPE.itemsize, "d2h_bytes_per_step": p.n_tet * 8,
            "note": "one mc_run per step (1e6 host sites copied in, SUM tally copied out)"}

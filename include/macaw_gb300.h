@@ -110,13 +110,13 @@ typedef struct {
                               (coarsened to at most 65536 buckets) before each walk launch */
   int32_t profile;         /* 1: time every advance launch with CUDA events (mc_stats.ms_advance) */
   int32_t refill;          /* event mode: 1 lets an advance lane take the next queued particle when
-                              its particle reaches an event; 0 one particle per lane per launch */
+                              its particle reaches an event; 0: lanes walk their warp's chunk of the
+                              queue one visit at a time */
   int32_t n_batches;       /* > 1: consecutive batches of batch_sizes histories run through one
                               pipeline, each folded into SUM/SUM_SQ when it drains (needs accumulate) */
   int32_t graph;           /* event mode: 1 captures a cycle of event iterations once as a CUDA
                               graph and replays it (ignored with profile) */
-  int32_t walk_plain;      /* mixed event walk: 0 requests each next element's record one step ahead
-                              (fewer resident warps), 1 at the top of its step */
+  int32_t pad;
   const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
   const int64_t* batch_sizes; /* HOST array of n_batches sizes adding up to n_histories */
 } mc_run_desc;

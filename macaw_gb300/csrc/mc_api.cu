@@ -510,7 +510,6 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.precision = d->precision;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
-  a.walk_plain = d->walk_plain;
   a.sort_shift = -1;
   a.sort_buckets = 0;
   a.sort_tmp = nullptr;

@@ -474,10 +474,10 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
 // direction, float 1/Sigma_t for the cached materials, 64-bit RNG state and
 // trace hash.  Only the bank fields the walk reads or changes move; the
 // rest of a particle is touched only when its history ends here.  Same
-// arithmetic as segment_mixed.
-template <bool kAhead>
-__global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B,
-                                                                         EventQueues Q, EventCtl* ctl, int par) {
+// arithmetic as segment_mixed.  Each lane walks the particles of its warp's
+// queue chunks one visit at a time.
+__global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B, EventQueues Q,
+                                                             EventCtl* ctl, int par) {
   MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_adv[par];
   const int nxt = par ^ 1;
@@ -507,16 +507,14 @@ __global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMes
     }
     int r = 0, face = -1;
     int k = 0;
-    // kAhead: the record of the element being walked is loaded one step
-    // ahead -- at each crossing the neighbour's planes, entries and (after a
-    // flagged side) material are requested before that segment's tally,
-    // hash and position update, so the loads are in flight while those run
-    // (more registers: 24 resident warps per SM instead of 32).  Otherwise
-    // the record is loaded at the top of each step.
+    // The record of the element being walked is loaded one step ahead: at
+    // each crossing the neighbour's planes, entries and (after a flagged
+    // side) material are requested before that segment's tally, hash and
+    // position update, so the loads are in flight while those run.
     float4 P0, P1, P2, P3;
     int4 nb4;
     int mnext = 0;  // material of elem, valid while mat < 0
-    if (kAhead) {
+    {
       const Tet32* T = M.tet + elem;
       P0 = __ldg(&T->p[0]);
       P1 = __ldg(&T->p[1]);
@@ -531,21 +529,12 @@ __global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMes
         face = -2;  // stuck
         break;
       }
-      // this segment's draw depends on no load: with kAhead it is formed
-      // while they land, committed to the RNG state only when the segment
-      // is scored (without, it is formed after the exit search, which keeps
-      // fewer registers live across the loads)
+      // this segment's draw depends on no load: formed while they land,
+      // committed to the RNG state only when the segment is scored
       const uint64_t seed_n = kPrnMult * seed + kPrnAdd;
-      auto draw = [&]() {
-        uint64_t wv = ((seed_n >> ((seed_n >> 59u) + 5u)) ^ seed_n) * 12605985483714917081ULL;
-        wv = (wv >> 43u) ^ wv;
-        return -__logf((float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f);
-      };
-      float lnxi = kAhead ? draw() : 0.0f;
-      if (!kAhead) {
-        nb4 = __ldg(&M.tet[elem].nbr);
-        if (mat < 0) mnext = __ldg(M.tmat + elem);
-      }
+      uint64_t wv = ((seed_n >> ((seed_n >> 59u) + 5u)) ^ seed_n) * 12605985483714917081ULL;
+      wv = (wv >> 43u) ^ wv;
+      const float lnxi = -__logf((float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f);
       if (mat < 0) {  // after a side flagged kMatChange
         const int m = mnext;
         const int sl = m < 0 ? -1 : xs_cache_slot(cm, m);
@@ -560,9 +549,8 @@ __global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMes
       }
       int bf = -1;
       float t1 = 3.0e38f, t2 = 3.0e38f;
-      auto side = [&](const float4& held, int f) {
+      auto side = [&](const float4& pl, int f) {
         if (f == fin) return;
-        const float4 pl = kAhead ? held : __ldg(&M.tet[elem].p[f]);  // plain: the three planes needed
         const float den = fmaf(pl.x, u, fmaf(pl.y, v, pl.z * w));
         if (den > 0.0f) {
           const float num = pl.w - fmaf(pl.x, x, fmaf(pl.y, y, pl.z * z));
@@ -596,12 +584,11 @@ __global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMes
         Ls = fmaxf(t1, 0.0f);
       }
       seed = seed_n;
-      if (!kAhead) lnxi = draw();
       const float dist = lnxi * inv_sig;
       const bool cross = dist > Ls;
       const int nb = side_entry(nb4, bf);
       const int next = (nb & (kMatChange - 1)) >> 2;
-      if (kAhead && cross && nb >= 0) {
+      if (cross && nb >= 0) {
         const Tet32* T = M.tet + next;
         P0 = __ldg(&T->p[0]);
         P1 = __ldg(&T->p[1]);
@@ -636,8 +623,7 @@ __global__ void __launch_bounds__(256, kAhead ? 3 : 4) k_ev_advance_mixed(DevMes
         const int bid = -1 - nb;
         if (bid < M.n_bid && M.bc_type[bid] == 1) {
           // no load is issued for a boundary side: P0..P3 are still this element's
-          const float4 pb = !kAhead ? __ldg(&M.tet[elem].p[bf])
-                            : bf == 0 ? P0 : bf == 1 ? P1 : bf == 2 ? P2 : P3;
+          const float4 pb = bf == 0 ? P0 : bf == 1 ? P1 : bf == 2 ? P2 : P3;
           const float t2r = 2.0f * fmaf(u, pb.x, fmaf(v, pb.y, w * pb.z));
           u = fmaf(-t2r, pb.x, u);
           v = fmaf(-t2r, pb.y, v);
@@ -901,14 +887,11 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
     if (n_launch) *n_launch += 4;
   }
   if (adv0) cudaEventRecord(adv0, st);
-  if (a.refill) {
-    if (a.precision == MC_PREC_MIXED) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.precision == MC_PREC_MIXED) {
+    if (a.refill) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_advance_mixed<<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
   } else {
-    if (a.precision == MC_PREC_MIXED) {
-      if (a.walk_plain) k_ev_advance_mixed<false><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
-      else k_ev_advance_mixed<true><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
-    }
+    if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else k_ev_advance_static<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   }
   if (adv1) cudaEventRecord(adv1, st);

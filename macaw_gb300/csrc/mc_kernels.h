@@ -90,7 +90,6 @@ struct RunArgs {
   const DevRequest* req;        // device: birth-sequence entries sorted by start, or null
   int n_req;
   int* live;                    // event mode: in-flight counters per tally slot, or null
-  int walk_plain;               // mixed walk: 1 loads each element's record at the top of its step
   mc_trace* traces;
   unsigned long long* counters;
   double* leak_w;

@@ -164,7 +164,6 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.tol = v.tol;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
-  a.walk_plain = d->walk_plain;
   a.sort_shift = -1;  // ordering needs scratch beyond the fixed array
   a.sort_buckets = 0;
   a.sort_tmp = nullptr;

@@ -1,8 +1,8 @@
 // mc_tune.cpp -- autotuner for the event form's execution parameters.
 //
 // Bank size, block shape, segments per walk launch, the advance-queue
-// ordering granularity, lane refill, CUDA-graph replay and the mixed walk's
-// load placement all move throughput, and their best
+// ordering granularity, lane refill and CUDA-graph replay all move
+// throughput, and their best
 // values depend on the mesh, the cross sections and the precision form.
 // mc_autotune measures them on trial runs of the context's own problem
 // (device time from the CUDA events inside mc_run) by coordinate descent:
@@ -70,14 +70,13 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
   };
   const int64_t t = trial_histories;
   std::vector<Knob> knobs = {
-      {0, {0, 16, 32, 64, 128, 256}},                              // segments per walk launch
+      {0, {0, 16, 32, 48, 64, 96, 128, 256}},                      // segments per walk launch
       {1, {64, 128, 256}},                                         // threads per block
       {2, {0, 1, 5, 9, 13}},                                       // queue ordering granularity
       {3, {std::max<int64_t>(16384, t / 8), std::max<int64_t>(16384, t / 4), std::max<int64_t>(16384, t / 2)}},
       // (bank sizes only when the caller left the bank open)
       {4, {0, 1}},                                                 // lane refill
       {5, {0, 1}},                                                 // CUDA-graph event cycles
-      {6, {0, 1}},                                                 // mixed walk: loads ahead / plain
   };
   auto apply = [](mc_run_desc& d, int kind, int64_t v) {
     switch (kind) {
@@ -86,8 +85,7 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       case 2: d.sort_queue = (int32_t)v; break;
       case 3: d.bank_size = v; break;
       case 4: d.refill = (int32_t)v; break;
-      case 5: d.graph = (int32_t)v; break;
-      default: d.walk_plain = (int32_t)v; break;
+      default: d.graph = (int32_t)v; break;
     }
   };
   for (int pass = 0; pass < 2; ++pass) {
@@ -112,7 +110,6 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
   best->sort_queue = cur.sort_queue;
   best->refill = cur.refill;
   best->graph = cur.graph;
-  best->walk_plain = cur.walk_plain;
   best->bank_size = base->bank_size > 0 ? base->bank_size : cur.bank_size;
   if (best_rate) *best_rate = rate;
   return MC_OK;

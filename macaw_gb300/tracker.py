@@ -114,7 +114,7 @@ class Tracker:
             precision: int = MC_PREC_FP64, bank_size: int = 0, block_size: int = 0,
             max_seg: int = 0, traces: bool = False, accumulate: bool = False,
             sort_queue: bool = False, profile: bool = False, sites: np.ndarray | None = None,
-            refill: bool = False, batch_sizes=None, graph: bool = False, walk_plain: bool = False) -> Stats:
+            refill: bool = False, batch_sizes=None, graph: bool = False) -> Stats:
         """One batch of n histories, or, with batch_sizes (adding up to n),
         consecutive batches run through one pipeline (needs accumulate)."""
         if sites is not None:
@@ -122,7 +122,7 @@ class Tracker:
         bs = None if batch_sizes is None else np.ascontiguousarray(batch_sizes, np.int64)
         d = RunDesc(first, n, bank_size, seed, precision, mode, block_size, max_seg, int(traces),
                     int(accumulate), int(sort_queue), int(profile), int(refill), 0 if bs is None else bs.size,
-                    int(graph), int(walk_plain), None if sites is None else sites.ctypes.data,
+                    int(graph), 0, None if sites is None else sites.ctypes.data,
                     None if bs is None else bs.ctypes.data)
         self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
         return self.stats()
@@ -132,13 +132,13 @@ class Tracker:
         d = RunDesc(base.get("first", 0), trial, base.get("bank_size", 0), base.get("seed", 1),
                     base.get("precision", MC_PREC_FP64), MC_MODE_EVENT, base.get("block_size", 0),
                     base.get("max_seg", 0), 0, 0, base.get("sort_queue", 0), 0, base.get("refill", 0), 0,
-                    base.get("graph", 0), base.get("walk_plain", 0), None, None)
+                    base.get("graph", 0), 0, None, None)
         out = RunDesc()
         rate = C.c_double()
         self._ck(lib.mc_autotune(self._h, C.byref(d), trial, C.byref(out), C.byref(rate)), "mc_autotune")
         return ({"bank_size": out.bank_size, "block_size": out.block_size, "max_seg": out.max_seg_per_advance,
-                 "sort_queue": out.sort_queue, "refill": bool(out.refill), "graph": bool(out.graph),
-                 "walk_plain": bool(out.walk_plain)}, rate.value)
+                 "sort_queue": out.sort_queue, "refill": bool(out.refill), "graph": bool(out.graph)},
+                rate.value)
 
     def sample_sites(self, n: int, first: int = 0, seed: int = 1, out: np.ndarray | None = None) -> np.ndarray:
         if out is None:

@@ -32,11 +32,13 @@ def fp64_tally(lattice):
         return t.tally()
 
 
-@pytest.mark.parametrize("mode", [MC_MODE_EVENT, MC_MODE_HISTORY])
-def test_mixed_matches_fp64_tallies(lattice, fp64_tally, mode):
+@pytest.mark.parametrize("mode,walk", [(MC_MODE_EVENT, {}), (MC_MODE_EVENT, {"refill": True, "max_seg": 64}),
+                                       (MC_MODE_EVENT, {"sort_queue": 9, "max_seg": 96, "graph": True}),
+                                       (MC_MODE_HISTORY, {})])
+def test_mixed_matches_fp64_tallies(lattice, fp64_tally, mode, walk):
     with Tracker(0) as t:
         t.load(lattice)
-        st = t.run(200000, seed=9, mode=mode, precision=MC_PREC_MIXED)
+        st = t.run(200000, seed=9, mode=mode, precision=MC_PREC_MIXED, **walk)
         m = t.tally()
     assert st.n_hist == 200000
     assert st.n_stuck == 0 and st.n_lost == 0 and st.n_badxs == 0
