@@ -50,6 +50,16 @@ extern "C" {
 #define MC_SRC_WATT 0
 #define MC_SRC_MONO 1
 
+/* tally estimators and scores (OpenMCTally `estimator` and `scores`) */
+#define MC_EST_TRACKLENGTH 1
+#define MC_EST_COLLISION 2
+#define MC_SCORE_FLUX 0
+#define MC_SCORE_TOTAL 1
+#define MC_SCORE_SCATTER 2
+#define MC_SCORE_ABSORPTION 3
+#define MC_MAX_SCORES 4
+#define MC_MAX_ENERGY_BINS 4096
+
 /* tally readback kinds */
 #define MC_TALLY_BATCH 0   /* raw sum of wgt*track length of the current batch */
 #define MC_TALLY_SUM 1     /* OpenMC results SUM: sum over batches of batch/weight */
@@ -200,17 +210,42 @@ int mc_source_sample(mc_ctx* ctx, int64_t first, int64_t n, uint64_t seed, mc_si
 int mc_ctx_set_stream(mc_ctx* ctx, void* stream);
 /* Autotuner (no counterpart in the reference, whose MPI/thread layout is set
  * by hand on the command line): picks segments per walk launch, threads per
- * block, advance-queue ordering, bank size and lane refill of the event form
- * that give the most histories/s on trial batches of trial_histories
- * (>= 1024) histories of this context's problem, starting from *base;
+ * block, advance-queue ordering, bank size (when base->bank_size is 0), lane
+ * refill and CUDA-graph replay of the event form that give the most
+ * histories/s on trials of trial_histories (>= 1024) histories of this
+ * context's problem (four pipelined batches each), starting from *base;
  * writes *base with those fields replaced to *best and the rate reached to
- * *best_rate.  Trial scores go to the batch tally, which is cleared. */
+ * *best_rate.  SUM, SUM_SQ and the batch count are restored afterwards and
+ * the batch tally is left cleared. */
 int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_histories, mc_run_desc* best,
                 double* best_rate);
 
+/* ---- tally definition ------------------------------------------------- */
+typedef struct {
+  int32_t estimator;       /* MC_EST_TRACKLENGTH or MC_EST_COLLISION */
+  int32_t n_scores;        /* 1..MC_MAX_SCORES */
+  int32_t scores[MC_MAX_SCORES]; /* MC_SCORE_*: track length scores flux and total; collision all four */
+  int32_t n_energy_bins;   /* 0: no energy filter; else the bins between n_energy_bins+1 edges */
+  int32_t pad;
+  const double* energy_edges; /* HOST array of ascending edges (eV); energies outside score nothing */
+} mc_tally_desc;
+
+/* Replaces: OpenMCTally (src/userobjects/OpenMCTally.C:30-101, 103-198):
+ * the estimator, scores and energy filter of the element tally (cell
+ * filter: one bin per element).  Results are laid out [element][energy
+ * bin][score] in every tally kind; mc_tally_size gives their number.
+ *   track length, per segment: flux wgt*l, total wgt*l*Sigma_t;
+ *   collision, per collision:  flux wgt/Sigma_t, total wgt, scatter
+ *   wgt*Sigma_s/Sigma_t, absorption wgt*(Sigma_t-Sigma_s)/Sigma_t,
+ * at the energy before the collision.  Without a call the tally is the
+ * track-length flux per element.  Clears every tally and the batch count;
+ * an upload of a new mesh restores the default. */
+int mc_tally_configure(mc_ctx* ctx, const mc_tally_desc* desc);
+int mc_tally_size(mc_ctx* ctx, int64_t* n_values);
+
 /* ---- results --------------------------------------------------------- */
 /* Replaces: OpenMCTallyAux::computeValue element readback
- * (src/auxkernels/OpenMCTallyAux.C:187-205), for the element flux tally. */
+ * (src/auxkernels/OpenMCTallyAux.C:187-205).  n must equal mc_tally_size. */
 int mc_tally_download(mc_ctx* ctx, int32_t kind, double* out, int64_t n);
 int mc_tally_reset(mc_ctx* ctx);
 /* Clears one tally (MC_TALLY_BATCH, MC_TALLY_SUM or MC_TALLY_SUM_SQ). */
@@ -235,8 +270,8 @@ int mc_batches_done(mc_ctx* ctx, int64_t* out);
  * - bank_size must be at most MC_NOALLOC_MAX_BANK (0 means the maximum);
  *   larger values are rejected with MC_ERR_ARG.  Any number of histories
  *   is fine: the bank is refilled as histories end.
- * - tally: caller-owned DEVICE buffer of n_tet doubles; scores are added to
- *   it, so clear it first.  traces: caller-owned DEVICE buffer of
+ * - tally: caller-owned DEVICE buffer of mc_tally_size doubles; scores are
+ *   added to it, so clear it first.  traces: caller-owned DEVICE buffer of
  *   n_histories records when record_traces is set, else NULL.
  * - The mesh, tables, block map, boundary conditions and source must already
  *   be on the device: after the last set-up call, run mc_run once (for
@@ -253,7 +288,8 @@ int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* desc, double* tally, mc_trace
 /* ---- serving: continuous batching of fixed-source requests ------------
  * No counterpart in the reference (MaCaw runs one input file per process).
  * A context with its mesh and cross sections resident takes requests as
- * they arrive.  Each admitted request gets a tally slot (n_tet doubles) and
+ * they arrive.  Each admitted request gets a tally slot (mc_tally_size
+ * doubles, the context's tally definition) and
  * its histories join the shared particle bank, born as slots free up, so
  * requests overlap on the device without draining between them.  Request
  * particle ids are 1..n_histories under the request's seed: a request's
@@ -264,7 +300,7 @@ typedef struct {
   uint64_t seed;
   mc_source_desc source;  /* point or box space; Watt or mono energy */
 } mc_request;
-/* max_slots requests in flight (tally memory max_slots*n_tet*8 bytes),
+/* max_slots requests in flight (tally memory max_slots*mc_tally_size*8 bytes),
  * bank_size particles in flight, precision MC_PREC_*, max_seg segments per
  * walk launch (0: until an event). */
 int mc_serve_open(mc_ctx* ctx, int32_t max_slots, int64_t bank_size, int32_t precision, int32_t max_seg);
@@ -275,10 +311,33 @@ int mc_serve_step(mc_ctx* ctx, int32_t iterations);
 /* Waits for launched work; retires finished requests, writing up to
  * capacity tickets into done and their count into n_done. */
 int mc_serve_poll(mc_ctx* ctx, int64_t* done, int32_t capacity, int32_t* n_done);
-/* FP64 element track-length tally (sum of wgt*length) of a finished request. */
-int mc_serve_result(mc_ctx* ctx, int64_t ticket, double* tally, int64_t n_tet);
+/* FP64 tally of a finished request (raw sums, mc_tally_size values; the
+ * default definition: wgt*length per element). */
+int mc_serve_result(mc_ctx* ctx, int64_t ticket, double* tally, int64_t n);
 int mc_serve_status(mc_ctx* ctx, int32_t* queued, int32_t* active, int32_t* free_slots);
 int mc_serve_close(mc_ctx* ctx);
+
+/* ---- Exodus II output --------------------------------------------------
+ * Replaces: MOOSE's Exodus output of a MaCaw run's element AuxVariables
+ * ([Outputs] exodus = true; the reference's gold results are Exodus files,
+ * test/tests/study/gold/openmc_study_rays.e).  Writes path as an Exodus II
+ * file in netCDF's 64-bit-offset format: nodes, one TETRA4 element block
+ * per subdomain (ascending id, elements in mesh order), side sets from
+ * tet_side_bid (optional, as for mc_mesh_upload; only faces no other tet
+ * shares), n_vars element variables named names[i] with
+ * values[i*n_tet + elem], one time step. */
+int mc_exodus_write(const char* path, const char* title, int64_t n_vtx, const double* xyz, int64_t n_tet,
+                    const int32_t* tet_vtx, const int32_t* tet_block, const int32_t* tet_side_bid, int32_t n_vars,
+                    const char* const* names, const double* values, double time);
+/* Replaces: MOOSE FileMeshGenerator reading the mesh MaCaw traces on
+ * (examples/beavrs_assembly/run_assembly.i [Mesh]).  Reads an Exodus II
+ * file (netCDF classic or 64-bit offset): every element block must be
+ * 4-node tetrahedra; elements are numbered in block order and take their
+ * block's id; side sets set tet_side_bid (optional, 4 per tet, -1 where no
+ * side set names the face).  On failure err (optional) holds the reason. */
+int mc_exodus_read_sizes(const char* path, int64_t* n_vtx, int64_t* n_tet, char* err, int64_t err_len);
+int mc_exodus_read(const char* path, double* xyz, int32_t* tet_vtx, int32_t* tet_block, int32_t* tet_side_bid,
+                   char* err, int64_t err_len);
 
 /* ---- input-file front end ---------------------------------------------
  * Replaces: running a MaCaw input (MooseApp::run on an .i file; src/main.C)

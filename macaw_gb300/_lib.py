@@ -21,6 +21,8 @@ MC_MODE_HISTORY, MC_MODE_EVENT = 0, 1
 MC_SRC_POINT, MC_SRC_BOX, MC_SRC_CYLINDERS = 0, 1, 2
 MC_SRC_WATT, MC_SRC_MONO = 0, 1
 MC_TALLY_BATCH, MC_TALLY_SUM, MC_TALLY_SUM_SQ = 0, 1, 2
+MC_EST_TRACKLENGTH, MC_EST_COLLISION = 1, 2
+MC_SCORE_FLUX, MC_SCORE_TOTAL, MC_SCORE_SCATTER, MC_SCORE_ABSORPTION = 0, 1, 2, 3
 STATUS_NAMES = {1: "leaked", 2: "absorbed", 3: "cutoff", 4: "stuck", 5: "lost", 6: "bad_xs"}
 
 
@@ -30,6 +32,11 @@ class SourceDesc(C.Structure):
                 ("n_cyl", C.c_int32), ("pad", C.c_int32), ("cyl_xy", C.POINTER(C.c_double)),
                 ("cyl_r", C.c_double), ("cyl_z0", C.c_double), ("cyl_z1", C.c_double),
                 ("watt_a", C.c_double), ("watt_b", C.c_double), ("mono_E", C.c_double)]
+
+
+class TallyDesc(C.Structure):
+    _fields_ = [("estimator", C.c_int32), ("n_scores", C.c_int32), ("scores", C.c_int32 * 4),
+                ("n_energy_bins", C.c_int32), ("pad", C.c_int32), ("energy_edges", C.c_void_p)]
 
 
 class RunDesc(C.Structure):
@@ -92,6 +99,11 @@ SIGNATURES = {
     "mc_app_run": ([C.c_char_p, C.c_int, C.c_char_p, C.c_char_p, _I64], C.c_int),
     "mc_app_check": ([C.c_char_p, C.c_char_p, _I64], C.c_int),
     "mc_tally_download": ([_P, _I32, _P, _I64], C.c_int),
+    "mc_tally_configure": ([_P, C.c_void_p], C.c_int),
+    "mc_exodus_read_sizes": ([C.c_char_p, C.POINTER(_I64), C.POINTER(_I64), C.c_char_p, _I64], C.c_int),
+    "mc_exodus_read": ([C.c_char_p, _P, _P, _P, _P, C.c_char_p, _I64], C.c_int),
+    "mc_exodus_write": ([C.c_char_p, C.c_char_p, _I64, _P, _I64, _P, _P, _P, _I32, _P, _P, _D], C.c_int),
+    "mc_tally_size": ([_P, C.POINTER(_I64)], C.c_int),
     "mc_tally_reset": ([_P], C.c_int),
     "mc_tally_clear": ([_P, _I32], C.c_int),
     "mc_autotune": ([_P, C.POINTER(RunDesc), _I64, C.POINTER(RunDesc), C.POINTER(_D)], C.c_int),

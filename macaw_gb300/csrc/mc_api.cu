@@ -84,6 +84,11 @@ struct mc_ctx {
   int64_t batches_save = 0;
   DevBuf d_sort_tmp, d_sort_cnt;
   bool tally2_clear = false;  // d_tally2 is all zeros between runs
+  // tally definition (mc_tally_configure); the default scores the
+  // track-length flux, one value per element
+  TallySpec tspec{};           // device view (edges point into d_edges)
+  DevBuf d_edges;
+  int64_t n_tally = 0;         // values per tally: elements x energy bins x scores
   long long h_limit = 0;
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
@@ -366,9 +371,15 @@ int mc_mesh_upload(mc_ctx* c, int64_t n_vtx, const double* xyz, int64_t n_tet,
   CK(upload(c->d_gstart, c->mesh.gstart, c->stream), "upload locator");
   CK(upload(c->d_gtets, c->mesh.gtets, c->stream), "upload locator");
   CK(upload(c->d_gseed, c->mesh.gseed, c->stream), "upload locator");
-  CK(c->d_tally.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
-  CK(c->d_sum.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
-  CK(c->d_sumsq.alloc(sizeof(double) * (size_t)n_tet), "allocate tally");
+  c->tspec = TallySpec{};
+  c->tspec.est = MC_EST_TRACKLENGTH;
+  c->tspec.nb = 1;
+  c->tspec.ns = 1;
+  c->n_tally = n_tet;
+  c->tally2_clear = false;
+  CK(c->d_tally.alloc(sizeof(double) * (size_t)c->n_tally), "allocate tally");
+  CK(c->d_sum.alloc(sizeof(double) * (size_t)c->n_tally), "allocate tally");
+  CK(c->d_sumsq.alloc(sizeof(double) * (size_t)c->n_tally), "allocate tally");
   CK(cudaMemsetAsync(c->d_tally.p, 0, c->d_tally.bytes, c->stream), "clear tally");
   CK(cudaMemsetAsync(c->d_sum.p, 0, c->d_sum.bytes, c->stream), "clear tally");
   CK(cudaMemsetAsync(c->d_sumsq.p, 0, c->d_sumsq.bytes, c->stream), "clear tally");
@@ -575,7 +586,7 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       q.has_src = 0;
     }
     CK(upload(c->d_batch_end, rq, c->stream), "upload batch table");
-    const size_t need = sizeof(double) * (size_t)c->mesh.n_tet * (size_t)(slots - 1);
+    const size_t need = sizeof(double) * (size_t)c->n_tally * (size_t)(slots - 1);
     if (c->d_tally2.bytes < need) {
       CK(c->d_tally2.alloc(need), "allocate batch tallies");
       c->tally2_clear = false;
@@ -593,16 +604,17 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
     a.req = nullptr;
     a.n_req = 0;
   }
-  a.n_tet = c->mesh.n_tet;
+  a.n_tally = c->n_tally;
+  a.ts = c->tspec;
   a.live = nullptr;
   // history-form batches all score into slot 0 (one runs at a time);
   // event-form batch b scores into slot b % slots
   auto fold = [&](int b) -> int {
     const int64_t size = bend[b] - (b ? bend[b - 1] : 0);
     const int sl = (d->mode == MC_MODE_EVENT) ? b % slots : 0;
-    double* buf = sl ? a.tally2 + (int64_t)(sl - 1) * c->mesh.n_tet : a.tally;
+    double* buf = sl ? a.tally2 + (int64_t)(sl - 1) * c->n_tally : a.tally;
     CK(launch_accumulate(buf, c->d_sum.as<double>(), c->d_sumsq.as<double>(),
-                         c->mesh.n_tet, size > 0 ? 1.0 / (double)size : 0.0, c->stream),
+                         c->n_tally, size > 0 ? 1.0 / (double)size : 0.0, c->stream),
        "launch accumulate");
     c->batches += 1;
     return MC_OK;
@@ -829,7 +841,8 @@ int mc_tally_download(mc_ctx* c, int32_t kind, double* out, int64_t n) {
   if (!c || !out) return MC_ERR_ARG;
   std::lock_guard<std::mutex> g(c->mu);
   if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh");
-  if (n != c->mesh.n_tet) return set_err(c, MC_ERR_ARG, "tally length must equal the number of tets");
+  if (n != c->n_tally)
+    return set_err(c, MC_ERR_ARG, "tally length must equal mc_tally_size (" + std::to_string(c->n_tally) + ")");
   DevBuf* b = kind == MC_TALLY_BATCH ? &c->d_tally : kind == MC_TALLY_SUM ? &c->d_sum
               : kind == MC_TALLY_SUM_SQ ? &c->d_sumsq : nullptr;
   if (!b) return set_err(c, MC_ERR_ARG, "unknown tally kind");
@@ -849,6 +862,73 @@ int mc_tally_reset(mc_ctx* c) {
   CK(cudaMemsetAsync(c->d_sumsq.p, 0, c->d_sumsq.bytes, c->stream), "clear tally");
   CK(cudaStreamSynchronize(c->stream), "clear tally");
   c->batches = 0;
+  return MC_OK;
+}
+
+int mc_tally_configure(mc_ctx* c, const mc_tally_desc* d) {
+  if (!c || !d) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh");
+  if (c->serving) return set_err(c, MC_ERR_STATE, "the tally cannot change while serving is open");
+  if (d->estimator != MC_EST_TRACKLENGTH && d->estimator != MC_EST_COLLISION)
+    return set_err(c, MC_ERR_ARG, "estimator must be MC_EST_TRACKLENGTH or MC_EST_COLLISION");
+  if (d->n_scores < 1 || d->n_scores > MC_MAX_SCORES) return set_err(c, MC_ERR_ARG, "1 to 4 scores");
+  int sc = 0;
+  bool need_ss = false;
+  for (int j = 0; j < d->n_scores; ++j) {
+    const int s = d->scores[j];
+    if (s < MC_SCORE_FLUX || s > MC_SCORE_ABSORPTION) return set_err(c, MC_ERR_ARG, "unknown score");
+    if (d->estimator == MC_EST_TRACKLENGTH && s != MC_SCORE_FLUX && s != MC_SCORE_TOTAL)
+      return set_err(c, MC_ERR_ARG, "the track-length estimator scores flux and total only");
+    for (int i = 0; i < j; ++i)
+      if (d->scores[i] == s) return set_err(c, MC_ERR_ARG, "repeated score");
+    if (s == MC_SCORE_SCATTER || s == MC_SCORE_ABSORPTION) need_ss = true;
+    sc |= s << (8 * j);
+  }
+  const int nb = d->n_energy_bins > 0 ? d->n_energy_bins : 1;
+  if (d->n_energy_bins > MC_MAX_ENERGY_BINS) return set_err(c, MC_ERR_ARG, "too many energy bins");
+  if (d->n_energy_bins > 0) {
+    if (!d->energy_edges) return set_err(c, MC_ERR_ARG, "null energy edges");
+    for (int b = 0; b < d->n_energy_bins; ++b)
+      if (!(d->energy_edges[b + 1] > d->energy_edges[b]))
+        return set_err(c, MC_ERR_ARG, "energy edges must ascend strictly");
+  }
+  cudaSetDevice(c->device);
+  TallySpec t{};
+  t.general = 1;
+  t.est = d->estimator;
+  t.nb = nb;
+  t.ns = d->n_scores;
+  t.sc = sc;
+  t.need_ss = need_ss;
+  t.edges = nullptr;
+  if (d->n_energy_bins > 0) {
+    std::vector<double> e(d->energy_edges, d->energy_edges + d->n_energy_bins + 1);
+    CK(upload(c->d_edges, e, c->stream), "upload energy edges");
+    t.edges = c->d_edges.as<double>();
+  }
+  // the default definition keeps the one-value-per-element fast path
+  if (t.est == MC_EST_TRACKLENGTH && t.ns == 1 && sc == MC_SCORE_FLUX && d->n_energy_bins <= 0) t.general = 0;
+  c->tspec = t;
+  c->n_tally = c->mesh.n_tet * (int64_t)nb * (int64_t)t.ns;
+  c->tally2_clear = false;
+  c->d_tally2.release();
+  CK(c->d_tally.alloc(sizeof(double) * (size_t)c->n_tally), "allocate tally");
+  CK(c->d_sum.alloc(sizeof(double) * (size_t)c->n_tally), "allocate tally");
+  CK(c->d_sumsq.alloc(sizeof(double) * (size_t)c->n_tally), "allocate tally");
+  CK(cudaMemsetAsync(c->d_tally.p, 0, c->d_tally.bytes, c->stream), "clear tally");
+  CK(cudaMemsetAsync(c->d_sum.p, 0, c->d_sum.bytes, c->stream), "clear tally");
+  CK(cudaMemsetAsync(c->d_sumsq.p, 0, c->d_sumsq.bytes, c->stream), "clear tally");
+  CK(cudaStreamSynchronize(c->stream), "configure tally");
+  c->batches = 0;
+  return MC_OK;
+}
+
+int mc_tally_size(mc_ctx* c, int64_t* n) {
+  if (!c || !n) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh");
+  *n = c->n_tally;
   return MC_OK;
 }
 
@@ -907,6 +987,8 @@ bool ctx_view(mc_ctx* c, CtxView* v) {
   v->n_sm = c->n_sm;
   v->stream = c->stream;
   v->n_tet = c->mesh.n_tet;
+  v->n_tally = c->n_tally;
+  v->ts = c->tspec;
   v->n_mat = (int)c->xs.mat_ids.size();
   const bool tables = c->have_mesh && !c->nucs.empty() && !c->mats.empty() && !c->xs_dirty && !c->tmat_dirty &&
                       !c->bc_dirty;

@@ -282,16 +282,21 @@ struct Problem {
   struct Tally {
     int id;
     std::string filter;  // cell | universe
+    int estimator;       // MC_EST_*
+    std::vector<int> scores;
+    std::vector<double> edges;  // energy filter edges, empty: none
   };
   std::vector<Tally> tallies;
   struct Aux {
     std::string name, variable, granularity;
     int tally_id;
+    int score;       // MC_SCORE_*
+    int energy_bin;  // -1: summed over the energy bins
   };
   std::vector<Aux> aux;
   int64_t batches = 1;
   std::string file_base;
-  bool csv = false;
+  bool csv = false, exodus = false;
 };
 
 const std::map<std::string, int> kSideNames = {{"back", 0}, {"bottom", 1}, {"right", 2},
@@ -346,6 +351,29 @@ void tet_lattice_mesh(Params& p, Problem& P) {
   P.hi[0] = nx * pitch;
   P.hi[1] = ny * pitch;
   P.hi[2] = height;
+}
+
+// MOOSE FileMeshGenerator: a tet mesh from an Exodus II file (path relative
+// to the working directory); blocks and side sets from the file.
+void file_mesh(Params& p, Problem& P) {
+  const std::string file = p.str("file");
+  char err[512] = {0};
+  if (mc_exodus_read_sizes(file.c_str(), &P.n_vtx, &P.n_tet, err, sizeof err)) p.error("file", err);
+  P.xyz.resize(3 * P.n_vtx);
+  P.tv.resize(4 * P.n_tet);
+  P.blk.resize(P.n_tet);
+  P.bid.resize(4 * P.n_tet);
+  if (mc_exodus_read(file.c_str(), P.xyz.data(), P.tv.data(), P.blk.data(), P.bid.data(), err, sizeof err))
+    p.error("file", err);
+  for (int k = 0; k < 3; ++k) {
+    P.lo[k] = INFINITY;
+    P.hi[k] = -INFINITY;
+  }
+  for (int64_t v = 0; v < P.n_vtx; ++v)
+    for (int k = 0; k < 3; ++k) {
+      P.lo[k] = std::min(P.lo[k], P.xyz[3 * v + k]);
+      P.hi[k] = std::max(P.hi[k], P.xyz[3 * v + k]);
+    }
 }
 
 // --- [RayKernels] -------------------------------------------------------------
@@ -468,22 +496,59 @@ void openmc_study(Params& p, Problem& P) {
   P.have_study = true;
 }
 
-// OpenMCTally (src/userobjects/OpenMCTally.C:30-101): the GPU path scores the
-// element track-length flux, so the estimator must be TRACKLENGTH and the
-// score flux; the filter selects cell (element) or universe (block) bins.
+// Score names of the synthetic tables (no fission data: fission scores are
+// rejected).
+int score_of(Params& p, const char* key, const std::string& s) {
+  if (s == "flux") return MC_SCORE_FLUX;
+  if (s == "total") return MC_SCORE_TOTAL;
+  if (s == "scatter") return MC_SCORE_SCATTER;
+  if (s == "absorption") return MC_SCORE_ABSORPTION;
+  p.error(key, "score '" + s + "' is not available: the synthetic tables give flux, total, scatter and "
+                           "absorption");
+  return -1;
+}
+
+// OpenMCTally (src/userobjects/OpenMCTally.C:30-101): estimator (COLLISION
+// by default, as in the reference, or TRACKLENGTH), scores, and the filters
+// cell (element bins) or universe (block bins), energy (with energy_bins)
+// and particle (neutron).
 void openmc_tally(Params& p, Problem& P) {
   Problem::Tally t;
   t.id = (int)p.integer("id", 0, true);
   if (p.choice("particle_type", {"neutron", "photon", "electron", "positron"}, "neutron") != "neutron")
     p.error("particle_type", "Only neutrons are currently supported.");
-  if (p.choice("estimator", {"ANALOG", "TRACKLENGTH", "COLLISION"}, "TRACKLENGTH") != "TRACKLENGTH")
-    p.error("estimator", "Only the tracklength estimator is available on the GPU path");
-  for (auto& s : p.list("scores", true))
-    if (s != "flux") p.error("scores", "Only the flux score is available on the GPU path");
-  auto f = p.list("filters", true);
-  if (f.size() != 1 || (f[0] != "cell" && f[0] != "universe"))
-    p.error("filters", "Use one of the filters 'cell' or 'universe'");
-  t.filter = f[0];
+  const std::string est = p.choice("estimator", {"ANALOG", "TRACKLENGTH", "COLLISION"}, "COLLISION");
+  if (est == "ANALOG") p.error("estimator", "the analog estimator is not available on the GPU path");
+  t.estimator = est == "TRACKLENGTH" ? MC_EST_TRACKLENGTH : MC_EST_COLLISION;
+  for (auto& s : p.list("scores", true)) {
+    const int sc = score_of(p, "scores", s);
+    if (t.estimator == MC_EST_TRACKLENGTH && sc != MC_SCORE_FLUX && sc != MC_SCORE_TOTAL)
+      p.error("scores", "the tracklength estimator scores flux and total only");
+    for (int o : t.scores)
+      if (o == sc) p.error("scores", "repeated score '" + s + "'");
+    t.scores.push_back(sc);
+  }
+  if (t.scores.size() > MC_MAX_SCORES) p.error("scores", "at most 4 scores");
+  bool energy = false;
+  for (auto& f : p.list("filters", true)) {
+    if (f == "cell" || f == "universe") {
+      if (!t.filter.empty()) p.error("filters", "use one of the filters 'cell' or 'universe'");
+      t.filter = f;
+    } else if (f == "energy") {
+      energy = true;
+    } else if (f != "particle") {
+      p.error("filters", "unknown filter '" + f + "' (cell, universe, energy, particle)");
+    }
+  }
+  if (t.filter.empty()) p.error("filters", "a 'cell' or 'universe' filter is needed for element results");
+  if (energy) {
+    if (!p.has("energy_bins"))
+      p.error("energy_bins", "The energy bins parameter should be supplied if an energy filter is requested.");
+    for (auto& e : p.list("energy_bins", true)) t.edges.push_back(std::stod(e));
+    if (t.edges.size() < 2) p.error("energy_bins", "at least two edges");
+    for (size_t b = 1; b < t.edges.size(); ++b)
+      if (!(t.edges[b] > t.edges[b - 1])) p.error("energy_bins", "edges must ascend");
+  }
   if (p.has("execute_on")) p.raw("execute_on");
   for (auto& o : P.tallies)
     if (o.id == t.id) p.error("id", "duplicate tally id");
@@ -497,7 +562,8 @@ void openmc_tally_aux(Params& p, Problem& P) {
   a.tally_id = (int)p.integer("tally_id", 0, true);
   a.granularity = p.choice("granularity", {"global", "universe", "cell"}, "cell");
   if (a.granularity == "global") p.error("granularity", "Global Tally retrieving currently not supported");
-  if (p.str("score") != "flux") p.error("score", "The specified score does not exist in given tally");
+  a.score = score_of(p, "score", p.str("score"));
+  a.energy_bin = p.has("energy_bin") ? (int)p.integer("energy_bin", 0) : -1;
   p.choice("estimator", {"ANALOG", "TRACKLENGTH", "COLLISION"}, "COLLISION");
   p.choice("particle_type", {"neutron", "photon", "electron", "positron"}, "neutron");
   a.variable = p.str("variable");
@@ -510,6 +576,7 @@ std::map<std::string, Factory>& registry() {
   static std::map<std::string, Factory> r = {
       {"TetCubeMeshGenerator", tet_cube_mesh},
       {"TetLatticeMeshGenerator", tet_lattice_mesh},
+      {"FileMeshGenerator", file_mesh},
       {"CollisionKernel", collision_kernel},
       {"KillRayBC", [](Params& p, Problem& P) { ray_bc(p, P, MC_BC_VACUUM); }},
       {"ReflectRayBC", [](Params& p, Problem& P) { ray_bc(p, P, MC_BC_REFLECT); }},
@@ -574,6 +641,64 @@ int check(mc_ctx* ctx, int rc, const char* what) {
 
 }  // namespace
 
+// One device tally serves every OpenMCTally of an input: they must share the
+// estimator and energy bins; its scores are the union of theirs in order of
+// appearance.  Checks each OpenMCTallyAux against its tally (granularity,
+// score, energy bin) and resolves the score's position.
+struct TallyPlan {
+  mc_tally_desc desc{};
+  std::vector<double> edges;
+  std::vector<int> scores;
+  int nb = 1;
+  bool general = false;
+  std::vector<int> aux_score_pos;
+};
+
+TallyPlan plan_tallies(const Problem& P) {
+  TallyPlan T;
+  T.desc.estimator = MC_EST_TRACKLENGTH;
+  T.scores = {MC_SCORE_FLUX};
+  if (!P.tallies.empty()) {
+    const auto& t0 = P.tallies[0];
+    T.scores.clear();
+    for (auto& t : P.tallies) {
+      if (t.estimator != t0.estimator || t.edges != t0.edges)
+        throw InputError("[UserObjects]: all OpenMCTally objects must share the estimator and energy bins on the "
+                         "GPU path");
+      for (int s : t.scores)
+        if (std::find(T.scores.begin(), T.scores.end(), s) == T.scores.end()) T.scores.push_back(s);
+    }
+    if (T.scores.size() > MC_MAX_SCORES) throw InputError("[UserObjects]: at most 4 distinct scores in all");
+    T.desc.estimator = t0.estimator;
+    T.edges = t0.edges;
+  }
+  T.nb = T.edges.empty() ? 1 : (int)T.edges.size() - 1;
+  T.desc.n_scores = (int32_t)T.scores.size();
+  for (size_t j = 0; j < T.scores.size(); ++j) T.desc.scores[j] = T.scores[j];
+  T.desc.n_energy_bins = T.edges.empty() ? 0 : T.nb;
+  T.desc.energy_edges = T.edges.empty() ? nullptr : T.edges.data();
+  T.general = !(T.desc.estimator == MC_EST_TRACKLENGTH && T.scores.size() == 1 && T.scores[0] == MC_SCORE_FLUX &&
+                T.edges.empty());
+  for (auto& a : P.aux) {
+    const Problem::Tally* tt = nullptr;
+    for (auto& t : P.tallies)
+      if (t.id == a.tally_id) tt = &t;
+    if (!tt)
+      throw InputError("AuxKernels/" + a.name + "/tally_id: no OpenMCTally with id " + std::to_string(a.tally_id));
+    if (a.granularity == "universe" && tt->filter != "universe")
+      throw InputError("AuxKernels/" + a.name + ": Tally does not have a universe filter");
+    if (a.granularity == "cell" && tt->filter != "cell")
+      throw InputError("AuxKernels/" + a.name + ": Specified tally does not contain a cell filter");
+    if (std::find(tt->scores.begin(), tt->scores.end(), a.score) == tt->scores.end())
+      throw InputError("AuxKernels/" + a.name + "/score: The specified score does not exist in given tally");
+    if (a.energy_bin >= 0 && a.energy_bin >= T.nb)
+      throw InputError("AuxKernels/" + a.name + "/energy_bin: the tally has " + std::to_string(T.nb) +
+                       " energy bin(s)");
+    T.aux_score_pos.push_back((int)(std::find(T.scores.begin(), T.scores.end(), a.score) - T.scores.begin()));
+  }
+  return T;
+}
+
 // Runs a whole input: setup, `batches` batches, readback of every
 // OpenMCTallyAux variable.  Writes a JSON summary into report (truncated to
 // report_len) and, when [Outputs] csv = true, <file_base>_<variable>.csv.
@@ -620,21 +745,10 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
     if (Block* out = root.child("Outputs")) {
       Params p(out);
       P.csv = p.boolean("csv", false);
+      P.exodus = p.boolean("exodus", false);
       if (p.has("file_base")) P.file_base = p.raw("file_base");
     }
-    for (auto& a : P.aux) {
-      bool found = false;
-      for (auto& t : P.tallies)
-        if (t.id == a.tally_id) {
-          found = true;
-          if (a.granularity == "universe" && t.filter != "universe")
-            throw InputError("AuxKernels/" + a.name + ": Tally does not have a universe filter");
-          if (a.granularity == "cell" && t.filter != "cell")
-            throw InputError("AuxKernels/" + a.name + ": Specified tally does not contain a cell filter");
-        }
-      if (!found) throw InputError("AuxKernels/" + a.name + "/tally_id: no OpenMCTally with id " +
-                                   std::to_string(a.tally_id));
-    }
+    TallyPlan TP = plan_tallies(P);
 
     // ---- device setup (OpenMCStudy constructor + initialSetup) ----
     check(nullptr, mc_ctx_create(device, &ctx), "mc_ctx_create");
@@ -650,6 +764,10 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
           "CollisionKernel");
     if (P.src.space == MC_SRC_CYLINDERS) P.src.cyl_xy = P.cyl_xy.data();
     check(ctx, mc_source_set(ctx, &P.src), "OpenMCStudy source");
+    if (TP.general) check(ctx, mc_tally_configure(ctx, &TP.desc), "OpenMCTally");
+    int64_t n_tally = 0;
+    check(ctx, mc_tally_size(ctx, &n_tally), "OpenMCTally");
+    const int ns = TP.desc.n_scores, nb = TP.nb;
 
     // ---- batches (Transient steps) ----
     const auto t0 = std::chrono::steady_clock::now();
@@ -678,9 +796,9 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 
     // ---- AuxKernel readback ----
-    std::vector<double> sum((size_t)P.n_tet), sq((size_t)P.n_tet);
-    check(ctx, mc_tally_download(ctx, MC_TALLY_SUM, sum.data(), P.n_tet), "tally");
-    check(ctx, mc_tally_download(ctx, MC_TALLY_SUM_SQ, sq.data(), P.n_tet), "tally");
+    std::vector<double> sum((size_t)n_tally), sq((size_t)n_tally);
+    check(ctx, mc_tally_download(ctx, MC_TALLY_SUM, sum.data(), n_tally), "tally");
+    check(ctx, mc_tally_download(ctx, MC_TALLY_SUM_SQ, sq.data(), n_tally), "tally");
     std::ostringstream js;
     js.precision(17);
     js << "{\"histories\": " << tot.n_hist << ", \"segments\": " << tot.n_seg << ", \"collisions\": " << tot.n_coll
@@ -688,37 +806,66 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
        << ", \"lost\": " << tot.n_lost << ", \"batches\": " << P.batches << ", \"seconds\": " << secs
        << ", \"neutrons_per_s\": " << (secs > 0 ? tot.n_hist / secs : 0.0) << ", \"aux\": {";
     bool first = true;
-    for (auto& a : P.aux) {
+    std::vector<std::string> ex_names;
+    std::vector<double> ex_vals;  // per variable, n_tet values (per batch, as the csv)
+    for (size_t ai = 0; ai < P.aux.size(); ++ai) {
+      const auto& a = P.aux[ai];
+      const int j = TP.aux_score_pos[ai];
+      // the element's value: its score summed over the energy bins, or the one bin asked for
+      // (OpenMCTallyAux.C:187-205); the relative error is kept for a single bin
+      const int b0 = a.energy_bin >= 0 ? a.energy_bin : 0, b1 = a.energy_bin >= 0 ? a.energy_bin + 1 : nb;
+      const bool single = b1 - b0 == 1;
+      std::vector<double> cell((size_t)P.n_tet), cell_sq((size_t)P.n_tet);
+      for (int64_t t = 0; t < P.n_tet; ++t)
+        for (int b = b0; b < b1; ++b) {
+          cell[t] += sum[((size_t)t * nb + b) * ns + j];
+          cell_sq[t] += sq[((size_t)t * nb + b) * ns + j];
+        }
       std::vector<double> val((size_t)P.n_tet);
       if (a.granularity == "cell") {
-        val = sum;
+        val = cell;
       } else {
         std::map<int, double> per_block;
-        for (int64_t t = 0; t < P.n_tet; ++t) per_block[P.blk[t]] += sum[t];
+        for (int64_t t = 0; t < P.n_tet; ++t) per_block[P.blk[t]] += cell[t];
         for (int64_t t = 0; t < P.n_tet; ++t) val[t] = per_block[P.blk[t]];
       }
       double total = 0.0;
       for (double v : val) total += v;
       js << (first ? "" : ", ") << "\"" << a.variable << "\": {\"sum\": " << total << "}";
       first = false;
+      if (P.exodus) {
+        ex_names.push_back(a.variable);
+        for (int64_t t = 0; t < P.n_tet; ++t) ex_vals.push_back(val[t] / (double)P.batches);
+      }
       if (P.csv && !P.file_base.empty()) {
         std::ofstream f(P.file_base + "_" + a.variable + ".csv");
         if (!f) throw std::runtime_error("cannot write " + P.file_base + "_" + a.variable + ".csv");
         f.precision(17);
         f << "elem,block," << a.variable << ",rel_err\n";
-        const double nb = (double)P.batches;
+        const double nbat = (double)P.batches;
         for (int64_t t = 0; t < P.n_tet; ++t) {
           double re = 0.0;
-          if (a.granularity == "cell" && sum[t] > 0 && nb > 1) {
-            const double mean = sum[t] / nb;
-            const double var = (sq[t] / nb - mean * mean) / (nb - 1);
+          if (a.granularity == "cell" && single && cell[t] > 0 && nbat > 1) {
+            const double mean = cell[t] / nbat;
+            const double var = (cell_sq[t] / nbat - mean * mean) / (nbat - 1);
             re = var > 0 ? sqrt(var) / mean : 0.0;
           }
-          f << t << "," << P.blk[t] << "," << val[t] / nb << "," << re << "\n";
+          f << t << "," << P.blk[t] << "," << val[t] / nbat << "," << re << "\n";
         }
       }
     }
-    js << "}}";
+    js << "}";
+    if (P.exodus && !P.file_base.empty()) {
+      // MOOSE's Exodus output of the AuxVariables at the last step
+      std::vector<const char*> nm;
+      for (auto& s : ex_names) nm.push_back(s.c_str());
+      const std::string path = P.file_base + ".e";
+      if (mc_exodus_write(path.c_str(), "macaw_gb300", P.n_vtx, P.xyz.data(), P.n_tet, P.tv.data(), P.blk.data(),
+                          P.bid.data(), (int32_t)nm.size(), nm.data(), ex_vals.data(), (double)P.batches) != MC_OK)
+        throw std::runtime_error("cannot write " + path);
+      js << ", \"exodus\": \"" << path << "\"";
+    }
+    js << "}";
     put(js.str());
     mc_ctx_destroy(ctx);
     return MC_OK;
@@ -765,6 +912,7 @@ extern "C" int mc_app_check(const char* input_text, char* report, int64_t report
         p.error("type", "Only a Transient executioner is supported (one step per batch)");
       if (p.has("num_steps")) P.batches = p.integer("num_steps", 1);
     }
+    const TallyPlan TP = plan_tallies(P);
     std::ostringstream js;
     js << "{\"tets\": " << P.n_tet << ", \"vertices\": " << P.n_vtx << ", \"nuclides\": " << P.nucs.size()
        << ", \"materials\": " << P.mats.size() << ", \"particles\": " << P.particles << ", \"batches\": "
@@ -773,7 +921,8 @@ extern "C" int mc_app_check(const char* input_text, char* report, int64_t report
             for (auto& b : P.bcs) n += b.second == MC_BC_REFLECT;
             return n;
           }()
-       << ", \"tallies\": " << P.tallies.size() << ", \"aux\": " << P.aux.size() << ", \"precision\": \""
+       << ", \"tallies\": " << P.tallies.size() << ", \"tally_values_per_element\": " << TP.nb * TP.desc.n_scores
+       << ", \"aux\": " << P.aux.size() << ", \"precision\": \""
        << (P.precision == MC_PREC_MIXED ? "mixed" : "fp64") << "\"}";
     put(js.str());
     return MC_OK;

@@ -15,6 +15,8 @@ struct CtxView {
   int device = 0, n_sm = 0, n_mat = 0;
   cudaStream_t stream = nullptr;
   int64_t n_tet = 0;
+  int64_t n_tally = 0;  // values per tally: elements x energy bins x scores
+  TallySpec ts{};       // the context's tally definition
   float tol = 0.0f;
   bool ready = false;  // mesh, tables, block map, BCs and source resident on the device
                        // (M, X and S are filled whenever the tables are resident)

@@ -117,6 +117,46 @@ struct Particle {
   double cs0, cs1, cs2, cs3;
 };
 
+// Tally definition of a run (mc_tally_configure).  general = 0 is the
+// default: the track-length flux, one value per element.
+struct TallySpec {
+  int general;
+  int est;     // MC_EST_*
+  int nb, ns;  // energy bins (>= 1) and scores per element
+  int sc;      // score j (MC_SCORE_*) in bits 8j..8j+7
+  int need_ss; // a score needs the macroscopic scattering cross section
+  const double* __restrict__ edges;  // nb+1 ascending energy edges, or null: no energy filter
+};
+
+// Energy filter bin of E (OpenMC EnergyFilter: edges[b] <= E < edges[b+1]),
+// -1 outside the edges.
+__device__ __forceinline__ int energy_bin(const TallySpec& T, double E) {
+  if (!T.edges) return 0;
+  if (!(E >= __ldg(T.edges)) || !(E < __ldg(T.edges + T.nb))) return -1;
+  int lo = 0, hi = T.nb;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (E < __ldg(T.edges + mid)) hi = mid;
+    else lo = mid;
+  }
+  return lo;
+}
+
+// Track-length scores of one segment, v = wgt * scored length
+// (CollisionKernel.C:153-154 scores this length).
+__device__ __forceinline__ void score_track(const TallySpec& T, double* tally, int elem, double E, double v,
+                                            double sigt) {
+  if (!T.general) {
+    atomicAdd(tally + elem, v);
+    return;
+  }
+  if (T.est != MC_EST_TRACKLENGTH) return;
+  const int b = energy_bin(T, E);
+  if (b < 0) return;
+  double* t = tally + ((int64_t)elem * T.nb + b) * T.ns;
+  for (int j = 0; j < T.ns; ++j) atomicAdd(t + j, ((T.sc >> (8 * j)) & 0xff) == MC_SCORE_TOTAL ? v * sigt : v);
+}
+
 __device__ __forceinline__ void xs_cache_clear(Particle& p) { p.cm = make_int4(-1, -1, -1, -1); }
 
 // Slot of material mat in a cache key set, or -1.
@@ -514,6 +554,40 @@ __device__ __forceinline__ void start(const DevMesh& M, const mc_site& o, int64_
 }
 
 // ---------------------------------------------------------------------------
+// Collision-estimator scores at a collision, at the energy before it (the
+// estimator OpenMCTally admits, OpenMCTally.C:86-87): flux wgt/Sigma_t,
+// total wgt, scatter wgt*Sigma_s/Sigma_t, absorption
+// wgt*(Sigma_t-Sigma_s)/Sigma_t; Sigma_s summed over the material's
+// nuclides in material order.
+__device__ __forceinline__ void score_collision(const DevXS& X, const TallySpec& T, double* tally,
+                                                const Particle& p) {
+  if (!T.general || T.est != MC_EST_COLLISION) return;
+  const int b = energy_bin(T, p.E);
+  if (b < 0) return;
+  double ss = 0.0;
+  if (T.need_ss) {
+    const int k = xs_bucket(X, mc::log64(p.E));
+    GridCursor gc;
+    const int j1 = __ldg(X.mat_off + p.mat + 1);
+    for (int j = __ldg(X.mat_off + p.mat); j < j1; ++j) {
+      double st, sj;
+      micro_xs(X, __ldg(X.mat_nuc + j), k, p.E, gc, st, sj);
+      ss = ss + __ldg(X.mat_dens + j) * sj;
+    }
+  }
+  double* t = tally + ((int64_t)p.elem * T.nb + b) * T.ns;
+  for (int j = 0; j < T.ns; ++j) {
+    const int sc = (T.sc >> (8 * j)) & 0xff;
+    double v;
+    if (sc == MC_SCORE_FLUX) v = p.wgt / p.sigt;
+    else if (sc == MC_SCORE_TOTAL) v = p.wgt;
+    else if (sc == MC_SCORE_SCATTER) v = p.wgt * ss / p.sigt;
+    else v = p.wgt * (p.sigt - ss) / p.sigt;
+    atomicAdd(t + j, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Collision at the current position (OpenMC event_collide as MaCaw calls
 // it, CollisionKernel.C:185-230): nuclide by cumulative N_i sigma_t,i,
 // absorption if xi*sigma_t < sigma_a, else elastic scattering isotropic in
@@ -603,7 +677,7 @@ __device__ __forceinline__ void prefetch_neighbours(const DevMesh& M, const int4
 
 template <bool kInlineXS>
 __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Particle& p,
-                                            double* __restrict__ tally, float& sigt32,
+                                            double* __restrict__ tally, const TallySpec& T, float& sigt32,
                                             unsigned long long& n_xs) {
   if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
     p.status = kStuck;
@@ -669,7 +743,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     cross = dist > L;
   }
   const double score = cross ? L : dist;  // (L < dist) ? L : dist
-  atomicAdd(tally + p.elem, p.wgt * score);
+  score_track(T, tally, p.elem, p.E, p.wgt * score, p.sigt);
   ++p.n_seg;
   if (L == 0.0) ++p.zero_run;
   else p.zero_run = 0;
@@ -735,7 +809,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
 template <bool kInlineXS, bool kPrefetch = false>
 __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, Particle& p,
                                              const float uf, const float vf, const float wf,
-                                             double* __restrict__ tally, float& sigt32,
+                                             double* __restrict__ tally, const TallySpec& T, float& sigt32,
                                              unsigned long long& n_xs) {
   if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
     p.status = kStuck;
@@ -794,7 +868,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     }
   }
   if (!sure || bf < 0 || !(tb + eb < lo_other)) {
-    const int r = segment_fp64<kInlineXS>(M, X, p, tally, sigt32, n_xs);
+    const int r = segment_fp64<kInlineXS>(M, X, p, tally, T, sigt32, n_xs);
     return (r == 0 && p.fin < 0) ? 5 : r;  // a reflection changed the direction
   }
   const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
@@ -823,7 +897,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     cross = dist > L;
   }
   const double score = cross ? L : dist;
-  atomicAdd(tally + p.elem, p.wgt == 1.0 ? score : p.wgt * score);
+  score_track(T, tally, p.elem, p.E, p.wgt == 1.0 ? score : p.wgt * score, p.sigt);
   ++p.n_seg;
   if (L == 0.0) ++p.zero_run;
   else p.zero_run = 0;
@@ -917,7 +991,8 @@ __device__ __forceinline__ int exit_fp64(const DevMesh& M, int elem, int fin, co
 
 template <bool kInlineXS, bool kPrefetch = false>
 __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, Particle& p,
-                                             Geo32& g, double* __restrict__ tally, float& inv_sig,
+                                             Geo32& g, double* __restrict__ tally, const TallySpec& T,
+                                             float& inv_sig,
                                              float tol, unsigned long long& n_xs,
                                              unsigned long long& n_fb) {
   if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
@@ -989,7 +1064,7 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
   const float dist = -__logf(xi) * inv_sig;
   const bool cross = dist > L;
   const float score = cross ? L : dist;
-  atomicAdd(tally + p.elem, p.wgt * (double)score);
+  score_track(T, tally, p.elem, p.E, p.wgt * (double)score, p.sigt);
   ++p.n_seg;
   if (L == 0.0f) ++p.zero_run;
   else p.zero_run = 0;

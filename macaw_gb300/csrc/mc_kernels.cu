@@ -57,7 +57,7 @@ __device__ __forceinline__ void live_add(int* live, int tag, int v) {
 
 // Batch tally a particle scores into.
 __device__ __forceinline__ double* tally_of(const RunArgs& a, int tag) {
-  return tag ? a.tally2 + (int64_t)(tag - 1) * a.n_tet : a.tally;
+  return tag ? a.tally2 + (int64_t)(tag - 1) * a.n_tally : a.tally;
 }
 
 // End of a history: closing hash word, counters, optional trace record.
@@ -232,8 +232,11 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
       float sigt32 = 0.0f;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
-        if (r == 1) collide(X, p);
+        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
+        if (r == 1) {
+          score_collision(X, a.ts, tally_of(a, p.tag), p);
+          collide(X, p);
+        }
         if (r == 1 || r == 5) {
           uf = (float)p.u;
           vf = (float)p.v;
@@ -245,9 +248,10 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
       geo_load(p, g);
       float inv_sig = 0.0f;
       while (p.status == kAlive) {
-        const int r = segment_mixed<true>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
+        const int r = segment_mixed<true>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
         if (r == 1) {
           geo_store(g, p);
+          score_collision(X, a.ts, tally_of(a, p.tag), p);
           collide(X, p);
           geo_load(p, g);
         }
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       for (;;) {
-        r = segment_fp64g<false>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
+        r = segment_fp64g<false>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 5) {
           uf = (float)p.u;
           vf = (float)p.v;
@@ -367,7 +371,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       geo_load(p, g);
       float inv_sig = (float)(1.0 / p.sigt);
       for (;;) {
-        r = segment_mixed<false>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
+        r = segment_mixed<false>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
         if (r != 0) break;
         if (a.max_seg > 0 && ++k >= a.max_seg) {
           r = 4;
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     if (s < 0) continue;
     int r;
     if (kPrec == MC_PREC_FP64) {
-      r = segment_fp64g<false>(M, X, p, g.u, g.v, g.w, tally_of(a, p.tag), f32, nxs);
+      r = segment_fp64g<false>(M, X, p, g.u, g.v, g.w, tally_of(a, p.tag), a.ts, f32, nxs);
       if (r == 5) {
         g.u = (float)p.u;
         g.v = (float)p.v;
@@ -437,7 +441,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
         r = 0;
       }
     } else {
-      r = segment_mixed<false>(M, X, p, g, tally_of(a, p.tag), f32, a.tol, nxs, nfb);
+      r = segment_mixed<false>(M, X, p, g, tally_of(a, p.tag), a.ts, f32, a.tol, nxs, nfb);
     }
     if (r == 0) {
       if (a.max_seg <= 0 || ++k < a.max_seg) continue;
@@ -691,6 +695,7 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
     const int s = Q.coll[i];
     Particle p;
     load(B, s, p);
+    score_collision(X, a.ts, tally_of(a, p.tag), p);
     collide(X, p);
     if (p.status != kAlive) {
       finish(p, a, L);
@@ -759,8 +764,11 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true, true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), sigt32, nxs);
-        if (r == 1) collide(X, p);
+        const int r = segment_fp64g<true, true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
+        if (r == 1) {
+          score_collision(X, a.ts, tally_of(a, p.tag), p);
+          collide(X, p);
+        }
         if (r == 1 || r == 5) {
           uf = (float)p.u;
           vf = (float)p.v;
@@ -772,9 +780,10 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       geo_load(p, g);
       float inv_sig = (p.mat >= 0) ? (float)(1.0 / p.sigt) : 0.0f;
       while (p.status == kAlive) {
-        const int r = segment_mixed<true, true>(M, X, p, g, tally_of(a, p.tag), inv_sig, a.tol, nxs, nfb);
+        const int r = segment_mixed<true, true>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
         if (r == 1) {
           geo_store(g, p);
+          score_collision(X, a.ts, tally_of(a, p.tag), p);
           collide(X, p);
           geo_load(p, g);
         }
@@ -888,7 +897,8 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
   }
   if (adv0) cudaEventRecord(adv0, st);
   if (a.precision == MC_PREC_MIXED) {
-    if (a.refill) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    // the compact walk scores the default tally only
+    if (a.refill || a.ts.general) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else k_ev_advance_mixed<<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
   } else {
     if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);

@@ -85,8 +85,9 @@ struct RunArgs {
   uint64_t master;
   double* tally;                // scores of even batches
   double* tally2;               // tally slot 1 (== tally for a single batch); slots k >= 1 are
-                                // tally2 + (k-1)*n_tet
-  int64_t n_tet;
+                                // tally2 + (k-1)*n_tally
+  int64_t n_tally;              // values per tally slot: elements x energy bins x scores
+  TallySpec ts;                 // what the tally scores
   const DevRequest* req;        // device: birth-sequence entries sorted by start, or null
   int n_req;
   int* live;                    // event mode: in-flight counters per tally slot, or null

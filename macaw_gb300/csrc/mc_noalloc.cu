@@ -153,7 +153,8 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.tally2 = tally;
   a.req = nullptr;
   a.n_req = 0;
-  a.n_tet = v.n_tet;
+  a.n_tally = v.n_tally;
+  a.ts = v.ts;
   a.live = nullptr;
   a.traces = d->record_traces ? traces : nullptr;
   a.counters = counters;

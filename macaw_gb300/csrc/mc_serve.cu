@@ -36,7 +36,7 @@ struct Serve {
   int max_slots = 0;
   int64_t bank = 0;
   int precision = MC_PREC_MIXED, max_seg = 0;
-  double* slots = nullptr;     // max_slots x n_tet tallies
+  double* slots = nullptr;     // max_slots x n_tally tallies
   int* live = nullptr;         // in-flight particles per slot
   DevRequest* table = nullptr; // active requests, sorted by start
   DevRequest* h_table[2] = {nullptr, nullptr};  // pinned staging
@@ -93,8 +93,9 @@ RunArgs args(const Serve& s) {
   a.n = (int64_t)1 << 62;
   a.master = 0;
   a.tally = s.slots;
-  a.tally2 = s.slots + s.v.n_tet;
-  a.n_tet = s.v.n_tet;
+  a.tally2 = s.slots + s.v.n_tally;
+  a.n_tally = s.v.n_tally;
+  a.ts = s.v.ts;
   a.req = s.table;
   a.n_req = (int)s.active.size();
   a.live = s.live;
@@ -163,7 +164,7 @@ extern "C" int mc_serve_open(mc_ctx* c, int32_t max_slots, int64_t bank_size, in
     return cuda_fail(c, e, what);
   };
   cudaError_t e;
-  if ((e = cudaMalloc(&s->slots, sizeof(double) * (size_t)max_slots * (size_t)s->v.n_tet)) != cudaSuccess)
+  if ((e = cudaMalloc(&s->slots, sizeof(double) * (size_t)max_slots * (size_t)s->v.n_tally)) != cudaSuccess)
     return bad(e, "allocate request tallies");
   if ((e = cudaMalloc(&s->live, sizeof(int) * (size_t)max_slots)) != cudaSuccess) return bad(e, "allocate slots");
   if ((e = cudaMalloc(&s->table, sizeof(DevRequest) * (size_t)max_slots)) != cudaSuccess)
@@ -232,7 +233,7 @@ extern "C" int mc_serve_step(mc_ctx* c, int32_t iterations) {
     s->queue.pop_front();
     const int slot = s->free_slots.back();
     s->free_slots.pop_back();
-    SCK(cudaMemsetAsync(s->slots + (size_t)slot * (size_t)s->v.n_tet, 0, sizeof(double) * (size_t)s->v.n_tet, st),
+    SCK(cudaMemsetAsync(s->slots + (size_t)slot * (size_t)s->v.n_tally, 0, sizeof(double) * (size_t)s->v.n_tally, st),
         "clear request tally");
     Active a;
     a.ticket = qr.first;
@@ -297,8 +298,8 @@ extern "C" int mc_serve_poll(mc_ctx* c, int64_t* done, int32_t capacity, int32_t
   for (const Active& a : s->active) {
     if (h.next_hist >= a.dr.end && s->h_live[a.slot] == 0 && *n_done < capacity) {
       std::vector<double>& out = s->results[a.ticket];
-      out.resize((size_t)s->v.n_tet);
-      SCK(cudaMemcpy(out.data(), s->slots + (size_t)a.slot * (size_t)s->v.n_tet, sizeof(double) * (size_t)s->v.n_tet,
+      out.resize((size_t)s->v.n_tally);
+      SCK(cudaMemcpy(out.data(), s->slots + (size_t)a.slot * (size_t)s->v.n_tally, sizeof(double) * (size_t)s->v.n_tally,
                      cudaMemcpyDeviceToHost),
           "copy request tally");
       s->free_slots.push_back(a.slot);
@@ -313,14 +314,14 @@ extern "C" int mc_serve_poll(mc_ctx* c, int64_t* done, int32_t capacity, int32_t
   return MC_OK;
 }
 
-extern "C" int mc_serve_result(mc_ctx* c, int64_t ticket, double* tally, int64_t n_tet) {
+extern "C" int mc_serve_result(mc_ctx* c, int64_t ticket, double* tally, int64_t n) {
   if (!c || !tally) return MC_ERR_ARG;
   Serve* s = find(c);
   if (!s) return ctx_fail(c, MC_ERR_STATE, "serving is not open (mc_serve_open)");
   std::lock_guard<std::mutex> g(ctx_mutex(c));
   auto it = s->results.find(ticket);
   if (it == s->results.end()) return ctx_fail(c, MC_ERR_ARG, "no finished request with this ticket");
-  if (n_tet != (int64_t)it->second.size()) return ctx_fail(c, MC_ERR_ARG, "tally length must equal the number of tets");
+  if (n != (int64_t)it->second.size()) return ctx_fail(c, MC_ERR_ARG, "tally length must equal mc_tally_size");
   std::copy(it->second.begin(), it->second.end(), tally);
   s->results.erase(it);
   return MC_OK;

@@ -64,6 +64,15 @@ class Source:
 
 
 @dataclass
+class TallyDef:
+    """OpenMCTally's estimator, scores and energy filter for the element
+    tally (MC_EST_*, MC_SCORE_*; energy_edges None: no energy filter)."""
+    estimator: int = 1
+    scores: tuple = (0,)
+    energy_edges: np.ndarray | None = None
+
+
+@dataclass
 class Problem:
     name: str
     xyz: np.ndarray
@@ -77,6 +86,7 @@ class Problem:
     source: Source
     bcs: dict = field(default_factory=dict)  # boundary id -> MC_BC_*
     hash_bins: int = 8000
+    tally: TallyDef | None = None  # None: track-length flux per element
 
     @property
     def n_tet(self) -> int:

@@ -52,7 +52,7 @@ class Server:
         for p in problems:
             t = Tracker(device)
             t.load(p)
-            per_slot = p.n_tet * 8
+            per_slot = t.tally_size() * 8
             n_slots = int(max(1, min(max_slots, spare // (len(problems) * per_slot))))
             t._ck(lib.mc_serve_open(t._h, n_slots, bank, precision, max_seg), "mc_serve_open")
             self.trackers.append(t)
@@ -103,7 +103,7 @@ class Server:
 
     def result(self, key: tuple) -> np.ndarray:
         t = self.trackers[key[0]]
-        out = np.zeros(t.n_tet)
+        out = np.zeros(t.tally_size())
         t._ck(lib.mc_serve_result(t._h, key[1], C.c_void_p(out.ctypes.data), out.size), "mc_serve_result")
         return out
 

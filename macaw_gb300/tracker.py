@@ -12,8 +12,8 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (MC_MODE_EVENT, MC_PREC_FP64, MC_TALLY_BATCH, MC_TALLY_SUM, MC_TALLY_SUM_SQ,
-                   SITE_DTYPE, TRACE_DTYPE, MCError, RunDesc, SourceDesc, Stats, lib, ptr)
-from .problems import Problem, Source
+                   SITE_DTYPE, TRACE_DTYPE, MCError, RunDesc, SourceDesc, Stats, TallyDesc, lib, ptr)
+from .problems import Problem, Source, TallyDef
 
 
 class Tracker:
@@ -107,7 +107,25 @@ class Tracker:
         self.block_material_map(p.blocks, p.block_materials)
         self.set_hash_bins(p.hash_bins)
         self.set_source(p.source)
+        if p.tally is not None:
+            self.configure_tally(p.tally)
         return self
+
+    def configure_tally(self, t: TallyDef) -> None:
+        d = TallyDesc()
+        d.estimator = t.estimator
+        d.n_scores = len(t.scores)
+        for j, s in enumerate(t.scores):
+            d.scores[j] = s
+        e = None if t.energy_edges is None else np.ascontiguousarray(t.energy_edges, np.float64)
+        d.n_energy_bins = 0 if e is None else e.size - 1
+        d.energy_edges = None if e is None else e.ctypes.data
+        self._ck(lib.mc_tally_configure(self._h, C.byref(d)), "mc_tally_configure")
+
+    def tally_size(self) -> int:
+        n = C.c_int64()
+        self._ck(lib.mc_tally_size(self._h, C.byref(n)), "mc_tally_size")
+        return n.value
 
     # -- run --------------------------------------------------------------
     def run(self, n: int, first: int = 0, seed: int = 1, mode: int = MC_MODE_EVENT,
@@ -159,7 +177,7 @@ class Tracker:
 
     def tally(self, kind: int = MC_TALLY_BATCH, out: np.ndarray | None = None) -> np.ndarray:
         if out is None:
-            out = np.zeros(self.n_tet, np.float64)
+            out = np.zeros(self.tally_size(), np.float64)
         self._ck(lib.mc_tally_download(self._h, kind, ptr(out), out.size), "mc_tally_download")
         return out
 

@@ -168,6 +168,12 @@ struct oracle_problem {
   int data_ready;
   oracle_source src;
   double* src_cyl;
+  /* tally definition (OpenMCTally estimator, scores, energy filter);
+     results [element][energy bin][score] */
+  int t_est;        /* 1 track length, 2 collision */
+  int t_ns, t_nb;   /* scores, energy bins (>= 1) */
+  int t_sc[4];      /* 0 flux, 1 total, 2 scatter, 3 absorption */
+  double* t_edges;  /* t_nb+1 edges, or NULL: no energy filter */
 };
 
 static int fail(oracle_problem* p, const char* msg)
@@ -184,6 +190,9 @@ oracle_problem* oracle_create(void)
   p->src.energy = 0;
   p->src.watt_a = 0.988e6;
   p->src.watt_b = 2.249e-6;
+  p->t_est = 1;
+  p->t_ns = 1;
+  p->t_nb = 1;
   return p;
 }
 
@@ -205,7 +214,7 @@ void oracle_destroy(oracle_problem* p)
   free(p->nucs);
   for (int i = 0; i < p->n_mat; ++i) { free(p->mats[i].nuc); free(p->mats[i].dens); }
   free(p->mats);
-  free(p->map_blocks); free(p->map_mats); free(p->src_cyl);
+  free(p->map_blocks); free(p->map_mats); free(p->src_cyl); free(p->t_edges);
   free(p);
 }
 
@@ -480,6 +489,33 @@ int oracle_set_hash_bins(oracle_problem* p, int32_t n_bins)
   return 0;
 }
 
+/* Tally definition: OpenMCTally's estimator, scores and energy filter
+ * (src/userobjects/OpenMCTally.C:30-101), restated for the element tally. */
+int oracle_set_tally(oracle_problem* p, int32_t estimator, int32_t n_scores, const int32_t* scores,
+                     int32_t n_energy_bins, const double* edges)
+{
+  if (estimator != 1 && estimator != 2) return fail(p, "bad estimator");
+  if (n_scores < 1 || n_scores > 4) return fail(p, "1 to 4 scores");
+  for (int j = 0; j < n_scores; ++j) {
+    if (scores[j] < 0 || scores[j] > 3) return fail(p, "bad score");
+    if (estimator == 1 && scores[j] > 1) return fail(p, "track length scores flux and total");
+    p->t_sc[j] = scores[j];
+  }
+  p->t_est = estimator;
+  p->t_ns = n_scores;
+  free(p->t_edges);
+  p->t_edges = NULL;
+  p->t_nb = 1;
+  if (n_energy_bins > 0) {
+    p->t_edges = (double*)malloc(sizeof(double) * (size_t)(n_energy_bins + 1));
+    memcpy(p->t_edges, edges, sizeof(double) * (size_t)(n_energy_bins + 1));
+    p->t_nb = n_energy_bins;
+  }
+  return 0;
+}
+
+int64_t oracle_tally_size(const oracle_problem* p) { return p->n_tet * p->t_nb * p->t_ns; }
+
 /* ------------------------------------------------------------------ */
 /* Energy-grid search: logarithmic hash bins over the common energy range
  * (F. B. Brown, "New hash-based energy lookup algorithm for Monte Carlo
@@ -751,6 +787,66 @@ static void birth(const oracle_problem* p, int64_t id, uint64_t* ssrc, double* x
   (void)id;
 }
 
+/* Energy filter bin (OpenMC EnergyFilter: edges[b] <= E < edges[b+1]),
+ * -1 outside. */
+static int energy_bin(const oracle_problem* p, double E)
+{
+  if (!p->t_edges) return 0;
+  if (!(E >= p->t_edges[0]) || !(E < p->t_edges[p->t_nb])) return -1;
+  int lo = 0, hi = p->t_nb;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (E < p->t_edges[mid]) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+/* Track-length scores of one segment; v = wgt * scored length
+ * (CollisionKernel.C:153-154). */
+static void score_track(const oracle_problem* p, double* tally, int elem, double E, double v, double sigt)
+{
+  if (p->t_est != 1) return;
+  int b = energy_bin(p, E);
+  if (b < 0) return;
+  double* t = tally + ((int64_t)elem * p->t_nb + b) * p->t_ns;
+  for (int j = 0; j < p->t_ns; ++j) t[j] += (p->t_sc[j] == 1) ? v * sigt : v;
+}
+
+/* Collision-estimator scores at a collision, before its energy change:
+ * flux wgt/Sigma_t, total wgt, scatter wgt*Sigma_s/Sigma_t, absorption
+ * wgt*(Sigma_t-Sigma_s)/Sigma_t, Sigma_s summed in material order. */
+static void score_collision(const oracle_problem* p, double* tally, int elem, int mat, double E, double wgt,
+                            double sigt)
+{
+  if (p->t_est != 2) return;
+  int b = energy_bin(p, E);
+  if (b < 0) return;
+  double ss = 0.0;
+  int need = 0;
+  for (int j = 0; j < p->t_ns; ++j)
+    if (p->t_sc[j] >= 2) need = 1;
+  if (need) {
+    const material_t* m = p->mats + mat;
+    int k = bucket_of(p, oracle_log(E));
+    for (int j = 0; j < m->n; ++j) {
+      double st, sj;
+      micro_xs(p->nucs + m->nuc[j], k, E, &st, &sj);
+      ss = ss + m->dens[j] * sj;
+    }
+  }
+  double* t = tally + ((int64_t)elem * p->t_nb + b) * p->t_ns;
+  for (int j = 0; j < p->t_ns; ++j) {
+    double v;
+    switch (p->t_sc[j]) {
+      case 0: v = wgt / sigt; break;
+      case 1: v = wgt; break;
+      case 2: v = wgt * ss / sigt; break;
+      default: v = wgt * (sigt - ss) / sigt; break;
+    }
+    t[j] += v;
+  }
+}
+
 static void track(const oracle_problem* p, int64_t h, uint64_t master, double* tally,
                   oracle_trace* tr, lstats* ls)
 {
@@ -793,7 +889,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
     if (!(L > 0.0)) L = 0.0;
     double dist = -oracle_log(oracle_prn(&strk)) / sigt;
     double score = (L < dist) ? L : dist;
-    tally[elem] += wgt * score;
+    score_track(p, tally, elem, E, wgt * score, sigt);
     ++n_seg;
     if (L == 0.0) ++zero_run; else zero_run = 0;
     if (dist > L) {
@@ -828,6 +924,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
     x[2] = ez - back * u[2];
     ++n_coll;
     zero_run = 0;
+    score_collision(p, tally, elem, mat, E, wgt, sigt);
     const material_t* m = p->mats + mat;
     int k = bucket_of(p, oracle_log(E));
     double cutoff = oracle_prn(&strk) * sigt;
@@ -906,14 +1003,14 @@ int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n
 #pragma omp parallel num_threads(nt)
     {
       int tid = omp_get_thread_num();
-      priv[tid] = (double*)calloc((size_t)p->n_tet, sizeof(double));
+      priv[tid] = (double*)calloc((size_t)oracle_tally_size(p), sizeof(double));
 #pragma omp for schedule(dynamic, 64)
       for (int64_t i = 0; i < n; ++i)
         track(p, first + i, seed, priv[tid], traces ? traces + i : NULL, pl + tid);
     }
     for (int t = 0; t < nt; ++t) {
       if (priv[t]) {
-        for (int64_t e = 0; e < p->n_tet; ++e) tally[e] += priv[t][e];
+        for (int64_t e = 0; e < oracle_tally_size(p); ++e) tally[e] += priv[t][e];
         free(priv[t]);
       }
       tot.n_seg += pl[t].n_seg; tot.n_coll += pl[t].n_coll; tot.n_leak += pl[t].n_leak;

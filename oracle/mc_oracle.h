@@ -83,6 +83,13 @@ int oracle_add_material(oracle_problem* p, int32_t material_id, int32_t n, const
 int oracle_block_map(oracle_problem* p, int32_t n, const int32_t* blocks, const int32_t* materials);
 int oracle_set_source(oracle_problem* p, const oracle_source* s);
 int oracle_set_hash_bins(oracle_problem* p, int32_t n_bins);
+/* estimator 1 track length (scores 0 flux, 1 total), 2 collision (0 flux,
+ * 1 total, 2 scatter, 3 absorption); n_energy_bins 0: no energy filter.
+ * oracle_run's tally then holds oracle_tally_size values laid out
+ * [element][energy bin][score]. */
+int oracle_set_tally(oracle_problem* p, int32_t estimator, int32_t n_scores, const int32_t* scores,
+                     int32_t n_energy_bins, const double* edges);
+int64_t oracle_tally_size(const oracle_problem* p);
 
 /* Track histories [first, first+n) (0-based history index h, particle id
  * h+1).  tally (n_tet doubles) accumulates raw wgt*track-length sums;

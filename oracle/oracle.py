@@ -48,6 +48,8 @@ _SIG = {
     "oracle_block_map": ([_P, _I32, _P, _P], C.c_int),
     "oracle_set_source": ([_P, C.POINTER(OracleSource)], C.c_int),
     "oracle_set_hash_bins": ([_P, _I32], C.c_int),
+    "oracle_set_tally": ([C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "oracle_tally_size": ([C.c_void_p], C.c_int64),
     "oracle_run": ([_P, _I64, _I64, _U64, C.c_int, _P, _P, C.POINTER(OracleStats)], C.c_int),
     "oracle_log": ([_D], _D),
     "oracle_prn": ([C.POINTER(_U64)], _D),
@@ -133,11 +135,20 @@ class Oracle:
         d.cyl_r, d.cyl_z0, d.cyl_z1 = s.cyl_r, s.cyl_z0, s.cyl_z1
         d.watt_a, d.watt_b, d.mono_E = s.watt_a, s.watt_b, s.mono_E
         self._ck(lib.oracle_set_source(self.h, C.byref(d)), "oracle_set_source")
+        if getattr(p, "tally", None) is not None:
+            self.set_tally(p.tally)
         return self
+
+    def set_tally(self, t) -> None:
+        """t: macaw_gb300.problems.TallyDef."""
+        sc = np.ascontiguousarray(t.scores, np.int32)
+        e = None if t.energy_edges is None else np.ascontiguousarray(t.energy_edges, np.float64)
+        self._ck(lib.oracle_set_tally(self.h, t.estimator, sc.size, _p(sc), 0 if e is None else e.size - 1, _p(e)),
+                 "oracle_set_tally")
 
     def run(self, n: int, first: int = 0, seed: int = 1, threads: int = 1, traces: bool = True):
         """Returns (tally, traces or None, stats dict, seconds)."""
-        tally = np.zeros(self.n_tet)
+        tally = np.zeros(lib.oracle_tally_size(self.h))
         tr = np.zeros(n, TRACE_DTYPE) if traces else None
         st = OracleStats()
         t0 = time.perf_counter()

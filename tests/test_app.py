@@ -24,25 +24,40 @@ def test_reflective_bcs_and_paths():
     assert app.check_input(txt.replace(nested, path))["reflective"] == 6
 
 
-@pytest.mark.parametrize("change,message", [
-    ("blocks = '0'", "same size as the materials parameter"),
-    ("estimator = 'TRACKLENGTH'", "Only the tracklength estimator"),
-    ("type = CollisionKernel", "unknown object type"),
-    ("scores = 'flux'", "Only the flux score"),
-    ("particles = 100000", "must be positive"),
-    ("granularity = cell", "Global Tally retrieving currently not supported"),
+@pytest.mark.parametrize("change,bad,message", [
+    ("blocks = '0'", "blocks = '0 1'", "same size as the materials parameter"),
+    ("estimator = 'TRACKLENGTH'", "estimator = 'ANALOG'", "analog estimator is not available"),
+    ("type = CollisionKernel", "type = CollisionKernelX", "unknown object type"),
+    ("scores = 'flux'", "scores = 'flux fission'", "score 'fission' is not available"),
+    ("scores = 'flux'", "scores = 'flux scatter'", "scores flux and total only"),
+    ("filters = 'cell'", "filters = 'cell energy'", "energy bins parameter should be supplied"),
+    ("filters = 'cell'", "filters = 'mesh'", "unknown filter"),
+    ("score = 'flux'", "score = 'total'", "score does not exist in given tally"),
+    ("particles = 100000", "particles = 0", "must be positive"),
+    ("granularity = cell", "granularity = global", "Global Tally retrieving currently not supported"),
 ])
-def test_parameter_errors_name_the_parameter(change, message):
-    bad = {
-        "blocks = '0'": "blocks = '0 1'",
-        "estimator = 'TRACKLENGTH'": "estimator = 'COLLISION'",
-        "type = CollisionKernel": "type = CollisionKernelX",
-        "scores = 'flux'": "scores = 'flux fission'",
-        "particles = 100000": "particles = 0",
-        "granularity = cell": "granularity = global",
-    }[change]
+def test_parameter_errors_name_the_parameter(change, bad, message):
+    assert change in CUBE
     with pytest.raises(ValueError, match=message):
         app.check_input(CUBE.replace(change, bad))
+
+
+# a tally block as the reference's own inputs write it (test/tests/tally/openmc_tally.i,
+# test/tests/assembly/run_assembly.i): collision estimator, several scores, energy filter
+REF_STYLE = CUBE.replace("estimator = 'TRACKLENGTH'\n    scores = 'flux'\n    filters = 'cell'",
+                         "estimator = 'COLLISION'\n    scores = 'flux scatter absorption'\n"
+                         "    filters = 'energy particle cell'\n    energy_bins = '1e-5 1e3 2e7'").replace(
+    "estimator = TRACKLENGTH", "estimator = COLLISION")
+
+
+def test_reference_style_collision_tally_checks():
+    assert "COLLISION" in REF_STYLE and "energy_bins" in REF_STYLE
+    c = app.check_input(REF_STYLE)
+    assert c["tally_values_per_element"] == 2 * 3
+    one_bin = REF_STYLE.replace("score = 'flux'", "score = 'scatter'\n    energy_bin = 1")
+    assert app.check_input(one_bin)["aux"] == 1
+    with pytest.raises(ValueError, match="energy bin"):
+        app.check_input(REF_STYLE.replace("score = 'flux'", "score = 'flux'\n    energy_bin = 2"))
 
 
 def test_unused_parameter_and_syntax_errors():
@@ -59,6 +74,8 @@ def test_run_matches_direct_api(tmp_path):
     from macaw_gb300 import Tracker, problems
     from macaw_gb300._lib import MC_TALLY_SUM
     txt = CUBE.replace("particles = 100000", "particles = 20000").replace("num_steps = 1", "num_steps = 2")
+    txt = txt.replace("csv = true", "csv = true\n  exodus = true")
+    assert "exodus = true" in txt
     rep = app.run_input(txt, 0, str(tmp_path / "cube"))
     assert rep["histories"] == 40000 and rep["stuck"] == 0 and rep["lost"] == 0
     csv = np.loadtxt(tmp_path / "cube_flux.csv", delimiter=",", skiprows=1)
@@ -72,3 +89,40 @@ def test_run_matches_direct_api(tmp_path):
     nz = ref > 0
     assert np.all(np.abs(got[nz] - ref[nz]) <= 1e-12 * ref[nz])
     assert rep["aux"]["flux"]["sum"] == pytest.approx(2 * ref.sum(), rel=1e-12)
+    # the same field in the Exodus output (one block: the cube's subdomain 0)
+    from scipy.io import netcdf_file
+    with netcdf_file(rep["exodus"], "r", mmap=False) as f:
+        assert np.array_equal(f.variables["vals_elem_var1eb1"][0], got)
+
+
+@pytest.mark.gpu
+def test_reference_style_collision_tally_runs(tmp_path):
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_EST_COLLISION, MC_SCORE_ABSORPTION, MC_SCORE_FLUX, MC_SCORE_SCATTER, MC_TALLY_SUM
+    txt = REF_STYLE.replace("particles = 100000", "particles = 20000").replace(
+        "score = 'flux'", "score = 'scatter'")
+    rep = app.run_input(txt, 0, str(tmp_path / "cube"))
+    assert rep["histories"] == 20000 and rep["collisions"] > 0
+    p = problems.cube_problem()
+    p.tally = problems.TallyDef(MC_EST_COLLISION, (MC_SCORE_FLUX, MC_SCORE_SCATTER, MC_SCORE_ABSORPTION),
+                                np.array([1e-5, 1e3, 2e7]))
+    with Tracker(0) as t:
+        t.load(p)
+        t.run(20000, seed=1, accumulate=True)
+        ref = t.tally(MC_TALLY_SUM).reshape(p.n_tet, 2, 3)[:, :, 1].sum(axis=1)  # scatter, both bins
+    csv = np.loadtxt(tmp_path / "cube_flux.csv", delimiter=",", skiprows=1)
+    nz = ref > 0
+    assert np.all(np.abs(csv[nz, 2] - ref[nz]) <= 1e-12 * ref[nz])
+
+
+def test_file_mesh_generator_reads_an_exodus_tet_mesh(tmp_path, monkeypatch):
+    from macaw_gb300 import exodus, problems
+    p = problems.cube_problem()
+    exodus.write(str(tmp_path / "cube_mesh.e"), p, {})
+    monkeypatch.chdir(tmp_path)
+    start, end = CUBE.index("[Mesh]"), CUBE.index("[]\n[]", CUBE.index("[Mesh]")) + 5
+    txt = CUBE[:start] + "[Mesh]\n  [fmg]\n    type = FileMeshGenerator\n    file = 'cube_mesh.e'\n  []\n[]\n" + CUBE[end:]
+    c = app.check_input(txt)
+    assert c["tets"] == p.n_tet and c["vertices"] == p.xyz.shape[0]
+    with pytest.raises(ValueError, match="file"):
+        app.check_input(txt.replace("cube_mesh.e", "missing.e"))
