@@ -317,6 +317,32 @@ int mc_serve_result(mc_ctx* ctx, int64_t ticket, double* tally, int64_t n);
 int mc_serve_status(mc_ctx* ctx, int32_t* queued, int32_t* active, int32_t* free_slots);
 int mc_serve_close(mc_ctx* ctx);
 
+/* ---- ray segments ------------------------------------------------------
+ * Replaces: MOOSE RayTracingExodus output of a study's rays with their data
+ * and aux data (test/tests/study/openmc_study.i [Outputs/rays]; gold
+ * test/tests/study/gold/openmc_study_rays.e).  mc_rays_enable makes the
+ * following runs record every segment of their first n_rays histories (in
+ * birth order), up to max_segments each; mc_rays_download returns the
+ * recorded segments of the last run, ray by ray in segment order. */
+typedef struct {
+  int64_t id;             /* particle id (1-based); the ray is id - 1 - first_history of the run */
+  int32_t segment;        /* index along the ray, from 0 */
+  int32_t intersections;  /* sides the ray crossed so far, this segment's included */
+  int32_t elem;           /* element the segment lies in */
+  int32_t pad;
+  double start[3], end[3];
+  double E, wgt;          /* energy and weight along the segment */
+  uint64_t seed_tracking; /* tracking-stream state after the segment's draw */
+} mc_ray_segment;
+int mc_rays_enable(mc_ctx* ctx, int32_t n_rays, int32_t max_segments);
+int mc_rays_download(mc_ctx* ctx, mc_ray_segment* out, int64_t capacity, int64_t* n_out);
+/* Writes recorded segments as RayTracingExodus does: one EDGE2 element per
+ * segment, consecutive segments of a ray sharing their node, element
+ * variables aux_energy, aux_id, aux_n_progeny, aux_particle_type,
+ * aux_seed_URR, aux_seed_source, aux_seed_tracking, aux_weight,
+ * intersections and ray_id (seeds as doubles, as MaCaw stores them). */
+int mc_exodus_write_rays(const char* path, const mc_ray_segment* seg, int64_t n, int64_t first_history);
+
 /* ---- Exodus II output --------------------------------------------------
  * Replaces: MOOSE's Exodus output of a MaCaw run's element AuxVariables
  * ([Outputs] exodus = true; the reference's gold results are Exodus files,

@@ -66,6 +66,10 @@ TRACE_DTYPE = np.dtype([("id", "<i8"), ("hash", "<u8"), ("status", "<i4"), ("n_s
                         ("n_coll", "<i4"), ("elem", "<i4"), ("face", "<i4"), ("pad", "<i4"),
                         ("E", "<f8"), ("x", "<f8"), ("y", "<f8"), ("z", "<f8")])
 
+RAY_SEGMENT_DTYPE = np.dtype([("id", "<i8"), ("segment", "<i4"), ("intersections", "<i4"), ("elem", "<i4"),
+                              ("pad", "<i4"), ("start", "<f8", (3,)), ("end", "<f8", (3,)), ("E", "<f8"),
+                              ("wgt", "<f8"), ("seed_tracking", "<u8")])
+
 SITE_DTYPE = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("u", "<f8"), ("v", "<f8"),
                        ("w", "<f8"), ("E", "<f8"), ("wgt", "<f8")])
 
@@ -102,6 +106,9 @@ SIGNATURES = {
     "mc_tally_configure": ([_P, C.c_void_p], C.c_int),
     "mc_exodus_read_sizes": ([C.c_char_p, C.POINTER(_I64), C.POINTER(_I64), C.c_char_p, _I64], C.c_int),
     "mc_exodus_read": ([C.c_char_p, _P, _P, _P, _P, C.c_char_p, _I64], C.c_int),
+    "mc_rays_enable": ([_P, _I32, _I32], C.c_int),
+    "mc_rays_download": ([_P, _P, _I64, C.POINTER(_I64)], C.c_int),
+    "mc_exodus_write_rays": ([C.c_char_p, _P, _I64, _I64], C.c_int),
     "mc_exodus_write": ([C.c_char_p, C.c_char_p, _I64, _P, _I64, _P, _P, _P, _I32, _P, _P, _D], C.c_int),
     "mc_tally_size": ([_P, C.POINTER(_I64)], C.c_int),
     "mc_tally_reset": ([_P], C.c_int),

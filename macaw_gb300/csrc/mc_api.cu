@@ -89,6 +89,10 @@ struct mc_ctx {
   TallySpec tspec{};           // device view (edges point into d_edges)
   DevBuf d_edges;
   int64_t n_tally = 0;         // values per tally: elements x energy bins x scores
+  // recorded ray segments (mc_rays_enable): ray_n rays of ray_cap segments
+  DevBuf d_rays;
+  int32_t ray_n = 0, ray_cap = 0;
+  int64_t ray_first = 0;       // first_history of the last run that recorded
   long long h_limit = 0;
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
@@ -606,6 +610,14 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   }
   a.n_tally = c->n_tally;
   a.ts = c->tspec;
+  if (c->ray_n > 0 && d->n_histories > 0) {
+    CK(cudaMemsetAsync(c->d_rays.p, 0, c->d_rays.bytes, c->stream), "clear ray segments");
+    a.ts.rays = c->d_rays.as<mc_ray_segment>();
+    a.ts.ray_first = d->first_history;
+    a.ts.ray_n = c->ray_n;
+    a.ts.ray_cap = c->ray_cap;
+    c->ray_first = d->first_history;
+  }
   a.live = nullptr;
   // history-form batches all score into slot 0 (one runs at a time);
   // event-form batch b scores into slot b % slots
@@ -921,6 +933,46 @@ int mc_tally_configure(mc_ctx* c, const mc_tally_desc* d) {
   CK(cudaMemsetAsync(c->d_sumsq.p, 0, c->d_sumsq.bytes, c->stream), "clear tally");
   CK(cudaStreamSynchronize(c->stream), "configure tally");
   c->batches = 0;
+  return MC_OK;
+}
+
+int mc_rays_enable(mc_ctx* c, int32_t n_rays, int32_t max_segments) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n_rays < 0 || max_segments < 0) return set_err(c, MC_ERR_ARG, "negative ray count or segment limit");
+  if (n_rays == 0 || max_segments == 0) {
+    c->ray_n = c->ray_cap = 0;
+    c->d_rays.release();
+    return MC_OK;
+  }
+  const size_t bytes = sizeof(mc_ray_segment) * (size_t)n_rays * (size_t)max_segments;
+  if (bytes > ((size_t)16 << 30)) return set_err(c, MC_ERR_ARG, "ray segment buffer over 16 GiB");
+  cudaSetDevice(c->device);
+  CK(c->d_rays.alloc(bytes), "allocate ray segments");
+  CK(cudaMemsetAsync(c->d_rays.p, 0, bytes, c->stream), "clear ray segments");
+  CK(cudaStreamSynchronize(c->stream), "clear ray segments");
+  c->ray_n = n_rays;
+  c->ray_cap = max_segments;
+  return MC_OK;
+}
+
+int mc_rays_download(mc_ctx* c, mc_ray_segment* out, int64_t capacity, int64_t* n_out) {
+  if (!c || !n_out || (capacity > 0 && !out)) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  *n_out = 0;
+  if (c->ray_n == 0) return set_err(c, MC_ERR_STATE, "ray recording is not enabled");
+  cudaSetDevice(c->device);
+  std::vector<mc_ray_segment> all((size_t)c->ray_n * (size_t)c->ray_cap);
+  CK(cudaMemcpyAsync(all.data(), c->d_rays.p, c->d_rays.bytes, cudaMemcpyDeviceToHost, c->stream), "download rays");
+  CK(cudaStreamSynchronize(c->stream), "download rays");
+  int64_t n = 0;
+  for (const mc_ray_segment& s : all) {
+    if (s.id == 0) continue;  // slots past a ray's last segment stay empty
+    if (n < capacity) out[n] = s;
+    ++n;
+  }
+  *n_out = n;
+  if (n > capacity) return set_err(c, MC_ERR_ARG, "capacity below the " + std::to_string(n) + " recorded segments");
   return MC_OK;
 }
 

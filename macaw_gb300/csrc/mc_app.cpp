@@ -297,6 +297,10 @@ struct Problem {
   int64_t batches = 1;
   std::string file_base;
   bool csv = false, exodus = false;
+  // RayTracingExodus output: rays of the last batch, segments per ray
+  bool rays = false;
+  std::string rays_name;
+  int32_t rays_n = 0, rays_cap = 0;
 };
 
 const std::map<std::string, int> kSideNames = {{"back", 0}, {"bottom", 1}, {"right", 2},
@@ -746,6 +750,25 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
       Params p(out);
       P.csv = p.boolean("csv", false);
       P.exodus = p.boolean("exodus", false);
+      // [Outputs/<name>] type = RayTracingExodus (MOOSE ray_tracing module, as
+      // test/tests/study/openmc_study.i uses it): the segments of the last
+      // batch's first max_rays histories, up to max_segments each
+      for (const Block& c : out->children) {
+        Params q(&c);
+        if (!q.has("type")) continue;
+        if (q.raw("type") != "RayTracingExodus") q.error("type", "unknown output type (use RayTracingExodus)");
+        if (q.has("study")) q.raw("study");
+        q.boolean("output_data", true);
+        q.boolean("output_aux_data", true);
+        if (q.has("execute_on")) q.raw("execute_on");
+        P.rays = true;
+        P.rays_name = c.name;
+        P.rays_n = (int32_t)q.integer("max_rays", 1000);
+        P.rays_cap = (int32_t)q.integer("max_segments", 4096);
+        if (P.rays_n < 1 || P.rays_cap < 1) q.error("max_rays", "must be positive");
+        for (auto& k : c.order)
+          if (!q.used.count(k)) q.error(k, "unused parameter for RayTracingExodus");
+      }
       if (p.has("file_base")) P.file_base = p.raw("file_base");
     }
     TallyPlan TP = plan_tallies(P);
@@ -773,6 +796,8 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
     const auto t0 = std::chrono::steady_clock::now();
     mc_stats tot{};
     for (int64_t b = 0; b < P.batches; ++b) {
+      if (P.rays && b == P.batches - 1)
+        check(ctx, mc_rays_enable(ctx, (int32_t)std::min<int64_t>(P.rays_n, P.particles), P.rays_cap), "rays");
       mc_run_desc d{};
       d.first_history = b * P.particles;
       d.n_histories = P.particles;
@@ -855,6 +880,17 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
       }
     }
     js << "}";
+    if (P.rays && !P.file_base.empty()) {
+      // MOOSE names the file <file_base>_<output name>.e
+      int64_t n = 0;
+      mc_rays_download(ctx, nullptr, 0, &n);
+      std::vector<mc_ray_segment> seg((size_t)n);
+      check(ctx, mc_rays_download(ctx, seg.data(), n, &n), "rays");
+      const std::string path = P.file_base + "_" + P.rays_name + ".e";
+      if (n > 0 && mc_exodus_write_rays(path.c_str(), seg.data(), n, (P.batches - 1) * P.particles) != MC_OK)
+        throw std::runtime_error("cannot write " + path);
+      js << ", \"rays\": \"" << path << "\", \"ray_segments\": " << n;
+    }
     if (P.exodus && !P.file_base.empty()) {
       // MOOSE's Exodus output of the AuxVariables at the last step
       std::vector<const char*> nm;

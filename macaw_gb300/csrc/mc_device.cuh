@@ -126,7 +126,38 @@ struct TallySpec {
   int sc;      // score j (MC_SCORE_*) in bits 8j..8j+7
   int need_ss; // a score needs the macroscopic scattering cross section
   const double* __restrict__ edges;  // nb+1 ascending energy edges, or null: no energy filter
+  // segment recording (mc_rays_enable): histories first .. first+ray_n-1 of
+  // the run, ray_cap segments each, or rays null
+  mc_ray_segment* rays;
+  int64_t ray_first;
+  int ray_n, ray_cap;
 };
+
+// Records the segment that just ended, from (sx, sy, sz) to (ex, ey, ez),
+// when the particle's history is one of the recorded rays.  The FP64 walk
+// functions take kRays = false where a launch records no rays, so that the
+// walk without recording carries none of its registers.
+static __device__ __noinline__ void record_ray(const TallySpec& T, const Particle& p, double sx, double sy, double sz,
+                                        double ex, double ey, double ez) {
+  const int64_t r = p.id - 1 - T.ray_first;
+  const int k = p.n_seg - 1;
+  if (r < 0 || r >= T.ray_n || k >= T.ray_cap) return;
+  mc_ray_segment& o = T.rays[r * T.ray_cap + k];
+  o.id = p.id;
+  o.segment = k;
+  o.intersections = p.n_seg - p.n_coll;
+  o.elem = p.elem;
+  o.pad = 0;
+  o.start[0] = sx;
+  o.start[1] = sy;
+  o.start[2] = sz;
+  o.end[0] = ex;
+  o.end[1] = ey;
+  o.end[2] = ez;
+  o.E = p.E;
+  o.wgt = p.wgt;
+  o.seed_tracking = p.seed;
+}
 
 // Energy filter bin of E (OpenMC EnergyFilter: edges[b] <= E < edges[b+1]),
 // -1 outside the edges.
@@ -675,7 +706,7 @@ __device__ __forceinline__ void prefetch_neighbours(const DevMesh& M, const int4
   }
 }
 
-template <bool kInlineXS>
+template <bool kInlineXS, bool kRays = true>
 __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Particle& p,
                                             double* __restrict__ tally, const TallySpec& T, float& sigt32,
                                             unsigned long long& n_xs) {
@@ -749,9 +780,11 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
   else p.zero_run = 0;
   if (cross) {
     p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
+    const double sx = p.x, sy = p.y, sz = p.z;
     p.x = p.x + L * p.u;
     p.y = p.y + L * p.v;
     p.z = p.z + L * p.w;
+    if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
     const int nb = side_entry(M.tet[p.elem].nbr, bf);
     if (nb >= 0) {
       if (nb & kMatChange) p.mat = -2;
@@ -777,10 +810,12 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
   p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
   const double ex = p.x + L * p.u, ey = p.y + L * p.v, ez = p.z + L * p.w;
   const double back = L - dist;
+  const double sx = p.x, sy = p.y, sz = p.z;
   p.x = ex - back * p.u;
   p.y = ey - back * p.v;
   p.z = ez - back * p.w;
   ++p.n_coll;
+  if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
   p.zero_run = 0;
   return 1;
 }
@@ -806,7 +841,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
 // likewise |den32 - den| <= 12u |u|_1; t32 = num32/den32 rounded (0.5 ulp):
 // |t - t32| <= (E_num + |t32| E_den)/(den32 - E_den) + 4.8e-7 |t32|, padded
 // by 0.1%.
-template <bool kInlineXS, bool kPrefetch = false>
+template <bool kInlineXS, bool kPrefetch = false, bool kRays = true>
 __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, Particle& p,
                                              const float uf, const float vf, const float wf,
                                              double* __restrict__ tally, const TallySpec& T, float& sigt32,
@@ -868,7 +903,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     }
   }
   if (!sure || bf < 0 || !(tb + eb < lo_other)) {
-    const int r = segment_fp64<kInlineXS>(M, X, p, tally, T, sigt32, n_xs);
+    const int r = segment_fp64<kInlineXS, kRays>(M, X, p, tally, T, sigt32, n_xs);
     return (r == 0 && p.fin < 0) ? 5 : r;  // a reflection changed the direction
   }
   const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
@@ -903,9 +938,11 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   else p.zero_run = 0;
   if (cross) {
     p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
+    const double sx = p.x, sy = p.y, sz = p.z;
     p.x = p.x + L * p.u;
     p.y = p.y + L * p.v;
     p.z = p.z + L * p.w;
+    if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
     const int nb = side_entry(nb4, bf);
     if (nb >= 0) {
       if (nb & kMatChange) p.mat = -2;
@@ -930,10 +967,12 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
   const double ex = p.x + L * p.u, ey = p.y + L * p.v, ez = p.z + L * p.w;
   const double back = L - dist;
+  const double sx = p.x, sy = p.y, sz = p.z;
   p.x = ex - back * p.u;
   p.y = ey - back * p.v;
   p.z = ez - back * p.w;
   ++p.n_coll;
+  if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
   p.zero_run = 0;
   return 1;
 }
@@ -1070,9 +1109,11 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
   else p.zero_run = 0;
   if (cross) {
     p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
+    const float sx = g.x, sy = g.y, sz = g.z;
     g.x = fmaf(L, g.u, g.x);
     g.y = fmaf(L, g.v, g.y);
     g.z = fmaf(L, g.w, g.z);
+    if (T.rays) record_ray(T, p, sx, sy, sz, g.x, g.y, g.z);
     const int nb = side_entry(nb4, bf);
     if (nb >= 0) {
       if (nb & kMatChange) p.mat = -2;
@@ -1099,10 +1140,12 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
     return 2;
   }
   p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
+  const float sx = g.x, sy = g.y, sz = g.z;
   g.x = fmaf(dist, g.u, g.x);
   g.y = fmaf(dist, g.v, g.y);
   g.z = fmaf(dist, g.w, g.z);
   ++p.n_coll;
+  if (T.rays) record_ray(T, p, sx, sy, sz, g.x, g.y, g.z);
   p.zero_run = 0;
   return 1;
 }

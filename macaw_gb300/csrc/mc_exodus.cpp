@@ -169,6 +169,38 @@ std::vector<uint8_t> chars(const std::vector<std::string>& names, size_t len) {
   return out;
 }
 
+// Lays out and writes a one-record file: fixed-size variables after the
+// header, then the record variables.
+int write_nc(NcFile& f, const char* path) {
+  for (int pass = 0; pass < 2; ++pass) {
+    uint64_t off = f.header(1).size();
+    for (Var& v : f.vars)
+      if (!v.record) {
+        v.begin = off;
+        off += (v.data.size() + 3) / 4 * 4;
+      }
+    for (Var& v : f.vars)
+      if (v.record) {
+        v.begin = off;
+        off += (v.data.size() + 3) / 4 * 4;
+      }
+  }
+  FILE* fp = fopen(path, "wb");
+  if (!fp) return MC_ERR_STATE;
+  const std::vector<uint8_t> h = f.header(1);
+  bool ok = fwrite(h.data(), 1, h.size(), fp) == h.size();
+  const uint8_t zeros[4] = {0, 0, 0, 0};
+  for (int rec = 0; rec < 2 && ok; ++rec)
+    for (const Var& v : f.vars) {
+      if (v.record != (rec == 1)) continue;
+      ok = ok && fwrite(v.data.data(), 1, v.data.size(), fp) == v.data.size();
+      const size_t pad = (4 - v.data.size() % 4) % 4;
+      if (pad) ok = ok && fwrite(zeros, 1, pad, fp) == pad;
+    }
+  ok = (fclose(fp) == 0) && ok;
+  return ok ? MC_OK : MC_ERR_STATE;
+}
+
 // Exodus numbers a TETRA4's sides 1..4 as the faces (1,2,4), (2,3,4),
 // (1,4,3), (1,3,2) of its nodes; side f of a tet here is the face opposite
 // local vertex f.
@@ -344,34 +376,107 @@ extern "C" int mc_exodus_write(const char* path, const char* title, int64_t n_vt
       ++k;
     }
   }
-  // offsets: fixed-size variables after the header, then the one record
-  for (int pass = 0; pass < 2; ++pass) {
-    uint64_t off = f.header(1).size();
-    for (Var& v : f.vars)
-      if (!v.record) {
-        v.begin = off;
-        off += (v.data.size() + 3) / 4 * 4;
-      }
-    for (Var& v : f.vars)
-      if (v.record) {
-        v.begin = off;
-        off += (v.data.size() + 3) / 4 * 4;
-      }
-  }
-  FILE* fp = fopen(path, "wb");
-  if (!fp) return MC_ERR_STATE;
-  const std::vector<uint8_t> h = f.header(1);
-  bool ok = fwrite(h.data(), 1, h.size(), fp) == h.size();
-  const uint8_t zeros[4] = {0, 0, 0, 0};
-  for (int rec = 0; rec < 2 && ok; ++rec)
-    for (const Var& v : f.vars) {
-      if (v.record != (rec == 1)) continue;
-      ok = ok && fwrite(v.data.data(), 1, v.data.size(), fp) == v.data.size();
-      const size_t pad = (4 - v.data.size() % 4) % 4;
-      if (pad) ok = ok && fwrite(zeros, 1, pad, fp) == pad;
+  return write_nc(f, path);
+}
+
+// Recorded ray segments as MOOSE's RayTracingExodus writes them: one EDGE2
+// element per segment (block 0), the nodes of consecutive segments of a ray
+// shared, one time step, and the ray's data and aux data after each
+// segment as element variables, in the reference output's order.  MaCaw
+// keeps its OpenMC seeds in double aux fields, so seeds are written as the
+// nearest double; this tracker has no URR stream and keeps no source-stream
+// state after birth, so those two are 0.
+extern "C" int mc_exodus_write_rays(const char* path, const mc_ray_segment* seg, int64_t n, int64_t first_history) {
+  if (!path || n < 1 || !seg || n > INT32_MAX / 2) return MC_ERR_ARG;
+  std::vector<double> xyz;
+  std::vector<int32_t> conn;
+  int64_t prev_id = -1;
+  int32_t last_node = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const mc_ray_segment& r = seg[i];
+    if (r.id != prev_id) {  // a new ray: its first node is this segment's start
+      xyz.insert(xyz.end(), r.start, r.start + 3);
+      last_node = (int32_t)(xyz.size() / 3);
+      prev_id = r.id;
     }
-  ok = (fclose(fp) == 0) && ok;
-  return ok ? MC_OK : MC_ERR_STATE;
+    xyz.insert(xyz.end(), r.end, r.end + 3);
+    const int32_t end_node = (int32_t)(xyz.size() / 3);
+    conn.push_back(last_node);
+    conn.push_back(end_node);
+    last_node = end_node;
+  }
+  const int64_t nn = (int64_t)xyz.size() / 3;
+  const size_t kLen = 33;
+  NcFile f;
+  f.dim("len_string", kLen);
+  f.dim("len_line", 81);
+  f.dim("four", 4);
+  const int d_time = f.dim("time_step", 0);
+  const int d_len_name = f.dim("len_name", kLen);
+  const int d_num_dim = f.dim("num_dim", 3);
+  const int d_nodes = f.dim("num_nodes", (uint64_t)nn);
+  const int d_elem = f.dim("num_elem", (uint64_t)n);
+  const int d_blk = f.dim("num_el_blk", 1);
+  const int d_in = f.dim("num_el_in_blk1", (uint64_t)n);
+  const int d_per = f.dim("num_nod_per_el1", 2);
+  const int d_nvar = f.dim("num_elem_var", 10);
+  f.gatts = {attr_float("api_version", 5.22f), attr_float("version", 5.22f),
+             attr_int("floating_point_word_size", 8), attr_int("file_size", 1),
+             attr_int("maximum_name_length", 32), attr_text("title", "macaw_gb300 rays")};
+  auto ints_of = [](const std::vector<int32_t>& v) {
+    std::vector<uint8_t> b;
+    be_ints(b, v);
+    return b;
+  };
+  {
+    const double t = 1.0;
+    Var v{"time_whole", {d_time}, kDouble, {}, {}, true};
+    be_doubles(v.data, &t, 1);
+    f.vars.push_back(v);
+  }
+  f.vars.push_back(Var{"eb_status", {d_blk}, kInt, {}, ints_of({1})});
+  f.vars.push_back(Var{"eb_prop1", {d_blk}, kInt, {attr_text("name", "ID")}, ints_of({0})});
+  for (int k = 0; k < 3; ++k) {
+    Var v{std::string("coord") + "xyz"[k], {d_nodes}, kDouble, {}, {}};
+    be_doubles(v.data, xyz.data() + k, (size_t)nn, 3);
+    f.vars.push_back(v);
+  }
+  f.vars.push_back(Var{"eb_names", {d_blk, d_len_name}, kChar, {}, chars({""}, kLen)});
+  f.vars.push_back(Var{"coor_names", {d_num_dim, d_len_name}, kChar, {}, chars({"x", "y", "z"}, kLen)});
+  {
+    std::vector<int32_t> nmap((size_t)nn), emap((size_t)n);
+    for (int64_t i = 0; i < nn; ++i) nmap[(size_t)i] = (int32_t)(i + 1);
+    for (int64_t i = 0; i < n; ++i) emap[(size_t)i] = (int32_t)(i + 1);
+    f.vars.push_back(Var{"node_num_map", {d_nodes}, kInt, {}, ints_of(nmap)});
+    f.vars.push_back(Var{"connect1", {d_in, d_per}, kInt, {attr_text("elem_type", "EDGE2")}, ints_of(conn)});
+    f.vars.push_back(Var{"elem_num_map", {d_elem}, kInt, {}, ints_of(emap)});
+  }
+  const std::vector<std::string> names = {"aux_energy",        "aux_id",         "aux_n_progeny",    "aux_particle_type",
+                                          "aux_seed_URR",      "aux_seed_source", "aux_seed_tracking", "aux_weight",
+                                          "intersections",     "ray_id"};
+  f.vars.push_back(Var{"name_elem_var", {d_nvar, d_len_name}, kChar, {}, chars(names, kLen)});
+  f.vars.push_back(Var{"elem_var_tab", {d_blk, d_nvar}, kInt, {}, ints_of(std::vector<int32_t>(10, 1))});
+  for (int vi = 0; vi < 10; ++vi) {
+    std::vector<double> vals((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+      const mc_ray_segment& r = seg[i];
+      double v = 0.0;
+      switch (vi) {
+        case 0: v = r.E; break;
+        case 1: v = (double)r.id; break;
+        case 6: v = (double)r.seed_tracking; break;
+        case 7: v = r.wgt; break;
+        case 8: v = (double)r.intersections; break;
+        case 9: v = (double)(r.id - 1 - first_history); break;
+        default: v = 0.0; break;
+      }
+      vals[(size_t)i] = v;
+    }
+    Var v{"vals_elem_var" + std::to_string(vi + 1) + "eb1", {d_time, d_in}, kDouble, {}, {}, true};
+    be_doubles(v.data, vals.data(), vals.size());
+    f.vars.push_back(v);
+  }
+  return write_nc(f, path);
 }
 
 // ---------------------------------------------------------------------------

@@ -332,7 +332,7 @@ __device__ __forceinline__ int take_chunk(int* head) {
 
 // Segment walk, one queued particle per lane, queue entries taken by warp
 // chunks.
-template <int kPrec>
+template <int kPrec, bool kRays>
 __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                            EventQueues Q, EventCtl* ctl, int par) {
   MC_COUNTERS(L);
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       for (;;) {
-        r = segment_fp64g<false>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
+        r = segment_fp64g<false, false, kRays>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 5) {
           uf = (float)p.u;
           vf = (float)p.v;
@@ -897,12 +897,13 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
   }
   if (adv0) cudaEventRecord(adv0, st);
   if (a.precision == MC_PREC_MIXED) {
-    // the compact walk scores the default tally only
-    if (a.refill || a.ts.general) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    // the compact walk scores the default tally and records no rays
+    if (a.refill || a.ts.general || a.ts.rays) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else k_ev_advance_mixed<<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
   } else {
     if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else k_ev_advance_static<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else if (a.ts.rays) k_ev_advance_static<MC_PREC_FP64, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_advance_static<MC_PREC_FP64, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   }
   if (adv1) cudaEventRecord(adv1, st);
   k_ev_collide<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);

@@ -50,3 +50,12 @@ def read_mesh(path: str):
     if rc != 0:
         raise MCError(rc, err.value.decode())
     return xyz, tv, blk, bid
+
+
+def write_rays(path: str, segments: np.ndarray, first_history: int = 0) -> None:
+    """Recorded ray segments (Tracker.rays()) as a RayTracingExodus file."""
+    from ._lib import RAY_SEGMENT_DTYPE
+    seg = np.ascontiguousarray(segments, RAY_SEGMENT_DTYPE)
+    rc = lib.mc_exodus_write_rays(path.encode(), ptr(seg), seg.size, first_history)
+    if rc != 0:
+        raise MCError(rc, f"mc_exodus_write_rays({path}) failed")

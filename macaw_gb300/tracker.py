@@ -12,7 +12,8 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (MC_MODE_EVENT, MC_PREC_FP64, MC_TALLY_BATCH, MC_TALLY_SUM, MC_TALLY_SUM_SQ,
-                   SITE_DTYPE, TRACE_DTYPE, MCError, RunDesc, SourceDesc, Stats, TallyDesc, lib, ptr)
+                   RAY_SEGMENT_DTYPE, SITE_DTYPE, TRACE_DTYPE, MCError, RunDesc, SourceDesc, Stats, TallyDesc, lib,
+                   ptr)
 from .problems import Problem, Source, TallyDef
 
 
@@ -121,6 +122,18 @@ class Tracker:
         d.n_energy_bins = 0 if e is None else e.size - 1
         d.energy_edges = None if e is None else e.ctypes.data
         self._ck(lib.mc_tally_configure(self._h, C.byref(d)), "mc_tally_configure")
+
+    def enable_rays(self, n_rays: int, max_segments: int = 4096) -> None:
+        """Record every segment of the first n_rays histories of each run (0: off)."""
+        self._ck(lib.mc_rays_enable(self._h, n_rays, max_segments), "mc_rays_enable")
+
+    def rays(self) -> np.ndarray:
+        """Segments recorded by the last run (RAY_SEGMENT_DTYPE), ray by ray."""
+        n = C.c_int64()
+        lib.mc_rays_download(self._h, None, 0, C.byref(n))
+        out = np.zeros(n.value, RAY_SEGMENT_DTYPE)
+        self._ck(lib.mc_rays_download(self._h, ptr(out), out.size, C.byref(n)), "mc_rays_download")
+        return out
 
     def tally_size(self) -> int:
         n = C.c_int64()

@@ -126,3 +126,17 @@ def test_file_mesh_generator_reads_an_exodus_tet_mesh(tmp_path, monkeypatch):
     assert c["tets"] == p.n_tet and c["vertices"] == p.xyz.shape[0]
     with pytest.raises(ValueError, match="file"):
         app.check_input(txt.replace("cube_mesh.e", "missing.e"))
+
+
+@pytest.mark.gpu
+def test_ray_tracing_exodus_output(tmp_path):
+    from scipy.io import netcdf_file
+    txt = CUBE.replace("particles = 100000", "particles = 2000").replace(
+        "csv = true", "csv = true\n  [rays]\n    type = RayTracingExodus\n    study = study\n    output_data = true\n"
+                      "    output_aux_data = true\n    execute_on = final\n    max_rays = 30\n  []")
+    rep = app.run_input(txt, 0, str(tmp_path / "cube"))
+    assert rep["rays"].endswith("cube_rays.e") and rep["ray_segments"] > 30
+    with netcdf_file(rep["rays"], "r", mmap=False) as f:
+        assert f.dimensions["num_elem"] == rep["ray_segments"]
+        ray_id = f.variables["vals_elem_var10eb1"][0]
+        assert set(np.unique(ray_id).astype(int)) == set(range(30))

@@ -112,3 +112,35 @@ def test_reads_files_from_another_netcdf_writer(tmp_path):
     from macaw_gb300._lib import MCError
     with pytest.raises(MCError, match="only 4-node tetrahedra"):
         exodus.read_mesh(path)
+
+
+REF_RAY_VARS = ["aux_energy", "aux_id", "aux_n_progeny", "aux_particle_type", "aux_seed_URR", "aux_seed_source",
+                "aux_seed_tracking", "aux_weight", "intersections", "ray_id"]
+
+
+def test_ray_segments_layout_of_the_reference_output(tmp_path):
+    from macaw_gb300._lib import RAY_SEGMENT_DTYPE
+    # two rays: 3 and 2 segments, chained end to start
+    seg = np.zeros(5, RAY_SEGMENT_DTYPE)
+    pts = {11: [(0, 0, 0), (1, 0, 0), (1, 1, 0), (1, 1, 1)], 12: [(5, 5, 5), (6, 5, 5), (6, 6, 5)]}
+    i = 0
+    for rid, p in pts.items():
+        for k in range(len(p) - 1):
+            seg[i]["id"], seg[i]["segment"], seg[i]["intersections"] = rid, k, k + 1
+            seg[i]["start"], seg[i]["end"] = p[k], p[k + 1]
+            seg[i]["E"], seg[i]["wgt"], seg[i]["seed_tracking"] = 1e6 - k, 1.0, 2**60 + k
+            i += 1
+    path = str(tmp_path / "rays.e")
+    exodus.write_rays(path, seg, first_history=10)
+    with netcdf(path, "r", mmap=False) as f:
+        assert _chars(f.variables["name_elem_var"][:]) == REF_RAY_VARS
+        assert f.variables["connect1"].elem_type == b"EDGE2"
+        assert f.dimensions["num_elem"] == 5 and f.dimensions["num_nodes"] == 5 + 2  # shared nodes per ray
+        c = f.variables["connect1"][:] - 1
+        x = np.stack([f.variables["coord" + a][:] for a in "xyz"], axis=1)
+        assert np.array_equal(x[c[:, 0]], seg["start"]) and np.array_equal(x[c[:, 1]], seg["end"])
+        v = {n: f.variables[f"vals_elem_var{k + 1}eb1"][0] for k, n in enumerate(REF_RAY_VARS)}
+        assert v["ray_id"].tolist() == [0, 0, 0, 1, 1]
+        assert v["aux_id"].tolist() == [11, 11, 11, 12, 12]
+        assert v["intersections"].tolist() == [1, 2, 3, 1, 2]
+        assert np.array_equal(v["aux_seed_tracking"], seg["seed_tracking"].astype(np.float64))
