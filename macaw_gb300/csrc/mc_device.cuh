@@ -106,7 +106,7 @@ struct Particle {
   int64_t id;
   int elem, mat, n_seg, n_coll, status, face, zero_run;
   int fin;  // side the particle entered its element through (-1: none)
-  int tag;  // parity of the particle's batch (selects its batch tally)
+  int tag;  // tally slot of the particle's batch or request
   // Sigma_t at the current energy for up to four materials, most recently
   // inserted first (an insert shifts the others down one slot and drops the
   // last); -1 marks an empty slot.  Sigma_t is a pure function of

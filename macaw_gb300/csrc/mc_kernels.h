@@ -57,7 +57,6 @@ struct EventCtl {
   unsigned long long free_head, free_tail;  // ring of free bank slots (monotonic counters)
   long long next_hist;              // next history (relative to the run) to be born
   long long birth_limit;            // histories at or past this index wait (pipelined batches)
-  int live[2];                      // unused (per-slot counters live in RunArgs::live)
 };
 
 struct EventQueues {
