@@ -1,0 +1,72 @@
+"""Full-size workloads: the 2,039,184-tet lattice at 1e7 histories and the
+41,283,792-tet core.
+
+At these sizes the oracle checks a sample: the first 2,000 histories of the
+lattice run must match it trace for trace, bit for bit.  The rest is
+checked through properties that hold at any size: every history ends in
+exactly one state with none stuck or lost, the pipelined batches fold to
+the batch count, and the mixed form stays within the 1e-4 mean relative
+element-flux difference of the FP64 form on the same 1e7 histories.
+"""
+import numpy as np
+import pytest
+
+from macaw_gb300 import Tracker, problems
+from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+N, K = 1_000_000, 10
+
+
+@pytest.fixture(scope="module")
+def lattice():
+    return problems.lattice_problem()
+
+
+def _accounting(st, n):
+    assert st.n_hist == n and st.n_stuck == 0 and st.n_lost == 0 and st.n_badxs == 0
+    assert st.n_leak + st.n_absorb + st.n_cutoff == n
+
+
+def test_lattice_1e7_histories_fp64_and_mixed(lattice):
+    with Tracker(0) as t:
+        t.load(lattice)
+        kw = dict(seed=1, accumulate=True, batch_sizes=[N] * K, bank_size=N, max_seg=64, sort_queue=9, graph=True)
+        st = t.run(N * K, precision=MC_PREC_FP64, **kw)
+        _accounting(st, N * K)
+        assert t.batches_done() == K
+        fp64 = t.tally(MC_TALLY_SUM)
+        t.reset_tally()
+        sm = t.run(N * K, precision=MC_PREC_MIXED, **dict(kw, max_seg=128))
+        _accounting(sm, N * K)
+        mixed = t.tally(MC_TALLY_SUM)
+    nz = fp64 > 0
+    assert np.all(mixed[~nz] == 0)
+    rel = np.abs(mixed[nz] - fp64[nz]) / fp64[nz]
+    assert rel.mean() <= 1e-4, rel.mean()
+    assert sm.n_fallback < 1e-3 * sm.n_seg
+
+
+def test_lattice_sample_matches_the_oracle(lattice):
+    n = 2000
+    with Tracker(0) as t:
+        t.load(lattice)
+        t.run(n, first=5_000_000, seed=1, precision=MC_PREC_FP64, traces=True, bank_size=n, max_seg=64)
+        tr = t.traces(n)
+    _, otr, _, _ = O.Oracle(lattice).run(n, first=5_000_000, seed=1, threads=16)
+    for f in ("hash", "status", "n_seg", "n_coll", "elem", "face", "E", "x", "y", "z"):
+        assert np.array_equal(tr[f], otr[f]), f
+
+
+def test_core_histories_all_end():
+    p = problems.core_problem()
+    with Tracker(0) as t:
+        t.load(p)
+        sizes = [300_000, 100_000, 600_000]
+        for prec in (MC_PREC_FP64, MC_PREC_MIXED):
+            st = t.run(sum(sizes), seed=1, precision=prec, accumulate=True, batch_sizes=sizes, bank_size=500_000,
+                       max_seg=128, sort_queue=13)
+            _accounting(st, sum(sizes))
