@@ -59,6 +59,12 @@ REF_SAMPLE = 100_000
 # traffic per launch = this x the launch's segments
 ADVANCE_DRAM_BYTES_PER_SEG = 208.4
 MIXED_DRAM_BYTES_PER_SEG = 71.8
+# what bounds each walk instead of HBM, from the same captures' --set full
+# launch: the FP64 walk keeps the FP64 pipe 77% busy (GB300's FP64 rate is a
+# 64th of its FP32 rate); the mixed walk waits on its one dependent record
+# load per segment (L2 hit rate 43%, 29% of the warp slots occupied)
+FP64_PIPE_ACTIVE = 0.769
+MIXED_L2_HIT = 0.430
 
 
 def env_int(name, default):
@@ -406,6 +412,8 @@ def main():
                                  "advance_ms_per_launch": pst.ms_advance / max(pst.n_advance_launch, 1),
                                  "segments_per_launch": pst.n_seg_advance / max(pst.n_advance_launch, 1),
                                  "traffic": MIXED_DRAM_BYTES_PER_SEG * pst.n_seg_advance / max(pst.n_advance_launch, 1),
+                                 "limiter": {"dependent_record_loads_l2_hit": MIXED_L2_HIT,
+                                             "source": "ncu lts__t_sector_hit_rate (profiles/walk_mixed_lattice.md)"},
                                  "sample": f"one extra profiled batch of {n} histories"}
 
     # --- end to end through the C ABI with host buffers, one call per step ---
@@ -472,6 +480,8 @@ def main():
                 "advance_share_of_step": st.ms_advance / ms if ms > 0 else None,
                 "traffic_source": "ncu DRAM bytes per walked segment (profiles/walk_fp64_lattice.md) x segments "
                                   "per launch",
+                "limiter": {"fp64_pipe_active": FP64_PIPE_ACTIVE,
+                            "source": "ncu sm__pipe_fp64_cycles_active (profiles/walk_fp64_lattice.md)"},
                 "note": "the FP64 walk is bound by GB300's FP64 pipe, not HBM (see profiles/)"}
         cfg = dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single",
                    pipelined_batches=K, tuned=params64)
