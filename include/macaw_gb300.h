@@ -220,6 +220,17 @@ int mc_ctx_set_stream(mc_ctx* ctx, void* stream);
 int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_histories, mc_run_desc* best,
                 double* best_rate);
 
+/* Replaces: the 2-D mode of CollisionKernel (z_coord,
+ * src/raykernels/CollisionKernel.C:38,60-61,177-179,200-202) and of
+ * OpenMCStudy (src/userobjects/OpenMCStudy.C:355-356).  With on = 1 every
+ * source direction and every scattered direction loses its z component and
+ * is renormalised in the plane (a direction along z becomes +x), and
+ * histories are born at z = z_coord, so they stay in that plane.  The
+ * mesh is a 2-D mesh extruded into one layer of tets around z_coord (the
+ * lattice generator with nz = 1); a 2-D element's result is the sum over
+ * the tets of its prism. */
+int mc_set_2d(mc_ctx* ctx, int32_t on, double z_coord);
+
 /* ---- tally definition ------------------------------------------------- */
 typedef struct {
   int32_t estimator;       /* MC_EST_TRACKLENGTH or MC_EST_COLLISION */

@@ -104,6 +104,7 @@ SIGNATURES = {
     "mc_app_check": ([C.c_char_p, C.c_char_p, _I64], C.c_int),
     "mc_tally_download": ([_P, _I32, _P, _I64], C.c_int),
     "mc_tally_configure": ([_P, C.c_void_p], C.c_int),
+    "mc_set_2d": ([_P, _I32, _D], C.c_int),
     "mc_exodus_read_sizes": ([C.c_char_p, C.POINTER(_I64), C.POINTER(_I64), C.c_char_p, _I64], C.c_int),
     "mc_exodus_read": ([C.c_char_p, _P, _P, _P, _P, C.c_char_p, _I64], C.c_int),
     "mc_rays_enable": ([_P, _I32, _I32], C.c_int),

@@ -91,6 +91,9 @@ struct mc_ctx {
   int64_t n_tally = 0;         // values per tally: elements x energy bins x scores
   // recorded ray segments (mc_rays_enable): ray_n rays of ray_cap segments
   DevBuf d_rays;
+  // 2-D mode (mc_set_2d)
+  int two_d = 0;
+  double z2d = 0.0;
   int32_t ray_n = 0, ray_cap = 0;
   int64_t ray_first = 0;       // first_history of the last run that recorded
   long long h_limit = 0;
@@ -525,6 +528,8 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
   a.precision = d->precision;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.two_d = c->two_d;
+  a.z2d = c->z2d;
   a.sort_shift = -1;
   a.sort_buckets = 0;
   a.sort_tmp = nullptr;
@@ -976,6 +981,15 @@ int mc_rays_download(mc_ctx* c, mc_ray_segment* out, int64_t capacity, int64_t* 
   return MC_OK;
 }
 
+int mc_set_2d(mc_ctx* c, int32_t on, double z_coord) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (on && !(z_coord == z_coord)) return set_err(c, MC_ERR_ARG, "z_coord must be a number");
+  c->two_d = on ? 1 : 0;
+  c->z2d = on ? z_coord : 0.0;
+  return MC_OK;
+}
+
 int mc_tally_size(mc_ctx* c, int64_t* n) {
   if (!c || !n) return MC_ERR_ARG;
   std::lock_guard<std::mutex> g(c->mu);
@@ -1041,6 +1055,8 @@ bool ctx_view(mc_ctx* c, CtxView* v) {
   v->n_tet = c->mesh.n_tet;
   v->n_tally = c->n_tally;
   v->ts = c->tspec;
+  v->two_d = c->two_d;
+  v->z2d = c->z2d;
   v->n_mat = (int)c->xs.mat_ids.size();
   const bool tables = c->have_mesh && !c->nucs.empty() && !c->mats.empty() && !c->xs_dirty && !c->tmat_dirty &&
                       !c->bc_dirty;

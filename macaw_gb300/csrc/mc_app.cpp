@@ -297,6 +297,8 @@ struct Problem {
   int64_t batches = 1;
   std::string file_base;
   bool csv = false, exodus = false;
+  bool two_d = false;
+  double z2d = 0.0;
   // RayTracingExodus output: rays of the last batch, segments per ray
   bool rays = false;
   std::string rays_name;
@@ -388,7 +390,13 @@ void collision_kernel(Params& p, Problem& P) {
   const auto mats = p.ints("materials", true);
   if (blocks.size() != mats.size())
     p.error("blocks", "The blocks parameter must be the same size as the materials parameter.");
-  p.real("z_coord", 0.0);
+  // z_coord (CollisionKernel.C:38,60-61) makes the problem 2-D: the mesh is
+  // then one layer of tets around that plane (e.g. TetLatticeMeshGenerator
+  // with nz = 1), directions stay in the plane
+  if (p.has("z_coord")) {
+    P.two_d = true;
+    P.z2d = p.real("z_coord", 0.0);
+  }
   P.verbose = p.boolean("verbose", false) || P.verbose;
   P.blocks.assign(blocks.begin(), blocks.end());
   P.materials.assign(mats.begin(), mats.end());
@@ -787,6 +795,11 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
           "CollisionKernel");
     if (P.src.space == MC_SRC_CYLINDERS) P.src.cyl_xy = P.cyl_xy.data();
     check(ctx, mc_source_set(ctx, &P.src), "OpenMCStudy source");
+    if (P.two_d) {
+      if (!(P.z2d >= P.lo[2] && P.z2d <= P.hi[2]))
+        throw InputError("RayKernels/z_coord: outside the mesh's z range");
+      check(ctx, mc_set_2d(ctx, 1, P.z2d), "CollisionKernel z_coord");
+    }
     if (TP.general) check(ctx, mc_tally_configure(ctx, &TP.desc), "OpenMCTally");
     int64_t n_tally = 0;
     check(ctx, mc_tally_size(ctx, &n_tally), "OpenMCTally");

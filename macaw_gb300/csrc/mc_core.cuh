@@ -226,6 +226,22 @@ MC_HD void rotate_dir(double& u0, double& v0, double& w0, double mu, double cphi
   }
 }
 
+// 2-D problems (CollisionKernel z_coord, CollisionKernel.C:60-61,200-202;
+// OpenMCStudy.C:355-356): a direction loses its z component and is
+// renormalised in the plane (a direction along z becomes +x).
+MC_HD void planar_dir(double& u, double& v, double& w) {
+  w = 0.0;
+  const double n2 = u * u + v * v;
+  if (n2 > 0.0) {
+    const double n = sqrt(n2);
+    u = u / n;
+    v = v / n;
+  } else {
+    u = 1.0;
+    v = 0.0;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Per-history trace hash (FNV-1a over 64-bit words).
 constexpr uint64_t kFnvOffset = 14695981039346656037ULL;

@@ -17,6 +17,8 @@ struct CtxView {
   int64_t n_tet = 0;
   int64_t n_tally = 0;  // values per tally: elements x energy bins x scores
   TallySpec ts{};       // the context's tally definition
+  int two_d = 0;        // 2-D mode and its z coordinate
+  double z2d = 0.0;
   float tol = 0.0f;
   bool ready = false;  // mesh, tables, block map, BCs and source resident on the device
                        // (M, X and S are filled whenever the tables are resident)

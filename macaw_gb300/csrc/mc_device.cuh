@@ -624,7 +624,7 @@ __device__ __forceinline__ void score_collision(const DevXS& X, const TallySpec&
 // absorption if xi*sigma_t < sigma_a, else elastic scattering isotropic in
 // the centre-of-mass frame off a target at rest.  Absorption and energy
 // cutoff end the history; secondaries are not tracked (CollisionKernel.C:236).
-__device__ __forceinline__ void collide(const DevXS& X, Particle& p) {
+__device__ __forceinline__ void collide(const DevXS& X, Particle& p, bool two_d = false) {
   const int mat = p.mat;
   const int k = xs_bucket(X, mc::log64(p.E));
   const double cutoff = prn(p.seed) * p.sigt;
@@ -662,6 +662,7 @@ __device__ __forceinline__ void collide(const DevXS& X, Particle& p) {
   if (mu_lab > 1.0) mu_lab = 1.0;
   if (mu_lab < -1.0) mu_lab = -1.0;
   rotate_dir(p.u, p.v, p.w, mu_lab, cp, sp);
+  if (two_d) planar_dir(p.u, p.v, p.w);
   p.E = E2;
   p.mat = -2;  // energy changed: cross sections are recomputed
   p.fin = -1;

@@ -182,6 +182,10 @@ __device__ __forceinline__ void birth(const DevMesh& M, const DevXS& X, const De
   if (a.sites) o = a.sites[h - a.first];
   else if (a.precision == MC_PREC_MIXED) sample_source32(X, *src, k, master, o);
   else sample_source(X, *src, k, master, o);
+  if (a.two_d) {
+    o.z = a.z2d;
+    planar_dir(o.u, o.v, o.w);
+  }
   start(M, o, id - 1, k, master, p);
   p.tag = tag;
   if (a.live) live_add(a.live, p.tag, 1);
@@ -235,7 +239,7 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
         const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 1) {
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p);
+          collide(X, p, a.two_d);
         }
         if (r == 1 || r == 5) {
           uf = (float)p.u;
@@ -252,7 +256,7 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
         if (r == 1) {
           geo_store(g, p);
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p);
+          collide(X, p, a.two_d);
           geo_load(p, g);
         }
       }
@@ -696,7 +700,7 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
     Particle p;
     load(B, s, p);
     score_collision(X, a.ts, tally_of(a, p.tag), p);
-    collide(X, p);
+    collide(X, p, a.two_d);
     if (p.status != kAlive) {
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
@@ -767,7 +771,7 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
         const int r = segment_fp64g<true, true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 1) {
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p);
+          collide(X, p, a.two_d);
         }
         if (r == 1 || r == 5) {
           uf = (float)p.u;
@@ -784,7 +788,7 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
         if (r == 1) {
           geo_store(g, p);
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p);
+          collide(X, p, a.two_d);
           geo_load(p, g);
         }
       }

@@ -99,6 +99,8 @@ struct RunArgs {
   float tol;    // mixed form: exit ambiguity tolerance (cm)
   int max_seg;  // event mode: segments per advance launch (<= 0: until event)
   int refill;   // event mode: lanes take further queued particles within one launch
+  int two_d;    // 2-D problem: planar directions, births at z = z2d
+  double z2d;
   int sort_shift;    // event mode: advance queue ordered by elem >> sort_shift (-1: unordered)
   int sort_buckets;  // (n_tet >> sort_shift) + 1
   int* sort_tmp;     // bank-capacity scratch for the ordering

@@ -165,6 +165,8 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.tol = v.tol;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.two_d = v.two_d;
+  a.z2d = v.z2d;
   a.sort_shift = -1;  // ordering needs scratch beyond the fixed array
   a.sort_buckets = 0;
   a.sort_tmp = nullptr;

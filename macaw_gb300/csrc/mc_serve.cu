@@ -108,6 +108,8 @@ RunArgs args(const Serve& s) {
   a.tol = s.v.tol;
   a.max_seg = s.max_seg;
   a.refill = 0;
+  a.two_d = s.v.two_d;
+  a.z2d = s.v.z2d;
   a.sort_shift = -1;
   return a;
 }

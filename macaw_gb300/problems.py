@@ -25,7 +25,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import MC_BC_VACUUM, MC_SRC_CYLINDERS, MC_SRC_POINT, MC_SRC_WATT, lib, ptr
+from ._lib import MC_BC_REFLECT, MC_BC_VACUUM, MC_SRC_CYLINDERS, MC_SRC_POINT, MC_SRC_WATT, lib, ptr
 
 WATT_A = 0.988e6   # eV
 WATT_B = 2.249e-6  # 1/eV
@@ -87,6 +87,7 @@ class Problem:
     bcs: dict = field(default_factory=dict)  # boundary id -> MC_BC_*
     hash_bins: int = 8000
     tally: TallyDef | None = None  # None: track-length flux per element
+    z_2d: float | None = None      # 2-D mode (CollisionKernel z_coord): None for 3-D
 
     @property
     def n_tet(self) -> int:
@@ -231,3 +232,18 @@ def core_problem(pins: int = 17, nz: int = 6, n_sec: int = 8, n_fuel_rings: int 
                  cyl_z0=0.0, cyl_z1=height)
     return Problem(f"core{pins}x{nz}", xyz, tv, blk, bid, nucs, mats, blocks, blocks.copy(), src,
                    {b: MC_BC_VACUUM for b in range(7)})
+
+
+def lattice_2d_problem(nx: int = 17, ny: int = 17, n_sec: int = 16, n_fuel_rings: int = 2, pitch: float = 1.26,
+                       thickness: float = 1.0, n_pts: int = 20000, n_peaks: int = 20,
+                       nuclides_per_material=(15, 4, 3), seed: int = 20240611) -> Problem:
+    """2-D pin lattice (CollisionKernel z_coord): the lattice's 2-D mesh
+    extruded into one layer of tets of the given thickness, histories in
+    the mid-plane, reflective top and bottom (never reached: directions
+    stay in the plane)."""
+    p = lattice_problem(nx, ny, 1, n_sec, n_fuel_rings, pitch, thickness, n_pts, n_peaks, nuclides_per_material,
+                        seed)
+    p.name = f"lattice2d{nx}x{ny}"
+    p.z_2d = thickness / 2
+    p.bcs[0] = p.bcs[5] = MC_BC_REFLECT
+    return p

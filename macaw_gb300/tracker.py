@@ -110,6 +110,8 @@ class Tracker:
         self.set_source(p.source)
         if p.tally is not None:
             self.configure_tally(p.tally)
+        self._ck(lib.mc_set_2d(self._h, 0 if p.z_2d is None else 1, 0.0 if p.z_2d is None else p.z_2d),
+                 "mc_set_2d")
         return self
 
     def configure_tally(self, t: TallyDef) -> None:

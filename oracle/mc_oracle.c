@@ -174,6 +174,9 @@ struct oracle_problem {
   int t_ns, t_nb;   /* scores, energy bins (>= 1) */
   int t_sc[4];      /* 0 flux, 1 total, 2 scatter, 3 absorption */
   double* t_edges;  /* t_nb+1 edges, or NULL: no energy filter */
+  /* 2-D mode (CollisionKernel z_coord) */
+  int two_d;
+  double z2d;
 };
 
 static int fail(oracle_problem* p, const char* msg)
@@ -516,6 +519,14 @@ int oracle_set_tally(oracle_problem* p, int32_t estimator, int32_t n_scores, con
 
 int64_t oracle_tally_size(const oracle_problem* p) { return p->n_tet * p->t_nb * p->t_ns; }
 
+/* 2-D mode: CollisionKernel.C:60-61,200-202, OpenMCStudy.C:355-356. */
+int oracle_set_2d(oracle_problem* p, int32_t on, double z_coord)
+{
+  p->two_d = on ? 1 : 0;
+  p->z2d = on ? z_coord : 0.0;
+  return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* Energy-grid search: logarithmic hash bins over the common energy range
  * (F. B. Brown, "New hash-based energy lookup algorithm for Monte Carlo
@@ -710,6 +721,22 @@ static double sample_watt(uint64_t* s, double a, double b, double E_lo, double E
 
 static double pos0(double a) { return a > 0.0 ? a : 0.0; }
 
+/* A direction without its z component, renormalised in the plane (a
+ * direction along z becomes +x), as the 2-D mode sets it. */
+static void planar_dir(double* u)
+{
+  u[2] = 0.0;
+  double n2 = u[0] * u[0] + u[1] * u[1];
+  if (n2 > 0.0) {
+    double n = sqrt(n2);
+    u[0] = u[0] / n;
+    u[1] = u[1] / n;
+  } else {
+    u[0] = 1.0;
+    u[1] = 0.0;
+  }
+}
+
 static void rotate_dir(double* u, double mu, double cphi, double sphi)
 {
   double u0 = u[0], v0 = u[1], w0 = u[2];
@@ -855,6 +882,10 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
   uint64_t strk = oracle_init_seed(id, master, 0);
   double x[3], u[3], E, wgt = 1.0;
   birth(p, id, &ssrc, x, u, &E);
+  if (p->two_d) {
+    x[2] = p->z2d;
+    planar_dir(u);
+  }
   uint64_t hash = FNV_OFF;
   int status = 0, n_seg = 0, n_coll = 0, face_out = -1;
   int elem = oracle_locate(p, x, u);
@@ -950,6 +981,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
     if (mu_lab > 1.0) mu_lab = 1.0;
     if (mu_lab < -1.0) mu_lab = -1.0;
     rotate_dir(u, mu_lab, cp, sp);
+    if (p->two_d) planar_dir(u);
     E = E2;
     cur_mat = -2; /* energy changed: cross sections are recomputed */
   }

@@ -90,6 +90,8 @@ int oracle_set_hash_bins(oracle_problem* p, int32_t n_bins);
 int oracle_set_tally(oracle_problem* p, int32_t estimator, int32_t n_scores, const int32_t* scores,
                      int32_t n_energy_bins, const double* edges);
 int64_t oracle_tally_size(const oracle_problem* p);
+/* 2-D mode: planar directions, births at z = z_coord (CollisionKernel z_coord). */
+int oracle_set_2d(oracle_problem* p, int32_t on, double z_coord);
 
 /* Track histories [first, first+n) (0-based history index h, particle id
  * h+1).  tally (n_tet doubles) accumulates raw wgt*track-length sums;

@@ -50,6 +50,7 @@ _SIG = {
     "oracle_set_hash_bins": ([_P, _I32], C.c_int),
     "oracle_set_tally": ([C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "oracle_tally_size": ([C.c_void_p], C.c_int64),
+    "oracle_set_2d": ([C.c_void_p, C.c_int32, C.c_double], C.c_int),
     "oracle_run": ([_P, _I64, _I64, _U64, C.c_int, _P, _P, C.POINTER(OracleStats)], C.c_int),
     "oracle_log": ([_D], _D),
     "oracle_prn": ([C.POINTER(_U64)], _D),
@@ -137,6 +138,8 @@ class Oracle:
         self._ck(lib.oracle_set_source(self.h, C.byref(d)), "oracle_set_source")
         if getattr(p, "tally", None) is not None:
             self.set_tally(p.tally)
+        if getattr(p, "z_2d", None) is not None:
+            lib.oracle_set_2d(self.h, 1, p.z_2d)
         return self
 
     def set_tally(self, t) -> None:

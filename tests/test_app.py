@@ -140,3 +140,34 @@ def test_ray_tracing_exodus_output(tmp_path):
         assert f.dimensions["num_elem"] == rep["ray_segments"]
         ray_id = f.variables["vals_elem_var10eb1"][0]
         assert set(np.unique(ray_id).astype(int)) == set(range(30))
+
+
+def _lattice_2d_input():
+    txt = app.read("lattice.i")
+    txt = txt.replace("nz = 21", "nz = 1").replace("height = 50", "height = 1")
+    txt = txt.replace("materials = '1 2 3'\n[]", "materials = '1 2 3'\n  z_coord = 0.5\n[]")
+    txt = txt.replace("boundary = 'back front top right left bottom'",
+                      "boundary = 'top right left bottom'\n  []\n  [planes]\n    type = ReflectRayBC\n"
+                      "    boundary = 'back front'")
+    return txt.replace("particles = 1000000", "particles = 20000").replace("num_steps = 10", "num_steps = 1")
+
+
+def test_two_d_input_checks():
+    txt = _lattice_2d_input()
+    assert "z_coord = 0.5" in txt and "ReflectRayBC" in txt
+    c = app.check_input(txt)
+    assert c["tets"] == 2039184 // 21 and c["reflective"] == 2
+
+
+@pytest.mark.gpu
+def test_two_d_input_runs_like_the_direct_api(tmp_path):
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_TALLY_SUM
+    rep = app.run_input(_lattice_2d_input(), 0, str(tmp_path / "l2d"))
+    assert rep["histories"] == 20000 and rep["stuck"] == 0
+    p = problems.lattice_2d_problem()
+    with Tracker(0) as t:
+        t.load(p)
+        t.run(20000, seed=1, accumulate=True, bank_size=1000000)
+        ref = t.tally(MC_TALLY_SUM)
+    assert rep["aux"]["flux"]["sum"] == pytest.approx(ref.sum(), rel=1e-12)
