@@ -15,7 +15,11 @@ batches ("steps") of 1,000,000 histories with a 1,000,000-particle bank.
   roofline  HBM roofline of the dominant kernel (the segment walk)
   cpu_baseline  the CPU restatement (oracle) on the host cores, bounded sample
 
-Two more workloads print their own JSON line (not the default run):
+More workloads print their own JSON line (not the default run):
+  --workload cube   the plain FP64 configuration the reference runs on CPU:
+                    the 48,000-tet cube, 1e5 histories per step, FP64 and
+                    mixed, with the oracle's segments and collisions per
+                    history
   --workload core   the batched large-mesh form: cylindrical core, radius
                     180 cm, 400 cm, 41,283,792 tets, 200 materials of 5-40
                     nuclides (30,000-point grids); 1e8 histories in 64
@@ -52,6 +56,11 @@ HIST_PER_STEP = 1_000_000
 BANK = 1_000_000
 B_SEG_FP64 = 164   # algorithmic bytes per segment: planes 128 + neighbours 16 + material 4 + tally RMW 16
 B_SEG_MIXED = 100  # float planes 64 + neighbours 16 + material 4 + tally RMW 16
+# per cross-section event: about 64 B per nuclide evaluated; an event on the
+# lattice evaluates all three materials (15 + 4 + 3 nuclides); a collision
+# re-reads 16 B per nuclide of its material to pick one (fuel: 15)
+B_XS_EVENT = 64 * 22
+B_COLL_PICK = 16 * 15
 CPU_SAMPLE = 400_000
 REF_SAMPLE = 100_000
 # DRAM bytes per walked segment of the walk kernels, from ncu captures of
@@ -141,15 +150,30 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def history_roofline(hist_per_s, S, C, xs_evals, b_seg):
+    """Whole-history algorithmic bytes (segments, cross-section lookups and
+    collision nuclide picks) times histories/s against the HBM peak."""
+    peak, _ = load_peaks()
+    xs_events = xs_evals / 3.0  # each event evaluates the three materials
+    b = S * b_seg + xs_events * B_XS_EVENT + C * B_COLL_PICK
+    return {"bytes_per_history": b, "achieved": hist_per_s * b / 1e9, "unit": "GB/s", "peak": peak,
+            "frac": hist_per_s * b / 1e9 / peak,
+            "formula": "S*B_seg + xs_events*64*22 + C*16*15 (S, C, xs events per history measured)"}
+
+
 def cpu_baseline(problem, sample, seed=1):
     from oracle.oracle import Oracle, cpu_threads
     threads = cpu_threads()
     o = Oracle(problem)
     o.run(2000, first=10**9, seed=seed, threads=threads, traces=False)  # warm caches, page in
     _, _, st, dt = o.run(sample, first=0, seed=seed, threads=threads, traces=False)
+    one = max(2000, sample // 20)
+    _, _, _, dt1 = o.run(one, first=sample, seed=seed, threads=1, traces=False)
     return {"value": sample / dt, "unit": "histories/s", "cores": threads, "kind": "port",
             "sample": f"{sample} histories of the same lattice workload (C oracle, OpenMP over histories)",
-            "seconds": dt, "segments_per_history": st["n_seg"] / sample}
+            "seconds": dt, "segments_per_history": st["n_seg"] / sample,
+            "collisions_per_history": st["n_coll"] / sample,
+            "single_core": {"value": one / dt1, "sample": f"{one} histories on one thread"}}
 
 
 def run_reference(args):
@@ -253,6 +277,46 @@ def run_core(args):
     return 0
 
 
+def run_cube(args):
+    """The plain FP64 configuration the reference runs on CPU: the 48,000-tet
+    cube, 1e5 histories per step (one JSON line); S and C from the oracle."""
+    import torch
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED
+    from oracle.oracle import Oracle, cpu_threads
+    torch.cuda.set_device(0)
+    p = problems.cube_problem()
+    n, K = 100_000, max(args.steps, 1)
+    o = Oracle(p)
+    threads = cpu_threads()
+    _, _, ost, odt = o.run(n, first=0, seed=1, threads=threads, traces=False)
+    res = {}
+    with Tracker(0) as t:
+        t.load(p)
+        for name, prec in (("fp64", MC_PREC_FP64), ("mixed", MC_PREC_MIXED)):
+            kw = dict(seed=1, precision=prec, accumulate=True, bank_size=n, max_seg=64, sort_queue=0, graph=True)
+            t.run(n * 3, first=10**8, batch_sizes=[n] * 3, **kw)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            st = t.run(n * K, first=0, batch_sizes=[n] * K, **kw)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            res[name] = {"value": n * K / (ms / 1e3), "ms_per_step": ms / K, "segments_per_history": st.n_seg / (n * K),
+                         "collisions_per_history": st.n_coll / (n * K), "stuck": int(st.n_stuck), "lost": int(st.n_lost)}
+    out = {"metric": "histories/s, plain FP64 cube configuration", "unit": "histories/s", "n_gpus": 1,
+           "value": res["fp64"]["value"], "higher_is_better": True, "dtype": "f64", "steps": K,
+           "data": "synthetic (seeded generators)",
+           "config": {"workload": "cube 20 cm, 20^3 hexes x 6 tets (48,000 tets), 1 material x 10 nuclides x "
+                                  "10,000 pts, point source at the centre, 1e5 histories per step", "tets": p.n_tet},
+           "fp64": res["fp64"], "mixed": res["mixed"],
+           "oracle": {"segments_per_history": ost["n_seg"] / n, "collisions_per_history": ost["n_coll"] / n,
+                      "histories_per_s": n / odt, "cores": threads}}
+    print(json.dumps(out))
+    return 0
+
+
 def serve_problems():
     from macaw_gb300 import problems
     cubes = [(12, 12.0), (20, 20.0), (40, 40.0), (60, 60.0)]
@@ -305,7 +369,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (fixed parameters)")
     ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
-    ap.add_argument("--workload", default="lattice", choices=["lattice", "core", "serve"])
+    ap.add_argument("--workload", default="lattice", choices=["lattice", "cube", "core", "serve"])
     ap.add_argument("--core-histories", type=int, default=100_000_000)
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     args = ap.parse_args()
@@ -314,6 +378,8 @@ def main():
         return run_reference(args)
     if args.workload == "core":
         return run_core(args)
+    if args.workload == "cube":
+        return run_cube(args)
     if args.workload == "serve":
         return run_serve(args)
 
@@ -403,7 +469,9 @@ def main():
                  "flux_rel_diff_mean": float(rel.mean()), "flux_rel_diff_max": float(rel.max()),
                  "flux_rel_diff_note": "element SUM tallies, mixed vs FP64 (bit-exact to the oracle), same "
                                        f"{n * (W + K)} histories, elements with a score",
-                 "tuned": paramsm, "gpu_launches": int(mst.n_launch)}
+                 "tuned": paramsm, "gpu_launches": int(mst.n_launch),
+                 "roofline_history": history_roofline(world * n * K / (mms / 1e3), mst.n_seg / (n * K),
+                                                      mst.n_coll / (n * K), mst.n_xs / (n * K), B_SEG_MIXED)}
         if pst.ms_advance > 0:
             mach = pst.n_seg_advance * B_SEG_MIXED / (pst.ms_advance / 1e3) / 1e9
             mixed["roofline"] = {"bound": "hbm", "kernel": "k_ev_advance<MIXED>" if paramsm.get("refill")
@@ -494,6 +562,8 @@ def main():
                 "data": "synthetic (seeded generators; the reference's meshes and ENDF data are not shipped)",
                 "config": cfg, "segments_per_s": world * segs / (ms / 1e3), "segments_per_history": segs / (n * K),
                 "collisions_per_history": st.n_coll / (n * K),
+                "roofline_history": history_roofline(value, segs / (n * K), st.n_coll / (n * K),
+                                                     st.n_xs / (n * K), B_SEG_FP64),
                 "stuck": int(st.n_stuck), "lost": int(st.n_lost),
                 "roofline": roof, "e2e": e2e, "gpu_launches": int(st.n_launch), "clocks": clk}
         if mixed is not None:

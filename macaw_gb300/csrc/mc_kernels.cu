@@ -303,21 +303,30 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
   const int n = *(volatile int*)&ctl->n_xs[par];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int s = Q.xs[par][i];
+    // only the fields a cross-section event reads: element, energy, cache
     Particle p;
-    load(B, s, p);
-    if (refresh_xs(M, X, a.n_mat, a.precision == MC_PREC_MIXED, p, L)) {
+    p.elem = B.elem[s];
+    p.E = B.E[s];
+    p.cm = B.cm[s];
+    const double4_32a c0 = B.cs[s];
+    p.cs0 = c0.x; p.cs1 = c0.y; p.cs2 = c0.z; p.cs3 = c0.w;
+    p.status = kAlive;
+    const bool f32 = a.precision == MC_PREC_MIXED;
+    if (refresh_xs(M, X, a.n_mat, f32, p, L)) {
       B.sigt[s] = p.sigt;
       B.mat[s] = p.mat;
       B.cm[s] = p.cm;
       double4_32a c;
       c.x = p.cs0; c.y = p.cs1; c.z = p.cs2; c.w = p.cs3;
       B.cs[s] = c;
-      if (a.precision == MC_PREC_MIXED) {
-        B.cinv[s] = make_float4(p.cm.x >= 0 ? (float)(1.0 / p.cs0) : 0.0f, p.cm.y >= 0 ? (float)(1.0 / p.cs1) : 0.0f,
-                                p.cm.z >= 0 ? (float)(1.0 / p.cs2) : 0.0f, p.cm.w >= 0 ? (float)(1.0 / p.cs3) : 0.0f);
+      if (f32) {  // the cached values are floats widened: their float inverses
+        B.cinv[s] = make_float4(p.cm.x >= 0 ? 1.0f / narrow(p.cs0) : 0.0f, p.cm.y >= 0 ? 1.0f / narrow(p.cs1) : 0.0f,
+                                p.cm.z >= 0 ? 1.0f / narrow(p.cs2) : 0.0f, p.cm.w >= 0 ? 1.0f / narrow(p.cs3) : 0.0f);
       }
       push(Q.adv[par], &ctl->n_adv[par], s);
     } else {
+      load(B, s, p);  // the history ends: all of it
+      p.status = kBadXS;
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
     }
@@ -697,11 +706,23 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
   const int nxt = par ^ 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int s = Q.coll[i];
+    // only the fields a collision reads; the rest when the history ends here
     Particle p;
-    load(B, s, p);
+    p.E = B.E[s]; p.wgt = B.wgt[s]; p.sigt = B.sigt[s];
+    p.u = B.u[s]; p.v = B.v[s]; p.w = B.w[s];
+    p.seed = B.seed[s];
+    p.elem = B.elem[s]; p.mat = B.mat[s]; p.tag = B.tag[s];
+    p.status = kAlive;
     score_collision(X, a.ts, tally_of(a, p.tag), p);
     collide(X, p, a.two_d);
     if (p.status != kAlive) {
+      const int status = p.status;
+      const double E = p.E;
+      const uint64_t seed = p.seed;
+      load(B, s, p);
+      p.status = status;
+      p.E = E;
+      p.seed = seed;
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
       continue;
