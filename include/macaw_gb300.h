@@ -102,6 +102,20 @@ typedef struct {
   double wgt;
 } mc_site;
 
+/* One fission site (OpenMC SourceSite as create_fission_sites fills it):
+ * collision point, isotropic direction, prompt energy, weight 1, the id of
+ * the history that banked it and its index among that history's sites --
+ * the key OpenMC's sort_fission_bank orders the bank by. */
+typedef struct {
+  double x, y, z;
+  double u, v, w;
+  double E;
+  double wgt;
+  int64_t parent;
+  int32_t progeny;
+  int32_t pad;
+} mc_fission_site;
+
 /* One batch of histories (OpenMCStudy::generateRays + execute +
  * postExecuteStudy for a fixed-source batch;
  * src/userobjects/OpenMCStudy.C:218-242,366-402). */
@@ -230,6 +244,69 @@ int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_histories, m
  * lattice generator with nz = 1); a 2-D element's result is the sum over
  * the tets of its prism. */
 int mc_set_2d(mc_ctx* ctx, int32_t on, double z_coord);
+
+/* ---- k-eigenvalue runs -------------------------------------------------
+ * Replaces: OpenMC's eigenvalue run mode as OpenMCStudy drives it, one
+ * generation per batch (src/userobjects/OpenMCStudy.C:297-364 births from
+ * the source bank; :374-402 postExecuteStudy -> finalize_generation;
+ * :404-607 finalizeGeneration / synchronizeBanks) with the track-length
+ * keff score of CollisionKernel.C:153-154. */
+
+/* Fission data of a nuclide: nu*sigma_f (barn) at each point of the
+ * nuclide's energy grid (n_pts values, as given to mc_nuclide_add); NULL
+ * makes it non-fissionable.  A fissionable nuclide samples fission sites at
+ * every collision with it (OpenMC create_fission_sites): banked in
+ * eigenvalue runs, drawn and dropped in fixed-source runs. */
+int mc_nuclide_set_fission(mc_ctx* ctx, int32_t nuclide, const double* nu_sig_f);
+
+typedef struct {
+  int64_t n_particles;     /* settings particles: histories per generation */
+  int32_t n_batches;       /* settings batches: generations run by this call */
+  int32_t n_inactive;      /* settings inactive: generations that score no tally */
+  uint64_t seed;           /* master seed */
+  int32_t precision;       /* MC_PREC_* */
+  int32_t mode;            /* MC_MODE_* */
+  int64_t bank_size;       /* event form: particles in flight; 0 = all */
+  int32_t block_size;      /* 0 = default */
+  int32_t max_seg_per_advance; /* event form, as mc_run_desc */
+  int32_t sort_queue;      /* event form, as mc_run_desc */
+  int32_t graph;           /* event form, as mc_run_desc */
+  double keff0;            /* keff the first generation divides by (0: 1.0, OpenMC's start value) */
+  double watt_a, watt_b;   /* prompt fission spectrum (0: 0.988e6 eV, 2.249e-6 /eV) */
+  int64_t fission_bank_capacity; /* sites a generation may bank (0: 3 * n_particles, OpenMC's reservation) */
+  const mc_site* initial_source; /* optional HOST array of n_particles sites; NULL: sampled from the
+                                    source (mc_source_set) as OpenMC initialize_source does */
+} mc_eigen_desc;
+
+/* Results of one generation. */
+typedef struct {
+  double k_generation;     /* track-length estimate: sum of wgt*min(d,L)*nu*Sigma_f / n_particles */
+  double k_collision;      /* collision estimate: sum of wgt*nu*Sigma_f/Sigma_t / n_particles */
+  double k_absorption;     /* absorption estimate: sum of wgt*nu*sigma_f/sigma_a / n_particles */
+  double keff;             /* running estimate after this generation (OpenMC calculate_average_keff) */
+  double keff_std;         /* its standard deviation (0 until two active generations) */
+  double leakage;          /* leaked weight / n_particles */
+  int64_t n_sites;         /* fission sites banked */
+  int64_t n_seg, n_coll;
+  double ms;               /* device time of the generation, bank resampling included */
+} mc_eigen_gen;
+
+/* Runs n_batches generations of n_particles histories.  Generation g
+ * (0-based) tracks histories with ids g*n_particles + 1.. (tracking stream
+ * seeded from the id); the first starts from initial_source or the sampled
+ * source.  After each generation the fission bank is put in (parent id,
+ * progeny index) order and resampled to exactly n_particles sites
+ * (synchronizeBanks, OpenMCStudy.C:430-607, with one rank); keff
+ * estimators are summed over histories in a fixed order.  Active
+ * generations add their tally to SUM/SUM_SQ (one batch each).  out
+ * receives n_batches records.  MC_ERR_DEVICE when a generation banks no
+ * site or more than the capacity. */
+int mc_eigen_run(mc_ctx* ctx, const mc_eigen_desc* desc, mc_eigen_gen* out);
+/* The source sites of the next generation (n_particles, after the last
+ * generation's resampling). */
+int mc_eigen_source_download(mc_ctx* ctx, mc_site* out, int64_t n);
+/* The last generation's fission bank in sort order; *n_out = its size. */
+int mc_eigen_fission_bank_download(mc_ctx* ctx, mc_fission_site* out, int64_t capacity, int64_t* n_out);
 
 /* ---- tally definition ------------------------------------------------- */
 typedef struct {

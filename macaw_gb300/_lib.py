@@ -48,6 +48,14 @@ class RunDesc(C.Structure):
                 ("pad", C.c_int32), ("sites", C.c_void_p), ("batch_sizes", C.c_void_p)]
 
 
+class EigenDesc(C.Structure):
+    _fields_ = [("n_particles", C.c_int64), ("n_batches", C.c_int32), ("n_inactive", C.c_int32),
+                ("seed", C.c_uint64), ("precision", C.c_int32), ("mode", C.c_int32), ("bank_size", C.c_int64),
+                ("block_size", C.c_int32), ("max_seg_per_advance", C.c_int32), ("sort_queue", C.c_int32),
+                ("graph", C.c_int32), ("keff0", C.c_double), ("watt_a", C.c_double), ("watt_b", C.c_double),
+                ("fission_bank_capacity", C.c_int64), ("initial_source", C.c_void_p)]
+
+
 class Request(C.Structure):
     _fields_ = [("n_histories", C.c_int64), ("seed", C.c_uint64), ("source", SourceDesc)]
 
@@ -73,6 +81,14 @@ RAY_SEGMENT_DTYPE = np.dtype([("id", "<i8"), ("segment", "<i4"), ("intersections
 SITE_DTYPE = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("u", "<f8"), ("v", "<f8"),
                        ("w", "<f8"), ("E", "<f8"), ("wgt", "<f8")])
 
+FISSION_SITE_DTYPE = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("u", "<f8"), ("v", "<f8"),
+                               ("w", "<f8"), ("E", "<f8"), ("wgt", "<f8"), ("parent", "<i8"), ("progeny", "<i4"),
+                               ("pad", "<i4")])
+
+EIGEN_GEN_DTYPE = np.dtype([("k_generation", "<f8"), ("k_collision", "<f8"), ("k_absorption", "<f8"),
+                            ("keff", "<f8"), ("keff_std", "<f8"), ("leakage", "<f8"), ("n_sites", "<i8"),
+                            ("n_seg", "<i8"), ("n_coll", "<i8"), ("ms", "<f8")])
+
 _P = C.c_void_p
 _I32, _I64, _U64, _D = C.c_int32, C.c_int64, C.c_uint64, C.c_double
 
@@ -85,6 +101,10 @@ SIGNATURES = {
     "mc_bc_set": ([_P, _I32, _I32], C.c_int),
     "mc_nuclide_add": ([_P, _I64, _P, _P, _P, _D, C.POINTER(_I32)], C.c_int),
     "mc_material_add": ([_P, _I32, _I32, _P, _P], C.c_int),
+    "mc_nuclide_set_fission": ([_P, _I32, _P], C.c_int),
+    "mc_eigen_run": ([_P, C.POINTER(EigenDesc), _P], C.c_int),
+    "mc_eigen_source_download": ([_P, _P, _I64], C.c_int),
+    "mc_eigen_fission_bank_download": ([_P, _P, _I64, C.POINTER(_I64)], C.c_int),
     "mc_block_material_map": ([_P, _I32, _P, _P], C.c_int),
     "mc_set_hash_bins": ([_P, _I32], C.c_int),
     "mc_source_set": ([_P, C.POINTER(SourceDesc)], C.c_int),

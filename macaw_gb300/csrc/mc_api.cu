@@ -73,6 +73,7 @@ struct mc_ctx {
   // device copies
   DevBuf d_planes, d_tet, d_tmat, d_bc, d_gstart, d_gtets, d_gseed;
   DevBuf d_gE, d_goff, d_gn, d_ghidx, d_nuc_grid, d_nuc_off, d_sig, d_awr, d_mat_off, d_mat_nuc, d_mat_dens;
+  DevBuf d_nusf, d_nuc_fiss, d_mat_fiss;
   DevBuf d_cyl;
   DevBuf d_tally, d_sum, d_sumsq;
   DevBuf d_counters, d_leak_w;
@@ -100,6 +101,13 @@ struct mc_ctx {
   // event bank
   DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
   DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_tag, b_cm, b_cs, b_cinv;
+  DevBuf b_nuf, b_ktl, b_cn, b_nprog;  // k-eigenvalue runs only
+  // k-eigenvalue state (mc_eigen_run): source sites of the next generation,
+  // the last generation's fission bank (append order, then sorted),
+  // per-history estimator sums and site counts, scan scratch
+  DevBuf e_src, e_bank, e_sorted, e_ktl, e_kcol, e_kabs, e_prog, e_off, e_cnt, e_pos, e_tmp, e_part, e_nbank;
+  int64_t e_n = 0;      // sites in e_src
+  int64_t e_m = 0;      // sites in e_sorted
   DevBuf q_xs0, q_xs1, q_adv0, q_adv1, q_coll, q_free, d_ctl;
   int64_t bank_cap = 0;
 
@@ -109,6 +117,8 @@ struct mc_ctx {
 };
 
 namespace {
+
+int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const EigArgs* eig);
 
 int set_err(mc_ctx* c, int code, const std::string& msg) {
   c->err = msg;
@@ -152,6 +162,9 @@ int ensure_device_tables(mc_ctx* c) {
     CK(upload(c->d_mat_off, c->xs.mat_off, c->stream), "upload materials");
     CK(upload(c->d_mat_nuc, c->xs.mat_nuc, c->stream), "upload materials");
     CK(upload(c->d_mat_dens, c->xs.mat_dens, c->stream), "upload materials");
+    CK(upload(c->d_nusf, c->xs.nusf, c->stream), "upload fission data");
+    CK(upload(c->d_nuc_fiss, c->xs.nuc_fiss, c->stream), "upload fission data");
+    CK(upload(c->d_mat_fiss, c->xs.mat_fiss, c->stream), "upload fission data");
     c->xs_dirty = false;
     c->tmat_dirty = true;
   }
@@ -233,6 +246,9 @@ DevXS dev_xs(mc_ctx* c) {
   X.mat_off = c->d_mat_off.as<int>();
   X.mat_nuc = c->d_mat_nuc.as<int>();
   X.mat_dens = c->d_mat_dens.as<double>();
+  X.nusf = c->xs.nusf.empty() ? nullptr : c->d_nusf.as<double>();
+  X.nuc_fiss = c->d_nuc_fiss.as<int>();
+  X.mat_fiss = c->d_mat_fiss.as<int>();
   X.n_nuc = (int)c->xs.nuc_grid.size();
   X.n_grid = (int)c->xs.g_n.size();
   X.n_bins = c->xs.n_bins;
@@ -280,6 +296,17 @@ int ensure_bank(mc_ctx* c, int64_t cap) {
   return MC_OK;
 }
 
+// k-eigenvalue fields of the particle bank, sized to the bank.
+int ensure_eig_bank(mc_ctx* c) {
+  const size_t n = (size_t)c->bank_cap;
+  if (c->b_cn.bytes >= n * 32 && c->b_cn.p) return MC_OK;
+  CK(c->b_nuf.alloc(n * 8), "allocate eigenvalue bank fields");
+  CK(c->b_ktl.alloc(n * 8), "allocate eigenvalue bank fields");
+  CK(c->b_cn.alloc(n * 32), "allocate eigenvalue bank fields");
+  CK(c->b_nprog.alloc(n * 4), "allocate eigenvalue bank fields");
+  return MC_OK;
+}
+
 Bank dev_bank(mc_ctx* c) {
   Bank B{};
   B.x = c->b_x.as<double>(); B.y = c->b_y.as<double>(); B.z = c->b_z.as<double>();
@@ -291,6 +318,12 @@ Bank dev_bank(mc_ctx* c) {
   B.cm = c->b_cm.as<int4>(); B.cs = c->b_cs.as<double4_32a>(); B.fin = c->b_fin.as<int>();
   B.cinv = c->b_cinv.as<float4>();
   B.tag = c->b_tag.as<int>();
+  if (c->b_cn.p && c->b_cn.bytes >= (size_t)c->bank_cap * 32) {
+    B.nuf = c->b_nuf.as<double>();
+    B.ktl = c->b_ktl.as<double>();
+    B.cn = c->b_cn.as<double4_32a>();
+    B.n_prog = c->b_nprog.as<int>();
+  }
   B.cap = c->bank_cap;
   return B;
 }
@@ -431,6 +464,23 @@ int mc_nuclide_add(mc_ctx* c, int64_t n_pts, const double* E, const double* sig_
   return MC_OK;
 }
 
+int mc_nuclide_set_fission(mc_ctx* c, int32_t nuclide, const double* nu_sig_f) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (nuclide < 0 || nuclide >= (int32_t)c->nucs.size()) return set_err(c, MC_ERR_ARG, "nuclide index out of range");
+  Nuclide& n = c->nucs[nuclide];
+  if (!nu_sig_f) {
+    n.nusf.clear();
+  } else {
+    for (size_t i = 0; i < n.E.size(); ++i)
+      if (!(nu_sig_f[i] >= 0.0) || !(nu_sig_f[i] < 1e300))
+        return set_err(c, MC_ERR_ARG, "nu*sigma_f must be finite and non-negative");
+    n.nusf.assign(nu_sig_f, nu_sig_f + n.E.size());
+  }
+  c->xs_dirty = true;
+  return MC_OK;
+}
+
 int mc_material_add(mc_ctx* c, int32_t material_id, int32_t n, const int32_t* nuclides,
                     const double* densities) {
   if (!c) return MC_ERR_ARG;
@@ -497,6 +547,17 @@ int mc_source_set(mc_ctx* c, const mc_source_desc* s) {
 int mc_run(mc_ctx* c, const mc_run_desc* d) {
   if (!c || !d) return MC_ERR_ARG;
   std::lock_guard<std::mutex> g(c->mu);
+  return run_locked(c, d, nullptr, nullptr);
+}
+
+}  // extern "C"
+
+namespace {
+
+// One run of histories (mc_run's body, with the context lock held).
+// dev_sites: DEVICE source sites of the n_histories histories (instead of
+// d->sites or sampling); eig: k-eigenvalue generation state, or null.
+int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const EigArgs* eig) {
   if (d->n_histories < 0 || d->first_history < 0) return set_err(c, MC_ERR_ARG, "negative history range");
   if (d->precision != MC_PREC_FP64 && d->precision != MC_PREC_MIXED)
     return set_err(c, MC_ERR_ARG, "unknown precision form");
@@ -552,13 +613,18 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
     }
     a.tol = (float)(1e-6 * sqrt(dg));
   }
-  if (d->sites && d->n_histories > 0) {
+  if (dev_sites) {
+    a.sites = dev_sites;
+  } else if (d->sites && d->n_histories > 0) {
     CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)d->n_histories)), "allocate sites");
     CK(cudaMemcpyAsync(c->d_sites.p, d->sites, sizeof(mc_site) * (size_t)d->n_histories,
                        cudaMemcpyHostToDevice, c->stream),
        "upload sites");
     a.sites = c->d_sites.as<mc_site>();
   }
+  a.eig = EigArgs{};
+  a.eig.keff = 1.0;
+  if (eig) a.eig = *eig;
   const DevMesh M = dev_mesh(c);
   const DevXS X = dev_xs(c);
   const DevSource S = dev_source(c);
@@ -663,8 +729,14 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
       if (cap > ((int64_t)1 << 30)) return set_err(c, MC_ERR_ARG, "bank too large");
       rc = ensure_bank(c, std::max(cap, c->bank_cap));
       if (rc) return rc;
+      if (a.eig.on) {
+        rc = ensure_eig_bank(c);
+        if (rc) return rc;
+      }
       const Bank B = dev_bank(c);
       if (!bank_complete(B)) return set_err(c, MC_ERR_STATE, "internal: particle bank incomplete");
+      if (a.eig.on && !(B.nuf && B.ktl && B.cn && B.n_prog))
+        return set_err(c, MC_ERR_STATE, "internal: eigenvalue bank fields missing");
       const EventQueues Q = dev_queues(c);
       EventCtl* ctl = c->d_ctl.as<EventCtl>();
       int h_live[kPipeSlots] = {0};
@@ -818,6 +890,10 @@ int mc_run(mc_ctx* c, const mc_run_desc* d) {
                                          std::to_string(d->n_histories) + " histories");
   return MC_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int mc_source_sample(mc_ctx* c, int64_t first, int64_t n, uint64_t seed, mc_site* out) {
   if (!c || (!out && n > 0)) return MC_ERR_ARG;
@@ -1033,6 +1109,211 @@ int mc_batches_done(mc_ctx* c, int64_t* out) {
   if (!c || !out) return MC_ERR_ARG;
   std::lock_guard<std::mutex> g(c->mu);
   *out = c->batches;
+  return MC_OK;
+}
+
+// k-eigenvalue generations (OpenMCStudy's batch loop in eigenvalue mode:
+// defineRays from the source bank, execute, postExecuteStudy ->
+// finalize_generation -> sort, synchronize_bank, calculate_generation_keff,
+// calculate_average_keff; src/userobjects/OpenMCStudy.C:297-607).
+int mc_eigen_run(mc_ctx* c, const mc_eigen_desc* d, mc_eigen_gen* out) {
+  if (!c || !d || !out) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  const int64_t n = d->n_particles;
+  if (n < 1 || n > ((int64_t)1 << 30)) return set_err(c, MC_ERR_ARG, "particles must be in [1, 2^30]");
+  if (d->n_batches < 1) return set_err(c, MC_ERR_ARG, "batches must be at least 1");
+  if (d->n_inactive < 0 || d->n_inactive >= d->n_batches)
+    return set_err(c, MC_ERR_ARG, "inactive batches must be in [0, batches)");
+  if (!d->initial_source && !c->have_src) return set_err(c, MC_ERR_STATE, "no source (mc_source_set)");
+  if (c->serving && d->mode == MC_MODE_EVENT)
+    return set_err(c, MC_ERR_STATE, "a serving session holds this context's event state (mc_serve_close)");
+  if (d->watt_a < 0.0 || d->watt_b < 0.0 || d->keff0 < 0.0)
+    return set_err(c, MC_ERR_ARG, "keff0 and the fission spectrum parameters must be non-negative");
+  cudaSetDevice(c->device);
+  int rc = ensure_device_tables(c);
+  if (rc) return rc;
+  if (c->xs.nusf.empty()) return set_err(c, MC_ERR_STATE, "no fissionable nuclide (mc_nuclide_set_fission)");
+  const int64_t cap = d->fission_bank_capacity > 0 ? d->fission_bank_capacity : 3 * n;
+  if (cap > ((int64_t)1 << 31) - 1) return set_err(c, MC_ERR_ARG, "fission bank capacity too large");
+  auto grow = [&](DevBuf& b, size_t need) -> cudaError_t {
+    return b.bytes >= need && b.p ? cudaSuccess : b.alloc(need);
+  };
+  const int64_t nt = (n + kReduceTile - 1) / kReduceTile;
+  CK(grow(c->e_src, sizeof(mc_site) * (size_t)n), "allocate source bank");
+  CK(grow(c->e_bank, sizeof(mc_fission_site) * (size_t)cap), "allocate fission bank");
+  CK(grow(c->e_sorted, sizeof(mc_fission_site) * (size_t)cap), "allocate fission bank");
+  CK(grow(c->e_ktl, sizeof(double) * (size_t)n), "allocate estimators");
+  CK(grow(c->e_kcol, sizeof(double) * (size_t)n), "allocate estimators");
+  CK(grow(c->e_kabs, sizeof(double) * (size_t)n), "allocate estimators");
+  CK(grow(c->e_prog, sizeof(int) * (size_t)n), "allocate site counts");
+  CK(grow(c->e_off, sizeof(int64_t) * (size_t)(n + 1)), "allocate bank offsets");
+  CK(grow(c->e_cnt, sizeof(int) * (size_t)cap), "allocate resampling counts");
+  CK(grow(c->e_pos, sizeof(int64_t) * (size_t)(cap + 1)), "allocate resampling offsets");
+  CK(grow(c->e_tmp, sizeof(int64_t) * (size_t)std::max(scan_tmp_size(n), scan_tmp_size(cap))), "allocate scan");
+  CK(grow(c->e_part, sizeof(double) * (size_t)(3 * nt)), "allocate partial sums");
+  CK(grow(c->e_nbank, sizeof(unsigned long long)), "allocate site counter");
+  c->e_n = 0;
+  c->e_m = 0;
+  if (d->initial_source) {
+    CK(cudaMemcpyAsync(c->e_src.p, d->initial_source, sizeof(mc_site) * (size_t)n, cudaMemcpyHostToDevice,
+                       c->stream),
+       "upload initial source");
+  } else {
+    // OpenMC initialize_source: site i from the source stream of id i+1
+    CK(launch_sample(dev_xs(c), dev_source(c), 0, n, d->seed, c->e_src.as<mc_site>(), c->stream),
+       "sample initial source");
+  }
+  cudaEvent_t g0 = nullptr, g1 = nullptr;
+  CK(cudaEventCreate(&g0), "event");
+  struct EvGuard {
+    cudaEvent_t* a;
+    cudaEvent_t* b;
+    ~EvGuard() {
+      if (*a) cudaEventDestroy(*a);
+      if (*b) cudaEventDestroy(*b);
+    }
+  } evg{&g0, &g1};
+  CK(cudaEventCreate(&g1), "event");
+  std::vector<double> part((size_t)(3 * nt));
+  double keff = d->keff0 > 0.0 ? d->keff0 : 1.0;
+  double k_sum0 = 0.0, k_sum1 = 0.0, keff_std = 0.0;
+  int n_active = 0;
+  for (int gen = 0; gen < d->n_batches; ++gen) {
+    const bool active = gen >= d->n_inactive;
+    const int64_t first = (int64_t)gen * n;
+    CK(cudaEventRecord(g0, c->stream), "event");
+    CK(cudaMemsetAsync(c->e_ktl.p, 0, sizeof(double) * (size_t)n, c->stream), "clear estimators");
+    CK(cudaMemsetAsync(c->e_kcol.p, 0, sizeof(double) * (size_t)n, c->stream), "clear estimators");
+    CK(cudaMemsetAsync(c->e_kabs.p, 0, sizeof(double) * (size_t)n, c->stream), "clear estimators");
+    CK(cudaMemsetAsync(c->e_prog.p, 0, sizeof(int) * (size_t)n, c->stream), "clear site counts");
+    CK(cudaMemsetAsync(c->e_nbank.p, 0, sizeof(unsigned long long), c->stream), "clear site counter");
+    EigArgs e{};
+    e.on = 1;
+    e.keff = keff;
+    e.fa = d->watt_a > 0.0 ? d->watt_a : 0.988e6;
+    e.fb = d->watt_b > 0.0 ? d->watt_b : 2.249e-6;
+    e.first = first;
+    e.bank = c->e_bank.as<mc_fission_site>();
+    e.n_bank = c->e_nbank.as<unsigned long long>();
+    e.cap = cap;
+    e.ktl = c->e_ktl.as<double>();
+    e.kcol = c->e_kcol.as<double>();
+    e.kabs = c->e_kabs.as<double>();
+    e.prog = c->e_prog.as<int>();
+    mc_run_desc rd{};
+    rd.first_history = first;
+    rd.n_histories = n;
+    rd.bank_size = d->bank_size;
+    rd.seed = d->seed;
+    rd.precision = d->precision;
+    rd.mode = d->mode;
+    rd.block_size = d->block_size;
+    rd.max_seg_per_advance = d->max_seg_per_advance;
+    rd.sort_queue = d->sort_queue;
+    rd.graph = d->graph;
+    rd.accumulate = active ? 1 : 0;  // OpenMC scores tallies in active batches only
+    rc = run_locked(c, &rd, c->e_src.as<mc_site>(), &e);
+    if (rc) return rc;
+    if (!active) CK(cudaMemsetAsync(c->d_tally.p, 0, c->d_tally.bytes, c->stream), "clear batch tally");
+    const mc_stats st = c->last;
+    // estimator sums in a fixed order: tree per tile of 1024, then tiles in order
+    double* dp = c->e_part.as<double>();
+    CK(launch_tile_sums(c->e_ktl.as<double>(), n, dp, c->stream), "sum estimators");
+    CK(launch_tile_sums(c->e_kcol.as<double>(), n, dp + nt, c->stream), "sum estimators");
+    CK(launch_tile_sums(c->e_kabs.as<double>(), n, dp + 2 * nt, c->stream), "sum estimators");
+    unsigned long long m_all = 0;
+    CK(cudaMemcpyAsync(part.data(), dp, sizeof(double) * (size_t)(3 * nt), cudaMemcpyDeviceToHost, c->stream),
+       "read estimators");
+    CK(cudaMemcpyAsync(&m_all, c->e_nbank.p, sizeof m_all, cudaMemcpyDeviceToHost, c->stream), "read site count");
+    CK(cudaStreamSynchronize(c->stream), "generation");
+    double s_tl = 0.0, s_col = 0.0, s_abs = 0.0;
+    for (int64_t b = 0; b < nt; ++b) {
+      s_tl = s_tl + part[(size_t)b];
+      s_col = s_col + part[(size_t)(nt + b)];
+      s_abs = s_abs + part[(size_t)(2 * nt + b)];
+    }
+    if (m_all > (unsigned long long)cap)
+      return set_err(c, MC_ERR_DEVICE, "fission bank full: " + std::to_string(m_all) + " sites for a capacity of " +
+                                           std::to_string(cap) + " (fission_bank_capacity)");
+    const int64_t m = (int64_t)m_all;
+    if (m == 0) return set_err(c, MC_ERR_DEVICE, "no fission sites sampled, cannot sample a new generation");
+    // sort_fission_bank: (parent, progeny) order via the per-history counts
+    CK(launch_scan(c->e_prog.as<int>(), n, c->e_off.as<int64_t>(), c->e_tmp.as<int64_t>(), c->stream),
+       "scan site counts");
+    CK(launch_bank_sort(c->e_bank.as<mc_fission_site>(), m, c->e_off.as<int64_t>(), first, n,
+                        c->e_sorted.as<mc_fission_site>(), c->stream),
+       "sort fission bank");
+    // synchronize_bank with one rank (start = 0)
+    const int64_t needed = m < n ? n % m : n;
+    const double p_sample = (double)needed / (double)m;
+    const int copies = m < n ? (int)(n / m) : 0;
+    const uint64_t seed0 = stream_seed(skip_ahead((uint64_t)(gen + 1) * kPrnStride), d->seed, kStreamTracking);
+    CK(launch_bank_counts(m, seed0, copies, p_sample, c->e_cnt.as<int>(), c->stream), "resample fission bank");
+    CK(launch_scan(c->e_cnt.as<int>(), m, c->e_pos.as<int64_t>(), c->e_tmp.as<int64_t>(), c->stream),
+       "resample fission bank");
+    CK(launch_bank_fill(c->e_sorted.as<mc_fission_site>(), m, c->e_pos.as<int64_t>(), n, c->e_src.as<mc_site>(),
+                        c->stream),
+       "resample fission bank");
+    int64_t off_n = 0;
+    CK(cudaMemcpyAsync(&off_n, c->e_off.as<int64_t>() + n, sizeof off_n, cudaMemcpyDeviceToHost, c->stream),
+       "read bank size");
+    CK(cudaEventRecord(g1, c->stream), "event");
+    CK(cudaStreamSynchronize(c->stream), "resample fission bank");
+    if (off_n != m)
+      return set_err(c, MC_ERR_DEVICE, "fission bank holds " + std::to_string(m) + " sites but histories counted " +
+                                           std::to_string(off_n));
+    c->e_n = n;
+    c->e_m = m;
+    // calculate_generation_keff / calculate_average_keff
+    const double k_gen = s_tl / (double)n;
+    if (!active) {
+      keff = k_gen;
+    } else {
+      ++n_active;
+      k_sum0 += k_gen;
+      k_sum1 += k_gen * k_gen;
+      keff = k_sum0 / (double)n_active;
+      if (n_active > 1) keff_std = sqrt((k_sum1 / (double)n_active - keff * keff) / (double)(n_active - 1));
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, g0, g1);
+    mc_eigen_gen& o = out[gen];
+    o.k_generation = k_gen;
+    o.k_collision = s_col / (double)n;
+    o.k_absorption = s_abs / (double)n;
+    o.keff = keff;
+    o.keff_std = keff_std;
+    o.leakage = st.leak_weight / (double)n;
+    o.n_sites = m;
+    o.n_seg = st.n_seg;
+    o.n_coll = st.n_coll;
+    o.ms = ms;
+  }
+  return MC_OK;
+}
+
+int mc_eigen_source_download(mc_ctx* c, mc_site* out, int64_t n) {
+  if (!c || (!out && n > 0)) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n != c->e_n) return set_err(c, MC_ERR_ARG, "n must equal the last eigenvalue run's particles");
+  if (n == 0) return MC_OK;
+  cudaSetDevice(c->device);
+  CK(cudaMemcpyAsync(out, c->e_src.p, sizeof(mc_site) * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+     "download source bank");
+  CK(cudaStreamSynchronize(c->stream), "download source bank");
+  return MC_OK;
+}
+
+int mc_eigen_fission_bank_download(mc_ctx* c, mc_fission_site* out, int64_t capacity, int64_t* n_out) {
+  if (!c || !n_out || (!out && capacity > 0)) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  *n_out = c->e_m;
+  const int64_t k = std::min(capacity, c->e_m);
+  if (k <= 0) return MC_OK;
+  cudaSetDevice(c->device);
+  CK(cudaMemcpyAsync(out, c->e_sorted.p, sizeof(mc_fission_site) * (size_t)k, cudaMemcpyDeviceToHost, c->stream),
+     "download fission bank");
+  CK(cudaStreamSynchronize(c->stream), "download fission bank");
   return MC_OK;
 }
 

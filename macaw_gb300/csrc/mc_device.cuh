@@ -87,8 +87,33 @@ struct DevXS {
   const int* __restrict__ mat_off;
   const int* __restrict__ mat_nuc;
   const double* __restrict__ mat_dens;
+  // fission data (mc_nuclide_set_fission): nu*sigma_f per point, indexed
+  // like sig; null when no nuclide is fissionable
+  const double* __restrict__ nusf;
+  const int* __restrict__ nuc_fiss;  // per nuclide: 1 fissionable
+  const int* __restrict__ mat_fiss;  // per material: 1 holds a fissionable nuclide
   int n_nuc, n_grid, n_bins;
   double E_lo, E_hi, lE_lo, du;
+};
+
+// k-eigenvalue state of one generation (mc_eigen_run).  A fissionable
+// nuclide always samples its fission sites at a collision (OpenMC
+// create_fission_sites, called from sample_neutron_reaction for eigenvalue
+// runs and for fixed-source runs that create fission neutrons); only with
+// on = 1 are they banked and the keff estimators scored.  Per-history
+// arrays are indexed by history id - 1 - first.
+struct EigArgs {
+  int on;
+  double keff;            // the estimate site counts are divided by
+  double fa, fb;          // Watt fission spectrum (eV, 1/eV)
+  int64_t first;          // index of the generation's first history
+  mc_fission_site* bank;  // sites of this generation in append order
+  unsigned long long* n_bank;  // sites sampled (beyond cap: not stored)
+  int64_t cap;
+  double* ktl;            // track-length estimator, wgt*min(d,L)*nu*Sigma_f per segment
+  double* kcol;           // collision estimator, wgt*nu*Sigma_f/Sigma_t per collision
+  double* kabs;           // absorption estimator, wgt*nu*sigma_f/sigma_a per absorption
+  int* prog;              // sites banked by the history
 };
 
 struct DevSource {
@@ -115,6 +140,12 @@ struct Particle {
   // cache.
   int4 cm;
   double cs0, cs1, cs2, cs3;
+  // k-eigenvalue runs only: nu*Sigma_f of the current material at E (and
+  // of the cached materials, same slots as cs), the history's track-length
+  // keff sum and its count of banked fission sites
+  double nuf, ktl;
+  double cn0, cn1, cn2, cn3;
+  int n_prog;
 };
 
 // Tally definition of a run (mc_tally_configure).  general = 0 is the
@@ -195,23 +226,32 @@ __device__ __forceinline__ int xs_cache_slot(const int4& cm, int mat) {
   return cm.x == mat ? 0 : cm.y == mat ? 1 : cm.z == mat ? 2 : cm.w == mat ? 3 : -1;
 }
 
+// kEig: the nu*Sigma_f values move with the Sigma_t values.
+template <bool kEig = false>
 __device__ __forceinline__ bool xs_cache_get(Particle& p, int mat) {
   switch (xs_cache_slot(p.cm, mat)) {
-    case 0: p.sigt = p.cs0; return true;
-    case 1: p.sigt = p.cs1; return true;
-    case 2: p.sigt = p.cs2; return true;
-    case 3: p.sigt = p.cs3; return true;
+    case 0: p.sigt = p.cs0; if (kEig) p.nuf = p.cn0; return true;
+    case 1: p.sigt = p.cs1; if (kEig) p.nuf = p.cn1; return true;
+    case 2: p.sigt = p.cs2; if (kEig) p.nuf = p.cn2; return true;
+    case 3: p.sigt = p.cs3; if (kEig) p.nuf = p.cn3; return true;
     default: return false;
   }
 }
 
 // Insert on a miss (mat is not cached).
-__device__ __forceinline__ void xs_cache_put(Particle& p, int mat, double s) {
+template <bool kEig = false>
+__device__ __forceinline__ void xs_cache_put(Particle& p, int mat, double s, double nf = 0.0) {
   p.cm = make_int4(mat, p.cm.x, p.cm.y, p.cm.z);
   p.cs3 = p.cs2;
   p.cs2 = p.cs1;
   p.cs1 = p.cs0;
   p.cs0 = s;
+  if (kEig) {
+    p.cn3 = p.cn2;
+    p.cn2 = p.cn1;
+    p.cn1 = p.cn0;
+    p.cn0 = nf;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -290,6 +330,34 @@ __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E)
   return macro_total(X, mat, E, xs_bucket(X, mc::log64(E)));
 }
 
+// nu*sigma_f of nuclide nuc at the cursor's interval (the cursor located
+// nuc's grid), interpolated like sigma_t.
+__device__ __forceinline__ double micro_nusf(const DevXS& X, int nuc, const GridCursor& c) {
+  const double* F = X.nusf + __ldg(X.nuc_off + nuc) + c.i;
+  const double a = __ldg(F), b = __ldg(F + 1);
+  return a + c.f * (b - a);
+}
+
+// Sigma_t and nu*Sigma_f = sum over the fissionable nuclides of
+// N_i nu*sigma_f,i(E), both in material order, in one pass (OpenMC
+// Material::calculate_xs fills macro_xs.total and macro_xs.nu_fission).
+__device__ __forceinline__ double macro_total_nuf(const DevXS& X, int mat, double E, int k, double& nuf) {
+  double acc = 0.0, nf = 0.0;
+  GridCursor c;
+  const bool fis = X.nusf && __ldg(X.mat_fiss + mat);
+  const int j1 = __ldg(X.mat_off + mat + 1);
+  for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
+    const int nuc = __ldg(X.mat_nuc + j);
+    double st, ss;
+    micro_xs(X, nuc, k, E, c, st, ss);
+    const double N = __ldg(X.mat_dens + j);
+    acc = acc + N * st;
+    if (fis && __ldg(X.nuc_fiss + nuc)) nf = nf + N * micro_nusf(X, nuc, c);
+  }
+  nuf = nf;
+  return acc;
+}
+
 // Mixed-precision Sigma_t: the hash bin from a float log (grid_locate's
 // guards correct a bin that rounding moved by one), the grid interval
 // located in FP64 on the double grid, so the bracketing points are the
@@ -302,8 +370,10 @@ __device__ __forceinline__ int xs_bucket32(const DevXS& X, double E) {
   return k > X.n_bins - 1 ? X.n_bins - 1 : k;
 }
 
-__device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E, int k) {
-  float acc = 0.0f;
+template <bool kNuf = false>
+__device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E, int k, float* nuf = nullptr) {
+  float acc = 0.0f, nf = 0.0f;
+  const bool fis = kNuf && X.nusf && __ldg(X.mat_fiss + mat);
   int gc = -1, i = 0;
   float f = 0.0f;
   const int j1 = __ldg(X.mat_off + mat + 1);
@@ -319,8 +389,15 @@ __device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E
     }
     const double2* S = X.sig + __ldg(X.nuc_off + nuc) + i;
     const float a = narrow(__ldg(&S[0].x)), b = narrow(__ldg(&S[1].x));
-    acc = fmaf(narrow(__ldg(X.mat_dens + j)), fmaf(f, b - a, a), acc);
+    const float N = narrow(__ldg(X.mat_dens + j));
+    acc = fmaf(N, fmaf(f, b - a, a), acc);
+    if (kNuf && fis && __ldg(X.nuc_fiss + nuc)) {
+      const double* F = X.nusf + __ldg(X.nuc_off + nuc) + i;
+      const float fa = narrow(__ldg(F)), fb = narrow(__ldg(F + 1));
+      nf = fmaf(N, fmaf(f, fb - fa, fa), nf);
+    }
   }
+  if (kNuf) *nuf = nf;
   return acc;
 }
 
@@ -579,6 +656,9 @@ __device__ __forceinline__ void start(const DevMesh& M, const mc_site& o, int64_
   p.zero_run = 0;
   p.mat = -2;
   p.sigt = 0.0;
+  p.nuf = 0.0;
+  p.ktl = 0.0;
+  p.n_prog = 0;
   xs_cache_clear(p);
   p.elem = locate(M, p.x, p.y, p.z, p.u, p.v, p.w);
   if (p.elem < 0) p.status = kLost;
@@ -619,13 +699,68 @@ __device__ __forceinline__ void score_collision(const DevXS& X, const TallySpec&
 }
 
 // ---------------------------------------------------------------------------
+// Fission sites of a collision with fissionable nuclide nuc (OpenMC
+// create_fission_sites and sample_fission_neutron, with no uniform fission
+// source weighting and no delayed-neutron data): nu_t = wgt/keff *
+// nu*sigma_f/sigma_t sites, its fraction by one draw; each site starts at
+// the collision point with weight 1, an isotropic direction (polar cosine,
+// azimuth), one draw against the delayed fraction beta = 0, and a prompt
+// energy from the Watt spectrum.  Banked in eigenvalue runs; in fixed-source
+// runs they are drawn and dropped (MaCaw tracks no secondaries,
+// CollisionKernel.C:236).
+constexpr double kWattADefault = 0.988e6;   // eV
+constexpr double kWattBDefault = 2.249e-6;  // 1/eV
+
+__device__ __forceinline__ void fission_sites(const DevXS& X, Particle& p, const EigArgs& e, bool on,
+                                              double nf, double st) {
+  // fixed-source runs: keff 1 and the default spectrum
+  const double keff = on ? e.keff : 1.0;
+  const double fa = on ? e.fa : kWattADefault, fb = on ? e.fb : kWattBDefault;
+  const double nu_t = p.wgt / keff * nf / st;
+  int nu = (int)nu_t;
+  if (prn(p.seed) <= nu_t - (double)nu) ++nu;
+  for (int k = 0; k < nu; ++k) {
+    mc_fission_site o;
+    o.x = p.x;
+    o.y = p.y;
+    o.z = p.z;
+    const double mu = 2.0 * prn(p.seed) - 1.0;
+    double cp, sp;
+    sample_azimuth(p.seed, cp, sp);
+    const double sm = sqrt(fmax0(1.0 - mu * mu));
+    o.u = mu;
+    o.v = sm * cp;
+    o.w = sm * sp;
+    (void)prn(p.seed);  // delayed or prompt: beta = 0, always prompt
+    o.E = sample_watt(p.seed, fa, fb, X.E_lo, X.E_hi);
+    o.wgt = 1.0;
+    o.parent = p.id;
+    o.progeny = p.n_prog;
+    o.pad = 0;
+    p.n_prog += 1;
+    if (on) {
+      const unsigned long long i = atomicAdd(e.n_bank, 1ull);
+      if (i < (unsigned long long)e.cap) e.bank[i] = o;
+    }
+  }
+}
+
 // Collision at the current position (OpenMC event_collide as MaCaw calls
 // it, CollisionKernel.C:185-230): nuclide by cumulative N_i sigma_t,i,
-// absorption if xi*sigma_t < sigma_a, else elastic scattering isotropic in
-// the centre-of-mass frame off a target at rest.  Absorption and energy
-// cutoff end the history; secondaries are not tracked (CollisionKernel.C:236).
-__device__ __forceinline__ void collide(const DevXS& X, Particle& p, bool two_d = false) {
+// fission sites when that nuclide is fissionable, absorption if
+// xi*sigma_t < sigma_a, else elastic scattering isotropic in the
+// centre-of-mass frame off a target at rest.  Absorption and energy cutoff
+// end the history; secondaries are not tracked (CollisionKernel.C:236).
+// Eigenvalue runs score the collision estimate of keff before the nuclide
+// is drawn and the absorption estimate at an absorption (OpenMC
+// event_collide, absorption).
+// kEig = false: a fixed-source launch (e.on is not read).
+template <bool kEig>
+__device__ __forceinline__ void collide(const DevXS& X, Particle& p, bool two_d, const EigArgs& e) {
   const int mat = p.mat;
+  const bool on = kEig && e.on;
+  const int64_t h = p.id - 1 - e.first;
+  if (on && p.nuf > 0.0) e.kcol[h] += p.wgt * p.nuf / p.sigt;
   const int k = xs_bucket(X, mc::log64(p.E));
   const double cutoff = prn(p.seed) * p.sigt;
   double acc = 0.0, st = 0.0, ss = 0.0;
@@ -641,12 +776,20 @@ __device__ __forceinline__ void collide(const DevXS& X, Particle& p, bool two_d 
     }
   }
   if (pick < 0) pick = j1 - 1;
+  const int nuc = __ldg(X.mat_nuc + pick);
+  double nf = 0.0;
+  // the cursor holds the interval of the picked nuclide's grid
+  if (X.nusf && __ldg(X.nuc_fiss + nuc)) {
+    nf = micro_nusf(X, nuc, gc);
+    fission_sites(X, p, e, on, nf, st);
+  }
   const double sa = st - ss;
   if (prn(p.seed) * st < sa) {
+    if (on && nf > 0.0) e.kabs[h] += p.wgt * nf / sa;
     p.status = kAbsorbed;
     return;
   }
-  const double A = __ldg(X.awr + __ldg(X.mat_nuc + pick));
+  const double A = __ldg(X.awr + nuc);
   const double mu_cm = 2.0 * prn(p.seed) - 1.0;
   const double q = A * A + 2.0 * A * mu_cm + 1.0;
   const double Ap1 = A + 1.0;
@@ -707,7 +850,7 @@ __device__ __forceinline__ void prefetch_neighbours(const DevMesh& M, const int4
   }
 }
 
-template <bool kInlineXS, bool kRays = true>
+template <bool kInlineXS, bool kRays = true, bool kEig = false>
 __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Particle& p,
                                             double* __restrict__ tally, const TallySpec& T, float& sigt32,
                                             unsigned long long& n_xs) {
@@ -723,16 +866,19 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
       p.status = kBadXS;
       return 2;
     }
-    if (!xs_cache_get(p, mat)) {
+    if (!xs_cache_get<kEig>(p, mat)) {
       if (!kInlineXS) return 3;
-      const double s = macro_total(X, mat, p.E);
+      double nf = 0.0;
+      const double s = kEig ? macro_total_nuf(X, mat, p.E, xs_bucket(X, mc::log64(p.E)), nf)
+                            : macro_total(X, mat, p.E);
       ++n_xs;
       if (!(s > 0.0) || s != s) {
         p.status = kBadXS;
         return 2;
       }
       p.sigt = s;
-      xs_cache_put(p, mat, s);
+      if (kEig) p.nuf = nf;
+      xs_cache_put<kEig>(p, mat, s, nf);
     }
     p.mat = mat;
     sigt32 = (float)p.sigt;
@@ -776,6 +922,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
   }
   const double score = cross ? L : dist;  // (L < dist) ? L : dist
   score_track(T, tally, p.elem, p.E, p.wgt * score, p.sigt);
+  if (kEig) p.ktl = p.ktl + p.wgt * score * p.nuf;  // CollisionKernel.C:153-154
   ++p.n_seg;
   if (L == 0.0) ++p.zero_run;
   else p.zero_run = 0;
@@ -842,7 +989,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
 // likewise |den32 - den| <= 12u |u|_1; t32 = num32/den32 rounded (0.5 ulp):
 // |t - t32| <= (E_num + |t32| E_den)/(den32 - E_den) + 4.8e-7 |t32|, padded
 // by 0.1%.
-template <bool kInlineXS, bool kPrefetch = false, bool kRays = true>
+template <bool kInlineXS, bool kPrefetch = false, bool kRays = true, bool kEig = false>
 __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, Particle& p,
                                              const float uf, const float vf, const float wf,
                                              double* __restrict__ tally, const TallySpec& T, float& sigt32,
@@ -859,16 +1006,19 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
       p.status = kBadXS;
       return 2;
     }
-    if (!xs_cache_get(p, mat)) {
+    if (!xs_cache_get<kEig>(p, mat)) {
       if (!kInlineXS) return 3;
-      const double s = macro_total(X, mat, p.E);
+      double nf = 0.0;
+      const double s = kEig ? macro_total_nuf(X, mat, p.E, xs_bucket(X, mc::log64(p.E)), nf)
+                            : macro_total(X, mat, p.E);
       ++n_xs;
       if (!(s > 0.0) || s != s) {
         p.status = kBadXS;
         return 2;
       }
       p.sigt = s;
-      xs_cache_put(p, mat, s);
+      if (kEig) p.nuf = nf;
+      xs_cache_put<kEig>(p, mat, s, nf);
     }
     p.mat = mat;
     sigt32 = (float)p.sigt;
@@ -904,7 +1054,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     }
   }
   if (!sure || bf < 0 || !(tb + eb < lo_other)) {
-    const int r = segment_fp64<kInlineXS, kRays>(M, X, p, tally, T, sigt32, n_xs);
+    const int r = segment_fp64<kInlineXS, kRays, kEig>(M, X, p, tally, T, sigt32, n_xs);
     return (r == 0 && p.fin < 0) ? 5 : r;  // a reflection changed the direction
   }
   const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
@@ -934,6 +1084,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   }
   const double score = cross ? L : dist;
   score_track(T, tally, p.elem, p.E, p.wgt == 1.0 ? score : p.wgt * score, p.sigt);
+  if (kEig) p.ktl = p.ktl + p.wgt * score * p.nuf;  // CollisionKernel.C:153-154
   ++p.n_seg;
   if (L == 0.0) ++p.zero_run;
   else p.zero_run = 0;
@@ -1029,7 +1180,7 @@ __device__ __forceinline__ int exit_fp64(const DevMesh& M, int elem, int fin, co
   return bf;
 }
 
-template <bool kInlineXS, bool kPrefetch = false>
+template <bool kInlineXS, bool kPrefetch = false, bool kEig = false>
 __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, Particle& p,
                                              Geo32& g, double* __restrict__ tally, const TallySpec& T,
                                              float& inv_sig,
@@ -1047,16 +1198,18 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
       p.status = kBadXS;
       return 2;
     }
-    if (!xs_cache_get(p, mat)) {
+    if (!xs_cache_get<kEig>(p, mat)) {
       if (!kInlineXS) return 3;
-      const double s = widen(macro_total32(X, mat, p.E, xs_bucket32(X, p.E)));
+      float nf32 = 0.0f;
+      const double s = widen(macro_total32<kEig>(X, mat, p.E, xs_bucket32(X, p.E), &nf32));
       ++n_xs;
       if (!(s > 0.0) || s != s) {
         p.status = kBadXS;
         return 2;
       }
       p.sigt = s;
-      xs_cache_put(p, mat, s);
+      if (kEig) p.nuf = widen(nf32);
+      xs_cache_put<kEig>(p, mat, s, widen(nf32));
     }
     p.mat = mat;
     inv_sig = (float)(1.0 / p.sigt);
@@ -1105,6 +1258,7 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
   const bool cross = dist > L;
   const float score = cross ? L : dist;
   score_track(T, tally, p.elem, p.E, p.wgt * (double)score, p.sigt);
+  if (kEig) p.ktl = p.ktl + p.wgt * widen(score) * p.nuf;
   ++p.n_seg;
   if (L == 0.0f) ++p.zero_run;
   else p.zero_run = 0;

@@ -341,6 +341,21 @@ std::string build_xs_tables(const std::vector<Nuclide>& nucs, const std::vector<
       X.sig.push_back(n.ss[j]);
     }
   }
+  X.nuc_fiss.assign(nn, 0);
+  X.nusf.clear();
+  bool any_fiss = false;
+  for (int64_t i = 0; i < nn; ++i) {
+    if (!nucs[i].nusf.empty()) {
+      if (nucs[i].nusf.size() != nucs[i].E.size()) return "fission data size differs from the nuclide's grid";
+      X.nuc_fiss[i] = 1;
+      any_fiss = true;
+    }
+  }
+  if (any_fiss) {
+    X.nusf.assign(X.sig.size() / 2, 0.0);
+    for (int64_t i = 0; i < nn; ++i)
+      if (X.nuc_fiss[i]) std::copy(nucs[i].nusf.begin(), nucs[i].nusf.end(), X.nusf.begin() + X.nuc_off[i]);
+  }
   const int64_t ng = (int64_t)rep.size();
   X.ghidx.assign((size_t)(n_bins + 1) * ng, 0);
   for (int64_t g = 0; g < ng; ++g) {
@@ -358,11 +373,13 @@ std::string build_xs_tables(const std::vector<Nuclide>& nucs, const std::vector<
   X.mat_nuc.clear();
   X.mat_dens.clear();
   X.mat_ids.clear();
+  X.mat_fiss.assign(mats.size(), 0);
   for (size_t m = 0; m < mats.size(); ++m) {
     X.mat_ids.push_back(mats[m].id);
     for (size_t j = 0; j < mats[m].nuc.size(); ++j) {
       X.mat_nuc.push_back(mats[m].nuc[j]);
       X.mat_dens.push_back(mats[m].dens[j]);
+      if (X.nuc_fiss[mats[m].nuc[j]]) X.mat_fiss[m] = 1;
     }
     X.mat_off[m + 1] = (int32_t)X.mat_nuc.size();
   }

@@ -36,6 +36,7 @@ std::string build_mesh_tables(int64_t n_vtx, const double* xyz, int64_t n_tet,
 
 struct Nuclide {
   std::vector<double> E, st, ss;
+  std::vector<double> nusf;  // nu*sigma_f per point; empty: not fissionable
   double awr = 1.0;
 };
 
@@ -57,6 +58,9 @@ struct XSTables {
   std::vector<int64_t> nuc_off;   // first (sigma_t, sigma_s) pair of each nuclide
   std::vector<double> sig;        // 2 per point: (sigma_t, sigma_s), nuclides concatenated
   std::vector<double> awr;
+  std::vector<double> nusf;       // 1 per point, indexed like sig pairs; empty: nothing fissionable
+  std::vector<int32_t> nuc_fiss;  // per nuclide: 1 fissionable
+  std::vector<int32_t> mat_fiss;  // per material: 1 holds a fissionable nuclide
   std::vector<int32_t> mat_off; // n_mat+1
   std::vector<int32_t> mat_nuc;
   std::vector<double> mat_dens;

@@ -75,6 +75,11 @@ __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCount
     case kLost: L.add(kCntLost, 1); break;
     default: L.add(kCntBadXS, 1); break;
   }
+  if (a.eig.on) {  // the history's keff sum and site count (OpenMC event_death)
+    const int64_t h = p.id - 1 - a.eig.first;
+    a.eig.ktl[h] = p.ktl;
+    a.eig.prog[h] = p.n_prog;
+  }
   if (a.traces) {
     mc_trace t;
     t.id = p.id;
@@ -97,7 +102,20 @@ __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCount
 // the problem has at most four materials, of every material, so later
 // material changes at this energy hit the cache); false if unusable.
 // f32: the mixed-precision form's float interpolation (macro_total32).
-__device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int n_mat, bool f32,
+// eig: nu*Sigma_f of each evaluated material too.
+__device__ __forceinline__ double eval_xs(const DevXS& X, int mat, double E, int k, bool f32, bool eig,
+                                          double& nf) {
+  nf = 0.0;
+  if (f32) {
+    float n32 = 0.0f;
+    const double s = eig ? widen(macro_total32<true>(X, mat, E, k, &n32)) : widen(macro_total32(X, mat, E, k));
+    nf = widen(n32);
+    return s;
+  }
+  return eig ? macro_total_nuf(X, mat, E, k, nf) : macro_total(X, mat, E, k);
+}
+
+__device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int n_mat, bool f32, bool eig,
                                           Particle& p, LocalCounters& L) {
   const int mat = __ldg(M.tmat + p.elem);
   if (mat < 0) {
@@ -105,27 +123,38 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
     return false;
   }
   const int k = f32 ? xs_bucket32(X, p.E) : xs_bucket(X, mc::log64(p.E));
-  const double s = f32 ? widen(macro_total32(X, mat, p.E, k)) : macro_total(X, mat, p.E, k);
+  double nf;
+  const double s = eval_xs(X, mat, p.E, k, f32, eig, nf);
   L.add(kCntXS, 1);
   if (!(s > 0.0) || s != s) {
     p.status = kBadXS;
     return false;
   }
   p.sigt = s;
+  p.nuf = nf;
   p.mat = mat;
-  xs_cache_put(p, mat, s);
+  xs_cache_put<true>(p, mat, s, nf);
   if (n_mat <= 4) {
     for (int m = 0; m < n_mat; ++m) {
       if (m == mat) continue;
-      const double o = f32 ? widen(macro_total32(X, m, p.E, k)) : macro_total(X, m, p.E, k);
+      double onf;
+      const double o = eval_xs(X, m, p.E, k, f32, eig, onf);
       L.add(kCntXS, 1);
-      if (o > 0.0) xs_cache_put(p, m, o);
+      if (o > 0.0) xs_cache_put<true>(p, m, o, onf);
     }
   }
   return true;
 }
 
-__device__ __forceinline__ void load(const Bank& B, int s, Particle& p) {
+// eig: also the k-eigenvalue fields (a constant in the walk kernels).
+__device__ __forceinline__ void load(const Bank& B, int s, Particle& p, bool eig = false) {
+  if (eig) {
+    p.nuf = B.nuf[s];
+    p.ktl = B.ktl[s];
+    p.n_prog = B.n_prog[s];
+    const double4_32a n = B.cn[s];
+    p.cn0 = n.x; p.cn1 = n.y; p.cn2 = n.z; p.cn3 = n.w;
+  }
   p.x = B.x[s]; p.y = B.y[s]; p.z = B.z[s];
   p.u = B.u[s]; p.v = B.v[s]; p.w = B.w[s];
   p.E = B.E[s]; p.wgt = B.wgt[s]; p.sigt = B.sigt[s];
@@ -141,7 +170,15 @@ __device__ __forceinline__ void load(const Bank& B, int s, Particle& p) {
   p.face = -1;
 }
 
-__device__ __forceinline__ void store(const Bank& B, int s, const Particle& p) {
+__device__ __forceinline__ void store(const Bank& B, int s, const Particle& p, bool eig = false) {
+  if (eig) {
+    B.nuf[s] = p.nuf;
+    B.ktl[s] = p.ktl;
+    B.n_prog[s] = p.n_prog;
+    double4_32a n;
+    n.x = p.cn0; n.y = p.cn1; n.z = p.cn2; n.w = p.cn3;
+    B.cn[s] = n;
+  }
   B.x[s] = p.x; B.y[s] = p.y; B.z[s] = p.z;
   B.u[s] = p.u; B.v[s] = p.v; B.w[s] = p.w;
   B.E[s] = p.E; B.wgt[s] = p.wgt; B.sigt[s] = p.sigt;
@@ -224,7 +261,7 @@ __device__ __forceinline__ long long births_now(const EventCtl* ctl, int64_t n) 
 
 // ---------------------------------------------------------------------------
 // History form.
-template <int kPrec>
+template <int kPrec, bool kEig>
 __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S, RunArgs a) {
   MC_COUNTERS(L);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -236,10 +273,11 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
       float sigt32 = 0.0f;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
+        const int r = segment_fp64g<true, false, true, kEig>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts,
+                                                             sigt32, nxs);
         if (r == 1) {
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p, a.two_d);
+          collide<kEig>(X, p, a.two_d, a.eig);
         }
         if (r == 1 || r == 5) {
           uf = (float)p.u;
@@ -252,11 +290,12 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
       geo_load(p, g);
       float inv_sig = 0.0f;
       while (p.status == kAlive) {
-        const int r = segment_mixed<true>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
+        const int r = segment_mixed<true, false, kEig>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs,
+                                                        nfb);
         if (r == 1) {
           geo_store(g, p);
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p, a.two_d);
+          collide<kEig>(X, p, a.two_d, a.eig);
           geo_load(p, g);
         }
       }
@@ -287,7 +326,7 @@ __global__ void __launch_bounds__(256) k_ev_init(DevMesh M, DevXS X, DevSource S
       push_free(Q, ctl, (int)i, B.cap);
       continue;
     }
-    store(B, (int)i, p);
+    store(B, (int)i, p, a.eig.on);
     push(Q.xs[0], &ctl->n_xs[0], (int)i);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -297,6 +336,7 @@ __global__ void __launch_bounds__(256) k_ev_init(DevMesh M, DevXS X, DevSource S
   flush(L, a.counters, a.leak_w);
 }
 
+template <bool kEig>
 __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                EventQueues Q, EventCtl* ctl, int par) {
   MC_COUNTERS(L);
@@ -310,22 +350,33 @@ __global__ void __launch_bounds__(256) k_ev_xs(DevMesh M, DevXS X, RunArgs a, Ba
     p.cm = B.cm[s];
     const double4_32a c0 = B.cs[s];
     p.cs0 = c0.x; p.cs1 = c0.y; p.cs2 = c0.z; p.cs3 = c0.w;
+    const bool eig = kEig;
+    if (eig) {
+      const double4_32a n0 = B.cn[s];
+      p.cn0 = n0.x; p.cn1 = n0.y; p.cn2 = n0.z; p.cn3 = n0.w;
+    }
     p.status = kAlive;
     const bool f32 = a.precision == MC_PREC_MIXED;
-    if (refresh_xs(M, X, a.n_mat, f32, p, L)) {
+    if (refresh_xs(M, X, a.n_mat, f32, eig, p, L)) {
       B.sigt[s] = p.sigt;
       B.mat[s] = p.mat;
       B.cm[s] = p.cm;
       double4_32a c;
       c.x = p.cs0; c.y = p.cs1; c.z = p.cs2; c.w = p.cs3;
       B.cs[s] = c;
+      if (eig) {
+        B.nuf[s] = p.nuf;
+        double4_32a n;
+        n.x = p.cn0; n.y = p.cn1; n.z = p.cn2; n.w = p.cn3;
+        B.cn[s] = n;
+      }
       if (f32) {  // the cached values are floats widened: their float inverses
         B.cinv[s] = make_float4(p.cm.x >= 0 ? 1.0f / narrow(p.cs0) : 0.0f, p.cm.y >= 0 ? 1.0f / narrow(p.cs1) : 0.0f,
                                 p.cm.z >= 0 ? 1.0f / narrow(p.cs2) : 0.0f, p.cm.w >= 0 ? 1.0f / narrow(p.cs3) : 0.0f);
       }
       push(Q.adv[par], &ctl->n_adv[par], s);
     } else {
-      load(B, s, p);  // the history ends: all of it
+      load(B, s, p, eig);  // the history ends: all of it
       p.status = kBadXS;
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
@@ -345,7 +396,7 @@ __device__ __forceinline__ int take_chunk(int* head) {
 
 // Segment walk, one queued particle per lane, queue entries taken by warp
 // chunks.
-template <int kPrec, bool kRays>
+template <int kPrec, bool kRays, bool kEig>
 __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                            EventQueues Q, EventCtl* ctl, int par) {
   MC_COUNTERS(L);
@@ -357,7 +408,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
     if (i >= n) continue;
     const int s = Q.adv[par][i];
     Particle p;
-    load(B, s, p);
+    load(B, s, p, kEig);
     const int seg0 = p.n_seg;
     unsigned long long nxs = 0, nfb = 0;
     int r = 0;
@@ -366,7 +417,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       for (;;) {
-        r = segment_fp64g<false, false, kRays>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
+        r = segment_fp64g<false, false, kRays, kEig>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 5) {
           uf = (float)p.u;
           vf = (float)p.v;
@@ -384,7 +435,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       geo_load(p, g);
       float inv_sig = (float)(1.0 / p.sigt);
       for (;;) {
-        r = segment_mixed<false>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
+        r = segment_mixed<false, false, kEig>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
         if (r != 0) break;
         if (a.max_seg > 0 && ++k >= a.max_seg) {
           r = 4;
@@ -400,7 +451,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
       push_free(Q, ctl, s, B.cap);
       continue;
     }
-    store(B, s, p);
+    store(B, s, p, kEig);
     if (r == 1) push(Q.coll, &ctl->n_coll, s);
     else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
     else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
@@ -699,6 +750,7 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
   flush(L, a.counters, a.leak_w);
 }
 
+template <bool kEig>
 __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                     EventQueues Q, EventCtl* ctl, int par) {
   MC_COUNTERS(L);
@@ -713,16 +765,27 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
     p.seed = B.seed[s];
     p.elem = B.elem[s]; p.mat = B.mat[s]; p.tag = B.tag[s];
     p.status = kAlive;
+    // fission sites start at the collision point; eigenvalue runs also
+    // need the history's id, site count and nu*Sigma_f
+    const bool eig = kEig;
+    p.id = eig ? B.id[s] : 0;
+    p.n_prog = eig ? B.n_prog[s] : 0;
+    p.nuf = eig ? B.nuf[s] : 0.0;
+    if (X.nusf) {
+      p.x = B.x[s]; p.y = B.y[s]; p.z = B.z[s];
+    }
     score_collision(X, a.ts, tally_of(a, p.tag), p);
-    collide(X, p, a.two_d);
+    collide<kEig>(X, p, a.two_d, a.eig);
     if (p.status != kAlive) {
       const int status = p.status;
       const double E = p.E;
       const uint64_t seed = p.seed;
-      load(B, s, p);
+      const int n_prog = p.n_prog;
+      load(B, s, p, eig);
       p.status = status;
       p.E = E;
       p.seed = seed;
+      p.n_prog = n_prog;
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
       continue;
@@ -730,6 +793,7 @@ __global__ void __launch_bounds__(256) k_ev_collide(DevMesh M, DevXS X, RunArgs 
     B.u[s] = p.u; B.v[s] = p.v; B.w[s] = p.w;
     B.E[s] = p.E; B.seed[s] = p.seed; B.mat[s] = p.mat;
     B.cm[s] = p.cm; B.fin[s] = p.fin;
+    if (eig) B.n_prog[s] = p.n_prog;
     push(Q.xs[nxt], &ctl->n_xs[nxt], s);
   }
   flush(L, a.counters, a.leak_w);
@@ -752,7 +816,7 @@ __global__ void __launch_bounds__(256) k_ev_refill(DevMesh M, DevXS X, DevSource
       finish(p, a, L);
       continue;  // slot stays empty for the rest of the run
     }
-    store(B, s, p);
+    store(B, s, p, a.eig.on);
     push(Q.xs[nxt], &ctl->n_xs[nxt], s);
   }
   flush(L, a.counters, a.leak_w);
@@ -774,7 +838,7 @@ __global__ void k_ev_reset(EventCtl* ctl, int par, int64_t n) {
 
 // Tail of a batch: every particle still queued runs to completion in one
 // launch, one thread per particle, with cross sections and collisions inline.
-template <int kPrec>
+template <int kPrec, bool kEig>
 __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                    EventQueues Q, EventCtl* ctl, int par) {
   MC_COUNTERS(L);
@@ -783,16 +847,16 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx + na; i += gridDim.x * blockDim.x) {
     const int s = (i < nx) ? Q.xs[par][i] : Q.adv[par][i - nx];
     Particle p;
-    load(B, s, p);
+    load(B, s, p, kEig);
     unsigned long long nxs = 0, nfb = 0;
     if (kPrec == MC_PREC_FP64) {
       float sigt32 = (float)p.sigt;
       float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true, true>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
+        const int r = segment_fp64g<true, true, true, kEig>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 1) {
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p, a.two_d);
+          collide<kEig>(X, p, a.two_d, a.eig);
         }
         if (r == 1 || r == 5) {
           uf = (float)p.u;
@@ -805,11 +869,11 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       geo_load(p, g);
       float inv_sig = (p.mat >= 0) ? (float)(1.0 / p.sigt) : 0.0f;
       while (p.status == kAlive) {
-        const int r = segment_mixed<true, true>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
+        const int r = segment_mixed<true, true, kEig>(M, X, p, g, tally_of(a, p.tag), a.ts, inv_sig, a.tol, nxs, nfb);
         if (r == 1) {
           geo_store(g, p);
           score_collision(X, a.ts, tally_of(a, p.tag), p);
-          collide(X, p, a.two_d);
+          collide<kEig>(X, p, a.two_d, a.eig);
           geo_load(p, g);
         }
       }
@@ -893,8 +957,13 @@ __global__ void k_accumulate(double* __restrict__ batch, double* __restrict__ su
 
 cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
                            int block, int grid, cudaStream_t st) {
-  if (a.precision == MC_PREC_MIXED) k_history<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, S, a);
-  else k_history<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, S, a);
+  if (a.eig.on) {
+    if (a.precision == MC_PREC_MIXED) k_history<MC_PREC_MIXED, true><<<grid, block, 0, st>>>(M, X, S, a);
+    else k_history<MC_PREC_FP64, true><<<grid, block, 0, st>>>(M, X, S, a);
+  } else {
+    if (a.precision == MC_PREC_MIXED) k_history<MC_PREC_MIXED, false><<<grid, block, 0, st>>>(M, X, S, a);
+    else k_history<MC_PREC_FP64, false><<<grid, block, 0, st>>>(M, X, S, a);
+  }
   return cudaGetLastError();
 }
 
@@ -911,7 +980,8 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
                                    const RunArgs& a, const Bank& B, const EventQueues& Q,
                                    EventCtl* ctl, int par, int block, int grid, cudaStream_t st,
                                    int* n_launch, cudaEvent_t adv0, cudaEvent_t adv1) {
-  k_ev_xs<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.eig.on) k_ev_xs<true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  else k_ev_xs<false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   if (a.sort_shift >= 0) {
     cudaMemsetAsync(a.sort_cnt, 0, sizeof(int) * (size_t)(a.sort_buckets + 1), st);
     k_sort_copy<<<grid, block, 0, st>>>(Q.adv[par], a.sort_tmp, ctl, par);
@@ -921,17 +991,25 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
     if (n_launch) *n_launch += 4;
   }
   if (adv0) cudaEventRecord(adv0, st);
-  if (a.precision == MC_PREC_MIXED) {
+  if (a.eig.on) {
+    // k-eigenvalue generations: the chunked walk with the keff score (no
+    // lane refill, no ray recording)
+    if (a.precision == MC_PREC_MIXED)
+      k_ev_advance_static<MC_PREC_MIXED, false, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else
+      k_ev_advance_static<MC_PREC_FP64, false, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  } else if (a.precision == MC_PREC_MIXED) {
     // the compact walk scores the default tally and records no rays
     if (a.refill || a.ts.general || a.ts.rays) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else k_ev_advance_mixed<<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
   } else {
     if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else if (a.ts.rays) k_ev_advance_static<MC_PREC_FP64, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else k_ev_advance_static<MC_PREC_FP64, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else if (a.ts.rays) k_ev_advance_static<MC_PREC_FP64, true, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_advance_static<MC_PREC_FP64, false, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   }
   if (adv1) cudaEventRecord(adv1, st);
-  k_ev_collide<<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.eig.on) k_ev_collide<true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  else k_ev_collide<false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   k_ev_refill<<<grid, block, 0, st>>>(M, X, S, a, B, Q, ctl, par);
   k_ev_reset<<<1, 32, 0, st>>>(ctl, par, a.n);
   if (n_launch) *n_launch += 5;
@@ -942,8 +1020,13 @@ cudaError_t launch_event_finish(const DevMesh& M, const DevXS& X, const DevSourc
                                 const RunArgs& a, const Bank& B, const EventQueues& Q,
                                 EventCtl* ctl, int par, int block, int grid, cudaStream_t st) {
   (void)S;
-  if (a.precision == MC_PREC_MIXED) k_ev_finish<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-  else k_ev_finish<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  if (a.eig.on) {
+    if (a.precision == MC_PREC_MIXED) k_ev_finish<MC_PREC_MIXED, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_finish<MC_PREC_FP64, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  } else {
+    if (a.precision == MC_PREC_MIXED) k_ev_finish<MC_PREC_MIXED, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_finish<MC_PREC_FP64, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+  }
   return cudaGetLastError();
 }
 

@@ -37,6 +37,11 @@ struct Bank {
   int4* cm;            // cross-section cache keys
   double4_32a* cs;     // cross-section cache values
   float4* cinv;        // float 1/Sigma_t of the cached values (mixed-precision walk)
+  // k-eigenvalue runs only (null otherwise): nu*Sigma_f of the current
+  // material and of the cached ones, track-length keff sum, sites banked
+  double *nuf, *ktl;
+  double4_32a* cn;
+  int* n_prog;
   int64_t cap;
 };
 
@@ -101,6 +106,7 @@ struct RunArgs {
   int refill;   // event mode: lanes take further queued particles within one launch
   int two_d;    // 2-D problem: planar directions, births at z = z2d
   double z2d;
+  EigArgs eig;       // k-eigenvalue generation (eig.on = 0: fixed source)
   int sort_shift;    // event mode: advance queue ordered by elem >> sort_shift (-1: unordered)
   int sort_buckets;  // (n_tet >> sort_shift) + 1
   int* sort_tmp;     // bank-capacity scratch for the ordering
@@ -129,5 +135,29 @@ cudaError_t launch_sample(const DevXS& X, const DevSource& S, int64_t first, int
 
 cudaError_t launch_accumulate(double* batch, double* sum, double* sumsq, int64_t n, double inv_w,
                               cudaStream_t st);
+
+// k-eigenvalue bank processing (mc_eigen.cu).
+// Fixed-order sum of v[0..n): tile b of 1024 values (zero-padded) is summed
+// by a pairwise tree (v[t] += v[t+s], s = 512, 256, ..., 1) into part[b];
+// the caller adds the ceil(n/1024) partials in index order.
+constexpr int kReduceTile = 1024;
+cudaError_t launch_tile_sums(const double* v, int64_t n, double* part, cudaStream_t st);
+// Exclusive prefix sum of n counts into off[0..n] (off[n] = total);
+// tmp holds scan_tmp_size(n) entries.
+int64_t scan_tmp_size(int64_t n);
+cudaError_t launch_scan(const int* cnt, int64_t n, int64_t* off, int64_t* tmp, cudaStream_t st);
+// Fission bank in (parent id, progeny) order: site k goes to
+// off[parent - 1 - first] + progeny (off: scan of the n_hist histories'
+// site counts).
+cudaError_t launch_bank_sort(const mc_fission_site* in, int64_t m, const int64_t* off, int64_t first,
+                             int64_t n_hist, mc_fission_site* out, cudaStream_t st);
+// Resampling counts of the sorted bank (synchronize_bank): site i is kept
+// copies + (xi_i < p) times, xi_i the (i+1)-th draw from state seed0.
+cudaError_t launch_bank_counts(int64_t m, uint64_t seed0, int copies, double p, int* cnt, cudaStream_t st);
+// Writes the resampled sites to src[0..n): site i fills [pos[i], pos[i+1])
+// below n; then, if pos[m] < n, src[pos[m] + j] = sorted[max(0, m - need + j)]
+// for j < need = n - pos[m].
+cudaError_t launch_bank_fill(const mc_fission_site* sorted, int64_t m, const int64_t* pos, int64_t n,
+                             mc_site* src, cudaStream_t st);
 
 }  // namespace mc

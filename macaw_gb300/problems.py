@@ -11,6 +11,10 @@ cube_problem     -- 20 cm cube, 20^3 hexes x 6 tets (48,000 tets), one
 lattice_problem  -- 17x17 pin cells, pitch 1.26 cm, 50 cm tall, fuel/clad/
                     moderator rings (15/4/3 nuclides, 20,000-point grids),
                     about 2.0M tets, uniform source in the fuel cylinders.
+eigen_lattice_problem -- the pin lattice as a k-eigenvalue problem:
+                    fissionable fuel nuclides (nu*sigma_f a fixed share of
+                    their absorption), reflective sides, vacuum top and
+                    bottom.
 core_problem     -- cylindrical core, radius 180 cm, 400 cm tall: 193
                     assemblies of 17x17 pin cells plus a reflector of whole
                     cells, 6 axial layers (about 41M tets); 200 materials of
@@ -38,6 +42,7 @@ class Nuclide:
     sig_t: np.ndarray
     sig_s: np.ndarray
     awr: float
+    nu_sig_f: np.ndarray | None = None  # nu*sigma_f per point; None: not fissionable
 
 
 @dataclass
@@ -246,4 +251,34 @@ def lattice_2d_problem(nx: int = 17, ny: int = 17, n_sec: int = 16, n_fuel_rings
     p.name = f"lattice2d{nx}x{ny}"
     p.z_2d = thickness / 2
     p.bcs[0] = p.bcs[5] = MC_BC_REFLECT
+    return p
+
+
+def add_fission(nuc: Nuclide, nu: float = 2.43, fission_share: float = 0.8) -> Nuclide:
+    """Makes a nuclide fissionable: nu*sigma_f(E) = nu * fission_share *
+    sigma_a(E), sigma_a = sigma_t - sigma_s at every grid point."""
+    nuc.nu_sig_f = (nu * fission_share) * (nuc.sig_t - nuc.sig_s)
+    return nuc
+
+
+def eigen_lattice_problem(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fuel_rings: int = 2,
+                          pitch: float = 1.26, height: float = 50.0, n_pts: int = 20000, n_peaks: int = 20,
+                          nuclides_per_material=(15, 4, 3), scatter_b: float = 2.0, absorb_b: float = 0.5,
+                          nu: float = 2.43, fission_share: float = 0.6, seed: int = 20240611) -> Problem:
+    """k-eigenvalue pin lattice (about 2.0M tets at the defaults, k near 1):
+    the lattice's tables plus a constant scattering (scatter_b) and
+    absorption (absorb_b) cross section on every nuclide, so that fission
+    neutrons collide within a few pin cells; every fuel nuclide is
+    fissionable (add_fission); reflective sides (sidesets 1-4), vacuum top
+    and bottom (0, 5).  The first generation starts from the uniform source
+    in the fuel cylinders."""
+    p = lattice_problem(nx, ny, nz, n_sec, n_fuel_rings, pitch, height, n_pts, n_peaks, nuclides_per_material, seed)
+    p.name = f"eigen_lattice{nx}x{ny}x{nz}"
+    for n in p.nuclides:
+        n.sig_s = n.sig_s + scatter_b
+        n.sig_t = n.sig_t + (scatter_b + absorb_b)
+    for k in p.materials[0].nuclides:
+        add_fission(p.nuclides[int(k)], nu, fission_share)
+    for b in (1, 2, 3, 4):
+        p.bcs[b] = MC_BC_REFLECT
     return p

@@ -11,9 +11,9 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (MC_MODE_EVENT, MC_PREC_FP64, MC_TALLY_BATCH, MC_TALLY_SUM, MC_TALLY_SUM_SQ,
-                   RAY_SEGMENT_DTYPE, SITE_DTYPE, TRACE_DTYPE, MCError, RunDesc, SourceDesc, Stats, TallyDesc, lib,
-                   ptr)
+from ._lib import (EIGEN_GEN_DTYPE, FISSION_SITE_DTYPE, MC_MODE_EVENT, MC_PREC_FP64, MC_TALLY_BATCH, MC_TALLY_SUM,
+                   MC_TALLY_SUM_SQ, RAY_SEGMENT_DTYPE, SITE_DTYPE, TRACE_DTYPE, EigenDesc, MCError, RunDesc,
+                   SourceDesc, Stats, TallyDesc, lib, ptr)
 from .problems import Problem, Source, TallyDef
 
 
@@ -69,6 +69,11 @@ class Tracker:
                  "mc_nuclide_add")
         return idx.value
 
+    def set_fission(self, nuclide: int, nu_sig_f) -> None:
+        """nu*sigma_f per grid point of a nuclide (None: not fissionable)."""
+        f = None if nu_sig_f is None else np.ascontiguousarray(nu_sig_f, np.float64)
+        self._ck(lib.mc_nuclide_set_fission(self._h, nuclide, ptr(f)), "mc_nuclide_set_fission")
+
     def add_material(self, material_id: int, nuclides, densities) -> None:
         n = np.ascontiguousarray(nuclides, np.int32)
         d = np.ascontiguousarray(densities, np.float64)
@@ -102,7 +107,9 @@ class Tracker:
         for bid, t in p.bcs.items():
             self.set_bc(bid, t)
         for n in p.nuclides:
-            self.add_nuclide(n.E, n.sig_t, n.sig_s, n.awr)
+            k = self.add_nuclide(n.E, n.sig_t, n.sig_s, n.awr)
+            if n.nu_sig_f is not None:
+                self.set_fission(k, n.nu_sig_f)
         for m in p.materials:
             self.add_material(m.id, m.nuclides, m.densities)
         self.block_material_map(p.blocks, p.block_materials)
@@ -159,6 +166,37 @@ class Tracker:
                     None if bs is None else bs.ctypes.data)
         self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
         return self.stats()
+
+    def eigen(self, n: int, generations: int, inactive: int = 0, seed: int = 1, precision: int = MC_PREC_FP64,
+              mode: int = MC_MODE_EVENT, bank_size: int = 0, block_size: int = 0, max_seg: int = 0,
+              sort_queue: int = 0, graph: bool = False, keff0: float = 0.0, watt=(0.0, 0.0), capacity: int = 0,
+              initial_source: np.ndarray | None = None) -> np.ndarray:
+        """k-eigenvalue generations of n histories; returns one
+        EIGEN_GEN_DTYPE record per generation."""
+        if initial_source is not None:
+            assert initial_source.dtype == SITE_DTYPE and initial_source.size == n
+            initial_source = np.ascontiguousarray(initial_source)
+        d = EigenDesc(n, generations, inactive, seed, precision, mode, bank_size, block_size, max_seg,
+                      int(sort_queue), int(graph), keff0, watt[0], watt[1], capacity,
+                      None if initial_source is None else initial_source.ctypes.data)
+        out = np.zeros(generations, EIGEN_GEN_DTYPE)
+        self._ck(lib.mc_eigen_run(self._h, C.byref(d), ptr(out)), "mc_eigen_run")
+        return out
+
+    def eigen_source(self, n: int) -> np.ndarray:
+        """Source sites of the next generation after the last eigen run."""
+        out = np.zeros(n, SITE_DTYPE)
+        self._ck(lib.mc_eigen_source_download(self._h, ptr(out), n), "mc_eigen_source_download")
+        return out
+
+    def fission_bank(self) -> np.ndarray:
+        """The last generation's fission bank in (parent, progeny) order."""
+        m = C.c_int64()
+        self._ck(lib.mc_eigen_fission_bank_download(self._h, None, 0, C.byref(m)), "mc_eigen_fission_bank_download")
+        out = np.zeros(m.value, FISSION_SITE_DTYPE)
+        self._ck(lib.mc_eigen_fission_bank_download(self._h, ptr(out), out.size, C.byref(m)),
+                 "mc_eigen_fission_bank_download")
+        return out
 
     def autotune(self, trial: int = 200_000, **base) -> tuple[dict, float]:
         """Best event-form parameters on trial batches; returns (params, histories/s)."""

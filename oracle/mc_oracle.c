@@ -20,6 +20,11 @@
  *    element (CollisionKernel.C:204-205); absorption ends the history
  *    (CollisionKernel.C:226-230); no secondaries (CollisionKernel.C:236)
  *  - material of an element = block map id - 1 (CollisionKernel.C:110)
+ *  - fission sites at collisions with fissionable nuclides (OpenMC
+ *    create_fission_sites) and, in k-eigenvalue runs, the track-length,
+ *    collision and absorption keff estimators (CollisionKernel.C:153-154;
+ *    OpenMC event_collide, absorption), the bank sort and the resampling
+ *    of OpenMCStudy::synchronizeBanks (OpenMCStudy.C:430-607)
  *
  * Parity pin: the RNG (below) is checked against the seed states in
  * test/tests/study/gold/openmc_study_rays.e.  The rest is unpinned.
@@ -128,6 +133,7 @@ typedef struct {
   double* ss;
   double awr;
   int32_t* hidx; /* n_bins+1 */
+  double* nusf;  /* nu*sigma_f per point, or NULL: not fissionable */
 } nuclide_t;
 
 typedef struct {
@@ -213,6 +219,7 @@ void oracle_destroy(oracle_problem* p)
   free_mesh(p);
   for (int i = 0; i < p->n_nuc; ++i) {
     free(p->nucs[i].E); free(p->nucs[i].st); free(p->nucs[i].ss); free(p->nucs[i].hidx);
+    free(p->nucs[i].nusf);
   }
   free(p->nucs);
   for (int i = 0; i < p->n_mat; ++i) { free(p->mats[i].nuc); free(p->mats[i].dens); }
@@ -435,7 +442,22 @@ int oracle_add_nuclide(oracle_problem* p, int64_t n_pts, const double* E, const 
   memcpy(n->ss, sig_s, sizeof(double) * (size_t)n_pts);
   n->awr = awr;
   n->hidx = NULL;
+  n->nusf = NULL;
   p->data_ready = 0;
+  return 0;
+}
+
+/* Fission data of a nuclide (nu*sigma_f per grid point); NULL clears. */
+int oracle_set_fission(oracle_problem* p, int32_t nuclide, const double* nu_sig_f)
+{
+  if (nuclide < 0 || nuclide >= p->n_nuc) return fail(p, "nuclide index out of range");
+  nuclide_t* n = p->nucs + nuclide;
+  free(n->nusf);
+  n->nusf = NULL;
+  if (nu_sig_f) {
+    n->nusf = (double*)malloc(sizeof(double) * (size_t)n->n_pts);
+    memcpy(n->nusf, nu_sig_f, sizeof(double) * (size_t)n->n_pts);
+  }
   return 0;
 }
 
@@ -606,6 +628,29 @@ static double macro_total(const oracle_problem* p, int mat, double E)
     double st, ss;
     micro_xs(p->nucs + m->nuc[j], k, E, &st, &ss);
     acc = acc + m->dens[j] * st;
+  }
+  return acc;
+}
+
+/* nu*sigma_f of a fissionable nuclide at E, interpolated on sigma_t's
+ * interval with sigma_t's fraction. */
+static double micro_nusf(const nuclide_t* n, int k, double E)
+{
+  int i = grid_index(n, k, E);
+  double f = (E - n->E[i]) / (n->E[i + 1] - n->E[i]);
+  return n->nusf[i] + f * (n->nusf[i + 1] - n->nusf[i]);
+}
+
+/* nu*Sigma_f: sum over the material's fissionable nuclides of
+ * N_i nu*sigma_f,i(E), in material order (OpenMC macro_xs.nu_fission). */
+static double macro_nufission(const oracle_problem* p, int mat, double E)
+{
+  const material_t* m = p->mats + mat;
+  int k = bucket_of(p, oracle_log(E));
+  double acc = 0.0;
+  for (int j = 0; j < m->n; ++j) {
+    const nuclide_t* n = p->nucs + m->nuc[j];
+    if (n->nusf) acc = acc + m->dens[j] * micro_nusf(n, k, E);
   }
   return acc;
 }
@@ -874,18 +919,81 @@ static void score_collision(const oracle_problem* p, double* tally, int elem, in
   }
 }
 
-static void track(const oracle_problem* p, int64_t h, uint64_t master, double* tally,
-                  oracle_trace* tr, lstats* ls)
+/* k-eigenvalue state of one history: estimator sums and the fission
+ * sites it banks, in the order it banks them. */
+typedef struct {
+  int on;
+  double keff, fa, fb;
+  double ktl, kcol, kabs;
+  oracle_fsite* sites;
+  int n_sites, cap_sites;
+} heig;
+
+#define WATT_A_DEFAULT 0.988e6
+#define WATT_B_DEFAULT 2.249e-6
+
+/* Fission sites of a collision with a fissionable nuclide (OpenMC
+ * create_fission_sites with sample_fission_neutron; no uniform fission
+ * source weighting, no delayed-neutron data): nu_t = wgt/keff *
+ * nu*sigma_f/sigma_t, fraction by one draw; per site a polar cosine, an
+ * azimuth, one draw against beta = 0 and a Watt energy.  Fixed-source
+ * runs (e NULL or off) draw them with keff = 1 and drop them. */
+static void fission_sites(const oracle_problem* p, heig* e, int64_t id, const double* x, double wgt,
+                          double nf, double st, uint64_t* s)
+{
+  int on = e && e->on;
+  double keff = on ? e->keff : 1.0;
+  double fa = on ? e->fa : WATT_A_DEFAULT, fb = on ? e->fb : WATT_B_DEFAULT;
+  double nu_t = wgt / keff * nf / st;
+  int nu = (int)nu_t;
+  if (oracle_prn(s) <= nu_t - (double)nu) ++nu;
+  for (int k = 0; k < nu; ++k) {
+    double mu = 2.0 * oracle_prn(s) - 1.0;
+    double cp, sp;
+    sample_azimuth(s, &cp, &sp);
+    double sm = sqrt(pos0(1.0 - mu * mu));
+    (void)oracle_prn(s);
+    double E = sample_watt(s, fa, fb, p->E_lo, p->E_hi);
+    if (!on) continue;
+    if (e->n_sites == e->cap_sites) {
+      e->cap_sites = e->cap_sites ? 2 * e->cap_sites : 4;
+      e->sites = (oracle_fsite*)realloc(e->sites, sizeof(oracle_fsite) * (size_t)e->cap_sites);
+    }
+    oracle_fsite* o = e->sites + e->n_sites;
+    o->x = x[0]; o->y = x[1]; o->z = x[2];
+    o->u = mu; o->v = sm * cp; o->w = sm * sp;
+    o->E = E;
+    o->wgt = 1.0;
+    o->parent = id;
+    o->progeny = e->n_sites;
+    o->pad = 0;
+    e->n_sites++;
+  }
+}
+
+/* One history: id h+1, born from `site` (x, y, z, u, v, w, E, wgt) when
+ * given, else sampled from the source stream. */
+static void track(const oracle_problem* p, int64_t h, uint64_t master, const double* site, heig* e,
+                  double* tally, oracle_trace* tr, lstats* ls)
 {
   int64_t id = h + 1;
   uint64_t ssrc = oracle_init_seed(id, master, 2);
   uint64_t strk = oracle_init_seed(id, master, 0);
   double x[3], u[3], E, wgt = 1.0;
-  birth(p, id, &ssrc, x, u, &E);
+  if (site) {
+    x[0] = site[0]; x[1] = site[1]; x[2] = site[2];
+    u[0] = site[3]; u[1] = site[4]; u[2] = site[5];
+    E = site[6];
+    wgt = site[7];
+  } else {
+    birth(p, id, &ssrc, x, u, &E);
+  }
   if (p->two_d) {
     x[2] = p->z2d;
     planar_dir(u);
   }
+  const int eig = e && e->on;
+  double nuf = 0.0;
   uint64_t hash = FNV_OFF;
   int status = 0, n_seg = 0, n_coll = 0, face_out = -1;
   int elem = oracle_locate(p, x, u);
@@ -899,6 +1007,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
     if (mat < 0) { status = ST_BADXS; break; }
     if (mat != cur_mat) {
       sigt = macro_total(p, mat, E);
+      if (eig) nuf = macro_nufission(p, mat, E);
       cur_mat = mat;
       if (!(sigt > 0.0) || sigt != sigt) { status = ST_BADXS; break; }
     }
@@ -921,6 +1030,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
     double dist = -oracle_log(oracle_prn(&strk)) / sigt;
     double score = (L < dist) ? L : dist;
     score_track(p, tally, elem, E, wgt * score, sigt);
+    if (eig) e->ktl = e->ktl + wgt * score * nuf; /* CollisionKernel.C:153-154 */
     ++n_seg;
     if (L == 0.0) ++zero_run; else zero_run = 0;
     if (dist > L) {
@@ -956,6 +1066,8 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
     ++n_coll;
     zero_run = 0;
     score_collision(p, tally, elem, mat, E, wgt, sigt);
+    /* collision estimate of keff (OpenMC event_collide) */
+    if (eig && nuf > 0.0) e->kcol = e->kcol + wgt * nuf / sigt;
     const material_t* m = p->mats + mat;
     int k = bucket_of(p, oracle_log(E));
     double cutoff = oracle_prn(&strk) * sigt;
@@ -967,9 +1079,20 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, double* t
       if (acc >= cutoff) { pick = j; break; }
     }
     if (pick < 0) pick = m->n - 1; /* st/ss already hold the last nuclide */
+    const nuclide_t* pn = p->nucs + m->nuc[pick];
+    double nf = 0.0;
+    if (pn->nusf) {
+      nf = micro_nusf(pn, k, E);
+      fission_sites(p, e, id, x, wgt, nf, st, &strk);
+    }
     double sa = st - ss;
-    if (oracle_prn(&strk) * st < sa) { status = ST_ABSORB; break; }
-    double A = p->nucs[m->nuc[pick]].awr;
+    if (oracle_prn(&strk) * st < sa) {
+      /* absorption estimate of keff (OpenMC absorption) */
+      if (eig && nf > 0.0) e->kabs = e->kabs + wgt * nf / sa;
+      status = ST_ABSORB;
+      break;
+    }
+    double A = pn->awr;
     double mu_cm = 2.0 * oracle_prn(&strk) - 1.0;
     double q = A * A + 2.0 * A * mu_cm + 1.0;
     double Ap1 = A + 1.0;
@@ -1027,7 +1150,7 @@ int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n
   nt = 1;
 #endif
   if (nt == 1) {
-    for (int64_t i = 0; i < n; ++i) track(p, first + i, seed, tally, traces ? traces + i : NULL, &tot);
+    for (int64_t i = 0; i < n; ++i) track(p, first + i, seed, NULL, NULL, tally, traces ? traces + i : NULL, &tot);
   } else {
 #ifdef _OPENMP
     double** priv = (double**)calloc((size_t)nt, sizeof(double*));
@@ -1038,7 +1161,7 @@ int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n
       priv[tid] = (double*)calloc((size_t)oracle_tally_size(p), sizeof(double));
 #pragma omp for schedule(dynamic, 64)
       for (int64_t i = 0; i < n; ++i)
-        track(p, first + i, seed, priv[tid], traces ? traces + i : NULL, pl + tid);
+        track(p, first + i, seed, NULL, NULL, priv[tid], traces ? traces + i : NULL, pl + tid);
     }
     for (int t = 0; t < nt; ++t) {
       if (priv[t]) {
@@ -1066,4 +1189,199 @@ int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n
     stats->leak_weight = tot.leak_w;
   }
   return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* k-eigenvalue generations (OpenMC's eigenvalue mode as OpenMCStudy runs
+ * it, one generation per batch: births from the source bank,
+ * src/userobjects/OpenMCStudy.C:317-360; finalize_generation with one
+ * rank, :374-402; bank resampling as synchronizeBanks adapts OpenMC's
+ * synchronize_bank, :430-607). */
+
+/* Fixed-order sum: tiles of 1024 values (zero-padded), each reduced by the
+ * pairwise tree t[i] += t[i+s] for s = 512, 256, ..., 1, then the tile sums
+ * added in order. */
+static double fixed_sum(const double* v, int64_t n)
+{
+  double total = 0.0;
+  double t[1024];
+  for (int64_t b = 0; b < n; b += 1024) {
+    for (int i = 0; i < 1024; ++i) t[i] = (b + i < n) ? v[b + i] : 0.0;
+    for (int s = 512; s > 0; s >>= 1)
+      for (int i = 0; i < s; ++i) t[i] = t[i] + t[i + s];
+    total = total + t[0];
+  }
+  return total;
+}
+
+static void site_from(const oracle_fsite* f, double* o)
+{
+  o[0] = f->x; o[1] = f->y; o[2] = f->z;
+  o[3] = f->u; o[4] = f->v; o[5] = f->w;
+  o[6] = f->E; o[7] = f->wgt;
+}
+
+int oracle_eigen_run(oracle_problem* p, int64_t n, int32_t n_gen, int32_t n_inactive, uint64_t seed,
+                     double keff0, double fa, double fb, int64_t cap, int n_threads, const double* init_src,
+                     oracle_gen* out, double* src_out, oracle_fsite* bank_out, int64_t bank_cap,
+                     int64_t* bank_n, double* tally_sum)
+{
+  if (!p->planes) return fail(p, "no mesh");
+  if (prepare_data(p)) return 1;
+  if (p->n_mat < 1) return fail(p, "no materials");
+  if (n < 1 || n_gen < 1 || n_inactive < 0 || n_inactive >= n_gen) return fail(p, "bad generation counts");
+  int any = 0;
+  for (int i = 0; i < p->n_nuc; ++i)
+    if (p->nucs[i].nusf) any = 1;
+  if (!any) return fail(p, "no fissionable nuclide");
+  for (int64_t t = 0; t < p->n_tet; ++t) p->tmat[t] = material_of_block(p, p->blk[t]);
+  if (keff0 <= 0.0) keff0 = 1.0;
+  if (fa <= 0.0) fa = WATT_A_DEFAULT;
+  if (fb <= 0.0) fb = WATT_B_DEFAULT;
+  if (cap <= 0) cap = 3 * n;
+  int nt = n_threads < 1 ? 1 : n_threads;
+#ifndef _OPENMP
+  nt = 1;
+#endif
+  const int64_t ntal = oracle_tally_size(p);
+  double* src = (double*)malloc(sizeof(double) * 8 * (size_t)n);
+  double* nsrc = (double*)malloc(sizeof(double) * 8 * (size_t)n);
+  double* ktl = (double*)malloc(sizeof(double) * (size_t)n);
+  double* kcol = (double*)malloc(sizeof(double) * (size_t)n);
+  double* kabs = (double*)malloc(sizeof(double) * (size_t)n);
+  heig* he = (heig*)calloc((size_t)n, sizeof(heig));
+  double** priv = (double**)calloc((size_t)nt, sizeof(double*));
+  lstats* pl = (lstats*)calloc((size_t)nt, sizeof(lstats));
+  oracle_fsite* sorted = NULL;
+  int64_t m = 0;
+  int rc = 0;
+  for (int t = 0; t < nt; ++t) priv[t] = (double*)calloc((size_t)ntal, sizeof(double));
+  if (init_src) {
+    memcpy(src, init_src, sizeof(double) * 8 * (size_t)n);
+  } else {
+    /* OpenMC initialize_source: site i from the source stream of id i+1 */
+    for (int64_t i = 0; i < n; ++i) {
+      uint64_t ss = oracle_init_seed(i + 1, seed, 2);
+      double* o = src + 8 * i;
+      birth(p, i + 1, &ss, o, o + 3, o + 6);
+      o[7] = 1.0;
+    }
+  }
+  double keff = keff0, k_sum0 = 0.0, k_sum1 = 0.0, keff_std = 0.0;
+  int n_active = 0;
+  for (int g = 0; g < n_gen && rc == 0; ++g) {
+    const int active = g >= n_inactive;
+    for (int t = 0; t < nt; ++t) memset(pl + t, 0, sizeof(lstats));
+    for (int64_t i = 0; i < n; ++i) {
+      free(he[i].sites);
+      memset(he + i, 0, sizeof(heig));
+      he[i].on = 1;
+      he[i].keff = keff;
+      he[i].fa = fa;
+      he[i].fb = fb;
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+#endif
+    for (int64_t i = 0; i < n; ++i) {
+      int tid = 0;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      track(p, (int64_t)g * n + i, seed, src + 8 * i, he + i, priv[tid], NULL, pl + tid);
+    }
+    lstats tot;
+    memset(&tot, 0, sizeof tot);
+    for (int t = 0; t < nt; ++t) {
+      tot.n_seg += pl[t].n_seg;
+      tot.n_coll += pl[t].n_coll;
+      tot.leak_w += pl[t].leak_w;
+    }
+    /* the batch tally: active generations fold it (SUM += batch/n) */
+    if (active && tally_sum) {
+      for (int u = 1; u < nt; ++u)
+        for (int64_t e = 0; e < ntal; ++e) priv[0][e] += priv[u][e];
+      for (int64_t e = 0; e < ntal; ++e) tally_sum[e] += priv[0][e] * (1.0 / (double)n);
+    }
+    for (int t = 0; t < nt; ++t) memset(priv[t], 0, sizeof(double) * (size_t)ntal);
+    /* the bank in (parent, progeny) order: histories in order, each
+       history's sites in the order it banked them (sort_fission_bank) */
+    m = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      ktl[i] = he[i].ktl;
+      kcol[i] = he[i].kcol;
+      kabs[i] = he[i].kabs;
+      m += he[i].n_sites;
+    }
+    if (m > cap) { rc = fail(p, "fission bank full"); break; }
+    if (m == 0) { rc = fail(p, "no fission sites sampled"); break; }
+    free(sorted);
+    sorted = (oracle_fsite*)malloc(sizeof(oracle_fsite) * (size_t)m);
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      memcpy(sorted + k, he[i].sites, sizeof(oracle_fsite) * (size_t)he[i].n_sites);
+      k += he[i].n_sites;
+    }
+    /* synchronize_bank, one rank: sequential draws from the generation's
+       tracking-stream seed */
+    uint64_t s = oracle_init_seed(g + 1, seed, 0);
+    const int64_t needed = m < n ? n % m : n;
+    const double p_sample = (double)needed / (double)m;
+    int64_t idx = 0;
+    for (int64_t i = 0; i < m; ++i) {
+      if (m < n)
+        for (int64_t j = 1; j <= n / m; ++j) {
+          if (idx < n) site_from(sorted + i, nsrc + 8 * idx);
+          ++idx;
+        }
+      if (oracle_prn(&s) < p_sample) {
+        if (idx < n) site_from(sorted + i, nsrc + 8 * idx);
+        ++idx;
+      }
+    }
+    if (idx < n) {
+      const int64_t need = n - idx;
+      for (int64_t j = 0; j < need; ++j) {
+        int64_t b = m - need + j;
+        if (b < 0) b = 0;
+        site_from(sorted + b, nsrc + 8 * (idx + j));
+      }
+    }
+    double* sw = src;
+    src = nsrc;
+    nsrc = sw;
+    /* calculate_generation_keff / calculate_average_keff */
+    const double s_tl = fixed_sum(ktl, n), s_col = fixed_sum(kcol, n), s_abs = fixed_sum(kabs, n);
+    const double k_gen = s_tl / (double)n;
+    if (!active) {
+      keff = k_gen;
+    } else {
+      ++n_active;
+      k_sum0 += k_gen;
+      k_sum1 += k_gen * k_gen;
+      keff = k_sum0 / (double)n_active;
+      if (n_active > 1) keff_std = sqrt((k_sum1 / (double)n_active - keff * keff) / (double)(n_active - 1));
+    }
+    if (out) {
+      oracle_gen* o = out + g;
+      o->k_generation = k_gen;
+      o->k_collision = s_col / (double)n;
+      o->k_absorption = s_abs / (double)n;
+      o->keff = keff;
+      o->keff_std = keff_std;
+      o->leakage = tot.leak_w / (double)n;
+      o->n_sites = m;
+      o->n_seg = tot.n_seg;
+      o->n_coll = tot.n_coll;
+    }
+  }
+  if (rc == 0) {
+    if (src_out) memcpy(src_out, src, sizeof(double) * 8 * (size_t)n);
+    if (bank_n) *bank_n = m;
+    if (bank_out && sorted) memcpy(bank_out, sorted, sizeof(oracle_fsite) * (size_t)(m < bank_cap ? m : bank_cap));
+  }
+  for (int64_t i = 0; i < n; ++i) free(he[i].sites);
+  for (int t = 0; t < nt; ++t) free(priv[t]);
+  free(priv); free(pl); free(he); free(ktl); free(kcol); free(kabs); free(src); free(nsrc); free(sorted);
+  return rc;
 }

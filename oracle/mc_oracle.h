@@ -64,6 +64,20 @@ typedef struct {
   double leak_weight;
 } oracle_stats;
 
+/* One fission site (OpenMC SourceSite as create_fission_sites fills it). */
+typedef struct {
+  double x, y, z, u, v, w, E, wgt;
+  int64_t parent;   /* id of the history that banked it */
+  int32_t progeny;  /* its index among that history's sites */
+  int32_t pad;
+} oracle_fsite;
+
+/* Results of one k-eigenvalue generation. */
+typedef struct {
+  double k_generation, k_collision, k_absorption, keff, keff_std, leakage;
+  int64_t n_sites, n_seg, n_coll;
+} oracle_gen;
+
 oracle_problem* oracle_create(void);
 void oracle_destroy(oracle_problem* p);
 const char* oracle_error(oracle_problem* p);
@@ -98,6 +112,23 @@ int oracle_set_2d(oracle_problem* p, int32_t on, double z_coord);
  * traces (n entries) may be NULL. */
 int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n_threads,
                double* tally, oracle_trace* traces, oracle_stats* stats);
+
+/* nu*sigma_f per grid point of a nuclide (NULL: not fissionable).  A
+ * fissionable nuclide samples fission sites at each collision with it:
+ * banked by oracle_eigen_run, drawn and dropped by oracle_run. */
+int oracle_set_fission(oracle_problem* p, int32_t nuclide, const double* nu_sig_f);
+
+/* n_gen generations of n histories (generation g: history indices g*n..);
+ * the first from init_src (n x 8 doubles: x y z u v w E wgt) or, when NULL,
+ * from the source (ids 1..n, source stream).  keff0, fa, fb, cap <= 0 take
+ * 1, 0.988e6 eV, 2.249e-6 /eV, 3n.  out: n_gen records; src_out (n x 8):
+ * the sites of the next generation; bank_out: the last generation's sorted
+ * bank (first bank_cap sites), *bank_n its size; tally_sum (optional,
+ * oracle_tally_size values) accumulates batch/n over active generations. */
+int oracle_eigen_run(oracle_problem* p, int64_t n, int32_t n_gen, int32_t n_inactive, uint64_t seed,
+                     double keff0, double fa, double fb, int64_t cap, int n_threads, const double* init_src,
+                     oracle_gen* out, double* src_out, oracle_fsite* bank_out, int64_t bank_cap,
+                     int64_t* bank_n, double* tally_sum);
 
 /* Pieces exposed for unit tests. */
 double oracle_log(double x);

@@ -37,6 +37,12 @@ TRACE_DTYPE = np.dtype([("id", "<i8"), ("hash", "<u8"), ("status", "<i4"), ("n_s
                         ("n_coll", "<i4"), ("elem", "<i4"), ("face", "<i4"), ("pad", "<i4"),
                         ("E", "<f8"), ("x", "<f8"), ("y", "<f8"), ("z", "<f8")])
 
+FSITE_DTYPE = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("u", "<f8"), ("v", "<f8"), ("w", "<f8"),
+                        ("E", "<f8"), ("wgt", "<f8"), ("parent", "<i8"), ("progeny", "<i4"), ("pad", "<i4")])
+GEN_DTYPE = np.dtype([("k_generation", "<f8"), ("k_collision", "<f8"), ("k_absorption", "<f8"), ("keff", "<f8"),
+                      ("keff_std", "<f8"), ("leakage", "<f8"), ("n_sites", "<i8"), ("n_seg", "<i8"),
+                      ("n_coll", "<i8")])
+
 _SIG = {
     "oracle_create": ([], _P),
     "oracle_destroy": ([_P], None),
@@ -52,6 +58,9 @@ _SIG = {
     "oracle_tally_size": ([C.c_void_p], C.c_int64),
     "oracle_set_2d": ([C.c_void_p, C.c_int32, C.c_double], C.c_int),
     "oracle_run": ([_P, _I64, _I64, _U64, C.c_int, _P, _P, C.POINTER(OracleStats)], C.c_int),
+    "oracle_set_fission": ([_P, _I32, _P], C.c_int),
+    "oracle_eigen_run": ([_P, _I64, _I32, _I32, _U64, _D, _D, _D, _I64, C.c_int, _P, _P, _P, _P, _I64, _P, _P],
+                         C.c_int),
     "oracle_log": ([_D], _D),
     "oracle_prn": ([C.POINTER(_U64)], _D),
     "oracle_future_seed": ([_U64, _U64], _U64),
@@ -111,9 +120,12 @@ class Oracle:
         self.n_tet = tv.shape[0]
         for b, t in p.bcs.items():
             self._ck(lib.oracle_set_bc(self.h, b, t), "oracle_set_bc")
-        for n in p.nuclides:
+        for k, n in enumerate(p.nuclides):
             E, st, ss = (np.ascontiguousarray(a, np.float64) for a in (n.E, n.sig_t, n.sig_s))
             self._ck(lib.oracle_add_nuclide(self.h, E.size, _p(E), _p(st), _p(ss), n.awr), "oracle_add_nuclide")
+            if getattr(n, "nu_sig_f", None) is not None:
+                f = np.ascontiguousarray(n.nu_sig_f, np.float64)
+                self._ck(lib.oracle_set_fission(self.h, k, _p(f)), "oracle_set_fission")
         for m in p.materials:
             ni = np.ascontiguousarray(m.nuclides, np.int32)
             d = np.ascontiguousarray(m.densities, np.float64)
@@ -158,6 +170,26 @@ class Oracle:
         self._ck(lib.oracle_run(self.h, first, n, seed, threads, _p(tally), _p(tr), C.byref(st)), "oracle_run")
         dt = time.perf_counter() - t0
         return tally, tr, st.as_dict(), dt
+
+    def eigen(self, n: int, generations: int, inactive: int = 0, seed: int = 1, keff0: float = 0.0,
+              watt=(0.0, 0.0), capacity: int = 0, threads: int = 1, initial_source=None, tally: bool = False):
+        """k-eigenvalue generations.  Returns (per-generation records
+        (GEN_DTYPE), next source (n x 8: x y z u v w E wgt), last sorted
+        fission bank (FSITE_DTYPE), active-generation tally SUM or None,
+        seconds)."""
+        gens = np.zeros(generations, GEN_DTYPE)
+        src = np.zeros((n, 8))
+        cap = capacity if capacity > 0 else 3 * n
+        bank = np.zeros(cap, FSITE_DTYPE)
+        m = C.c_int64()
+        tsum = np.zeros(lib.oracle_tally_size(self.h)) if tally else None
+        init = None if initial_source is None else np.ascontiguousarray(initial_source, np.float64).reshape(n, 8)
+        t0 = time.perf_counter()
+        self._ck(lib.oracle_eigen_run(self.h, n, generations, inactive, seed, keff0, watt[0], watt[1], cap, threads,
+                                      _p(init), _p(gens), _p(src), _p(bank), cap, C.byref(m), _p(tsum)),
+                 "oracle_eigen_run")
+        dt = time.perf_counter() - t0
+        return gens, src, bank[:m.value].copy(), tsum, dt
 
     def mesh_tables(self):
         nb, pl = C.c_void_p(), C.c_void_p()
