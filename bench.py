@@ -26,6 +26,11 @@ More workloads print their own JSON line (not the default run):
                     batches of log-uniform size (1e5-5e6, rescaled) through
                     one pipelined, graph-replayed, autotuned call, mixed and
                     FP64 on the same histories
+  --workload eigen  the k-eigenvalue form: the lattice with fissionable fuel,
+                    reflective sides (2,039,184 tets, k near 1); 1e6
+                    particles per generation, W inactive then K active
+                    generations per precision, fission-bank sort and
+                    resampling on the device, keff of both precisions
   --workload serve  the serving form: a Poisson stream (50 requests/s) over
                     8 preloaded meshes of 10k-2M tets, continuous batching
                     with the mixed tracker and FP64 per-request tallies,
@@ -317,6 +322,75 @@ def run_cube(args):
     return 0
 
 
+def run_eigen(args):
+    """k-eigenvalue form (one JSON line): generations of 1e6 particles on the
+    fissionable lattice; value = active-generation histories / device time
+    of those generations (tracking, estimator sums, bank sort and
+    resampling; CUDA events on the tracker's stream)."""
+    import numpy as np
+    import torch
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED
+    from oracle.oracle import Oracle, cpu_threads
+    torch.cuda.set_device(0)
+    p = problems.eigen_lattice_problem()
+    n, K, W = 1_000_000, max(args.steps, 1), args.warmup
+    res = {}
+    with Tracker(0) as t:
+        t.load(p)
+        for name, prec, ms_ in (("fp64", MC_PREC_FP64, 64), ("mixed", MC_PREC_MIXED, 128)):
+            if name == "mixed" and args.no_mixed:
+                continue
+            clk = ClockSampler(0)
+            clk.start()
+            w0 = time.perf_counter()
+            g = t.eigen(n, W + K, W, seed=1, precision=prec, bank_size=n, max_seg=ms_, sort_queue=9, graph=True)
+            wall = time.perf_counter() - w0
+            clocks = clk.stop()
+            act = g[W:]
+            ms = float(act["ms"].sum())
+            S = float(act["n_seg"].sum()) / (n * K)
+            Cc = float(act["n_coll"].sum()) / (n * K)
+            res[name] = {"value": n * K / (ms / 1e3), "ms_per_generation": ms / K,
+                         "wall_histories_per_s": n * (W + K) / wall,
+                         "keff": float(act["keff"][-1]), "keff_std": float(act["keff_std"][-1]),
+                         "k_collision_mean": float(act["k_collision"].mean()),
+                         "k_absorption_mean": float(act["k_absorption"].mean()),
+                         "sites_per_generation": float(act["n_sites"].mean()),
+                         "segments_per_history": S, "collisions_per_history": Cc,
+                         "leakage": float(act["leakage"].mean()), "clocks": clocks}
+    peak, psrc = load_peaks()
+    f = res["fp64"]
+    # algorithmic bytes per history: segments (FP64 records, tally RMW), one
+    # cross-section event per flight (22 nuclides), a pick per collision, and
+    # per banked site its write, the sort's read and write and the
+    # resampled source write (80 + 160 + 64 B)
+    sites_ph = f["sites_per_generation"] / n
+    b_h = f["segments_per_history"] * B_SEG_FP64 + (f["collisions_per_history"] + 1) * B_XS_EVENT + \
+        f["collisions_per_history"] * B_COLL_PICK + sites_ph * (80 + 160 + 64)
+    threads = cpu_threads()
+    o = Oracle(p)
+    n_cpu = 20_000
+    og, _, _, _, odt = o.eigen(n_cpu, 2, 1, seed=1, threads=threads)
+    out = {"metric": "histories/s, k-eigenvalue generations", "unit": "histories/s", "n_gpus": 1,
+           "value": f["value"], "higher_is_better": True, "dtype": "f64", "steps": K, "warmup": W,
+           "data": "synthetic (seeded generators)",
+           "config": {"workload": f"eigen lattice 17x17 pins, 50 cm, {p.n_tet} tets, every fuel nuclide "
+                                  "fissionable, reflective sides, vacuum top/bottom; 1e6 particles per generation, "
+                                  f"{W} inactive + {K} active generations", "tets": p.n_tet,
+                      "l2": "inputs larger than L2 (mesh planes 261 MB, bank 80 MB)"},
+           "fp64": f, "mixed": res.get("mixed"),
+           "speedup_mixed_vs_fp64": res["mixed"]["value"] / f["value"] if "mixed" in res else None,
+           "roofline_history": {"bytes_per_history": b_h, "achieved": f["value"] * b_h / 1e9, "unit": "GB/s",
+                                "peak": peak, "peak_source": psrc, "frac": f["value"] * b_h / 1e9 / peak,
+                                "formula": "S*164 + (C+1)*64*22 + C*16*15 + sites*(80+160+64), FP64"},
+           "cpu_baseline": {"value": n_cpu * 2 / odt, "unit": "histories/s", "cores": threads, "kind": "port",
+                            "sample": f"{n_cpu} particles x 2 generations of the same problem (C oracle)",
+                            "keff_generation": [float(x) for x in og["k_generation"]]}}
+    print(json.dumps(out))
+    return 0
+
+
 def serve_problems():
     from macaw_gb300 import problems
     cubes = [(12, 12.0), (20, 20.0), (40, 40.0), (60, 60.0)]
@@ -369,7 +443,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (fixed parameters)")
     ap.add_argument("--hist", type=int, default=HIST_PER_STEP)
-    ap.add_argument("--workload", default="lattice", choices=["lattice", "cube", "core", "serve"])
+    ap.add_argument("--workload", default="lattice", choices=["lattice", "cube", "core", "serve", "eigen"])
     ap.add_argument("--core-histories", type=int, default=100_000_000)
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     args = ap.parse_args()
@@ -382,6 +456,8 @@ def main():
         return run_cube(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "eigen":
+        return run_eigen(args)
 
     import numpy as np
     import torch

@@ -70,3 +70,31 @@ def test_core_histories_all_end():
             st = t.run(sum(sizes), seed=1, precision=prec, accumulate=True, batch_sizes=sizes, bank_size=500_000,
                        max_seg=128, sort_queue=13)
             _accounting(st, sum(sizes))
+
+
+def test_eigen_lattice_full_size():
+    """k-eigenvalue generations on the full 2,039,184-tet lattice: three
+    FP64 generations of 200,000 particles bit-exact to the oracle (keff
+    estimators, site counts, sorted bank, next source), then 1e6 particles
+    per generation in both precisions with keff agreeing within statistics."""
+    p = problems.eigen_lattice_problem()
+    n = 200_000
+    g_ref, src_ref, bank_ref, _, _ = O.Oracle(p).eigen(n, 3, 1, seed=7, threads=16)
+    with Tracker(0) as t:
+        t.load(p)
+        g = t.eigen(n, 3, 1, seed=7, precision=MC_PREC_FP64, bank_size=n, max_seg=64, sort_queue=9, graph=True)
+        bank = t.fission_bank()
+        src = t.eigen_source(n)
+        for f in ("k_generation", "k_collision", "k_absorption", "keff", "keff_std", "n_sites", "n_seg", "n_coll"):
+            assert np.array_equal(g[f], g_ref[f]), f
+        for f in ("x", "y", "z", "u", "v", "w", "E", "parent", "progeny"):
+            assert np.array_equal(bank[f], bank_ref[f]), f
+        rows = np.stack([src[f] for f in ("x", "y", "z", "u", "v", "w", "E", "wgt")], axis=1)
+        assert np.array_equal(rows, src_ref)
+        N1 = 1_000_000
+        gd = t.eigen(N1, 6, 3, seed=8, precision=MC_PREC_FP64, bank_size=N1, max_seg=64, sort_queue=9, graph=True)
+        gm = t.eigen(N1, 6, 3, seed=8, precision=MC_PREC_MIXED, bank_size=N1, max_seg=128, sort_queue=9, graph=True)
+    kd, km = gd["keff"][-1], gm["keff"][-1]
+    sd = max(gd["keff_std"][-1], gm["keff_std"][-1], 1e-4)
+    assert abs(km - kd) < 5 * sd, (kd, km, sd)
+    assert 0.9 < kd < 1.2
