@@ -831,7 +831,11 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
         const int64_t inflight = (int64_t)h.n_xs[par] + h.n_adv[par];
         if (nb == 1 && inflight == 0 && h.next_hist >= a.n) break;
         if (h.next_hist >= a.n && inflight <= tail) {
-          CK(launch_event_finish(M, X, S, a, B, Q, ctl, par, block, grid, c->stream), "launch event finish");
+          // one warp per block: the few long histories left are spread over
+          // every SM instead of crowding the first blocks' SMs (their walks
+          // are latency chains that compete for each SM's FP64 pipe)
+          const int fgrid = (int)std::max<int64_t>(1, (inflight + 31) / 32);
+          CK(launch_event_finish(M, X, S, a, B, Q, ctl, par, 32, fgrid, c->stream), "launch event finish");
           ++n_launch;
           break;
         }

@@ -263,6 +263,7 @@ struct Problem {
   // data
   struct Nuc {
     std::vector<double> E, st, ss;
+    std::vector<double> nusf;  // nu*sigma_f; empty: not fissionable
     double awr;
   };
   std::vector<Nuc> nucs;
@@ -274,6 +275,10 @@ struct Problem {
   std::vector<Mat> mats;
   // study
   int64_t particles = 0, bank_size = 0;
+  // OpenMC settings run_mode eigenvalue: generations = batches, the first
+  // `inactive` of them score no tally
+  bool eigen = false;
+  int64_t inactive = 0;
   uint64_t seed = 1;
   int precision = MC_PREC_FP64, mode = MC_MODE_EVENT;
   mc_source_desc src{};
@@ -430,6 +435,18 @@ void synthetic_xs(Params& p, Problem& P) {
   const int n_peaks = (int)p.integer("n_peaks", 20);
   const double e_min = p.real("energy_min", 1e-5), e_max = p.real("energy_max", 2e7);
   const double d_lo = p.real("density_min", 1e-4), d_hi = p.real("density_max", 5e-2);
+  // constant cross sections added to every tabulated point (barn): elastic
+  // scattering (sigma_s and sigma_t) and absorption (sigma_t)
+  const double pot = p.real("scattering_offset", 0.0), absb = p.real("absorption_offset", 0.0);
+  if (!(pot >= 0.0) || !(absb >= 0.0)) p.error("scattering_offset", "offsets must be non-negative");
+  // fission data: every nuclide of the listed materials gets
+  // nu*sigma_f = nu * fission_share * sigma_a at each point
+  const auto fis = p.ints("fissionable_materials");
+  const double nu = p.real("nu", 2.43), share = p.real("fission_share", 0.6);
+  if (!(nu > 0.0) || !(share >= 0.0 && share <= 1.0)) p.error("nu", "nu must be positive, fission_share in [0, 1]");
+  for (int f : fis)
+    if (std::find(ids.begin(), ids.end(), f) == ids.end())
+      p.error("fissionable_materials", "material " + std::to_string(f) + " is not in material_ids");
   int k = 0;
   for (size_t m = 0; m < ids.size(); ++m) {
     Problem::Mat mat;
@@ -445,6 +462,16 @@ void synthetic_xs(Params& p, Problem& P) {
       n.ss.resize(n_pts);
       if (mc_gen_nuclide(seed, k, n_pts, e_min, e_max, n_peaks, n.E.data(), n.st.data(), n.ss.data(), &n.awr))
         p.error("n_points", "invalid nuclide table parameters");
+      if (pot > 0.0 || absb > 0.0)
+        for (int i = 0; i < n_pts; ++i) {
+          n.ss[i] = n.ss[i] + pot;
+          n.st[i] = n.st[i] + (pot + absb);
+        }
+      if (std::find(fis.begin(), fis.end(), ids[m]) != fis.end()) {
+        n.nusf.resize(n_pts);
+        const double c = nu * share;
+        for (int i = 0; i < n_pts; ++i) n.nusf[i] = c * (n.st[i] - n.ss[i]);
+      }
       mat.nuc.push_back((int32_t)P.nucs.size());
       P.nucs.push_back(std::move(n));
     }
@@ -468,6 +495,12 @@ void openmc_study(Params& p, Problem& P) {
   P.precision = p.choice("precision", {"fp64", "mixed"}, "fp64") == "mixed" ? MC_PREC_MIXED : MC_PREC_FP64;
   P.mode = p.choice("mode", {"event", "history"}, "event") == "history" ? MC_MODE_HISTORY : MC_MODE_EVENT;
   if (p.has("batches")) P.batches = p.integer("batches", 1);
+  // OpenMC settings.xml run mode (OpenMCStudy.C:133-136 rejects the
+  // particle, plotting and volume modes)
+  P.eigen = p.choice("run_mode", {"fixed source", "fixed_source", "eigenvalue"}, "fixed_source") == "eigenvalue";
+  P.inactive = p.integer("inactive", 0);
+  if (P.inactive < 0) p.error("inactive", "must be non-negative");
+  if (!P.eigen && P.inactive > 0) p.error("inactive", "inactive batches need run_mode = eigenvalue");
   mc_source_desc& s = P.src;
   const std::string space = p.choice("source_space", {"point", "box", "cylinders"}, "point");
   if (space == "point") {
@@ -786,9 +819,12 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
     check(ctx, mc_mesh_upload(ctx, P.n_vtx, P.xyz.data(), P.n_tet, P.tv.data(), P.blk.data(), P.bid.data()),
           "mesh");
     for (auto& b : P.bcs) check(ctx, mc_bc_set(ctx, b.first, b.second), "RayBCs");
-    for (auto& n : P.nucs)
-      check(ctx, mc_nuclide_add(ctx, (int64_t)n.E.size(), n.E.data(), n.st.data(), n.ss.data(), n.awr, nullptr),
+    for (auto& n : P.nucs) {
+      int32_t k = 0;
+      check(ctx, mc_nuclide_add(ctx, (int64_t)n.E.size(), n.E.data(), n.st.data(), n.ss.data(), n.awr, &k),
             "nuclide");
+      if (!n.nusf.empty()) check(ctx, mc_nuclide_set_fission(ctx, k, n.nusf.data()), "nuclide fission data");
+    }
     for (auto& m : P.mats)
       check(ctx, mc_material_add(ctx, m.id, (int32_t)m.nuc.size(), m.nuc.data(), m.dens.data()), "material");
     check(ctx, mc_block_material_map(ctx, (int32_t)P.blocks.size(), P.blocks.data(), P.materials.data()),
@@ -808,7 +844,34 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
     // ---- batches (Transient steps) ----
     const auto t0 = std::chrono::steady_clock::now();
     mc_stats tot{};
-    for (int64_t b = 0; b < P.batches; ++b) {
+    std::vector<mc_eigen_gen> gens;
+    if (P.eigen) {
+      // OpenMC eigenvalue mode: every batch is one generation; tallies and
+      // element results come from the active ones
+      if (P.inactive >= P.batches)
+        throw InputError("UserObjects/OpenMCStudy/inactive: must be below the number of batches");
+      bool any = false;
+      for (auto& n : P.nucs) any = any || !n.nusf.empty();
+      if (!any) throw InputError("UserObjects: run_mode = eigenvalue needs fissionable_materials");
+      if (P.rays) throw InputError("Outputs: RayTracingExodus output is available in fixed-source runs");
+      mc_eigen_desc e{};
+      e.n_particles = P.particles;
+      e.n_batches = (int32_t)P.batches;
+      e.n_inactive = (int32_t)P.inactive;
+      e.seed = P.seed;
+      e.precision = P.precision;
+      e.mode = P.mode;
+      e.bank_size = P.bank_size;
+      gens.resize((size_t)P.batches);
+      check(ctx, mc_eigen_run(ctx, &e, gens.data()), "eigenvalue generations");
+      for (auto& g : gens) {
+        tot.n_hist += P.particles;
+        tot.n_seg += g.n_seg;
+        tot.n_coll += g.n_coll;
+        tot.leak_weight += g.leakage * (double)P.particles;
+      }
+    }
+    for (int64_t b = 0; b < P.batches && !P.eigen; ++b) {
       if (P.rays && b == P.batches - 1)
         check(ctx, mc_rays_enable(ctx, (int32_t)std::min<int64_t>(P.rays_n, P.particles), P.rays_cap), "rays");
       mc_run_desc d{};
@@ -842,8 +905,31 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
     js << "{\"histories\": " << tot.n_hist << ", \"segments\": " << tot.n_seg << ", \"collisions\": " << tot.n_coll
        << ", \"leaked\": " << tot.n_leak << ", \"absorbed\": " << tot.n_absorb << ", \"stuck\": " << tot.n_stuck
        << ", \"lost\": " << tot.n_lost << ", \"batches\": " << P.batches << ", \"seconds\": " << secs
-       << ", \"neutrons_per_s\": " << (secs > 0 ? tot.n_hist / secs : 0.0) << ", \"aux\": {";
+       << ", \"neutrons_per_s\": " << (secs > 0 ? tot.n_hist / secs : 0.0);
+    if (P.eigen) {
+      // OpenMCStudy::postExecuteStudy prints "Keff <keff> (<std>) Generation: <k>" per batch
+      const mc_eigen_gen& L = gens.back();
+      js << ", \"keff\": " << L.keff << ", \"keff_std\": " << L.keff_std << ", \"inactive\": " << P.inactive
+         << ", \"generations\": [";
+      for (size_t g = 0; g < gens.size(); ++g)
+        js << (g ? ", " : "") << "{\"k_generation\": " << gens[g].k_generation << ", \"keff\": " << gens[g].keff
+           << ", \"keff_std\": " << gens[g].keff_std << ", \"k_collision\": " << gens[g].k_collision
+           << ", \"k_absorption\": " << gens[g].k_absorption << ", \"sites\": " << gens[g].n_sites << "}";
+      js << "]";
+      if (P.csv && !P.file_base.empty()) {
+        std::ofstream f(P.file_base + "_keff.csv");
+        if (!f) throw std::runtime_error("cannot write " + P.file_base + "_keff.csv");
+        f.precision(17);
+        f << "generation,k_generation,keff,keff_std,k_collision,k_absorption,fission_sites\n";
+        for (size_t g = 0; g < gens.size(); ++g)
+          f << g + 1 << "," << gens[g].k_generation << "," << gens[g].keff << "," << gens[g].keff_std << ","
+            << gens[g].k_collision << "," << gens[g].k_absorption << "," << gens[g].n_sites << "\n";
+      }
+    }
+    js << ", \"aux\": {";
     bool first = true;
+    // batches whose tallies were accumulated (eigenvalue runs: the active ones)
+    const double n_acc = P.eigen ? (double)(P.batches - P.inactive) : (double)P.batches;
     std::vector<std::string> ex_names;
     std::vector<double> ex_vals;  // per variable, n_tet values (per batch, as the csv)
     for (size_t ai = 0; ai < P.aux.size(); ++ai) {
@@ -873,14 +959,14 @@ extern "C" int mc_app_run(const char* input_text, int device, const char* file_b
       first = false;
       if (P.exodus) {
         ex_names.push_back(a.variable);
-        for (int64_t t = 0; t < P.n_tet; ++t) ex_vals.push_back(val[t] / (double)P.batches);
+        for (int64_t t = 0; t < P.n_tet; ++t) ex_vals.push_back(val[t] / n_acc);
       }
       if (P.csv && !P.file_base.empty()) {
         std::ofstream f(P.file_base + "_" + a.variable + ".csv");
         if (!f) throw std::runtime_error("cannot write " + P.file_base + "_" + a.variable + ".csv");
         f.precision(17);
         f << "elem,block," << a.variable << ",rel_err\n";
-        const double nbat = (double)P.batches;
+        const double nbat = n_acc;
         for (int64_t t = 0; t < P.n_tet; ++t) {
           double re = 0.0;
           if (a.granularity == "cell" && single && cell[t] > 0 && nbat > 1) {
@@ -972,7 +1058,14 @@ extern "C" int mc_app_check(const char* input_text, char* report, int64_t report
           }()
        << ", \"tallies\": " << P.tallies.size() << ", \"tally_values_per_element\": " << TP.nb * TP.desc.n_scores
        << ", \"aux\": " << P.aux.size() << ", \"precision\": \""
-       << (P.precision == MC_PREC_MIXED ? "mixed" : "fp64") << "\"}";
+       << (P.precision == MC_PREC_MIXED ? "mixed" : "fp64") << "\", \"run_mode\": \""
+       << (P.eigen ? "eigenvalue" : "fixed source") << "\", \"inactive\": " << P.inactive
+       << ", \"fissionable_nuclides\": " << [&] {
+            int n = 0;
+            for (auto& q : P.nucs) n += !q.nusf.empty();
+            return n;
+          }()
+       << "}";
     put(js.str());
     return MC_OK;
   } catch (const std::exception& e) {

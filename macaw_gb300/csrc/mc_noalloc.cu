@@ -192,7 +192,9 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
       const int64_t inflight = (int64_t)h.n_xs[par] + h.n_adv[par];
       if (inflight == 0 && h.next_hist >= a.n) break;
       if (h.next_hist >= a.n && inflight <= tail) {
-        e = launch_event_finish(v.M, v.X, v.S, a, B, Q, ctl, par, block, grid, st);
+        // one warp per block, spread over every SM (as mc_run does)
+        e = launch_event_finish(v.M, v.X, v.S, a, B, Q, ctl, par, 32, (int)std::max<int64_t>(1, (inflight + 31) / 32),
+                                st);
         if (e != cudaSuccess) return fail(MC_ERR_CUDA, std::string("event finish: ") + cudaGetErrorString(e));
         ++n_launch;
         break;

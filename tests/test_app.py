@@ -171,3 +171,43 @@ def test_two_d_input_runs_like_the_direct_api(tmp_path):
         t.run(20000, seed=1, accumulate=True, bank_size=1000000)
         ref = t.tally(MC_TALLY_SUM)
     assert rep["aux"]["flux"]["sum"] == pytest.approx(ref.sum(), rel=1e-12)
+
+
+def _small_eigen_input():
+    txt = app.read("eigen_lattice.i")
+    for a, b in (("nx = 17", "nx = 5"), ("ny = 17", "ny = 5"), ("nz = 21", "nz = 6"), ("height = 50", "height = 15"),
+                 ("n_points = 20000", "n_points = 3000"), ("particles = 1000000", "particles = 5000"),
+                 ("bank_size = 1000000", "bank_size = 2048"), ("inactive = 3", "inactive = 2"),
+                 ("num_steps = 13", "num_steps = 4")):
+        assert a in txt
+        txt = txt.replace(a, b)
+    return txt
+
+
+def test_eigen_input_checks():
+    c = app.check_input(app.read("eigen_lattice.i"))
+    assert c["run_mode"] == "eigenvalue" and c["inactive"] == 3 and c["fissionable_nuclides"] == 15
+    assert c["tets"] == 2039184 and c["reflective"] == 4 and c["batches"] == 13
+    with pytest.raises(ValueError, match="inactive batches need run_mode"):
+        app.check_input(app.read("lattice.i").replace("precision = fp64", "precision = fp64\n    inactive = 2"))
+    with pytest.raises(ValueError, match="not in material_ids"):
+        app.check_input(app.read("eigen_lattice.i").replace("fissionable_materials = '1'", "fissionable_materials = '7'"))
+
+
+@pytest.mark.gpu
+def test_eigen_input_runs_like_the_direct_api(tmp_path):
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_TALLY_SUM
+    rep = app.run_input(_small_eigen_input(), 0, str(tmp_path / "eig"))
+    p = problems.eigen_lattice_problem(nx=5, ny=5, nz=6, height=15.0, n_pts=3000)
+    with Tracker(0) as t:
+        t.load(p)
+        g = t.eigen(5000, 4, 2, seed=1, bank_size=2048)
+        ref = t.tally(MC_TALLY_SUM) / 2
+    assert [x["k_generation"] for x in rep["generations"]] == list(g["k_generation"])
+    assert rep["keff"] == g["keff"][-1] and rep["keff_std"] == g["keff_std"][-1]
+    k = np.loadtxt(tmp_path / "eig_keff.csv", delimiter=",", skiprows=1)
+    assert np.array_equal(k[:, 2], g["keff"])
+    csv = np.loadtxt(tmp_path / "eig_flux.csv", delimiter=",", skiprows=1)
+    nz = ref > 0
+    assert np.all(np.abs(csv[nz, 2] - ref[nz]) <= 1e-12 * ref[nz])
