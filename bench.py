@@ -338,13 +338,16 @@ def run_eigen(args):
     res = {}
     with Tracker(0) as t:
         t.load(p)
-        for name, prec, ms_ in (("fp64", MC_PREC_FP64, 64), ("mixed", MC_PREC_MIXED, 128)):
+        # walk budget and block from a sweep on this workload (8-32 segments,
+        # 128/256 threads): flights here are about 28 segments long
+        for name, prec, ms_ in (("fp64", MC_PREC_FP64, 32), ("mixed", MC_PREC_MIXED, 32)):
             if name == "mixed" and args.no_mixed:
                 continue
             clk = ClockSampler(0)
             clk.start()
             w0 = time.perf_counter()
-            g = t.eigen(n, W + K, W, seed=1, precision=prec, bank_size=n, max_seg=ms_, sort_queue=9, graph=True)
+            g = t.eigen(n, W + K, W, seed=1, precision=prec, bank_size=n, max_seg=ms_, sort_queue=9, graph=True,
+                        block_size=128)
             wall = time.perf_counter() - w0
             clocks = clk.stop()
             act = g[W:]

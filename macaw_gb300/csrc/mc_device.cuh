@@ -881,7 +881,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
       xs_cache_put<kEig>(p, mat, s, nf);
     }
     p.mat = mat;
-    sigt32 = (float)p.sigt;
+    sigt32 = narrow(p.sigt);
   }
   const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
   int bf = -1;
@@ -1021,9 +1021,12 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
       xs_cache_put<kEig>(p, mat, s, nf);
     }
     p.mat = mat;
-    sigt32 = (float)p.sigt;
+    sigt32 = narrow(p.sigt);
   }
-  const float xf = (float)p.x, yf = (float)p.y, zf = (float)p.z;
+  // float copies by integer operations (a conversion would issue on the
+  // FP64 pipe, which bounds this walk); narrow() differs from a conversion
+  // only below 2^-126, far inside the bounds' additive term
+  const float xf = narrow(p.x), yf = narrow(p.y), zf = narrow(p.z);
   const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
   const float Eden = 7.2e-7f * (fabsf(uf) + fabsf(vf) + fabsf(wf));
   const float4* P32 = M.tet[p.elem].p;
@@ -1032,26 +1035,27 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   bool sure = true;
   int bf = -1;
   float tb = 3.0e38f, eb = 0.0f, lo_other = 3.0e38f;
+  // Branch-free over the four sides (the entry side and sides facing away
+  // get t = 3e38, e = 0, which changes nothing below).  The divisions are
+  // __fdividef (at most 2 ulp for the normal divisors here), inside the
+  // 4.8e-7 |t| division term and the 0.1% padding of the bound.
 #pragma unroll
   for (int f = 0; f < 4; ++f) {
-    if (f == p.fin) continue;
     const float4 pl = __ldg(P32 + f);
     const float den = fmaf(pl.x, uf, fmaf(pl.y, vf, pl.z * wf));
-    if (fabsf(den) <= Eden) sure = false;
-    if (den > Eden) {
-      const float num = pl.w - fmaf(pl.x, xf, fmaf(pl.y, yf, pl.z * zf));
-      const float En = 7.2e-7f * (fabsf(pl.w) + xa);
-      const float t = num / den;
-      const float e = ((En + fabsf(t) * Eden) / (den - Eden) + 4.8e-7f * fabsf(t)) * 1.001f + 1e-30f;
-      if (t < tb) {
-        if (bf >= 0) lo_other = fminf(lo_other, tb - eb);
-        bf = f;
-        tb = t;
-        eb = e;
-      } else {
-        lo_other = fminf(lo_other, t - e);
-      }
-    }
+    const float num = pl.w - fmaf(pl.x, xf, fmaf(pl.y, yf, pl.z * zf));
+    const float En = 7.2e-7f * (fabsf(pl.w) + xa);
+    const bool other = f != p.fin;
+    if (other && fabsf(den) <= Eden) sure = false;
+    const bool cand = other && den > Eden;
+    const float t = cand ? __fdividef(num, den) : 3.0e38f;
+    const float e =
+        cand ? (__fdividef(En + fabsf(t) * Eden, den - Eden) + 4.8e-7f * fabsf(t)) * 1.001f + 1e-30f : 0.0f;
+    const bool nearer = t < tb;
+    lo_other = fminf(lo_other, nearer ? tb - eb : t - e);
+    bf = nearer ? f : bf;
+    tb = nearer ? t : tb;
+    eb = nearer ? e : eb;
   }
   if (!sure || bf < 0 || !(tb + eb < lo_other)) {
     const int r = segment_fp64<kInlineXS, kRays, kEig>(M, X, p, tally, T, sigt32, n_xs);
@@ -1062,16 +1066,20 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   const double bden = plb.x * p.u + plb.y * p.v + plb.z * p.w;
   const double bnum = plb.w - (plb.x * p.x + plb.y * p.y + plb.z * p.z);
   double L = bnum / bden;
-  if (!(L > 0.0)) L = 0.0;
+  // L > 0 as a sign test on the bits (bden > 0 is certified and bnum is
+  // finite, so L is not NaN; -0 clamps to +0 as before)
+  if ((long long)dbits(L) <= 0) L = 0.0;
   // one draw per segment: advance the state once, derive both forms
   p.seed = kPrnMult * p.seed + kPrnAdd;
   uint64_t wv = ((p.seed >> ((p.seed >> 59u) + 5u)) ^ p.seed) * 12605985483714917081ULL;
   wv = (wv >> 43u) ^ wv;
-  // xi = (wv >> 11) 2^-53 < (hi32 + 1) 2^-32 <= xhi; -logf(xhi) is a lower
-  // bound of -ln(xi) up to logf's 1-ulp error
+  // xi = (wv >> 11) 2^-53 < (hi32 + 1) 2^-32 <= xhi; lf is a lower bound of
+  // -ln(xi): __logf's documented error is at most 2^-21.41 absolute on
+  // [0.5, 2] and 3 ulp elsewhere, inside the 1e-6 relative and 1e-6
+  // absolute margins
   const float xhi = fmaf((float)(uint32_t)(wv >> 32), 2.3283064365386963e-10f, 2.3283064365386963e-10f) *
                     1.00000024f;
-  const float lf = -logf(xhi) * 0.99999976f - 1e-7f;
+  const float lf = -__logf(xhi) * 0.999999f - 1e-6f;
   const float thr = fmaxf(tb + eb, 0.0f) * sigt32;
   bool cross;
   double dist = 0.0;
@@ -1083,10 +1091,11 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     cross = dist > L;
   }
   const double score = cross ? L : dist;
-  score_track(T, tally, p.elem, p.E, p.wgt == 1.0 ? score : p.wgt * score, p.sigt);
+  // weight 1 and L == 0 tested on the bits (integer pipe)
+  score_track(T, tally, p.elem, p.E, dbits(p.wgt) == dbits(1.0) ? score : p.wgt * score, p.sigt);
   if (kEig) p.ktl = p.ktl + p.wgt * score * p.nuf;  // CollisionKernel.C:153-154
   ++p.n_seg;
-  if (L == 0.0) ++p.zero_run;
+  if (dbits(L) == 0) ++p.zero_run;
   else p.zero_run = 0;
   if (cross) {
     p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
@@ -1142,14 +1151,15 @@ struct Geo32 {
   float x, y, z, u, v, w;
 };
 
+// Conversions by integer operations (narrow, widen), off the FP64 pipe.
 __device__ __forceinline__ void geo_load(const Particle& p, Geo32& g) {
-  g.x = (float)p.x; g.y = (float)p.y; g.z = (float)p.z;
-  g.u = (float)p.u; g.v = (float)p.v; g.w = (float)p.w;
+  g.x = narrow(p.x); g.y = narrow(p.y); g.z = narrow(p.z);
+  g.u = narrow(p.u); g.v = narrow(p.v); g.w = narrow(p.w);
 }
 
 __device__ __forceinline__ void geo_store(const Geo32& g, Particle& p) {
-  p.x = g.x; p.y = g.y; p.z = g.z;
-  p.u = g.u; p.v = g.v; p.w = g.w;
+  p.x = widen(g.x); p.y = widen(g.y); p.z = widen(g.z);
+  p.u = widen(g.u); p.v = widen(g.v); p.w = widen(g.w);
 }
 
 // FP64 re-solve of the exit side for a float position/direction.

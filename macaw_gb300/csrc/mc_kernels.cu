@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
     unsigned long long nxs = 0, nfb = 0;
     if (kPrec == MC_PREC_FP64) {
       float sigt32 = 0.0f;
-      float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
+      float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
       while (p.status == kAlive) {
         const int r = segment_fp64g<true, false, true, kEig>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts,
                                                              sigt32, nxs);
@@ -280,9 +280,9 @@ __global__ void __launch_bounds__(256) k_history(DevMesh M, DevXS X, DevSource S
           collide<kEig>(X, p, a.two_d, a.eig);
         }
         if (r == 1 || r == 5) {
-          uf = (float)p.u;
-          vf = (float)p.v;
-          wf = (float)p.w;
+          uf = narrow(p.u);
+          vf = narrow(p.v);
+          wf = narrow(p.w);
         }
       }
     } else {
@@ -414,14 +414,14 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
     int r = 0;
     int k = 0;
     if (kPrec == MC_PREC_FP64) {
-      float sigt32 = (float)p.sigt;
-      float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
+      float sigt32 = narrow(p.sigt);
+      float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
       for (;;) {
         r = segment_fp64g<false, false, kRays, kEig>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 5) {
-          uf = (float)p.u;
-          vf = (float)p.v;
-          wf = (float)p.w;
+          uf = narrow(p.u);
+          vf = narrow(p.v);
+          wf = narrow(p.w);
           r = 0;
         }
         if (r != 0) break;
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
       load(B, s, p);
       seg0 = p.n_seg;
       geo_load(p, g);
-      f32 = (kPrec == MC_PREC_FP64) ? (float)p.sigt : (float)(1.0 / p.sigt);
+      f32 = (kPrec == MC_PREC_FP64) ? narrow(p.sigt) : (float)(1.0 / p.sigt);
     }
   }
   while (__any_sync(0xffffffffu, s >= 0)) {
@@ -499,9 +499,9 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
     if (kPrec == MC_PREC_FP64) {
       r = segment_fp64g<false>(M, X, p, g.u, g.v, g.w, tally_of(a, p.tag), a.ts, f32, nxs);
       if (r == 5) {
-        g.u = (float)p.u;
-        g.v = (float)p.v;
-        g.w = (float)p.w;
+        g.u = narrow(p.u);
+        g.v = narrow(p.v);
+        g.w = narrow(p.w);
         r = 0;
       }
     } else {
@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
       load(B, s, p);
       seg0 = p.n_seg;
       geo_load(p, g);
-      f32 = (kPrec == MC_PREC_FP64) ? (float)p.sigt : (float)(1.0 / p.sigt);
+      f32 = (kPrec == MC_PREC_FP64) ? narrow(p.sigt) : (float)(1.0 / p.sigt);
     }
   }
   L.add(kCntFallback, nfb);
@@ -617,20 +617,16 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
       }
       int bf = -1;
       float t1 = 3.0e38f, t2 = 3.0e38f;
+      // branch-free: every lane runs the same instructions for every side
+      // (a side that is the entry side or faces away gets t = 3e38)
       auto side = [&](const float4& pl, int f) {
-        if (f == fin) return;
         const float den = fmaf(pl.x, u, fmaf(pl.y, v, pl.z * w));
-        if (den > 0.0f) {
-          const float num = pl.w - fmaf(pl.x, x, fmaf(pl.y, y, pl.z * z));
-          const float t = __fdividef(num, den);
-          if (t < t1) {
-            t2 = t1;
-            t1 = t;
-            bf = f;
-          } else if (t < t2) {
-            t2 = t;
-          }
-        }
+        const float num = pl.w - fmaf(pl.x, x, fmaf(pl.y, y, pl.z * z));
+        const float t = (f != fin && den > 0.0f) ? __fdividef(num, den) : 3.0e38f;
+        const bool lt1 = t < t1;
+        t2 = lt1 ? t1 : fminf(t2, t);
+        bf = lt1 ? f : bf;
+        t1 = lt1 ? t : t1;
       };
       side(P0, 0);
       side(P1, 1);
@@ -850,8 +846,8 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
     load(B, s, p, kEig);
     unsigned long long nxs = 0, nfb = 0;
     if (kPrec == MC_PREC_FP64) {
-      float sigt32 = (float)p.sigt;
-      float uf = (float)p.u, vf = (float)p.v, wf = (float)p.w;
+      float sigt32 = narrow(p.sigt);
+      float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
       while (p.status == kAlive) {
         const int r = segment_fp64g<true, true, true, kEig>(M, X, p, uf, vf, wf, tally_of(a, p.tag), a.ts, sigt32, nxs);
         if (r == 1) {
@@ -859,9 +855,9 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
           collide<kEig>(X, p, a.two_d, a.eig);
         }
         if (r == 1 || r == 5) {
-          uf = (float)p.u;
-          vf = (float)p.v;
-          wf = (float)p.w;
+          uf = narrow(p.u);
+          vf = narrow(p.v);
+          wf = narrow(p.w);
         }
       }
     } else {
