@@ -525,10 +525,13 @@ def main():
     timed(t, MC_PREC_FP64, params64, 0, W, False)
     clocks = ClockSampler(local)
     clocks.start()
-    ms, st = timed(t, MC_PREC_FP64, params64, W, K, True)
+    ms, st = timed(t, MC_PREC_FP64, params64, W, K, False)
     clk = clocks.stop()
     value = world * n * K / (ms / 1e3)
     sum64 = t.tally(MC_TALLY_SUM)
+    # one more batch with the walk launches timed (CUDA events around each
+    # walk launch, which turns graph replay off), for the walk's roofline
+    _, pst64 = timed(t, MC_PREC_FP64, params64, W + K, 1, True)
 
     # --- mixed-precision form on the same histories ---
     mixed = None
@@ -611,20 +614,21 @@ def main():
     if rank == 0:
         peak, peak_kind = load_peaks()
         segs = st.n_seg
-        walk = st.n_seg_advance  # segments inside the timed walk launches (the rest: tail kernel)
+        walk = pst64.n_seg_advance  # segments inside the timed walk launches (the rest: tail kernel)
         adv_bytes = walk * B_SEG_FP64
-        achieved = adv_bytes / (st.ms_advance / 1e3) / 1e9 if st.ms_advance > 0 else None
+        achieved = adv_bytes / (pst64.ms_advance / 1e3) / 1e9 if pst64.ms_advance > 0 else None
         roof = {"bound": "hbm", "kernel": "k_ev_advance<FP64>" if params64.get("refill")
                 else "k_ev_advance_static<FP64>",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * walk / max(st.n_advance_launch, 1))
+                "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * walk / max(pst64.n_advance_launch, 1))
                 if ADVANCE_DRAM_BYTES_PER_SEG else None,
-                "segments_per_launch": walk / max(st.n_advance_launch, 1),
+                "segments_per_launch": walk / max(pst64.n_advance_launch, 1),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes_per_segment": B_SEG_FP64,
-                "advance_ms_per_launch": st.ms_advance / max(st.n_advance_launch, 1),
-                "advance_share_of_step": st.ms_advance / ms if ms > 0 else None,
+                "advance_ms_per_launch": pst64.ms_advance / max(pst64.n_advance_launch, 1),
+                "advance_share_of_step": pst64.ms_advance / pst64.ms_total if pst64.ms_total > 0 else None,
+                "sample": f"one extra profiled batch of {n} histories",
                 "traffic_source": "ncu DRAM bytes per walked segment (profiles/walk_fp64_lattice.md) x segments "
                                   "per launch",
                 "limiter": {"fp64_pipe_active": FP64_PIPE_ACTIVE,

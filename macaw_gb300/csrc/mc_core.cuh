@@ -47,8 +47,40 @@ struct Skip {
   uint64_t G, C;
 };
 
+// The maps for 2^k steps, k = 0..63 (each the previous one applied twice).
+struct SkipTable {
+  uint64_t G[64], C[64];
+};
+constexpr SkipTable make_skip_table() {
+  SkipTable t{};
+  uint64_t g = kPrnMult, c = kPrnAdd;
+  for (int k = 0; k < 64; ++k) {
+    t.G[k] = g;
+    t.C[k] = c;
+    c = (g + 1ULL) * c;
+    g = g * g;
+  }
+  return t;
+}
+#ifdef __CUDACC__
+__constant__ SkipTable kSkipTable = make_skip_table();
+#endif
+
+// The maps of the LCG commute, so composing the 2^k-step maps of n's set
+// bits in any order gives the same (G, C); on the device the 2^k maps come
+// from the table instead of being squared up on the way.
 MC_HD Skip skip_ahead(uint64_t n) {
-  uint64_t g = kPrnMult, c = kPrnAdd, G = 1, C = 0;
+  uint64_t G = 1, C = 0;
+#ifdef __CUDA_ARCH__
+  for (int k = 0; n > 0; ++k, n >>= 1) {
+    if (n & 1ULL) {
+      const uint64_t g = kSkipTable.G[k], c = kSkipTable.C[k];
+      G = G * g;
+      C = C * g + c;
+    }
+  }
+#else
+  uint64_t g = kPrnMult, c = kPrnAdd;
   while (n > 0) {
     if (n & 1ULL) {
       G = G * g;
@@ -58,6 +90,7 @@ MC_HD Skip skip_ahead(uint64_t n) {
     g = g * g;
     n >>= 1;
   }
+#endif
   return Skip{G, C};
 }
 
