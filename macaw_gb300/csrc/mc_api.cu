@@ -757,7 +757,7 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
       int oldest = 0;
       EventCtl h;
       const int kGroup = 4;
-      const int64_t tail = std::max<int64_t>(4096, cap / 64);
+      const int64_t tail = d->tail > 0 ? (int64_t)d->tail : d->tail < 0 ? -1 : std::max<int64_t>(4096, cap / 64);
       // a graph replays one group of iterations (parity 0,1,0,1: the group
       // always starts at parity 0), captured on first use
       const bool use_graph = d->graph && !d->profile;

@@ -179,7 +179,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
     n_launch = 1;
     int par = 0;
     EventCtl h;
-    const int64_t tail = std::max<int64_t>(1024, cap / 64);
+    const int64_t tail = d->tail > 0 ? (int64_t)d->tail : d->tail < 0 ? -1 : std::max<int64_t>(1024, cap / 64);
     for (int64_t it = 0;; ++it) {
       for (int gi = 0; gi < 4; ++gi) {
         e = launch_event_iteration(v.M, v.X, v.S, a, B, Q, ctl, par, block, grid, st, &n_launch);

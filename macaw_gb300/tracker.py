@@ -154,7 +154,7 @@ class Tracker:
             precision: int = MC_PREC_FP64, bank_size: int = 0, block_size: int = 0,
             max_seg: int = 0, traces: bool = False, accumulate: bool = False,
             sort_queue: bool = False, profile: bool = False, sites: np.ndarray | None = None,
-            refill: bool = False, batch_sizes=None, graph: bool = False) -> Stats:
+            refill: bool = False, batch_sizes=None, graph: bool = False, tail: int = 0) -> Stats:
         """One batch of n histories, or, with batch_sizes (adding up to n),
         consecutive batches run through one pipeline (needs accumulate)."""
         if sites is not None:
@@ -162,7 +162,7 @@ class Tracker:
         bs = None if batch_sizes is None else np.ascontiguousarray(batch_sizes, np.int64)
         d = RunDesc(first, n, bank_size, seed, precision, mode, block_size, max_seg, int(traces),
                     int(accumulate), int(sort_queue), int(profile), int(refill), 0 if bs is None else bs.size,
-                    int(graph), 0, None if sites is None else sites.ctypes.data,
+                    int(graph), int(tail), None if sites is None else sites.ctypes.data,
                     None if bs is None else bs.ctypes.data)
         self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
         return self.stats()
