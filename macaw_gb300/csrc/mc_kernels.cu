@@ -538,12 +538,208 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
   flush(L, a.counters, a.leak_w);
 }
 
-// Mixed-precision segment walk with a compact state: float position and
-// direction, float 1/Sigma_t for the cached materials, 64-bit RNG state and
-// trace hash.  Only the bank fields the walk reads or changes move; the
-// rest of a particle is touched only when its history ends here.  Same
-// arithmetic as segment_mixed.  Each lane walks the particles of its warp's
-// queue chunks one visit at a time.
+// One visit of the compact mixed-precision walk to the particle in bank
+// slot s: float position and direction, float 1/Sigma_t for the cached
+// materials, 64-bit RNG state and trace hash; only the bank fields the walk
+// reads or changes move, the rest of a particle is touched only when its
+// history ends here.  Same arithmetic as segment_mixed.  Walks until an
+// event or max_seg segments (max_seg <= 0: until an event) and returns r:
+// 1 collision, 2 history ended (finished here), 3 cross-section event due,
+// 4 segment budget.  queue: hand the particle to the queue of its next
+// event (the event loop); otherwise the caller handles the event.
+__device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, const Bank& B, const EventQueues& Q,
+                                           EventCtl* ctl, int nxt, int s, int max_seg, float tol, bool hashing,
+                                           bool queue, LocalCounters& L) {
+  // (queue = false: the tail kernel; its segments are not walk-launch segments)
+  float x = narrow(B.x[s]), y = narrow(B.y[s]), z = narrow(B.z[s]);
+  float u = narrow(B.u[s]), v = narrow(B.v[s]), w = narrow(B.w[s]);
+  int elem = B.elem[s], fin = B.fin[s], mat = B.mat[s], n_seg = B.n_seg[s], zrun = B.zero_run[s];
+  const int seg0 = n_seg;
+  uint64_t seed = B.seed[s], hash = B.hash[s];
+  const double wgt = B.wgt[s];
+  const bool unit_w = __double_as_longlong(wgt) == __double_as_longlong(1.0);
+  double* const tal = tally_of(a, B.tag[s]);
+  const int4 cm = B.cm[s];
+  const float4 ci = B.cinv[s];
+  int slot = -1;  // cache slot whose Sigma_t is current, if the walk changed material
+  // the cached float 1/Sigma_t of the current material (set below when mat < 0)
+  float inv_sig = 0.0f;
+  if (mat >= 0) {
+    const int sl = xs_cache_slot(cm, mat);
+    inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
+  }
+  int r = 0, face = -1;
+  int k = 0;
+  // The record of the element being walked is loaded one step ahead: at
+  // each crossing the neighbour's planes, entries and (after a flagged
+  // side) material are requested before that segment's tally, hash and
+  // position update, so the loads are in flight while those run.
+  float4 P0, P1, P2, P3;
+  int4 nb4;
+  int mnext = 0;  // material of elem, valid while mat < 0
+  {
+    const Tet32* T = M.tet + elem;
+    P0 = __ldg(&T->p[0]);
+    P1 = __ldg(&T->p[1]);
+    P2 = __ldg(&T->p[2]);
+    P3 = __ldg(&T->p[3]);
+    nb4 = __ldg(&T->nbr);
+    if (mat < 0) mnext = __ldg(M.tmat + elem);
+  }
+  for (;;) {
+    if (n_seg >= kMaxSegments || zrun >= kMaxZeroRun) {
+      r = 2;
+      face = -2;  // stuck
+      break;
+    }
+    // this segment's draw depends on no load: formed while they land,
+    // committed to the RNG state only when the segment is scored
+    const uint64_t seed_n = kPrnMult * seed + kPrnAdd;
+    uint64_t wv = ((seed_n >> ((seed_n >> 59u) + 5u)) ^ seed_n) * 12605985483714917081ULL;
+    wv = (wv >> 43u) ^ wv;
+    const float lnxi = -__logf((float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f);
+    if (mat < 0) {  // after a side flagged kMatChange
+      const int m = mnext;
+      const int sl = m < 0 ? -1 : xs_cache_slot(cm, m);
+      if (sl < 0) {
+        r = (m < 0) ? 2 : 3;
+        if (m < 0) face = -3;  // no material: bad cross section
+        break;
+      }
+      mat = m;
+      slot = sl;
+      inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
+    }
+    int bf = -1;
+    float t1 = 3.0e38f, t2 = 3.0e38f;
+    // branch-free: every lane runs the same instructions for every side
+    // (a side that is the entry side or faces away gets t = 3e38)
+    auto side = [&](const float4& pl, int f) {
+      const float den = fmaf(pl.x, u, fmaf(pl.y, v, pl.z * w));
+      const float num = pl.w - fmaf(pl.x, x, fmaf(pl.y, y, pl.z * z));
+      const float t = (f != fin && den > 0.0f) ? __fdividef(num, den) : 3.0e38f;
+      const bool lt1 = t < t1;
+      t2 = lt1 ? t1 : fminf(t2, t);
+      bf = lt1 ? f : bf;
+      t1 = lt1 ? t : t1;
+    };
+    side(P0, 0);
+    side(P1, 1);
+    side(P2, 2);
+    side(P3, 3);
+    float Ls;
+    if (bf < 0 || t2 - t1 <= tol || t1 < -tol) {
+      L.add(kCntFallback, 1);
+      Geo32 g{x, y, z, u, v, w};
+      double Ld = 0.0;
+      bf = exit_fp64(M, elem, fin, g, Ld);
+      if (bf < 0) {
+        r = 2;
+        face = -2;
+        break;
+      }
+      Ls = (float)Ld;
+    } else {
+      Ls = fmaxf(t1, 0.0f);
+    }
+    seed = seed_n;
+    const float dist = lnxi * inv_sig;
+    const bool cross = dist > Ls;
+    const int nb = side_entry(nb4, bf);
+    const int next = (nb & (kMatChange - 1)) >> 2;
+    if (cross && nb >= 0) {
+      const Tet32* T = M.tet + next;
+      P0 = __ldg(&T->p[0]);
+      P1 = __ldg(&T->p[1]);
+      P2 = __ldg(&T->p[2]);
+      P3 = __ldg(&T->p[3]);
+      nb4 = __ldg(&T->nbr);
+      if (nb & kMatChange) mnext = __ldg(M.tmat + next);
+    }
+    const float score = cross ? Ls : dist;
+    atomicAdd(tal + elem, unit_w ? widen(score) : wgt * widen(score));
+    ++n_seg;
+    if (Ls == 0.0f) ++zrun;
+    else zrun = 0;
+    if (!cross) {
+      if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + 4ULL);
+      x = fmaf(dist, u, x);
+      y = fmaf(dist, v, y);
+      z = fmaf(dist, w, z);
+      zrun = 0;
+      r = 1;
+      break;
+    }
+    if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + (uint64_t)bf);
+    x = fmaf(Ls, u, x);
+    y = fmaf(Ls, v, y);
+    z = fmaf(Ls, w, z);
+    if (nb >= 0) {
+      if (nb & kMatChange) mat = -2;
+      elem = next;
+      fin = nb & 3;
+    } else {
+      const int bid = -1 - nb;
+      if (bid < M.n_bid && M.bc_type[bid] == 1) {
+        // no load is issued for a boundary side: P0..P3 are still this element's
+        const float4 pb = bf == 0 ? P0 : bf == 1 ? P1 : bf == 2 ? P2 : P3;
+        const float t2r = 2.0f * fmaf(u, pb.x, fmaf(v, pb.y, w * pb.z));
+        u = fmaf(-t2r, pb.x, u);
+        v = fmaf(-t2r, pb.y, v);
+        w = fmaf(-t2r, pb.z, w);
+        const float nrm = rsqrtf(fmaf(u, u, fmaf(v, v, w * w)));
+        u *= nrm;
+        v *= nrm;
+        w *= nrm;
+        fin = -1;
+      } else {
+        r = 2;
+        face = bf;  // leaked through side bf
+        break;
+      }
+    }
+    if (a.max_seg > 0 && ++k >= a.max_seg) {
+      r = 4;
+      break;
+    }
+  }
+  if (queue) L.add(kCntSegWalk, (unsigned long long)(n_seg - seg0));
+  if (r == 2) {
+    Particle p;
+    load(B, s, p);
+    p.x = widen(x); p.y = widen(y); p.z = widen(z);
+    p.u = widen(u); p.v = widen(v); p.w = widen(w);
+    p.elem = elem; p.fin = fin; p.mat = mat; p.n_seg = n_seg; p.zero_run = zrun;
+    p.seed = seed; p.hash = hash;
+    if (face >= 0) {
+      p.status = kLeaked;
+      p.face = face;
+    } else {
+      p.status = face == -3 ? kBadXS : kStuck;
+    }
+    finish(p, a, L);
+    if (queue) push_free(Q, ctl, s, B.cap);
+    return 2;
+  }
+  B.x[s] = widen(x); B.y[s] = widen(y); B.z[s] = widen(z);
+  B.u[s] = widen(u); B.v[s] = widen(v); B.w[s] = widen(w);
+  B.elem[s] = elem; B.fin[s] = fin; B.mat[s] = mat; B.n_seg[s] = n_seg; B.zero_run[s] = zrun;
+  B.seed[s] = seed; B.hash[s] = hash;
+  if (slot >= 0) {
+    const double4_32a c = B.cs[s];
+    B.sigt[s] = slot == 0 ? c.x : slot == 1 ? c.y : slot == 2 ? c.z : c.w;
+  }
+  if (r == 1) B.n_coll[s] = B.n_coll[s] + 1;
+  if (queue) {
+    if (r == 1) push(Q.coll, &ctl->n_coll, s);
+    else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+    else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
+  }
+  return r;
+}
+
+// Mixed-precision segment walk (mixed_visit), each lane walking the
+// particles of its warp's queue chunks one visit at a time.
 __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B, EventQueues Q,
                                                              EventCtl* ctl, int par) {
   MC_COUNTERS(L);
@@ -556,192 +752,7 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
     if (__shfl_sync(0xffffffffu, i, 0) >= n) break;
     if (i >= n) continue;
     const int s = Q.adv[par][i];
-    float x = narrow(B.x[s]), y = narrow(B.y[s]), z = narrow(B.z[s]);
-    float u = narrow(B.u[s]), v = narrow(B.v[s]), w = narrow(B.w[s]);
-    int elem = B.elem[s], fin = B.fin[s], mat = B.mat[s], n_seg = B.n_seg[s], zrun = B.zero_run[s];
-    const int seg0 = n_seg;
-    uint64_t seed = B.seed[s], hash = B.hash[s];
-    const double wgt = B.wgt[s];
-    const bool unit_w = __double_as_longlong(wgt) == __double_as_longlong(1.0);
-    double* const tal = tally_of(a, B.tag[s]);
-    const int4 cm = B.cm[s];
-    const float4 ci = B.cinv[s];
-    int slot = -1;  // cache slot whose Sigma_t is current, if the walk changed material
-    // the cached float 1/Sigma_t of the current material (set below when mat < 0)
-    float inv_sig = 0.0f;
-    if (mat >= 0) {
-      const int sl = xs_cache_slot(cm, mat);
-      inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
-    }
-    int r = 0, face = -1;
-    int k = 0;
-    // The record of the element being walked is loaded one step ahead: at
-    // each crossing the neighbour's planes, entries and (after a flagged
-    // side) material are requested before that segment's tally, hash and
-    // position update, so the loads are in flight while those run.
-    float4 P0, P1, P2, P3;
-    int4 nb4;
-    int mnext = 0;  // material of elem, valid while mat < 0
-    {
-      const Tet32* T = M.tet + elem;
-      P0 = __ldg(&T->p[0]);
-      P1 = __ldg(&T->p[1]);
-      P2 = __ldg(&T->p[2]);
-      P3 = __ldg(&T->p[3]);
-      nb4 = __ldg(&T->nbr);
-      if (mat < 0) mnext = __ldg(M.tmat + elem);
-    }
-    for (;;) {
-      if (n_seg >= kMaxSegments || zrun >= kMaxZeroRun) {
-        r = 2;
-        face = -2;  // stuck
-        break;
-      }
-      // this segment's draw depends on no load: formed while they land,
-      // committed to the RNG state only when the segment is scored
-      const uint64_t seed_n = kPrnMult * seed + kPrnAdd;
-      uint64_t wv = ((seed_n >> ((seed_n >> 59u) + 5u)) ^ seed_n) * 12605985483714917081ULL;
-      wv = (wv >> 43u) ^ wv;
-      const float lnxi = -__logf((float)(uint32_t)(wv >> 32) * 2.3283064365386963e-10f);
-      if (mat < 0) {  // after a side flagged kMatChange
-        const int m = mnext;
-        const int sl = m < 0 ? -1 : xs_cache_slot(cm, m);
-        if (sl < 0) {
-          r = (m < 0) ? 2 : 3;
-          if (m < 0) face = -3;  // no material: bad cross section
-          break;
-        }
-        mat = m;
-        slot = sl;
-        inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
-      }
-      int bf = -1;
-      float t1 = 3.0e38f, t2 = 3.0e38f;
-      // branch-free: every lane runs the same instructions for every side
-      // (a side that is the entry side or faces away gets t = 3e38)
-      auto side = [&](const float4& pl, int f) {
-        const float den = fmaf(pl.x, u, fmaf(pl.y, v, pl.z * w));
-        const float num = pl.w - fmaf(pl.x, x, fmaf(pl.y, y, pl.z * z));
-        const float t = (f != fin && den > 0.0f) ? __fdividef(num, den) : 3.0e38f;
-        const bool lt1 = t < t1;
-        t2 = lt1 ? t1 : fminf(t2, t);
-        bf = lt1 ? f : bf;
-        t1 = lt1 ? t : t1;
-      };
-      side(P0, 0);
-      side(P1, 1);
-      side(P2, 2);
-      side(P3, 3);
-      float Ls;
-      if (bf < 0 || t2 - t1 <= tol || t1 < -tol) {
-        L.add(kCntFallback, 1);
-        Geo32 g{x, y, z, u, v, w};
-        double Ld = 0.0;
-        bf = exit_fp64(M, elem, fin, g, Ld);
-        if (bf < 0) {
-          r = 2;
-          face = -2;
-          break;
-        }
-        Ls = (float)Ld;
-      } else {
-        Ls = fmaxf(t1, 0.0f);
-      }
-      seed = seed_n;
-      const float dist = lnxi * inv_sig;
-      const bool cross = dist > Ls;
-      const int nb = side_entry(nb4, bf);
-      const int next = (nb & (kMatChange - 1)) >> 2;
-      if (cross && nb >= 0) {
-        const Tet32* T = M.tet + next;
-        P0 = __ldg(&T->p[0]);
-        P1 = __ldg(&T->p[1]);
-        P2 = __ldg(&T->p[2]);
-        P3 = __ldg(&T->p[3]);
-        nb4 = __ldg(&T->nbr);
-        if (nb & kMatChange) mnext = __ldg(M.tmat + next);
-      }
-      const float score = cross ? Ls : dist;
-      atomicAdd(tal + elem, unit_w ? widen(score) : wgt * widen(score));
-      ++n_seg;
-      if (Ls == 0.0f) ++zrun;
-      else zrun = 0;
-      if (!cross) {
-        if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + 4ULL);
-        x = fmaf(dist, u, x);
-        y = fmaf(dist, v, y);
-        z = fmaf(dist, w, z);
-        zrun = 0;
-        r = 1;
-        break;
-      }
-      if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + (uint64_t)bf);
-      x = fmaf(Ls, u, x);
-      y = fmaf(Ls, v, y);
-      z = fmaf(Ls, w, z);
-      if (nb >= 0) {
-        if (nb & kMatChange) mat = -2;
-        elem = next;
-        fin = nb & 3;
-      } else {
-        const int bid = -1 - nb;
-        if (bid < M.n_bid && M.bc_type[bid] == 1) {
-          // no load is issued for a boundary side: P0..P3 are still this element's
-          const float4 pb = bf == 0 ? P0 : bf == 1 ? P1 : bf == 2 ? P2 : P3;
-          const float t2r = 2.0f * fmaf(u, pb.x, fmaf(v, pb.y, w * pb.z));
-          u = fmaf(-t2r, pb.x, u);
-          v = fmaf(-t2r, pb.y, v);
-          w = fmaf(-t2r, pb.z, w);
-          const float nrm = rsqrtf(fmaf(u, u, fmaf(v, v, w * w)));
-          u *= nrm;
-          v *= nrm;
-          w *= nrm;
-          fin = -1;
-        } else {
-          r = 2;
-          face = bf;  // leaked through side bf
-          break;
-        }
-      }
-      if (a.max_seg > 0 && ++k >= a.max_seg) {
-        r = 4;
-        break;
-      }
-    }
-    L.add(kCntSegWalk, (unsigned long long)(n_seg - seg0));
-    if (r == 2) {
-      Particle p;
-      load(B, s, p);
-      p.x = widen(x); p.y = widen(y); p.z = widen(z);
-      p.u = widen(u); p.v = widen(v); p.w = widen(w);
-      p.elem = elem; p.fin = fin; p.mat = mat; p.n_seg = n_seg; p.zero_run = zrun;
-      p.seed = seed; p.hash = hash;
-      if (face >= 0) {
-        p.status = kLeaked;
-        p.face = face;
-      } else {
-        p.status = face == -3 ? kBadXS : kStuck;
-      }
-      finish(p, a, L);
-      push_free(Q, ctl, s, B.cap);
-      continue;
-    }
-    B.x[s] = widen(x); B.y[s] = widen(y); B.z[s] = widen(z);
-    B.u[s] = widen(u); B.v[s] = widen(v); B.w[s] = widen(w);
-    B.elem[s] = elem; B.fin[s] = fin; B.mat[s] = mat; B.n_seg[s] = n_seg; B.zero_run[s] = zrun;
-    B.seed[s] = seed; B.hash[s] = hash;
-    if (slot >= 0) {
-      const double4_32a c = B.cs[s];
-      B.sigt[s] = slot == 0 ? c.x : slot == 1 ? c.y : slot == 2 ? c.z : c.w;
-    }
-    if (r == 1) {
-      B.n_coll[s] = B.n_coll[s] + 1;
-      push(Q.coll, &ctl->n_coll, s);
-    } else if (r == 3) {
-      push(Q.xs[nxt], &ctl->n_xs[nxt], s);
-    } else {
-      push(Q.adv[nxt], &ctl->n_adv[nxt], s);
-    }
+    mixed_visit(M, a, B, Q, ctl, nxt, s, a.max_seg, tol, hashing, true, L);
   }
   flush(L, a.counters, a.leak_w);
 }
@@ -834,6 +845,39 @@ __global__ void k_ev_reset(EventCtl* ctl, int par, int64_t n) {
 
 // Tail of a batch: every particle still queued runs to completion in one
 // launch, one thread per particle, with cross sections and collisions inline.
+// Tail of the mixed walk with the default tally: the event loop's compact
+// visit without a segment budget, with the collision and cross-section
+// events it stops at handled here, until the history ends.
+__device__ __forceinline__ void mixed_tail(const DevMesh& M, const DevXS& X, const RunArgs& a, const Bank& B,
+                                           const EventQueues& Q, EventCtl* ctl, int s, bool need_xs,
+                                           LocalCounters& L) {
+  const float tol = a.tol;
+  const bool hashing = a.traces != nullptr;
+  int r = need_xs ? 3 : 0;
+  for (;;) {
+    if (r == 1 || r == 3) {
+      Particle p;
+      load(B, s, p);
+      if (r == 1) {
+        collide<false>(X, p, a.two_d, a.eig);
+        if (p.status != kAlive) {
+          finish(p, a, L);
+          return;
+        }
+      }
+      if (!refresh_xs(M, X, a.n_mat, true, false, p, L)) {
+        finish(p, a, L);
+        return;
+      }
+      store(B, s, p);
+      B.cinv[s] = make_float4(p.cm.x >= 0 ? 1.0f / narrow(p.cs0) : 0.0f, p.cm.y >= 0 ? 1.0f / narrow(p.cs1) : 0.0f,
+                              p.cm.z >= 0 ? 1.0f / narrow(p.cs2) : 0.0f, p.cm.w >= 0 ? 1.0f / narrow(p.cs3) : 0.0f);
+    }
+    r = mixed_visit(M, a, B, Q, ctl, 0, s, 0, tol, hashing, false, L);
+    if (r == 2) return;
+  }
+}
+
 template <int kPrec, bool kEig>
 __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a, Bank B,
                                                    EventQueues Q, EventCtl* ctl, int par) {
@@ -842,6 +886,10 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
   const int na = *(volatile int*)&ctl->n_adv[par];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx + na; i += gridDim.x * blockDim.x) {
     const int s = (i < nx) ? Q.xs[par][i] : Q.adv[par][i - nx];
+    if (kPrec == MC_PREC_MIXED && !kEig && !a.ts.general && !a.ts.rays) {
+      mixed_tail(M, X, a, B, Q, ctl, s, i < nx, L);
+      continue;
+    }
     Particle p;
     load(B, s, p, kEig);
     unsigned long long nxs = 0, nfb = 0;
