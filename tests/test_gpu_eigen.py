@@ -128,3 +128,52 @@ def test_eigen_errors(small):
         t.load(plain)
         with pytest.raises(MCError):
             t.eigen(100, 1, 0)  # nothing fissionable
+
+
+def test_eigen_with_a_collision_tally_and_energy_bins(small):
+    """Active generations score an OpenMCTally definition (collision
+    estimator, four scores, energy filter) as fixed-source runs do."""
+    from macaw_gb300._lib import (MC_EST_COLLISION, MC_SCORE_ABSORPTION, MC_SCORE_FLUX, MC_SCORE_SCATTER,
+                                  MC_SCORE_TOTAL)
+    d = problems.TallyDef(MC_EST_COLLISION, (MC_SCORE_FLUX, MC_SCORE_TOTAL, MC_SCORE_SCATTER, MC_SCORE_ABSORPTION),
+                          np.array([1.0e-5, 1.0, 1.0e3, 1.0e6, 2.0e7]))
+    small.tally = d
+    try:
+        g_ref, _, _, t_ref, _ = O.Oracle(small).eigen(3000, 3, 1, seed=6, threads=16, tally=True)
+        with Tracker(0) as t:
+            t.load(small)
+            g = t.eigen(3000, 3, 1, seed=6, bank_size=1024, max_seg=16)
+            tally = t.tally(MC_TALLY_SUM)
+    finally:
+        small.tally = None
+    for f in FIELDS:
+        assert np.array_equal(g[f], g_ref[f]), f
+    assert tally.size == t_ref.size == small.n_tet * 4 * 4
+    nz = t_ref != 0
+    assert np.all(tally[~nz] == 0) and np.allclose(tally[nz], t_ref[nz], rtol=1e-12, atol=0)
+
+
+def test_eigen_in_two_d_mode():
+    """2-D eigenvalue generations (CollisionKernel z_coord): sites stay in the
+    plane and the generations equal the oracle's."""
+    p = problems.lattice_2d_problem(nx=5, ny=5, n_pts=3000)
+    for k in p.materials[0].nuclides:
+        problems.add_fission(p.nuclides[int(k)], 2.43, 0.6)
+    for n_ in p.nuclides:
+        n_.sig_s = n_.sig_s + 2.0
+        n_.sig_t = n_.sig_t + 2.5
+        if n_.nu_sig_f is not None:
+            n_.nu_sig_f = (2.43 * 0.6) * (n_.sig_t - n_.sig_s)
+    for b in (1, 2, 3, 4):
+        p.bcs[b] = 1
+    g_ref, src_ref, bank_ref, _, _ = O.Oracle(p).eigen(2000, 3, 1, seed=2, threads=16)
+    with Tracker(0) as t:
+        t.load(p)
+        g = t.eigen(2000, 3, 1, seed=2, bank_size=1024)
+        bank = t.fission_bank()
+        src = t.eigen_source(2000)
+    for f in FIELDS:
+        assert np.array_equal(g[f], g_ref[f]), f
+    _same_bank(bank, bank_ref)
+    assert np.all(bank["z"] == p.z_2d)
+    assert np.array_equal(_src_rows(src), src_ref)
