@@ -547,6 +547,7 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
 // 1 collision, 2 history ended (finished here), 3 cross-section event due,
 // 4 segment budget.  queue: hand the particle to the queue of its next
 // event (the event loop); otherwise the caller handles the event.
+template <bool kEig = false>
 __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, const Bank& B, const EventQueues& Q,
                                            EventCtl* ctl, int nxt, int s, int max_seg, float tol, bool hashing,
                                            bool queue, LocalCounters& L) {
@@ -564,9 +565,19 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   int slot = -1;  // cache slot whose Sigma_t is current, if the walk changed material
   // the cached float 1/Sigma_t of the current material (set below when mat < 0)
   float inv_sig = 0.0f;
+  // k-eigenvalue runs: nu*Sigma_f of the cached materials (float) and the
+  // visit's sum of score * nu*Sigma_f, added to the history's FP64
+  // track-length keff sum when the visit ends
+  float4 cnf = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float nuf = 0.0f, kacc = 0.0f;
+  if (kEig) {
+    const double4_32a c = B.cn[s];
+    cnf = make_float4(narrow(c.x), narrow(c.y), narrow(c.z), narrow(c.w));
+  }
   if (mat >= 0) {
     const int sl = xs_cache_slot(cm, mat);
     inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
+    if (kEig) nuf = sl == 0 ? cnf.x : sl == 1 ? cnf.y : sl == 2 ? cnf.z : cnf.w;
   }
   int r = 0, face = -1;
   int k = 0;
@@ -609,6 +620,7 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
       mat = m;
       slot = sl;
       inv_sig = sl == 0 ? ci.x : sl == 1 ? ci.y : sl == 2 ? ci.z : ci.w;
+      if (kEig) nuf = sl == 0 ? cnf.x : sl == 1 ? cnf.y : sl == 2 ? cnf.z : cnf.w;
     }
     int bf = -1;
     float t1 = 3.0e38f, t2 = 3.0e38f;
@@ -658,6 +670,7 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     }
     const float score = cross ? Ls : dist;
     atomicAdd(tal + elem, unit_w ? widen(score) : wgt * widen(score));
+    if (kEig) kacc = fmaf(score, nuf, kacc);  // CollisionKernel.C:153-154
     ++n_seg;
     if (Ls == 0.0f) ++zrun;
     else zrun = 0;
@@ -706,7 +719,8 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   if (queue) L.add(kCntSegWalk, (unsigned long long)(n_seg - seg0));
   if (r == 2) {
     Particle p;
-    load(B, s, p);
+    load(B, s, p, kEig);
+    if (kEig) p.ktl = p.ktl + wgt * widen(kacc);
     p.x = widen(x); p.y = widen(y); p.z = widen(z);
     p.u = widen(u); p.v = widen(v); p.w = widen(w);
     p.elem = elem; p.fin = fin; p.mat = mat; p.n_seg = n_seg; p.zero_run = zrun;
@@ -728,7 +742,12 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   if (slot >= 0) {
     const double4_32a c = B.cs[s];
     B.sigt[s] = slot == 0 ? c.x : slot == 1 ? c.y : slot == 2 ? c.z : c.w;
+    if (kEig) {
+      const double4_32a n = B.cn[s];
+      B.nuf[s] = slot == 0 ? n.x : slot == 1 ? n.y : slot == 2 ? n.z : n.w;
+    }
   }
+  if (kEig) B.ktl[s] = B.ktl[s] + wgt * widen(kacc);
   if (r == 1) B.n_coll[s] = B.n_coll[s] + 1;
   if (queue) {
     if (r == 1) push(Q.coll, &ctl->n_coll, s);
@@ -740,6 +759,7 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
 
 // Mixed-precision segment walk (mixed_visit), each lane walking the
 // particles of its warp's queue chunks one visit at a time.
+template <bool kEig>
 __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B, EventQueues Q,
                                                              EventCtl* ctl, int par) {
   MC_COUNTERS(L);
@@ -752,7 +772,7 @@ __global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs 
     if (__shfl_sync(0xffffffffu, i, 0) >= n) break;
     if (i >= n) continue;
     const int s = Q.adv[par][i];
-    mixed_visit(M, a, B, Q, ctl, nxt, s, a.max_seg, tol, hashing, true, L);
+    mixed_visit<kEig>(M, a, B, Q, ctl, nxt, s, a.max_seg, tol, hashing, true, L);
   }
   flush(L, a.counters, a.leak_w);
 }
@@ -873,7 +893,7 @@ __device__ __forceinline__ void mixed_tail(const DevMesh& M, const DevXS& X, con
       B.cinv[s] = make_float4(p.cm.x >= 0 ? 1.0f / narrow(p.cs0) : 0.0f, p.cm.y >= 0 ? 1.0f / narrow(p.cs1) : 0.0f,
                               p.cm.z >= 0 ? 1.0f / narrow(p.cs2) : 0.0f, p.cm.w >= 0 ? 1.0f / narrow(p.cs3) : 0.0f);
     }
-    r = mixed_visit(M, a, B, Q, ctl, 0, s, 0, tol, hashing, false, L);
+    r = mixed_visit<false>(M, a, B, Q, ctl, 0, s, 0, tol, hashing, false, L);
     if (r == 2) return;
   }
 }
@@ -1036,16 +1056,18 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
   }
   if (adv0) cudaEventRecord(adv0, st);
   if (a.eig.on) {
-    // k-eigenvalue generations: the chunked walk with the keff score (no
-    // lane refill, no ray recording)
-    if (a.precision == MC_PREC_MIXED)
+    // k-eigenvalue generations: the walks with the keff score (no lane
+    // refill, no ray recording; the compact mixed walk for the default tally)
+    if (a.precision == MC_PREC_MIXED && !a.ts.general)
+      k_ev_advance_mixed<true><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
+    else if (a.precision == MC_PREC_MIXED)
       k_ev_advance_static<MC_PREC_MIXED, false, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else
       k_ev_advance_static<MC_PREC_FP64, false, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
   } else if (a.precision == MC_PREC_MIXED) {
     // the compact walk scores the default tally and records no rays
     if (a.refill || a.ts.general || a.ts.rays) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else k_ev_advance_mixed<<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
+    else k_ev_advance_mixed<false><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
   } else {
     if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else if (a.ts.rays) k_ev_advance_static<MC_PREC_FP64, true, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
