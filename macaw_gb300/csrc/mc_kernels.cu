@@ -552,12 +552,15 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
                                            EventCtl* ctl, int nxt, int s, int max_seg, float tol, bool hashing,
                                            bool queue, LocalCounters& L) {
   // (queue = false: the tail kernel; its segments are not walk-launch segments)
-  float x = narrow(B.x[s]), y = narrow(B.y[s]), z = narrow(B.z[s]);
-  float u = narrow(B.u[s]), v = narrow(B.v[s]), w = narrow(B.w[s]);
-  int elem = B.elem[s], fin = B.fin[s], mat = B.mat[s], n_seg = B.n_seg[s], zrun = B.zero_run[s];
+  // bank state is read once and written once per visit: streaming
+  // (evict-first) accesses, so the L2 keeps the element records
+  float x = narrow(__ldcs(B.x + s)), y = narrow(__ldcs(B.y + s)), z = narrow(__ldcs(B.z + s));
+  float u = narrow(__ldcs(B.u + s)), v = narrow(__ldcs(B.v + s)), w = narrow(__ldcs(B.w + s));
+  int elem = __ldcs(B.elem + s), fin = __ldcs(B.fin + s), mat = __ldcs(B.mat + s), n_seg = __ldcs(B.n_seg + s),
+      zrun = __ldcs(B.zero_run + s);
   const int seg0 = n_seg;
-  uint64_t seed = B.seed[s], hash = B.hash[s];
-  const double wgt = B.wgt[s];
+  uint64_t seed = __ldcs((const unsigned long long*)B.seed + s), hash = __ldcs((const unsigned long long*)B.hash + s);
+  const double wgt = __ldcs(B.wgt + s);
   const bool unit_w = __double_as_longlong(wgt) == __double_as_longlong(1.0);
   double* const tal = tally_of(a, B.tag[s]);
   const int4 cm = B.cm[s];
@@ -735,10 +738,12 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     if (queue) push_free(Q, ctl, s, B.cap);
     return 2;
   }
-  B.x[s] = widen(x); B.y[s] = widen(y); B.z[s] = widen(z);
-  B.u[s] = widen(u); B.v[s] = widen(v); B.w[s] = widen(w);
-  B.elem[s] = elem; B.fin[s] = fin; B.mat[s] = mat; B.n_seg[s] = n_seg; B.zero_run[s] = zrun;
-  B.seed[s] = seed; B.hash[s] = hash;
+  __stcs(B.x + s, widen(x)); __stcs(B.y + s, widen(y)); __stcs(B.z + s, widen(z));
+  __stcs(B.u + s, widen(u)); __stcs(B.v + s, widen(v)); __stcs(B.w + s, widen(w));
+  __stcs(B.elem + s, elem); __stcs(B.fin + s, fin); __stcs(B.mat + s, mat); __stcs(B.n_seg + s, n_seg);
+  __stcs(B.zero_run + s, zrun);
+  __stcs((unsigned long long*)B.seed + s, (unsigned long long)seed);
+  __stcs((unsigned long long*)B.hash + s, (unsigned long long)hash);
   if (slot >= 0) {
     const double4_32a c = B.cs[s];
     B.sigt[s] = slot == 0 ? c.x : slot == 1 ? c.y : slot == 2 ? c.z : c.w;
