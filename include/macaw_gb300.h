@@ -145,6 +145,10 @@ typedef struct {
                               -1: never, the event loop runs until the bank is empty) */
   const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
   const int64_t* batch_sizes; /* HOST array of n_batches sizes adding up to n_histories */
+  double* const* batch_sum_out; /* optional HOST array of n_batches HOST buffers of mc_tally_size doubles:
+                                   buffer b receives the SUM tally as it stands when batch b has been
+                                   folded in (copied while later batches run; pinned buffers let the copy
+                                   overlap); needs accumulate */
 } mc_run_desc;
 
 /* Per-history outcome: element sequence hash, counts, end state. */

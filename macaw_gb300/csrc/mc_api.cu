@@ -637,6 +637,7 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
   // its last particle ends; births of batch b+slots wait until then, so the
   // long walks of one batch overlap the bulk of the next slots-1 batches
   const int nb = d->n_batches > 1 ? d->n_batches : 1;
+  if (d->batch_sum_out && !d->accumulate) return set_err(c, MC_ERR_ARG, "batch results need accumulate = 1");
   const int slots = std::min(nb, kPipeSlots);
   std::vector<int64_t> bend((size_t)nb);
   if (nb > 1) {
@@ -699,6 +700,10 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
     CK(launch_accumulate(buf, c->d_sum.as<double>(), c->d_sumsq.as<double>(),
                          c->n_tally, size > 0 ? 1.0 / (double)size : 0.0, c->stream),
        "launch accumulate");
+    if (d->batch_sum_out && d->batch_sum_out[b])
+      CK(cudaMemcpyAsync(d->batch_sum_out[b], c->d_sum.p, sizeof(double) * (size_t)c->n_tally,
+                         cudaMemcpyDeviceToHost, c->stream),
+         "copy batch result");
     c->batches += 1;
     return MC_OK;
   };

@@ -154,16 +154,27 @@ class Tracker:
             precision: int = MC_PREC_FP64, bank_size: int = 0, block_size: int = 0,
             max_seg: int = 0, traces: bool = False, accumulate: bool = False,
             sort_queue: bool = False, profile: bool = False, sites: np.ndarray | None = None,
-            refill: bool = False, batch_sizes=None, graph: bool = False, tail: int = 0) -> Stats:
+            refill: bool = False, batch_sizes=None, graph: bool = False, tail: int = 0,
+            batch_results=None) -> Stats:
         """One batch of n histories, or, with batch_sizes (adding up to n),
-        consecutive batches run through one pipeline (needs accumulate)."""
+        consecutive batches run through one pipeline (needs accumulate).
+        batch_results: one float64 array of tally_size() per batch, each
+        receiving the SUM tally as it stands once its batch is folded in."""
         if sites is not None:
             assert sites.dtype == SITE_DTYPE and sites.size >= n and sites.flags["C_CONTIGUOUS"]
         bs = None if batch_sizes is None else np.ascontiguousarray(batch_sizes, np.int64)
+        outs = None
+        if batch_results is not None:
+            nbat = 1 if bs is None else bs.size
+            assert len(batch_results) == nbat
+            for r in batch_results:
+                assert r.dtype == np.float64 and r.flags["C_CONTIGUOUS"] and r.size == self.tally_size()
+            outs = (C.c_void_p * nbat)(*[r.ctypes.data for r in batch_results])
         d = RunDesc(first, n, bank_size, seed, precision, mode, block_size, max_seg, int(traces),
                     int(accumulate), int(sort_queue), int(profile), int(refill), 0 if bs is None else bs.size,
                     int(graph), int(tail), None if sites is None else sites.ctypes.data,
-                    None if bs is None else bs.ctypes.data)
+                    None if bs is None else bs.ctypes.data,
+                    None if outs is None else C.cast(outs, C.c_void_p))
         self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
         return self.stats()
 

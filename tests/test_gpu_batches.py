@@ -125,3 +125,29 @@ def test_batch_arguments_are_checked(cube):
             t.run(100, accumulate=True, batch_sizes=[40, 50])
         with pytest.raises(MCError, match="accumulate"):
             t.run(90, accumulate=False, batch_sizes=[40, 50])
+
+
+def test_batch_results_stream_each_batch_sum(cube):
+    """batch_results: buffer b holds SUM once batch b is folded in, equal to
+    the SUM after b+1 separate runs; host sites feed the pipelined batches."""
+    sizes = SIZES_LONG
+    with Tracker(0) as t:
+        t.load(cube)
+        sites = t.sample_sites(sum(sizes), seed=5)
+        ref = []
+        first = 0
+        for s in sizes:
+            t.run(s, first=first, seed=5, accumulate=True, sites=sites[first:first + s])
+            ref.append(t.tally(MC_TALLY_SUM).copy())
+            first += s
+        t.reset_tally()
+        outs = [np.zeros(t.tally_size()) for _ in sizes]
+        t.run(sum(sizes), seed=5, accumulate=True, bank_size=2048, batch_sizes=sizes, sites=sites,
+              batch_results=outs)
+        assert t.batches_done() == len(sizes)
+        # batches are folded in birth order, each as soon as it and every
+        # older batch have drained
+        for b in range(len(sizes)):
+            assert close(outs[b], ref[b]), b
+        with pytest.raises(Exception):
+            t.run(sum(sizes), seed=5, accumulate=False, batch_sizes=sizes, batch_results=outs)
