@@ -268,17 +268,21 @@ __device__ __forceinline__ int xs_bucket(const DevXS& X, double lE) {
 // Bisection inside the hash bin of grid g, guarded so a bin estimate that is
 // off by rounding still ends on the right interval; returns the interval
 // index i (E_i <= E < E_i+1) and the interpolation fraction.
+// Energies and grid points are positive finite doubles, whose order is the
+// order of their bit patterns as integers: the comparisons run on the
+// integer pipe (exactly the same outcomes as double comparisons).
 __device__ __forceinline__ int grid_index(const DevXS& X, int g, int k, double E) {
-  const double* G = X.gE + __ldg(X.g_off + g);
+  const long long* G = reinterpret_cast<const long long*>(X.gE + __ldg(X.g_off + g));
+  const long long e = __double_as_longlong(E);
   int lo = __ldg(X.ghidx + (size_t)k * X.n_grid + g);
   int hi = __ldg(X.ghidx + (size_t)(k + 1) * X.n_grid + g) + 1;
   const int last = __ldg(X.g_n + g) - 1;
   if (hi > last) hi = last;
-  while (lo > 0 && E < __ldg(G + lo)) --lo;
-  while (hi < last && E >= __ldg(G + hi)) ++hi;
+  while (lo > 0 && e < __ldg(G + lo)) --lo;
+  while (hi < last && e >= __ldg(G + hi)) ++hi;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
-    if (E < __ldg(G + mid)) hi = mid;
+    if (e < __ldg(G + mid)) hi = mid;
     else lo = mid;
   }
   return lo;
