@@ -256,13 +256,16 @@ __device__ __forceinline__ void xs_cache_put(Particle& p, int mat, double s, dou
 
 // ---------------------------------------------------------------------------
 // Cross sections.
-__device__ __forceinline__ int xs_bucket(const DevXS& X, double lE) {
-  const double q = (lE - X.lE_lo) / X.du;
-  if (!(q >= 0.0)) return 0;
-  if (q >= (double)X.n_bins) return X.n_bins - 1;
-  int k = (int)q;
-  if (k > X.n_bins - 1) k = X.n_bins - 1;
-  return k;
+
+// The hash bin from a float log.  grid_index's guards move from any bin to
+// the right interval, so every lookup (FP64 ones too) starts from this bin:
+// a bin that rounding moved by one costs one more guard step, not a
+// different result, and the FP64 log stays off the narrow FP64 pipe.
+__device__ __forceinline__ int xs_bucket32(const DevXS& X, double E) {
+  const float q = (__logf(narrow(E)) - narrow(X.lE_lo)) / narrow(X.du);
+  if (!(q >= 0.0f)) return 0;
+  const int k = (int)q;
+  return k > X.n_bins - 1 ? X.n_bins - 1 : k;
 }
 
 // Bisection inside the hash bin of grid g, guarded so a bin estimate that is
@@ -331,7 +334,7 @@ __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E,
 }
 
 __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E) {
-  return macro_total(X, mat, E, xs_bucket(X, mc::log64(E)));
+  return macro_total(X, mat, E, xs_bucket32(X, E));
 }
 
 // nu*sigma_f of nuclide nuc at the cursor's interval (the cursor located
@@ -367,12 +370,6 @@ __device__ __forceinline__ double macro_total_nuf(const DevXS& X, int mat, doubl
 // located in FP64 on the double grid, so the bracketing points are the
 // FP64 ones; the fraction, the interpolation and the sum over nuclides in
 // float.
-__device__ __forceinline__ int xs_bucket32(const DevXS& X, double E) {
-  const float q = (__logf(narrow(E)) - narrow(X.lE_lo)) / narrow(X.du);
-  if (!(q >= 0.0f)) return 0;
-  const int k = (int)q;
-  return k > X.n_bins - 1 ? X.n_bins - 1 : k;
-}
 
 template <bool kNuf = false>
 __device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E, int k, float* nuf = nullptr) {
@@ -681,7 +678,7 @@ __device__ __forceinline__ void score_collision(const DevXS& X, const TallySpec&
   if (b < 0) return;
   double ss = 0.0;
   if (T.need_ss) {
-    const int k = xs_bucket(X, mc::log64(p.E));
+    const int k = xs_bucket32(X, p.E);
     GridCursor gc;
     const int j1 = __ldg(X.mat_off + p.mat + 1);
     for (int j = __ldg(X.mat_off + p.mat); j < j1; ++j) {
@@ -765,7 +762,7 @@ __device__ __forceinline__ void collide(const DevXS& X, Particle& p, bool two_d,
   const bool on = kEig && e.on;
   const int64_t h = p.id - 1 - e.first;
   if (on && p.nuf > 0.0) e.kcol[h] += p.wgt * p.nuf / p.sigt;
-  const int k = xs_bucket(X, mc::log64(p.E));
+  const int k = xs_bucket32(X, p.E);
   const double cutoff = prn(p.seed) * p.sigt;
   double acc = 0.0, st = 0.0, ss = 0.0;
   const int j0 = __ldg(X.mat_off + mat), j1 = __ldg(X.mat_off + mat + 1);
@@ -873,7 +870,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     if (!xs_cache_get<kEig>(p, mat)) {
       if (!kInlineXS) return 3;
       double nf = 0.0;
-      const double s = kEig ? macro_total_nuf(X, mat, p.E, xs_bucket(X, mc::log64(p.E)), nf)
+      const double s = kEig ? macro_total_nuf(X, mat, p.E, xs_bucket32(X, p.E), nf)
                             : macro_total(X, mat, p.E);
       ++n_xs;
       if (!(s > 0.0) || s != s) {
@@ -1013,7 +1010,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     if (!xs_cache_get<kEig>(p, mat)) {
       if (!kInlineXS) return 3;
       double nf = 0.0;
-      const double s = kEig ? macro_total_nuf(X, mat, p.E, xs_bucket(X, mc::log64(p.E)), nf)
+      const double s = kEig ? macro_total_nuf(X, mat, p.E, xs_bucket32(X, p.E), nf)
                             : macro_total(X, mat, p.E);
       ++n_xs;
       if (!(s > 0.0) || s != s) {

@@ -122,7 +122,7 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
     p.status = kBadXS;
     return false;
   }
-  const int k = f32 ? xs_bucket32(X, p.E) : xs_bucket(X, mc::log64(p.E));
+  const int k = xs_bucket32(X, p.E);
   double nf;
   const double s = eval_xs(X, mat, p.E, k, f32, eig, nf);
   L.add(kCntXS, 1);
