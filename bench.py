@@ -81,6 +81,11 @@ MIXED_DRAM_BYTES_PER_SEG = 72.6
 # load per segment (L2 hit rate 43%, 30% of the warp slots occupied)
 FP64_PIPE_ACTIVE = 0.680
 MIXED_L2_HIT = 0.432
+# the same captures' L2 hit rate and warp execution efficiency (active
+# threads per executed instruction / 32), for the report
+FP64_L2_HIT = 0.329
+FP64_WARP_EFF = 22.08 / 32
+MIXED_WARP_EFF = 18.40 / 32
 
 
 def env_int(name, default):
@@ -569,6 +574,7 @@ def main():
                                  "traffic": MIXED_DRAM_BYTES_PER_SEG * pst.n_seg_advance / max(pst.n_advance_launch, 1),
                                  "limiter": {"dependent_record_loads_l2_hit": MIXED_L2_HIT,
                                              "source": "ncu lts__t_sector_hit_rate (profiles/walk_mixed_lattice.md)"},
+                                 "l2_hit_rate": MIXED_L2_HIT, "warp_execution_efficiency": MIXED_WARP_EFF,
                                  "sample": f"one extra profiled batch of {n} histories"}
 
     # --- end to end through the C ABI with host buffers ---
@@ -648,6 +654,9 @@ def main():
                                   "per launch",
                 "limiter": {"fp64_pipe_active": FP64_PIPE_ACTIVE,
                             "source": "ncu sm__pipe_fp64_cycles_active (profiles/walk_fp64_lattice.md)"},
+                "l2_hit_rate": FP64_L2_HIT, "warp_execution_efficiency": FP64_WARP_EFF,
+                "counters_source": "ncu lts__t_sector_hit_rate and smsp__thread_inst_executed_per_inst_executed "
+                                   "(profiles/walk_*_lattice.md)",
                 "note": "the FP64 walk is bound by GB300's FP64 pipe, not HBM (see profiles/)"}
         cfg = dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single",
                    pipelined_batches=K, tuned=params64)
