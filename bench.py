@@ -62,7 +62,7 @@ METRIC = "histories/s on 1 GB300, mixed vs plain FP64 at equal tally error; p50/
 HIST_PER_STEP = 1_000_000
 BANK = 1_000_000
 B_SEG_FP64 = 164   # algorithmic bytes per segment: planes 128 + neighbours 16 + material 4 + tally RMW 16
-B_SEG_MIXED = 100  # float planes 64 + neighbours 16 + material 4 + tally RMW 16
+B_SEG_MIXED = 84   # octahedral float planes 48 + neighbours 16 + material 4 + tally RMW 16
 # per cross-section event: about 64 B per nuclide evaluated; an event on the
 # lattice evaluates all three materials (15 + 4 + 3 nuclides); a collision
 # re-reads 16 B per nuclide of its material to pick one (fuel: 15)

@@ -71,7 +71,7 @@ struct mc_ctx {
   bool have_src = false;
 
   // device copies
-  DevBuf d_planes, d_tet, d_tmat, d_bc, d_gstart, d_gtets, d_gseed;
+  DevBuf d_planes, d_tet, d_teto, d_tmat, d_bc, d_gstart, d_gtets, d_gseed;
   DevBuf d_gE, d_goff, d_gn, d_ghidx, d_nuc_grid, d_nuc_off, d_sig, d_awr, d_mat_off, d_mat_nuc, d_mat_dens;
   DevBuf d_nusf, d_nuc_fiss, d_mat_fiss;
   DevBuf d_cyl;
@@ -203,6 +203,55 @@ int ensure_device_tables(mc_ctx* c) {
       r.nbr = make_int4(e[0], e[1], e[2], e[3]);
     }
     CK(upload(c->d_tet, rec, c->stream), "upload tet records");
+    // octahedral records: the FP64 unit normal n -> (a, b) = n.xy / |n|_1,
+    // folded over the lower half (z < 0), rounded to float; the offset is
+    // scaled by the length of the normal the walk decodes from (a, b)
+    std::vector<TetOct> oct((size_t)c->mesh.n_tet);
+    for (int64_t t = 0; t < c->mesh.n_tet; ++t) {
+      float ab[8], dd[4];
+      for (int f = 0; f < 4; ++f) {
+        const double* q = &c->mesh.planes[16 * t + 4 * f];
+        const double l1 = fabs(q[0]) + fabs(q[1]) + fabs(q[2]);
+        double a = q[0] / l1, b = q[1] / l1;
+        if (q[2] < 0.0) {
+          const double fa = (1.0 - fabs(b)) * (a >= 0.0 ? 1.0 : -1.0);
+          const double fb = (1.0 - fabs(a)) * (b >= 0.0 ? 1.0 : -1.0);
+          a = fa;
+          b = fb;
+        }
+        // of the float pairs next to (a, b), the one whose decoded normal
+        // points closest to n
+        const float a0 = (float)a, b0 = (float)b;
+        float best_a = a0, best_b = b0;
+        double best = -2.0;
+        for (int i = -1; i <= 1; ++i)
+          for (int j = -1; j <= 1; ++j) {
+            const float ca = i < 0 ? nextafterf(a0, -2.0f) : i > 0 ? nextafterf(a0, 2.0f) : a0;
+            const float cb = j < 0 ? nextafterf(b0, -2.0f) : j > 0 ? nextafterf(b0, 2.0f) : b0;
+            float x, y, z;
+            oct_normal(ca, cb, x, y, z);
+            const double l = sqrt((double)x * x + (double)y * y + (double)z * z);
+            const double cosang = ((double)x * q[0] + (double)y * q[1] + (double)z * q[2]) / l;
+            if (cosang > best) {
+              best = cosang;
+              best_a = ca;
+              best_b = cb;
+            }
+          }
+        ab[2 * f] = best_a;
+        ab[2 * f + 1] = best_b;
+        float nx, ny, nz;
+        oct_normal(best_a, best_b, nx, ny, nz);
+        const double len = sqrt((double)nx * nx + (double)ny * ny + (double)nz * nz);
+        dd[f] = (float)(q[3] * len);
+      }
+      TetOct& o = oct[t];
+      o.oct01 = make_float4(ab[0], ab[1], ab[2], ab[3]);
+      o.oct23 = make_float4(ab[4], ab[5], ab[6], ab[7]);
+      o.d = make_float4(dd[0], dd[1], dd[2], dd[3]);
+      o.nbr = rec[t].nbr;
+    }
+    CK(upload(c->d_teto, oct, c->stream), "upload octahedral records");
     CK(cudaStreamSynchronize(c->stream), "upload tet records");
     c->tmat_dirty = false;
   }
@@ -217,6 +266,7 @@ DevMesh dev_mesh(mc_ctx* c) {
   DevMesh M{};
   M.planes = c->d_planes.as<double4_32a>();
   M.tet = c->d_tet.as<Tet32>();
+  M.teto = c->d_teto.as<TetOct>();
   M.tmat = c->d_tmat.as<int>();
   M.bc_type = c->d_bc.as<int>();
   M.n_bid = (int)c->bc_type.size();

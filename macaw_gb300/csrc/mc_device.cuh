@@ -28,6 +28,36 @@ struct __align__(16) Tet32 {
 };
 constexpr int kMatChange = 1 << 30;
 
+// The mixed-precision walk's record, 64 bytes (two 32-byte sectors): each
+// side's outward normal in octahedral form (two floats), the four plane
+// offsets, the neighbour entries as in Tet32.  The normal is not unit: the
+// walk uses oct_normal's vector as it is, and the stored offset is the
+// unit plane's offset times that vector's length (computed on the host
+// from the same float operations), so exit distances (d - n.x)/(n.u) are
+// those of the unit plane with one float rounding per stored value.
+struct __align__(64) TetOct {
+  float4 oct01;  // sides 0 and 1: (a0, b0, a1, b1)
+  float4 oct23;  // sides 2 and 3
+  float4 d;      // plane offsets, scaled
+  int4 nbr;
+};
+
+// Normal from octahedral coordinates (a, b): (a, b, 1-|a|-|b|) with the
+// lower half folded back.  MC_HD: the host builds the scaled offsets from
+// exactly these operations.
+MC_HD void oct_normal(float a, float b, float& x, float& y, float& z) {
+  z = (1.0f - fabsf(a)) - fabsf(b);
+  const float t = z < 0.0f ? -z : 0.0f;
+  x = a >= 0.0f ? a - t : a + t;
+  y = b >= 0.0f ? b - t : b + t;
+}
+
+__device__ __forceinline__ float4 oct_plane(float a, float b, float d) {
+  float x, y, z;
+  oct_normal(a, b, x, y, z);
+  return make_float4(x, y, z, d);
+}
+
 // float <-> double by integer operations, for the mixed-precision walk: on
 // this GPU a conversion instruction issues on the narrow FP64 pipe, an
 // integer operation on the full-rate ALU.  widen() is exact for every
@@ -64,6 +94,7 @@ __device__ __forceinline__ int side_entry(const int4& n, int f) {
 struct DevMesh {
   const double4_32a* __restrict__ planes;   // 4 per tet (nx, ny, nz, d), outward
   const Tet32* __restrict__ tet;        // float planes + neighbour entries
+  const TetOct* __restrict__ teto;      // the same, normals in octahedral form (mixed walk)
   const int* __restrict__ tmat;         // material index per tet (-1: none)
   const int* __restrict__ bc_type;      // per boundary id: 0 vacuum, 1 reflect
   int n_bid;

@@ -547,6 +547,16 @@ __global__ void __launch_bounds__(256) k_ev_advance(DevMesh M, DevXS X, RunArgs 
 // 1 collision, 2 history ended (finished here), 3 cross-section event due,
 // 4 segment budget.  queue: hand the particle to the queue of its next
 // event (the event loop); otherwise the caller handles the event.
+// x + xl += d * u with the rounding error of the float sum kept in xl
+// (Knuth's TwoSum, exact for any magnitudes).
+__device__ __forceinline__ void advance2(float& x, float& xl, float d, float u) {
+  const float t = fmaf(d, u, xl);
+  const float s2 = x + t;
+  const float bb = s2 - x;
+  xl = (x - (s2 - bb)) + (t - bb);
+  x = s2;
+}
+
 template <bool kEig = false>
 __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, const Bank& B, const EventQueues& Q,
                                            EventCtl* ctl, int nxt, int s, int max_seg, float tol, bool hashing,
@@ -554,7 +564,13 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   // (queue = false: the tail kernel; its segments are not walk-launch segments)
   // bank state is read once and written once per visit: streaming
   // (evict-first) accesses, so the L2 keeps the element records
-  float x = narrow(__ldcs(B.x + s)), y = narrow(__ldcs(B.y + s)), z = narrow(__ldcs(B.z + s));
+  // position as float (x, y, z) plus a float low part (xl, yl, zl): the
+  // walk's plane tests use the float part; the low part carries what each
+  // advance rounds away, so float rounding does not accumulate along the
+  // walk (the bank keeps the double sum between visits)
+  const double xd = __ldcs(B.x + s), yd = __ldcs(B.y + s), zd = __ldcs(B.z + s);
+  float x = narrow(xd), y = narrow(yd), z = narrow(zd);
+  float xl = narrow(xd - widen(x)), yl = narrow(yd - widen(y)), zl = narrow(zd - widen(z));
   float u = narrow(__ldcs(B.u + s)), v = narrow(__ldcs(B.v + s)), w = narrow(__ldcs(B.w + s));
   int elem = __ldcs(B.elem + s), fin = __ldcs(B.fin + s), mat = __ldcs(B.mat + s), n_seg = __ldcs(B.n_seg + s),
       zrun = __ldcs(B.zero_run + s);
@@ -588,15 +604,14 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   // each crossing the neighbour's planes, entries and (after a flagged
   // side) material are requested before that segment's tally, hash and
   // position update, so the loads are in flight while those run.
-  float4 P0, P1, P2, P3;
+  float4 O01, O23, D;  // octahedral record (two 32-byte sectors)
   int4 nb4;
   int mnext = 0;  // material of elem, valid while mat < 0
   {
-    const Tet32* T = M.tet + elem;
-    P0 = __ldg(&T->p[0]);
-    P1 = __ldg(&T->p[1]);
-    P2 = __ldg(&T->p[2]);
-    P3 = __ldg(&T->p[3]);
+    const TetOct* T = M.teto + elem;
+    O01 = __ldg(&T->oct01);
+    O23 = __ldg(&T->oct23);
+    D = __ldg(&T->d);
     nb4 = __ldg(&T->nbr);
     if (mat < 0) mnext = __ldg(M.tmat + elem);
   }
@@ -638,6 +653,8 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
       bf = lt1 ? f : bf;
       t1 = lt1 ? t : t1;
     };
+    const float4 P0 = oct_plane(O01.x, O01.y, D.x), P1 = oct_plane(O01.z, O01.w, D.y);
+    const float4 P2 = oct_plane(O23.x, O23.y, D.z), P3 = oct_plane(O23.z, O23.w, D.w);
     side(P0, 0);
     side(P1, 1);
     side(P2, 2);
@@ -663,11 +680,10 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     const int nb = side_entry(nb4, bf);
     const int next = (nb & (kMatChange - 1)) >> 2;
     if (cross && nb >= 0) {
-      const Tet32* T = M.tet + next;
-      P0 = __ldg(&T->p[0]);
-      P1 = __ldg(&T->p[1]);
-      P2 = __ldg(&T->p[2]);
-      P3 = __ldg(&T->p[3]);
+      const TetOct* T = M.teto + next;
+      O01 = __ldg(&T->oct01);
+      O23 = __ldg(&T->oct23);
+      D = __ldg(&T->d);
       nb4 = __ldg(&T->nbr);
       if (nb & kMatChange) mnext = __ldg(M.tmat + next);
     }
@@ -679,17 +695,17 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     else zrun = 0;
     if (!cross) {
       if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + 4ULL);
-      x = fmaf(dist, u, x);
-      y = fmaf(dist, v, y);
-      z = fmaf(dist, w, z);
+      advance2(x, xl, dist, u);
+      advance2(y, yl, dist, v);
+      advance2(z, zl, dist, w);
       zrun = 0;
       r = 1;
       break;
     }
     if (hashing) hash = fnv(hash, (uint64_t)elem * 8ULL + (uint64_t)bf);
-    x = fmaf(Ls, u, x);
-    y = fmaf(Ls, v, y);
-    z = fmaf(Ls, w, z);
+    advance2(x, xl, Ls, u);
+    advance2(y, yl, Ls, v);
+    advance2(z, zl, Ls, w);
     if (nb >= 0) {
       if (nb & kMatChange) mat = -2;
       elem = next;
@@ -697,8 +713,13 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     } else {
       const int bid = -1 - nb;
       if (bid < M.n_bid && M.bc_type[bid] == 1) {
-        // no load is issued for a boundary side: P0..P3 are still this element's
-        const float4 pb = bf == 0 ? P0 : bf == 1 ? P1 : bf == 2 ? P2 : P3;
+        // no load is issued for a boundary side: the record is still this element's
+        float4 pb = bf == 0 ? oct_plane(O01.x, O01.y, D.x) : bf == 1 ? oct_plane(O01.z, O01.w, D.y)
+                  : bf == 2 ? oct_plane(O23.x, O23.y, D.z) : oct_plane(O23.z, O23.w, D.w);
+        const float rn = rsqrtf(fmaf(pb.x, pb.x, fmaf(pb.y, pb.y, pb.z * pb.z)));  // unit normal
+        pb.x *= rn;
+        pb.y *= rn;
+        pb.z *= rn;
         const float t2r = 2.0f * fmaf(u, pb.x, fmaf(v, pb.y, w * pb.z));
         u = fmaf(-t2r, pb.x, u);
         v = fmaf(-t2r, pb.y, v);
@@ -724,7 +745,7 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     Particle p;
     load(B, s, p, kEig);
     if (kEig) p.ktl = p.ktl + wgt * widen(kacc);
-    p.x = widen(x); p.y = widen(y); p.z = widen(z);
+    p.x = widen(x) + widen(xl); p.y = widen(y) + widen(yl); p.z = widen(z) + widen(zl);
     p.u = widen(u); p.v = widen(v); p.w = widen(w);
     p.elem = elem; p.fin = fin; p.mat = mat; p.n_seg = n_seg; p.zero_run = zrun;
     p.seed = seed; p.hash = hash;
@@ -738,7 +759,8 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     if (queue) push_free(Q, ctl, s, B.cap);
     return 2;
   }
-  __stcs(B.x + s, widen(x)); __stcs(B.y + s, widen(y)); __stcs(B.z + s, widen(z));
+  __stcs(B.x + s, widen(x) + widen(xl)); __stcs(B.y + s, widen(y) + widen(yl));
+  __stcs(B.z + s, widen(z) + widen(zl));
   __stcs(B.u + s, widen(u)); __stcs(B.v + s, widen(v)); __stcs(B.w + s, widen(w));
   __stcs(B.elem + s, elem); __stcs(B.fin + s, fin); __stcs(B.mat + s, mat); __stcs(B.n_seg + s, n_seg);
   __stcs(B.zero_run + s, zrun);
