@@ -31,10 +31,40 @@ def test_every_declared_symbol_is_exported():
         assert n in names, f"{n} bound in _lib.py but not declared in include/"
 
 
-def test_struct_layouts_match_header_sizes():
-    assert C.sizeof(_lib.SourceDesc) == 4 + 4 + 9 * 8 + 4 + 4 + 8 + 6 * 8
-    assert C.sizeof(_lib.RunDesc) == 4 * 8 + 12 * 4 + 8 + 8
-    assert _lib.TRACE_DTYPE.itemsize == 8 + 8 + 6 * 4 + 4 * 8
+def _header_sizes(tmp_path):
+    """sizeof and offsetof of the ABI structs as a C compiler lays them out
+    from include/macaw_gb300.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    inc = ROOT / "include"
+    src = tmp_path / "sizes.c"
+    structs = ["mc_source_desc", "mc_site", "mc_fission_site", "mc_run_desc", "mc_trace", "mc_stats",
+               "mc_tally_desc", "mc_ray_segment", "mc_eigen_desc", "mc_eigen_gen"]
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "macaw_gb300.h"\nint main(void){\n' +
+                   "".join(f'printf("{n} %zu\\n", sizeof({n}));\n' for n in structs) +
+                   'printf("batch_sum_out %zu\\n", offsetof(mc_run_desc, batch_sum_out));\nreturn 0;}\n')
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {k: int(v) for k, v in (line.split() for line in out.splitlines())}
+
+
+def test_struct_layouts_match_header_sizes(tmp_path):
+    h = _header_sizes(tmp_path)
+    assert C.sizeof(_lib.SourceDesc) == h["mc_source_desc"]
+    assert C.sizeof(_lib.RunDesc) == h["mc_run_desc"]
+    assert _lib.RunDesc.batch_sum_out.offset == h["batch_sum_out"]
+    assert C.sizeof(_lib.EigenDesc) == h["mc_eigen_desc"]
+    assert C.sizeof(_lib.TallyDesc) == h["mc_tally_desc"]
+    assert C.sizeof(_lib.Stats) == h["mc_stats"]
+    assert _lib.TRACE_DTYPE.itemsize == h["mc_trace"]
+    assert _lib.SITE_DTYPE.itemsize == h["mc_site"]
+    assert _lib.FISSION_SITE_DTYPE.itemsize == h["mc_fission_site"]
+    assert _lib.RAY_SEGMENT_DTYPE.itemsize == h["mc_ray_segment"]
+    assert _lib.EIGEN_GEN_DTYPE.itemsize == h["mc_eigen_gen"]
 
 
 def test_version():
