@@ -892,9 +892,11 @@ __global__ void k_ev_reset(EventCtl* ctl, int par, int64_t n) {
 
 // Tail of a batch: every particle still queued runs to completion in one
 // launch, one thread per particle, with cross sections and collisions inline.
-// Tail of the mixed walk with the default tally: the event loop's compact
-// visit without a segment budget, with the collision and cross-section
-// events it stops at handled here, until the history ends.
+// Tail of the mixed walk with the default tally (fixed-source or
+// k-eigenvalue): the event loop's compact visit without a segment budget,
+// with the collision and cross-section events it stops at handled here,
+// until the history ends.
+template <bool kEig>
 __device__ __forceinline__ void mixed_tail(const DevMesh& M, const DevXS& X, const RunArgs& a, const Bank& B,
                                            const EventQueues& Q, EventCtl* ctl, int s, bool need_xs,
                                            LocalCounters& L) {
@@ -904,23 +906,23 @@ __device__ __forceinline__ void mixed_tail(const DevMesh& M, const DevXS& X, con
   for (;;) {
     if (r == 1 || r == 3) {
       Particle p;
-      load(B, s, p);
+      load(B, s, p, kEig);
       if (r == 1) {
-        collide<false>(X, p, a.two_d, a.eig);
+        collide<kEig>(X, p, a.two_d, a.eig);
         if (p.status != kAlive) {
           finish(p, a, L);
           return;
         }
       }
-      if (!refresh_xs(M, X, a.n_mat, true, false, p, L)) {
+      if (!refresh_xs(M, X, a.n_mat, true, kEig, p, L)) {
         finish(p, a, L);
         return;
       }
-      store(B, s, p);
+      store(B, s, p, kEig);
       B.cinv[s] = make_float4(p.cm.x >= 0 ? 1.0f / narrow(p.cs0) : 0.0f, p.cm.y >= 0 ? 1.0f / narrow(p.cs1) : 0.0f,
                               p.cm.z >= 0 ? 1.0f / narrow(p.cs2) : 0.0f, p.cm.w >= 0 ? 1.0f / narrow(p.cs3) : 0.0f);
     }
-    r = mixed_visit<false>(M, a, B, Q, ctl, 0, s, 0, tol, hashing, false, L);
+    r = mixed_visit<kEig>(M, a, B, Q, ctl, 0, s, 0, tol, hashing, false, L);
     if (r == 2) return;
   }
 }
@@ -933,8 +935,8 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
   const int na = *(volatile int*)&ctl->n_adv[par];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx + na; i += gridDim.x * blockDim.x) {
     const int s = (i < nx) ? Q.xs[par][i] : Q.adv[par][i - nx];
-    if (kPrec == MC_PREC_MIXED && !kEig && !a.ts.general && !a.ts.rays) {
-      mixed_tail(M, X, a, B, Q, ctl, s, i < nx, L);
+    if (kPrec == MC_PREC_MIXED && !a.ts.general && !a.ts.rays) {
+      mixed_tail<kEig>(M, X, a, B, Q, ctl, s, i < nx, L);
       continue;
     }
     Particle p;

@@ -7,7 +7,8 @@
 // mc_autotune measures them on trial runs of the context's own problem
 // (device time from the CUDA events inside mc_run) by coordinate descent:
 // each parameter in turn over its candidate values, the others held at
-// their best so far, two passes.  A trial is four pipelined batches of a
+// their best so far, two passes; a candidate replaces the current value
+// only when the best of three trial runs beats it by more than 1%.  A trial is four pipelined batches of a
 // quarter of the trial size each, the way production runs stream batches
 // through the bank, so that the tail of one batch overlaps the next as it
 // will in use.  SUM/SUM_SQ and the batch count are set aside before the
@@ -61,7 +62,7 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       mc_tally_clear(c, MC_TALLY_BATCH);
     }
   } restore{ctx};
-  double rate = measure(ctx, cur, 2);
+  double rate = measure(ctx, cur, 3);
   if (rate < 0.0) return MC_ERR_STATE;
 
   struct Knob {
@@ -95,8 +96,10 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       for (int64_t v : k.values) {
         mc_run_desc trial = keep;
         apply(trial, k.kind, v);
-        const double r = measure(ctx, trial, 2);
-        if (r > rate) {
+        // best of three repeats, and a change must win by more than 1%:
+        // trials are short, and noise must not pick the parameters
+        const double r = measure(ctx, trial, 3);
+        if (r > rate * 1.01) {
           rate = r;
           cur = trial;
         }
