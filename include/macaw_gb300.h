@@ -277,6 +277,8 @@ typedef struct {
   int32_t max_seg_per_advance; /* event form, as mc_run_desc */
   int32_t sort_queue;      /* event form, as mc_run_desc */
   int32_t graph;           /* event form, as mc_run_desc */
+  int32_t tail;            /* event form, as mc_run_desc: particles left when a generation's tail kernel
+                              takes over (0: default, -1: never) */
   double keff0;            /* keff the first generation divides by (0: 1.0, OpenMC's start value) */
   double watt_a, watt_b;   /* prompt fission spectrum (0: 0.988e6 eV, 2.249e-6 /eV) */
   int64_t fission_bank_capacity; /* sites a generation may bank (0: 3 * n_particles, OpenMC's reservation) */

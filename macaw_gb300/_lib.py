@@ -53,7 +53,7 @@ class EigenDesc(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_batches", C.c_int32), ("n_inactive", C.c_int32),
                 ("seed", C.c_uint64), ("precision", C.c_int32), ("mode", C.c_int32), ("bank_size", C.c_int64),
                 ("block_size", C.c_int32), ("max_seg_per_advance", C.c_int32), ("sort_queue", C.c_int32),
-                ("graph", C.c_int32), ("keff0", C.c_double), ("watt_a", C.c_double), ("watt_b", C.c_double),
+                ("graph", C.c_int32), ("tail", C.c_int32), ("keff0", C.c_double), ("watt_a", C.c_double), ("watt_b", C.c_double),
                 ("fission_bank_capacity", C.c_int64), ("initial_source", C.c_void_p)]
 
 

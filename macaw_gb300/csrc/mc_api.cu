@@ -1270,6 +1270,7 @@ int mc_eigen_run(mc_ctx* c, const mc_eigen_desc* d, mc_eigen_gen* out) {
     rd.max_seg_per_advance = d->max_seg_per_advance;
     rd.sort_queue = d->sort_queue;
     rd.graph = d->graph;
+    rd.tail = d->tail;
     rd.accumulate = active ? 1 : 0;  // OpenMC scores tallies in active batches only
     rc = run_locked(c, &rd, c->e_src.as<mc_site>(), &e);
     if (rc) return rc;

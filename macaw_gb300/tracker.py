@@ -181,14 +181,14 @@ class Tracker:
     def eigen(self, n: int, generations: int, inactive: int = 0, seed: int = 1, precision: int = MC_PREC_FP64,
               mode: int = MC_MODE_EVENT, bank_size: int = 0, block_size: int = 0, max_seg: int = 0,
               sort_queue: int = 0, graph: bool = False, keff0: float = 0.0, watt=(0.0, 0.0), capacity: int = 0,
-              initial_source: np.ndarray | None = None) -> np.ndarray:
+              initial_source: np.ndarray | None = None, tail: int = 0) -> np.ndarray:
         """k-eigenvalue generations of n histories; returns one
         EIGEN_GEN_DTYPE record per generation."""
         if initial_source is not None:
             assert initial_source.dtype == SITE_DTYPE and initial_source.size == n
             initial_source = np.ascontiguousarray(initial_source)
         d = EigenDesc(n, generations, inactive, seed, precision, mode, bank_size, block_size, max_seg,
-                      int(sort_queue), int(graph), keff0, watt[0], watt[1], capacity,
+                      int(sort_queue), int(graph), int(tail), keff0, watt[0], watt[1], capacity,
                       None if initial_source is None else initial_source.ctypes.data)
         out = np.zeros(generations, EIGEN_GEN_DTYPE)
         self._ck(lib.mc_eigen_run(self._h, C.byref(d), ptr(out)), "mc_eigen_run")
