@@ -51,7 +51,9 @@ struct mc_ctx {
   int n_sm = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host source sites of later batches
   std::vector<cudaEvent_t> prof_ev;
+  std::vector<cudaEvent_t> site_ev;  // batch b's sites are on the device
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a0 = nullptr, ev_a1 = nullptr;
   std::mutex mu;
   std::string err;
@@ -409,6 +411,7 @@ int mc_ctx_create(int device, mc_ctx** out) {
   c->device = device;
   cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device);
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaEventCreate(&c->ev_a0) != cudaSuccess || cudaEventCreate(&c->ev_a1) != cudaSuccess) {
     delete c;
@@ -436,6 +439,9 @@ int mc_ctx_destroy(mc_ctx* c) {
   cudaEventDestroy(c->ev_a0);
   cudaEventDestroy(c->ev_a1);
   for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->site_ev) cudaEventDestroy(e);
+  cudaStreamSynchronize(c->copy_stream);
+  cudaStreamDestroy(c->copy_stream);
   cudaStreamDestroy(c->own_stream);
   delete c;
   return MC_OK;
@@ -663,15 +669,7 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
     }
     a.tol = (float)(1e-6 * sqrt(dg));
   }
-  if (dev_sites) {
-    a.sites = dev_sites;
-  } else if (d->sites && d->n_histories > 0) {
-    CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)d->n_histories)), "allocate sites");
-    CK(cudaMemcpyAsync(c->d_sites.p, d->sites, sizeof(mc_site) * (size_t)d->n_histories,
-                       cudaMemcpyHostToDevice, c->stream),
-       "upload sites");
-    a.sites = c->d_sites.as<mc_site>();
-  }
+  if (dev_sites) a.sites = dev_sites;
   a.eig = EigArgs{};
   a.eig.keff = 1.0;
   if (eig) a.eig = *eig;
@@ -743,6 +741,37 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
   a.live = nullptr;
   // history-form batches all score into slot 0 (one runs at a time);
   // event-form batch b scores into slot b % slots
+  // Host source sites: the first batches' sites are copied in stream order;
+  // in the event form the rest go on the copy stream, one copy per batch,
+  // and the birth limit reaches batch b only after the tracker's stream
+  // has waited for b's copy, so the copies overlap the first batches' walks.
+  int pre_b = nb;  // batches whose sites are copied in stream order
+  if (!dev_sites && d->sites && d->n_histories > 0) {
+    CK(cudaStreamSynchronize(c->copy_stream), "copy stream");
+    CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)d->n_histories)), "allocate sites");
+    a.sites = c->d_sites.as<mc_site>();
+    if (d->mode == MC_MODE_EVENT && nb > 2) pre_b = 2;
+    CK(cudaMemcpyAsync(c->d_sites.p, d->sites, sizeof(mc_site) * (size_t)bend[pre_b - 1], cudaMemcpyHostToDevice,
+                       c->stream),
+       "upload sites");
+    if (pre_b < nb) {
+      while (c->site_ev.size() < (size_t)nb) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+        c->site_ev.push_back(e);
+      }
+      // the copies start after the tracker's stream reached this point
+      CK(cudaEventRecord(c->site_ev[0], c->stream), "event");
+      CK(cudaStreamWaitEvent(c->copy_stream, c->site_ev[0], 0), "copy stream wait");
+      for (int b = pre_b; b < nb; ++b) {
+        CK(cudaMemcpyAsync(c->d_sites.as<mc_site>() + bend[b - 1], d->sites + bend[b - 1],
+                           sizeof(mc_site) * (size_t)(bend[b] - bend[b - 1]), cudaMemcpyHostToDevice,
+                           c->copy_stream),
+           "upload sites");
+        CK(cudaEventRecord(c->site_ev[b], c->copy_stream), "event");
+      }
+    }
+  }
   auto fold = [&](int b) -> int {
     const int64_t size = bend[b] - (b ? bend[b - 1] : 0);
     const int sl = (d->mode == MC_MODE_EVENT) ? b % slots : 0;
@@ -805,7 +834,9 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
         a.sort_tmp = c->d_sort_tmp.as<int>();
         a.sort_cnt = c->d_sort_cnt.as<int>();
       }
-      int64_t limit = nb > 1 ? bend[slots - 1] : d->n_histories;
+      // births are allowed up to the end of batch lim_b
+      int lim_b = std::min(slots, pre_b) - 1;
+      int64_t limit = nb > 1 ? bend[lim_b] : d->n_histories;
       CK(launch_event_init(M, X, S, a, B, Q, ctl, block, grid, c->stream, limit), "launch event init");
       n_launch = 1;
       int par = 0;
@@ -866,16 +897,29 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
         CK(cudaStreamSynchronize(c->stream), "event loop");
         if (nb > 1) {
           // retire drained batches, then let the next batches be born
-          bool moved = false;
           while (oldest < nb && h.next_hist >= bend[oldest] && h_live[oldest % slots] == 0) {
             rc = fold(oldest);
             if (rc) return rc;
             ++oldest;
             ++folded;
-            moved = true;
           }
-          if (moved && oldest < nb) {
-            c->h_limit = bend[std::min(oldest + slots - 1, nb - 1)];
+          // the limit moves over the batches within the slot window whose
+          // sites have landed (a copy still running is not waited for)
+          const int target = std::min(oldest + slots - 1, nb - 1);
+          int reach = lim_b;
+          while (oldest < nb && reach < target) {
+            const int b = reach + 1;
+            if (b >= pre_b) {
+              const cudaError_t q = cudaEventQuery(c->site_ev[b]);
+              if (q == cudaErrorNotReady) break;
+              CK(q, "site copy");
+              CK(cudaStreamWaitEvent(c->stream, c->site_ev[b], 0), "wait for sites");
+            }
+            reach = b;
+          }
+          if (reach > lim_b) {
+            lim_b = reach;
+            c->h_limit = bend[reach];
             CK(cudaMemcpyAsync(&ctl->birth_limit, &c->h_limit, sizeof(long long), cudaMemcpyHostToDevice,
                                c->stream),
                "raise birth limit");

@@ -151,3 +151,23 @@ def test_batch_results_stream_each_batch_sum(cube):
             assert close(outs[b], ref[b]), b
         with pytest.raises(Exception):
             t.run(sum(sizes), seed=5, accumulate=False, batch_sizes=sizes, batch_results=outs)
+
+
+def test_host_sites_reach_every_pipelined_batch(cube):
+    """Host sites of later batches are copied while the first batches walk;
+    births wait for their copy: every history equals the one born from the
+    device-sampled site (same site, same stream), bit for bit."""
+    sizes = SIZES_LONG * 2
+    n = sum(sizes)
+    with Tracker(0) as t:
+        t.load(cube)
+        t.run(n, seed=7, bank_size=1024, accumulate=True, traces=True, batch_sizes=sizes)
+        tr_dev = t.traces(n).copy()
+        sites = t.sample_sites(n, seed=7)
+        t.reset_tally()
+        t.run(n, seed=7, bank_size=1024, accumulate=True, traces=True, batch_sizes=sizes, sites=sites)
+        tr_host = t.traces(n)
+        assert t.batches_done() == len(sizes)
+    for f in ("hash", "status", "n_seg", "n_coll", "elem", "face"):
+        assert np.array_equal(tr_host[f], tr_dev[f]), f
+    assert np.array_equal(tr_host["E"].view(np.uint64), tr_dev["E"].view(np.uint64))
