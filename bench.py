@@ -47,6 +47,7 @@ the same workload.  Under torchrun every rank tracks its own history range
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -113,9 +114,11 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks/throttle reasons, sampled every 50 ms from before
+    the warm-up on; stop(window) keeps the samples whose timestamps fall
+    inside the timed region (wall-clock seconds from time.time())."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -129,12 +132,12 @@ class ClockSampler:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
-    def stop(self):
+    def stop(self, window=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -142,24 +145,26 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
             for line in f:
                 p = [x.strip() for x in line.split(",")]
-                if len(p) < 9:
+                if len(p) < 10:
                     continue
                 try:
-                    sm.append(float(p[1]))
-                    smax.append(float(p[2]))
+                    ts = datetime.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                    rows.append((ts, float(p[2]), float(p[3]), [n for n, v in zip(names, p[6:10])
+                                                                if v.lower() == "active"]))
                 except ValueError:
                     continue
-                for n, v in zip(names, p[5:9]):
-                    if v.lower() == "active":
-                        reasons.add(n)
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        inside = [r for r in rows if window and window[0] - 0.025 <= r[0] <= window[1] + 0.025]
+        use = inside or rows
+        sm = [r[1] for r in use]
+        reasons = sorted({n for r in use for n in r[3]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(r[2] for r in use) if use else None,
+                "reasons": reasons, "samples": len(sm), "in_timed_region": bool(inside)}
 
 
 def history_roofline(hist_per_s, S, C, xs_evals, b_seg):
@@ -356,10 +361,11 @@ def run_eigen(args):
             clk = ClockSampler(0)
             clk.start()
             w0 = time.perf_counter()
+            c0 = time.time()
             g = t.eigen(n, W + K, W, seed=1, precision=prec, bank_size=n, max_seg=ms_, sort_queue=9, graph=True,
                         block_size=128)
             wall = time.perf_counter() - w0
-            clocks = clk.stop()
+            clocks = clk.stop((c0, time.time()))
             act = g[W:]
             ms = float(act["ms"].sum())
             S = float(act["n_seg"].sum()) / (n * K)
@@ -532,11 +538,12 @@ def main():
     # --- FP64 (the configuration the metric is quoted on) ---
     t = tracker()
     params64, tune64 = tune(t, MC_PREC_FP64)
-    timed(t, MC_PREC_FP64, params64, 0, W, False)
     clocks = ClockSampler(local)
     clocks.start()
+    timed(t, MC_PREC_FP64, params64, 0, W, False)
+    w0 = time.time()
     ms, st = timed(t, MC_PREC_FP64, params64, W, K, False)
-    clk = clocks.stop()
+    clk = clocks.stop((w0, time.time()))
     value = world * n * K / (ms / 1e3)
     sum64 = t.tally(MC_TALLY_SUM)
     # one more batch with the walk launches timed (CUDA events around each
@@ -548,8 +555,12 @@ def main():
     if not args.no_mixed:
         tm = tracker()
         paramsm, tunem = tune(tm, MC_PREC_MIXED)
+        clocks_m = ClockSampler(local)
+        clocks_m.start()
         timed(tm, MC_PREC_MIXED, paramsm, 0, W, False)
+        w0m = time.time()
         mms, mst = timed(tm, MC_PREC_MIXED, paramsm, W, K, False)
+        clk_m = clocks_m.stop((w0m, time.time()))
         summ = tm.tally(MC_TALLY_SUM)
         # one more batch with the walk launches timed, for the walk's roofline
         _, pst = timed(tm, MC_PREC_MIXED, paramsm, W + K, 1, True)
@@ -561,7 +572,7 @@ def main():
                  "flux_rel_diff_mean": float(rel.mean()), "flux_rel_diff_max": float(rel.max()),
                  "flux_rel_diff_note": "element SUM tallies, mixed vs FP64 (bit-exact to the oracle), same "
                                        f"{n * (W + K)} histories, elements with a score",
-                 "tuned": paramsm, "gpu_launches": int(mst.n_launch),
+                 "tuned": paramsm, "gpu_launches": int(mst.n_launch), "clocks": clk_m,
                  "roofline_history": history_roofline(world * n * K / (mms / 1e3), mst.n_seg / (n * K),
                                                       mst.n_coll / (n * K), mst.n_xs / (n * K), B_SEG_MIXED)}
         if pst.ms_advance > 0:
