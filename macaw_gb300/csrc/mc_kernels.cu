@@ -914,7 +914,9 @@ __device__ __forceinline__ void mixed_tail(const DevMesh& M, const DevXS& X, con
           return;
         }
       }
-      if (!refresh_xs(M, X, a.n_mat, true, kEig, p, L)) {
+      // only the current material: a lone thread's lookups run one after
+      // another, and the walk asks for another material when it enters one
+      if (!refresh_xs(M, X, 0, true, kEig, p, L)) {
         finish(p, a, L);
         return;
       }
