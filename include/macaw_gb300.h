@@ -141,7 +141,8 @@ typedef struct {
   int32_t graph;           /* event mode: 1 captures a cycle of event iterations once as a CUDA
                               graph and replays it (ignored with profile) */
   int32_t tail;            /* event mode: once every history is born and at most this many particles
-                              are left, one tail kernel runs them to completion (0: max(4096, bank/64);
+                              are left, one tail kernel runs them to completion (0: max(4096, bank/16)
+                              for MC_PREC_MIXED, max(4096, bank/64) for MC_PREC_FP64;
                               -1: never, the event loop runs until the bank is empty) */
   const mc_site* sites;    /* optional HOST array of n_histories source sites; NULL: sample on the device */
   const int64_t* batch_sizes; /* HOST array of n_batches sizes adding up to n_histories */

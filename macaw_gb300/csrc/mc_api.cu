@@ -843,7 +843,8 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
       int oldest = 0;
       EventCtl h;
       const int kGroup = 4;
-      const int64_t tail = d->tail > 0 ? (int64_t)d->tail : d->tail < 0 ? -1 : std::max<int64_t>(4096, cap / 64);
+      const int64_t tail = d->tail > 0 ? (int64_t)d->tail : d->tail < 0 ? -1
+                                                          : std::max<int64_t>(4096, cap / tail_divisor(a));
       // a graph replays one group of iterations (parity 0,1,0,1: the group
       // always starts at parity 0), captured on first use
       const bool use_graph = d->graph && !d->profile;
@@ -930,11 +931,12 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
         const int64_t inflight = (int64_t)h.n_xs[par] + h.n_adv[par];
         if (nb == 1 && inflight == 0 && h.next_hist >= a.n) break;
         if (h.next_hist >= a.n && inflight <= tail) {
-          // one warp per block: the few long histories left are spread over
-          // every SM instead of crowding the first blocks' SMs (their walks
-          // are latency chains that compete for each SM's FP64 pipe)
-          const int fgrid = (int)std::max<int64_t>(1, (inflight + 31) / 32);
-          CK(launch_event_finish(M, X, S, a, B, Q, ctl, par, 32, fgrid, c->stream), "launch event finish");
+          // a few particles per warp (tail_block): the long histories left
+          // are latency chains, spread over every SM instead of serialised
+          // by divergence inside full warps
+          const int tb = tail_block(a.precision);
+          const int fgrid = (int)std::max<int64_t>(1, (inflight + tb - 1) / tb);
+          CK(launch_event_finish(M, X, S, a, B, Q, ctl, par, tb, fgrid, c->stream), "launch event finish");
           ++n_launch;
           break;
         }

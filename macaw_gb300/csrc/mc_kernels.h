@@ -141,6 +141,22 @@ cudaError_t launch_accumulate(double* batch, double* sum, double* sumsq, int64_t
 // by a pairwise tree (v[t] += v[t+s], s = 512, 256, ..., 1) into part[b];
 // the caller adds the ceil(n/1024) partials in index order.
 constexpr int kReduceTile = 1024;
+
+// Threads per block of the tail kernel: the histories left are long
+// latency chains whose steps diverge, so a warp carries only a few of them
+// (one in the mixed form, four in the FP64 form, where fewer, busier warps
+// share each SM's FP64 pipe better); measured on the 2M-tet lattice, single
+// 1e6-history calls ran 134.6M (mixed) and 50.1M (FP64) histories/s
+// against 116.5M and 47.0M with 32.
+inline int tail_block(int precision) { return precision == MC_PREC_MIXED ? 1 : 4; }
+
+// Default hand-over to the tail kernel: bank/16 particles left for the
+// mixed form of fixed-source runs, whose tail is a pure walk (single 1e6
+// calls on the lattice: 150.3M against 134.4M histories/s at bank/64);
+// bank/64 otherwise (FP64: no difference; k-eigenvalue generations, whose
+// tail histories collide about five times each, ran 27.6 against 31.2 ms
+// per mixed generation).
+inline int64_t tail_divisor(const RunArgs& a) { return (a.precision == MC_PREC_MIXED && !a.eig.on) ? 16 : 64; }
 cudaError_t launch_tile_sums(const double* v, int64_t n, double* part, cudaStream_t st);
 // Exclusive prefix sum of n counts into off[0..n] (off[n] = total);
 // tmp holds scan_tmp_size(n) entries.

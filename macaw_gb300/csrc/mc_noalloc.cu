@@ -179,7 +179,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
     n_launch = 1;
     int par = 0;
     EventCtl h;
-    const int64_t tail = d->tail > 0 ? (int64_t)d->tail : d->tail < 0 ? -1 : std::max<int64_t>(1024, cap / 64);
+    const int64_t tail = d->tail > 0 ? (int64_t)d->tail : d->tail < 0 ? -1 : std::max<int64_t>(1024, cap / tail_divisor(a));
     for (int64_t it = 0;; ++it) {
       for (int gi = 0; gi < 4; ++gi) {
         e = launch_event_iteration(v.M, v.X, v.S, a, B, Q, ctl, par, block, grid, st, &n_launch);
@@ -192,8 +192,10 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
       const int64_t inflight = (int64_t)h.n_xs[par] + h.n_adv[par];
       if (inflight == 0 && h.next_hist >= a.n) break;
       if (h.next_hist >= a.n && inflight <= tail) {
-        // one warp per block, spread over every SM (as mc_run does)
-        e = launch_event_finish(v.M, v.X, v.S, a, B, Q, ctl, par, 32, (int)std::max<int64_t>(1, (inflight + 31) / 32),
+        // a few particles per warp, spread over every SM (as mc_run does)
+        e = launch_event_finish(v.M, v.X, v.S, a, B, Q, ctl, par, tail_block(a.precision),
+                                (int)std::max<int64_t>(1, (inflight + tail_block(a.precision) - 1) /
+                                                              tail_block(a.precision)),
                                 st);
         if (e != cudaSuccess) return fail(MC_ERR_CUDA, std::string("event finish: ") + cudaGetErrorString(e));
         ++n_launch;
