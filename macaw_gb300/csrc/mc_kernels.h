@@ -8,10 +8,11 @@
 
 namespace mc {
 
-// Device counters, one 64-bit slot each.
 // Batches of one pipelined mc_run in flight at once (one tally slot each).
-constexpr int kPipeSlots = 8;
+constexpr int kPipeSlots = 32;                      // batches in flight at most
+constexpr size_t kSlotBudget = (size_t)8 << 30;     // bytes of batch tallies at most
 
+// Device counters, one 64-bit slot each.
 enum Counter : int {
   kCntSeg = 0,
   kCntColl,
