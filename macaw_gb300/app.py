@@ -39,3 +39,23 @@ def run_input(text: str, device: int = 0, file_base: str | None = None) -> dict:
 
 def read(name: str) -> str:
     return (INPUTS / name).read_text()
+
+
+def main(argv: list[str] | None = None) -> int:
+    """python -m macaw_gb300.app INPUT [--check] [--file-base BASE]: run (or
+    only check) an input file and print its JSON report."""
+    import argparse
+    ap = argparse.ArgumentParser(prog="python -m macaw_gb300.app")
+    ap.add_argument("input")
+    ap.add_argument("--check", action="store_true", help="parse and validate only (no GPU)")
+    ap.add_argument("--file-base", default=None, help="output file base (CSV, Exodus)")
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args(argv)
+    text = Path(args.input).read_text()
+    rep = check_input(text) if args.check else run_input(text, args.device, args.file_base)
+    print(json.dumps(rep, indent=1))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -211,3 +211,13 @@ def test_eigen_input_runs_like_the_direct_api(tmp_path):
     csv = np.loadtxt(tmp_path / "eig_flux.csv", delimiter=",", skiprows=1)
     nz = ref > 0
     assert np.all(np.abs(csv[nz, 2] - ref[nz]) <= 1e-12 * ref[nz])
+
+
+def test_command_line_check(capsys):
+    """python -m macaw_gb300.app INPUT --check prints the validated summary."""
+    import json
+    from macaw_gb300 import app
+    from macaw_gb300.app import INPUTS
+    assert app.main([str(INPUTS / "eigen_lattice.i"), "--check"]) == 0
+    rep = json.loads(capsys.readouterr().out)
+    assert rep["tets"] == 2039184 and rep["run_mode"] == "eigenvalue"
