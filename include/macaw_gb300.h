@@ -252,6 +252,17 @@ int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_histories, m
  * the tets of its prism. */
 int mc_set_2d(mc_ctx* ctx, int32_t on, double z_coord);
 
+/* Segments one history may walk before it is ended as stuck (status
+ * MC_ST_STUCK, counted in mc_stats.n_stuck).  No counterpart in MaCaw's own
+ * sources, whose tracer (MOOSE's TraceRay) runs a ray until a kernel or a
+ * boundary ends it.  0 restores the default: 4096 * ceil(cbrt(n_tet)),
+ * at least 65,536 and at most 10,000,000 (a straight flight crosses of the
+ * order of cbrt(n_tet) elements; the default allows 4096 such flights), so
+ * a runaway walk on a small mesh is stopped early.  mc_segment_limit
+ * returns the limit in force for the uploaded mesh. */
+int mc_set_segment_limit(mc_ctx* ctx, int64_t max_segments);
+int mc_segment_limit(mc_ctx* ctx, int64_t* out);
+
 /* ---- k-eigenvalue runs -------------------------------------------------
  * Replaces: OpenMC's eigenvalue run mode as OpenMCStudy drives it, one
  * generation per batch (src/userobjects/OpenMCStudy.C:297-364 births from
@@ -476,6 +487,15 @@ int mc_app_run(const char* input_text, int device, const char* file_base, char* 
 int mc_app_check(const char* input_text, char* report, int64_t report_len);
 
 /* ---- synthetic problem generators (host only; no device needed) ------ */
+/* Box [lo, hi] of nx x ny x nz hexes, six Kuhn tets each (split along each
+ * hex's main diagonal): MOOSE's GeneratedMeshGenerator with dim = 3, as
+ * test/tests/study/openmc_study.i:2-14 builds its 5 x 5 x 1 box, cut into
+ * tets.  Vertex (i, j, k) sits at lo + i * (hi - lo) / n per axis (the last
+ * plane at hi itself); sidesets 0..5 as MOOSE's GeneratedMesh (back,
+ * bottom, right, top, left, front); every tet in block 0. */
+int mc_gen_box_sizes(int32_t nx, int32_t ny, int32_t nz, int64_t* n_vtx, int64_t* n_tet);
+int mc_gen_box(int32_t nx, int32_t ny, int32_t nz, const double* lo, const double* hi, double* xyz,
+               int32_t* tet_vtx, int32_t* tet_block, int32_t* tet_side_bid);
 /* Cube [0,L]^3 of n^3 hexes, six Kuhn tets each; sidesets 0..5 as MOOSE's
  * GeneratedMesh (back, bottom, right, top, left, front). */
 int mc_gen_cube_sizes(int32_t n, int64_t* n_vtx, int64_t* n_tet);

@@ -126,6 +126,8 @@ SIGNATURES = {
     "mc_tally_download": ([_P, _I32, _P, _I64], C.c_int),
     "mc_tally_configure": ([_P, C.c_void_p], C.c_int),
     "mc_set_2d": ([_P, _I32, _D], C.c_int),
+    "mc_set_segment_limit": ([_P, _I64], C.c_int),
+    "mc_segment_limit": ([_P, C.POINTER(_I64)], C.c_int),
     "mc_exodus_read_sizes": ([C.c_char_p, C.POINTER(_I64), C.POINTER(_I64), C.c_char_p, _I64], C.c_int),
     "mc_exodus_read": ([C.c_char_p, _P, _P, _P, _P, C.c_char_p, _I64], C.c_int),
     "mc_rays_enable": ([_P, _I32, _I32], C.c_int),
@@ -139,6 +141,8 @@ SIGNATURES = {
     "mc_trace_download": ([_P, _P, _I64], C.c_int),
     "mc_stats_get": ([_P, C.POINTER(Stats)], C.c_int),
     "mc_batches_done": ([_P, C.POINTER(_I64)], C.c_int),
+    "mc_gen_box_sizes": ([_I32, _I32, _I32, C.POINTER(_I64), C.POINTER(_I64)], C.c_int),
+    "mc_gen_box": ([_I32, _I32, _I32, _P, _P, _P, _P, _P, _P], C.c_int),
     "mc_gen_cube_sizes": ([_I32, C.POINTER(_I64), C.POINTER(_I64)], C.c_int),
     "mc_gen_cube": ([_I32, _D, _P, _P, _P, _P], C.c_int),
     "mc_gen_lattice_sizes": ([_I32, _I32, _I32, _I32, _I32, C.POINTER(_I64), C.POINTER(_I64)], C.c_int),

@@ -97,6 +97,9 @@ struct mc_ctx {
   // 2-D mode (mc_set_2d)
   int two_d = 0;
   double z2d = 0.0;
+  // segments a history may walk before it ends as stuck (mc_set_segment_limit;
+  // 0: default_segment_limit of the mesh)
+  int64_t seg_limit = 0;
   int32_t ray_n = 0, ray_cap = 0;
   int64_t ray_first = 0;       // first_history of the last run that recorded
   long long h_limit = 0;
@@ -273,6 +276,7 @@ DevMesh dev_mesh(mc_ctx* c) {
   M.bc_type = c->d_bc.as<int>();
   M.n_bid = (int)c->bc_type.size();
   M.n_tet = c->mesh.n_tet;
+  M.max_seg = (int)(c->seg_limit > 0 ? c->seg_limit : default_segment_limit(c->mesh.n_tet));
   for (int k = 0; k < 3; ++k) {
     M.glo[k] = c->mesh.glo[k];
     M.gh[k] = c->mesh.gh[k];
@@ -1181,6 +1185,23 @@ int mc_set_2d(mc_ctx* c, int32_t on, double z_coord) {
   if (on && !(z_coord == z_coord)) return set_err(c, MC_ERR_ARG, "z_coord must be a number");
   c->two_d = on ? 1 : 0;
   c->z2d = on ? z_coord : 0.0;
+  return MC_OK;
+}
+
+int mc_set_segment_limit(mc_ctx* c, int64_t max_segments) {
+  if (!c) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (max_segments < 0 || max_segments > 2000000000LL)
+    return set_err(c, MC_ERR_ARG, "segment limit must be in [0, 2e9] (0: the mesh-size default)");
+  c->seg_limit = max_segments;
+  return MC_OK;
+}
+
+int mc_segment_limit(mc_ctx* c, int64_t* out) {
+  if (!c || !out) return MC_ERR_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->have_mesh) return set_err(c, MC_ERR_STATE, "no mesh");
+  *out = c->seg_limit > 0 ? c->seg_limit : default_segment_limit(c->mesh.n_tet);
   return MC_OK;
 }
 

@@ -292,7 +292,16 @@ enum Status : int {
   kBadXS = 6,
 };
 
-constexpr int kMaxSegments = 10000000;
+// Segments a history may walk before it is ended as stuck, unless the
+// caller sets a limit (mc_set_segment_limit): a straight flight crosses of
+// the order of cbrt(n_tet) elements, and the default allows 4096 such
+// flights, at least 65,536 and at most 10,000,000 segments.
+inline int64_t default_segment_limit(int64_t n_tet) {
+  int64_t c = 1;
+  while (c * c * c < n_tet) ++c;
+  int64_t l = 4096 * c;
+  return l < 65536 ? 65536 : l > 10000000 ? 10000000 : l;
+}
 constexpr int kMaxZeroRun = 10000;
 constexpr double kLocateTol = 1e-9;
 

@@ -98,6 +98,7 @@ struct DevMesh {
   const int* __restrict__ tmat;         // material index per tet (-1: none)
   const int* __restrict__ bc_type;      // per boundary id: 0 vacuum, 1 reflect
   int n_bid;
+  int max_seg;                          // segments a history may walk before it ends as stuck
   int64_t n_tet;
   double glo[3], gh[3], ginv[3];  // locator origin, cell size, 1 / cell size
   int gn[3];
@@ -886,7 +887,7 @@ template <bool kInlineXS, bool kRays = true, bool kEig = false>
 __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Particle& p,
                                             double* __restrict__ tally, const TallySpec& T, float& sigt32,
                                             unsigned long long& n_xs) {
-  if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
+  if (p.n_seg >= M.max_seg || p.zero_run >= kMaxZeroRun) {
     p.status = kStuck;
     return 2;
   }
@@ -1026,7 +1027,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
                                              const float uf, const float vf, const float wf,
                                              double* __restrict__ tally, const TallySpec& T, float& sigt32,
                                              unsigned long long& n_xs) {
-  if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
+  if (p.n_seg >= M.max_seg || p.zero_run >= kMaxZeroRun) {
     p.status = kStuck;
     return 2;
   }
@@ -1228,7 +1229,7 @@ __device__ __forceinline__ int segment_mixed(const DevMesh& M, const DevXS& X, P
                                              float& inv_sig,
                                              float tol, unsigned long long& n_xs,
                                              unsigned long long& n_fb) {
-  if (p.n_seg >= kMaxSegments || p.zero_run >= kMaxZeroRun) {
+  if (p.n_seg >= M.max_seg || p.zero_run >= kMaxZeroRun) {
     p.status = kStuck;
     return 2;
   }

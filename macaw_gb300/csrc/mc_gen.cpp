@@ -33,9 +33,13 @@ struct Gen {
 };
 
 // ---------------------------------------------------------------------------
-// Cube of n^3 hexes, each split into the six Kuhn tets along its main diagonal.
-void cube_vertex_index(int n, int i, int j, int k, int32_t* id) {
-  *id = (int32_t)(((int64_t)k * (n + 1) + j) * (n + 1) + i);
+// Box of nx x ny x nz hexes, each split into the six Kuhn tets along its
+// main diagonal (vertex (i,j,k) -> (i+1,j+1,k+1)): MOOSE's
+// GeneratedMeshGenerator (dim = 3) with a tet split.  Every hex face is cut
+// into two triangles along a diagonal that the neighbouring hex cuts the
+// same way, so the tets conform.
+int64_t box_vertex_index(int nx, int ny, int i, int j, int k) {
+  return ((int64_t)k * (ny + 1) + j) * (nx + 1) + i;
 }
 
 // MOOSE GeneratedMesh 3D sideset ids: back=0 (z-), bottom=1 (y-), right=2
@@ -52,42 +56,50 @@ int box_side_id(const int* lo_hit, const int* hi_hit) {
 
 const int kFaceVtx[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
 
+bool box_dims_ok(int32_t nx, int32_t ny, int32_t nz) {
+  return nx >= 1 && ny >= 1 && nz >= 1 && nx <= 2000 && ny <= 2000 && nz <= 2000 &&
+         (int64_t)6 * nx * ny * nz <= 2000000000LL;
+}
+
 }  // namespace
 
-extern "C" int mc_gen_cube_sizes(int32_t n, int64_t* n_vtx, int64_t* n_tet) {
-  if (n < 1 || n > 1000) return MC_ERR_ARG;
-  *n_vtx = (int64_t)(n + 1) * (n + 1) * (n + 1);
-  *n_tet = (int64_t)6 * n * n * n;
+extern "C" int mc_gen_box_sizes(int32_t nx, int32_t ny, int32_t nz, int64_t* n_vtx, int64_t* n_tet) {
+  if (!box_dims_ok(nx, ny, nz) || !n_vtx || !n_tet) return MC_ERR_ARG;
+  *n_vtx = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
+  *n_tet = (int64_t)6 * nx * ny * nz;
   return MC_OK;
 }
 
-extern "C" int mc_gen_cube(int32_t n, double L, double* xyz, int32_t* tet_vtx, int32_t* tet_block,
-                           int32_t* tet_side_bid) {
-  if (n < 1 || n > 1000 || !(L > 0.0)) return MC_ERR_ARG;
-  const double h = L / n;
-  for (int k = 0; k <= n; ++k)
-    for (int j = 0; j <= n; ++j)
-      for (int i = 0; i <= n; ++i) {
-        int32_t v;
-        cube_vertex_index(n, i, j, k, &v);
-        xyz[3 * (int64_t)v + 0] = (i == n) ? L : i * h;
-        xyz[3 * (int64_t)v + 1] = (j == n) ? L : j * h;
-        xyz[3 * (int64_t)v + 2] = (k == n) ? L : k * h;
+extern "C" int mc_gen_box(int32_t nx, int32_t ny, int32_t nz, const double* lo, const double* hi, double* xyz,
+                          int32_t* tet_vtx, int32_t* tet_block, int32_t* tet_side_bid) {
+  if (!box_dims_ok(nx, ny, nz) || !lo || !hi || !xyz || !tet_vtx || !tet_block) return MC_ERR_ARG;
+  const int n[3] = {nx, ny, nz};
+  double h[3];
+  for (int a = 0; a < 3; ++a) {
+    if (!(hi[a] > lo[a])) return MC_ERR_ARG;
+    h[a] = (hi[a] - lo[a]) / n[a];
+  }
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const int c[3] = {i, j, k};
+        const int64_t v = box_vertex_index(nx, ny, i, j, k);
+        // the last plane is the upper bound itself, not lo + n*h
+        for (int a = 0; a < 3; ++a) xyz[3 * v + a] = (c[a] == n[a]) ? hi[a] : lo[a] + c[a] * h[a];
       }
   static const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
   int64_t t = 0;
-  for (int k = 0; k < n; ++k)
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i < n; ++i)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
         for (int p = 0; p < 6; ++p, ++t) {
-          int c[3] = {i, j, k};
-          int cell[4][3];
-          for (int a = 0; a < 3; ++a) cell[0][a] = c[a];
+          int cell[4][3] = {{i, j, k}};
           for (int s = 1; s < 4; ++s) {
             for (int a = 0; a < 3; ++a) cell[s][a] = cell[s - 1][a];
             cell[s][perms[p][s - 1]] += 1;
           }
-          for (int s = 0; s < 4; ++s) cube_vertex_index(n, cell[s][0], cell[s][1], cell[s][2], &tet_vtx[4 * t + s]);
+          for (int s = 0; s < 4; ++s)
+            tet_vtx[4 * t + s] = (int32_t)box_vertex_index(nx, ny, cell[s][0], cell[s][1], cell[s][2]);
           tet_block[t] = 0;
           if (tet_side_bid) {
             for (int f = 0; f < 4; ++f) {
@@ -96,7 +108,7 @@ extern "C" int mc_gen_cube(int32_t n, double L, double* xyz, int32_t* tet_vtx, i
                 const int* v = cell[kFaceVtx[f][q]];
                 for (int a = 0; a < 3; ++a) {
                   if (v[a] != 0) lo_hit[a] = 0;
-                  if (v[a] != n) hi_hit[a] = 0;
+                  if (v[a] != n[a]) hi_hit[a] = 0;
                 }
               }
               tet_side_bid[4 * t + f] = box_side_id(lo_hit, hi_hit);
@@ -104,6 +116,20 @@ extern "C" int mc_gen_cube(int32_t n, double L, double* xyz, int32_t* tet_vtx, i
           }
         }
   return MC_OK;
+}
+
+extern "C" int mc_gen_cube_sizes(int32_t n, int64_t* n_vtx, int64_t* n_tet) {
+  if (n < 1 || n > 1000) return MC_ERR_ARG;
+  return mc_gen_box_sizes(n, n, n, n_vtx, n_tet);
+}
+
+// The cube [0, L]^3 is the box with lower corner 0 (0 + i*h == i*h exactly,
+// so the coordinates are those of the box generator bit for bit).
+extern "C" int mc_gen_cube(int32_t n, double L, double* xyz, int32_t* tet_vtx, int32_t* tet_block,
+                           int32_t* tet_side_bid) {
+  if (n < 1 || n > 1000 || !(L > 0.0)) return MC_ERR_ARG;
+  const double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {L, L, L};
+  return mc_gen_box(n, n, n, lo, hi, xyz, tet_vtx, tet_block, tet_side_bid);
 }
 
 // ---------------------------------------------------------------------------

@@ -616,7 +616,7 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     if (mat < 0) mnext = __ldg(M.tmat + elem);
   }
   for (;;) {
-    if (n_seg >= kMaxSegments || zrun >= kMaxZeroRun) {
+    if (n_seg >= M.max_seg || zrun >= kMaxZeroRun) {
       r = 2;
       face = -2;  // stuck
       break;

@@ -15,6 +15,10 @@ eigen_lattice_problem -- the pin lattice as a k-eigenvalue problem:
                     fissionable fuel nuclides (nu*sigma_f a fixed share of
                     their absorption), reflective sides, vacuum top and
                     bottom.
+study_box_problem -- the mesh of the reference's study test (a 5x5x1 box of
+                    hexes over [-5, 5]^3 cut into tets, centre hex in block 1,
+                    reflective on every side) with transparent materials,
+                    for pure-geometry walks.
 core_problem     -- cylindrical core, radius 180 cm, 400 cm tall: 193
                     assemblies of 17x17 pin cells plus a reflector of whole
                     cells, 6 axial layers (about 41M tets); 200 materials of
@@ -119,6 +123,19 @@ def cube_mesh(n: int = 20, L: float = 20.0):
     return xyz, tv, blk, bid
 
 
+def box_mesh(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0)):
+    nv, nt = C.c_int64(), C.c_int64()
+    _check(lib.mc_gen_box_sizes(nx, ny, nz, C.byref(nv), C.byref(nt)), "mc_gen_box_sizes")
+    xyz = np.zeros((nv.value, 3), np.float64)
+    tv = np.zeros((nt.value, 4), np.int32)
+    blk = np.zeros(nt.value, np.int32)
+    bid = np.zeros((nt.value, 4), np.int32)
+    lo_a = np.ascontiguousarray(lo, np.float64)
+    hi_a = np.ascontiguousarray(hi, np.float64)
+    _check(lib.mc_gen_box(nx, ny, nz, ptr(lo_a), ptr(hi_a), ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_box")
+    return xyz, tv, blk, bid
+
+
 def lattice_mesh(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fuel_rings: int = 2,
                  pitch: float = 1.26, height: float = 50.0, r_fuel: float = 0.41, r_clad: float = 0.475):
     nv, nt = C.c_int64(), C.c_int64()
@@ -182,6 +199,30 @@ def cube_problem(n: int = 20, L: float = 20.0, n_nuc: int = 10, n_pts: int = 100
     src = Source(space=MC_SRC_POINT, point=(L / 2, L / 2, L / 2))
     return Problem(f"cube{n}", xyz, tv, blk, bid, nucs, [mat], np.array([0], np.int32),
                    np.array([1], np.int32), src, {b: MC_BC_VACUUM for b in range(6)})
+
+
+def study_box_problem(sigma_b: float = 1e-20, density: float = 1e-4) -> Problem:
+    """The mesh of MaCaw's study test (test/tests/study/openmc_study.i:1-22):
+    GeneratedMeshGenerator 5 x 5 x 1 hexes over [-5, 5]^3, each hex cut
+    into six Kuhn tets; SubdomainBoundingBoxGenerator puts the hex inside
+    [-1, 1]^3 into block 1, the rest stays in block 0; ReflectRayBC on all
+    six sides (:49-54); blocks 0 and 1 map to materials 1 and 2 (CollisionKernel
+    `blocks = "0 1 2"`, `materials = "1 2 3"`, :42-47).  The materials are
+    transparent (one nuclide of sigma_b barn at `density`), so histories
+    fly without colliding: the walk and the reflections alone set their
+    paths."""
+    xyz, tv, blk, bid = box_mesh(5, 5, 1, (-5.0, -5.0, -5.0), (5.0, 5.0, 5.0))
+    # hex centres (the six Kuhn tets of a hex are consecutive; their
+    # centroids average to the hex centre), as SubdomainBoundingBoxGenerator
+    # tests element centres against the box
+    hc = np.repeat(xyz[tv].mean(axis=1).reshape(-1, 6, 3).mean(axis=1), 6, axis=0)
+    blk[:] = np.where(np.all(np.abs(hc) < 1.0, axis=1), 1, 0).astype(np.int32)
+    E = np.array([E_MIN, E_MAX])
+    nuc = Nuclide(E, np.full(2, sigma_b), np.full(2, sigma_b), 1.0)
+    mats = [Material(m, np.array([0], np.int32), np.array([density])) for m in (1, 2, 3)]
+    src = Source(space=MC_SRC_POINT, point=(0.0, 0.0, 0.0))
+    return Problem("study_box", xyz, tv, blk, bid, [nuc], mats, np.array([0, 1, 2], np.int32),
+                   np.array([1, 2, 3], np.int32), src, {b: MC_BC_REFLECT for b in range(6)}, hash_bins=16)
 
 
 def lattice_problem(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fuel_rings: int = 2,

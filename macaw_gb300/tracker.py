@@ -132,6 +132,15 @@ class Tracker:
         d.energy_edges = None if e is None else e.ctypes.data
         self._ck(lib.mc_tally_configure(self._h, C.byref(d)), "mc_tally_configure")
 
+    def set_segment_limit(self, n: int) -> None:
+        """Segments a history may walk before it ends as stuck (0: the mesh-size default)."""
+        self._ck(lib.mc_set_segment_limit(self._h, n), "mc_set_segment_limit")
+
+    def segment_limit(self) -> int:
+        v = C.c_int64()
+        self._ck(lib.mc_segment_limit(self._h, C.byref(v)), "mc_segment_limit")
+        return v.value
+
     def enable_rays(self, n_rays: int, max_segments: int = 4096) -> None:
         """Record every segment of the first n_rays histories of each run (0: off)."""
         self._ck(lib.mc_rays_enable(self._h, n_rays, max_segments), "mc_rays_enable")

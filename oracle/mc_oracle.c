@@ -183,6 +183,14 @@ struct oracle_problem {
   /* 2-D mode (CollisionKernel z_coord) */
   int two_d;
   double z2d;
+  /* segments a history may walk before it is ended as stuck (0: the
+     mesh-size default, segment_limit()) */
+  int64_t seg_limit;
+  /* segment recording (oracle_rays_enable): histories first..first+ray_n-1
+     of the last run, ray_cap segments each */
+  int32_t ray_n, ray_cap;
+  oracle_ray_seg* rays;
+  int32_t* ray_cnt;
 };
 
 static int fail(oracle_problem* p, const char* msg)
@@ -225,6 +233,7 @@ void oracle_destroy(oracle_problem* p)
   for (int i = 0; i < p->n_mat; ++i) { free(p->mats[i].nuc); free(p->mats[i].dens); }
   free(p->mats);
   free(p->map_blocks); free(p->map_mats); free(p->src_cyl); free(p->t_edges);
+  free(p->rays); free(p->ray_cnt);
   free(p);
 }
 
@@ -806,7 +815,20 @@ static void rotate_dir(double* u, double mu, double cphi, double sphi)
 #define ST_STUCK 4
 #define ST_LOST 5
 #define ST_BADXS 6
-#define MAX_SEG 10000000
+/* Segments a history may walk before it is ended as stuck.  A straight
+ * flight crosses of the order of cbrt(n_tet) elements, so the default
+ * allows 4096 such flights: 4096 * ceil(cbrt(n_tet)), at least 65,536 and
+ * at most 10,000,000 (the same rule as the GPU library's default). */
+static int64_t segment_limit(const oracle_problem* p)
+{
+  if (p->seg_limit > 0) return p->seg_limit;
+  int64_t c = 1;
+  while (c * c * c < p->n_tet) ++c;
+  int64_t l = 4096 * c;
+  if (l < 65536) l = 65536;
+  if (l > 10000000) l = 10000000;
+  return l;
+}
 #define MAX_ZERO_RUN 10000
 
 #define FNV_OFF 14695981039346656037ULL
@@ -973,8 +995,28 @@ static void fission_sites(const oracle_problem* p, heig* e, int64_t id, const do
 
 /* One history: id h+1, born from `site` (x, y, z, u, v, w, E, wgt) when
  * given, else sampled from the source stream. */
+/* Appends the segment that just ended to a recorded ray (the same fields
+ * as the GPU library's mc_ray_segment). */
+static void record_seg(oracle_ray_seg* rec, int32_t* rec_n, int32_t cap, int64_t id, int n_seg, int n_coll,
+                       int elem, const double* s, const double* x, double E, double wgt, uint64_t seed)
+{
+  const int k = n_seg - 1;
+  if (!rec || k >= cap) return;
+  oracle_ray_seg* o = rec + k;
+  o->id = id;
+  o->segment = k;
+  o->intersections = n_seg - n_coll;
+  o->elem = elem;
+  o->pad = 0;
+  for (int a = 0; a < 3; ++a) { o->start[a] = s[a]; o->end[a] = x[a]; }
+  o->E = E;
+  o->wgt = wgt;
+  o->seed_tracking = seed;
+  *rec_n = k + 1;
+}
+
 static void track(const oracle_problem* p, int64_t h, uint64_t master, const double* site, heig* e,
-                  double* tally, oracle_trace* tr, lstats* ls)
+                  double* tally, oracle_trace* tr, lstats* ls, oracle_ray_seg* rec, int32_t* rec_n)
 {
   int64_t id = h + 1;
   uint64_t ssrc = oracle_init_seed(id, master, 2);
@@ -1000,9 +1042,12 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
   int cur_mat = -2;
   double sigt = 0.0;
   int zero_run = 0;
+  const int64_t max_seg = segment_limit(p);
+  const int32_t rec_cap = p->ray_cap;
+  double s0[3];
   if (elem < 0) status = ST_LOST;
   while (status == 0) {
-    if (n_seg >= MAX_SEG || zero_run >= MAX_ZERO_RUN) { status = ST_STUCK; break; }
+    if (n_seg >= max_seg || zero_run >= MAX_ZERO_RUN) { status = ST_STUCK; break; }
     int mat = p->tmat[elem];
     if (mat < 0) { status = ST_BADXS; break; }
     if (mat != cur_mat) {
@@ -1033,11 +1078,13 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
     if (eig) e->ktl = e->ktl + wgt * score * nuf; /* CollisionKernel.C:153-154 */
     ++n_seg;
     if (L == 0.0) ++zero_run; else zero_run = 0;
+    s0[0] = x[0]; s0[1] = x[1]; s0[2] = x[2];
     if (dist > L) {
       hash = (hash ^ ((uint64_t)elem * 8ULL + (uint64_t)bf)) * FNV_PRIME;
       x[0] = x[0] + L * u[0];
       x[1] = x[1] + L * u[1];
       x[2] = x[2] + L * u[2];
+      record_seg(rec, rec_n, rec_cap, id, n_seg, n_coll, elem, s0, x, E, wgt, strk);
       int32_t nb = p->nbr[4 * (int64_t)elem + bf];
       if (nb >= 0) { elem = nb; continue; }
       int32_t bid = p->side_bid[4 * (int64_t)elem + bf];
@@ -1064,6 +1111,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
     x[1] = ey - back * u[1];
     x[2] = ez - back * u[2];
     ++n_coll;
+    record_seg(rec, rec_n, rec_cap, id, n_seg, n_coll, elem, s0, x, E, wgt, strk);
     zero_run = 0;
     score_collision(p, tally, elem, mat, E, wgt, sigt);
     /* collision estimate of keff (OpenMC event_collide) */
@@ -1135,13 +1183,24 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
   }
 }
 
-int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n_threads,
-               double* tally, oracle_trace* traces, oracle_stats* stats)
+/* Recorded ray of history i of a run (NULL when i is not recorded). */
+static oracle_ray_seg* ray_slot(const oracle_problem* p, int64_t i, int32_t** cnt)
+{
+  if (!p->rays || i >= p->ray_n) { *cnt = NULL; return NULL; }
+  *cnt = p->ray_cnt + i;
+  return p->rays + i * (int64_t)p->ray_cap;
+}
+
+/* Histories [first, first+n): born from sites (n x 8 doubles) when given,
+ * else sampled from the source. */
+static int run_histories(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, const double* sites,
+                         int n_threads, double* tally, oracle_trace* traces, oracle_stats* stats)
 {
   if (!p->planes) return fail(p, "no mesh");
   if (prepare_data(p)) return 1;
   if (p->n_mat < 1) return fail(p, "no materials");
   for (int64_t t = 0; t < p->n_tet; ++t) p->tmat[t] = material_of_block(p, p->blk[t]);
+  if (p->rays) memset(p->ray_cnt, 0, sizeof(int32_t) * (size_t)p->ray_n);
   if (n_threads < 1) n_threads = 1;
   lstats tot;
   memset(&tot, 0, sizeof tot);
@@ -1150,7 +1209,12 @@ int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n
   nt = 1;
 #endif
   if (nt == 1) {
-    for (int64_t i = 0; i < n; ++i) track(p, first + i, seed, NULL, NULL, tally, traces ? traces + i : NULL, &tot);
+    for (int64_t i = 0; i < n; ++i) {
+      int32_t* rc;
+      oracle_ray_seg* rec = ray_slot(p, i, &rc);
+      track(p, first + i, seed, sites ? sites + 8 * i : NULL, NULL, tally, traces ? traces + i : NULL, &tot,
+            rec, rc);
+    }
   } else {
 #ifdef _OPENMP
     double** priv = (double**)calloc((size_t)nt, sizeof(double*));
@@ -1160,8 +1224,12 @@ int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n
       int tid = omp_get_thread_num();
       priv[tid] = (double*)calloc((size_t)oracle_tally_size(p), sizeof(double));
 #pragma omp for schedule(dynamic, 64)
-      for (int64_t i = 0; i < n; ++i)
-        track(p, first + i, seed, NULL, NULL, priv[tid], traces ? traces + i : NULL, pl + tid);
+      for (int64_t i = 0; i < n; ++i) {
+        int32_t* rc;
+        oracle_ray_seg* rec = ray_slot(p, i, &rc);
+        track(p, first + i, seed, sites ? sites + 8 * i : NULL, NULL, priv[tid], traces ? traces + i : NULL,
+              pl + tid, rec, rc);
+      }
     }
     for (int t = 0; t < nt; ++t) {
       if (priv[t]) {
@@ -1189,6 +1257,58 @@ int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n
     stats->leak_weight = tot.leak_w;
   }
   return 0;
+}
+
+int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n_threads,
+               double* tally, oracle_trace* traces, oracle_stats* stats)
+{
+  return run_histories(p, first, n, seed, NULL, n_threads, tally, traces, stats);
+}
+
+int oracle_run_sites(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, const double* sites,
+                     int n_threads, double* tally, oracle_trace* traces, oracle_stats* stats)
+{
+  if (!sites) return fail(p, "no sites");
+  return run_histories(p, first, n, seed, sites, n_threads, tally, traces, stats);
+}
+
+int oracle_set_segment_limit(oracle_problem* p, int64_t max_segments)
+{
+  if (max_segments < 0 || max_segments > 2000000000LL) return fail(p, "segment limit out of range");
+  p->seg_limit = max_segments;
+  return 0;
+}
+
+int64_t oracle_segment_limit(const oracle_problem* p) { return segment_limit(p); }
+
+int oracle_rays_enable(oracle_problem* p, int32_t n_rays, int32_t max_segments)
+{
+  if (n_rays < 0 || max_segments < 0 || (int64_t)n_rays * max_segments > 100000000LL)
+    return fail(p, "ray recording size out of range");
+  free(p->rays);
+  free(p->ray_cnt);
+  p->rays = NULL;
+  p->ray_cnt = NULL;
+  p->ray_n = 0;
+  p->ray_cap = 0;
+  if (n_rays == 0 || max_segments == 0) return 0;
+  p->rays = (oracle_ray_seg*)calloc((size_t)n_rays * (size_t)max_segments, sizeof(oracle_ray_seg));
+  p->ray_cnt = (int32_t*)calloc((size_t)n_rays, sizeof(int32_t));
+  if (!p->rays || !p->ray_cnt) return fail(p, "out of memory");
+  p->ray_n = n_rays;
+  p->ray_cap = max_segments;
+  return 0;
+}
+
+int oracle_rays(oracle_problem* p, oracle_ray_seg* out, int64_t capacity, int64_t* n_out)
+{
+  int64_t m = 0;
+  for (int32_t r = 0; r < p->ray_n; ++r) {
+    for (int32_t k = 0; k < p->ray_cnt[r]; ++k, ++m)
+      if (out && m < capacity) out[m] = p->rays[(int64_t)r * p->ray_cap + k];
+  }
+  *n_out = m;
+  return (out && m > capacity) ? fail(p, "capacity too small") : 0;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1288,7 +1408,7 @@ int oracle_eigen_run(oracle_problem* p, int64_t n, int32_t n_gen, int32_t n_inac
 #ifdef _OPENMP
       tid = omp_get_thread_num();
 #endif
-      track(p, (int64_t)g * n + i, seed, src + 8 * i, he + i, priv[tid], NULL, pl + tid);
+      track(p, (int64_t)g * n + i, seed, src + 8 * i, he + i, priv[tid], NULL, pl + tid, NULL, NULL);
     }
     lstats tot;
     memset(&tot, 0, sizeof tot);

@@ -59,6 +59,20 @@ typedef struct {
   double x, y, z;   /* last position */
 } oracle_trace;
 
+/* One recorded segment of a history (the fields of the GPU library's
+ * mc_ray_segment, the per-segment output MOOSE's RayTracingExodus writes for
+ * a study's rays; test/tests/study/gold/openmc_study_rays.e). */
+typedef struct {
+  int64_t id;             /* particle id (1-based) */
+  int32_t segment;        /* index along the ray */
+  int32_t intersections;  /* segments that ended on a side, this one included */
+  int32_t elem;
+  int32_t pad;
+  double start[3], end[3];
+  double E, wgt;          /* energy and weight along the segment */
+  uint64_t seed_tracking; /* tracking-stream state after the segment's draw */
+} oracle_ray_seg;
+
 typedef struct {
   int64_t n_hist, n_seg, n_coll, n_leak, n_absorb, n_cutoff, n_stuck, n_lost, n_badxs;
   double leak_weight;
@@ -112,6 +126,21 @@ int oracle_set_2d(oracle_problem* p, int32_t on, double z_coord);
  * traces (n entries) may be NULL. */
 int oracle_run(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, int n_threads,
                double* tally, oracle_trace* traces, oracle_stats* stats);
+
+/* As oracle_run, with history i born from sites[8i..8i+7] (x y z u v w E
+ * wgt) instead of the source; the tracking stream is still keyed by the id. */
+int oracle_run_sites(oracle_problem* p, int64_t first, int64_t n, uint64_t seed, const double* sites,
+                     int n_threads, double* tally, oracle_trace* traces, oracle_stats* stats);
+/* Segments a history may walk before it ends as stuck (0: the default,
+ * 4096 * ceil(cbrt(n_tet)) clamped to [65536, 1e7]); oracle_segment_limit
+ * returns the limit in force. */
+int oracle_set_segment_limit(oracle_problem* p, int64_t max_segments);
+int64_t oracle_segment_limit(const oracle_problem* p);
+/* Records every segment of the first n_rays histories of each following
+ * run, up to max_segments each (0: off); oracle_rays returns them ray by
+ * ray in segment order (*n_out: their number). */
+int oracle_rays_enable(oracle_problem* p, int32_t n_rays, int32_t max_segments);
+int oracle_rays(oracle_problem* p, oracle_ray_seg* out, int64_t capacity, int64_t* n_out);
 
 /* nu*sigma_f per grid point of a nuclide (NULL: not fissionable).  A
  * fissionable nuclide samples fission sites at each collision with it:

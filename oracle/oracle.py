@@ -39,6 +39,9 @@ TRACE_DTYPE = np.dtype([("id", "<i8"), ("hash", "<u8"), ("status", "<i4"), ("n_s
 
 FSITE_DTYPE = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("u", "<f8"), ("v", "<f8"), ("w", "<f8"),
                         ("E", "<f8"), ("wgt", "<f8"), ("parent", "<i8"), ("progeny", "<i4"), ("pad", "<i4")])
+RAY_DTYPE = np.dtype([("id", "<i8"), ("segment", "<i4"), ("intersections", "<i4"), ("elem", "<i4"),
+                      ("pad", "<i4"), ("start", "<f8", (3,)), ("end", "<f8", (3,)), ("E", "<f8"),
+                      ("wgt", "<f8"), ("seed_tracking", "<u8")])
 GEN_DTYPE = np.dtype([("k_generation", "<f8"), ("k_collision", "<f8"), ("k_absorption", "<f8"), ("keff", "<f8"),
                       ("keff_std", "<f8"), ("leakage", "<f8"), ("n_sites", "<i8"), ("n_seg", "<i8"),
                       ("n_coll", "<i8")])
@@ -58,6 +61,11 @@ _SIG = {
     "oracle_tally_size": ([C.c_void_p], C.c_int64),
     "oracle_set_2d": ([C.c_void_p, C.c_int32, C.c_double], C.c_int),
     "oracle_run": ([_P, _I64, _I64, _U64, C.c_int, _P, _P, C.POINTER(OracleStats)], C.c_int),
+    "oracle_run_sites": ([_P, _I64, _I64, _U64, _P, C.c_int, _P, _P, C.POINTER(OracleStats)], C.c_int),
+    "oracle_set_segment_limit": ([_P, _I64], C.c_int),
+    "oracle_segment_limit": ([_P], _I64),
+    "oracle_rays_enable": ([_P, _I32, _I32], C.c_int),
+    "oracle_rays": ([_P, _P, _I64, C.POINTER(_I64)], C.c_int),
     "oracle_set_fission": ([_P, _I32, _P], C.c_int),
     "oracle_eigen_run": ([_P, _I64, _I32, _I32, _U64, _D, _D, _D, _I64, C.c_int, _P, _P, _P, _P, _I64, _P, _P],
                          C.c_int),
@@ -161,15 +169,45 @@ class Oracle:
         self._ck(lib.oracle_set_tally(self.h, t.estimator, sc.size, _p(sc), 0 if e is None else e.size - 1, _p(e)),
                  "oracle_set_tally")
 
-    def run(self, n: int, first: int = 0, seed: int = 1, threads: int = 1, traces: bool = True):
-        """Returns (tally, traces or None, stats dict, seconds)."""
+    def run(self, n: int, first: int = 0, seed: int = 1, threads: int = 1, traces: bool = True, sites=None):
+        """Returns (tally, traces or None, stats dict, seconds).  sites: n
+        source sites (x y z u v w E wgt per row, or a structured array of
+        those fields) to start from instead of sampling the source."""
         tally = np.zeros(lib.oracle_tally_size(self.h))
         tr = np.zeros(n, TRACE_DTYPE) if traces else None
         st = OracleStats()
         t0 = time.perf_counter()
-        self._ck(lib.oracle_run(self.h, first, n, seed, threads, _p(tally), _p(tr), C.byref(st)), "oracle_run")
+        if sites is None:
+            self._ck(lib.oracle_run(self.h, first, n, seed, threads, _p(tally), _p(tr), C.byref(st)), "oracle_run")
+        else:
+            s = np.asarray(sites)
+            if s.dtype.names:
+                s = np.stack([s[k] for k in ("x", "y", "z", "u", "v", "w", "E", "wgt")], axis=1)
+            s = np.ascontiguousarray(s, np.float64).reshape(-1, 8)
+            assert s.shape[0] >= n
+            self._ck(lib.oracle_run_sites(self.h, first, n, seed, _p(s), threads, _p(tally), _p(tr), C.byref(st)),
+                     "oracle_run_sites")
         dt = time.perf_counter() - t0
         return tally, tr, st.as_dict(), dt
+
+    def set_segment_limit(self, n: int) -> None:
+        """Segments a history may walk before it ends as stuck (0: default)."""
+        self._ck(lib.oracle_set_segment_limit(self.h, n), "oracle_set_segment_limit")
+
+    def segment_limit(self) -> int:
+        return lib.oracle_segment_limit(self.h)
+
+    def enable_rays(self, n_rays: int, max_segments: int = 4096) -> None:
+        """Record every segment of the first n_rays histories of each run (0: off)."""
+        self._ck(lib.oracle_rays_enable(self.h, n_rays, max_segments), "oracle_rays_enable")
+
+    def rays(self) -> np.ndarray:
+        """Segments recorded by the last run (RAY_DTYPE), ray by ray."""
+        m = C.c_int64()
+        self._ck(lib.oracle_rays(self.h, None, 0, C.byref(m)), "oracle_rays")
+        out = np.zeros(m.value, RAY_DTYPE)
+        self._ck(lib.oracle_rays(self.h, _p(out), out.size, C.byref(m)), "oracle_rays")
+        return out
 
     def eigen(self, n: int, generations: int, inactive: int = 0, seed: int = 1, keff0: float = 0.0,
               watt=(0.0, 0.0), capacity: int = 0, threads: int = 1, initial_source=None, tally: bool = False):
