@@ -16,6 +16,10 @@ batches ("steps") of 1,000,000 histories with a 1,000,000-particle bank.
          memory; "one_call_per_step" times one mc_run per step instead
   roofline  HBM roofline of the dominant kernel (the segment walk)
   cpu_baseline  the CPU restatement (oracle) on the host cores, bounded sample
+  core, serve, eigen  the other forms at bounded sizes, each with its own
+         clock record: the core at 1e7 histories in 64 batches (fixed
+         parameters), a 5 s Poisson serving trace, two active k-eigenvalue
+         generations of 1e6 (--no-extra leaves them out)
 
 More workloads print their own JSON line (not the default run):
   --workload cube   the plain FP64 configuration the reference runs on CPU:
@@ -41,8 +45,12 @@ More workloads print their own JSON line (not the default run):
 
 --impl reference times the reference path's CPU implementation (the oracle
 restatement; MaCaw itself needs MOOSE/OpenMC/libMesh/MPI, absent here) on
-the same workload.  Under torchrun every rank tracks its own history range
-(weak scaling, no collective on the data path).
+the same workload; its inputs come from the oracle library's own build of
+the generators, so that arm loads nothing of the CUDA tracker.
+--profile-run runs one workload once, untimed, for ncu (run_profile).
+Under torchrun every rank tracks its own history range (weak scaling, no
+collective on the data path) and the ranks' SUM tallies are summed once
+after the timed region (macaw_gb300/shard.py).
 """
 from __future__ import annotations
 
@@ -197,9 +205,12 @@ def run_reference(args):
     rank = env_int("RANK", 0)
     if rank != 0:
         return 0
+    # the inputs come from the oracle library's own build of the generator
+    # sources: this arm loads no part of the CUDA tracker
     from macaw_gb300 import problems
+    from oracle.oracle import Oracle, cpu_threads, generator_library
+    problems.use_generator_library(generator_library())
     p = problems.lattice_problem()
-    from oracle.oracle import Oracle, cpu_threads
     threads = cpu_threads()
     o = Oracle(p)
     n = REF_SAMPLE
@@ -236,8 +247,11 @@ def core_batch_sizes(total=100_000_000, n=64, lo=1e5, hi=5e6, seed=64):
     return s
 
 
-def run_core(args):
-    """Batched large-mesh form (one JSON line)."""
+def core_result(total, tune=True, batches=64):
+    """Batched large-mesh form: mixed and FP64 on the same histories, each
+    leg through one pipelined call of log-uniform batches, with its own
+    clock record.  tune: the autotuner picks each leg's parameters (else the
+    parameters it picked on this workload before)."""
     import numpy as np
     import torch
     from macaw_gb300 import Tracker, problems
@@ -245,55 +259,78 @@ def run_core(args):
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
     p = problems.core_problem()
-    sizes = core_batch_sizes(args.core_histories)
+    sizes = core_batch_sizes(total, n=batches)
     stream = torch.cuda.Stream()
     # particles in flight: the mixed walk gains from a larger bank on this
     # mesh (more particles per element bucket of the ordered queue; 10.1M ->
     # 11.2M histories/s from 2M to 8M), the FP64 walk does not
     banks = {"mixed": 8_000_000, "fp64": 2_000_000}
+    fixed = {"mixed": {"block_size": 256, "max_seg": 128, "sort_queue": 13, "refill": False, "graph": True},
+             "fp64": {"block_size": 256, "max_seg": 64, "sort_queue": 13, "refill": False, "graph": True}}
     out = {"metric": "histories/s, batched large-mesh form", "unit": "histories/s", "n_gpus": 1,
            "higher_is_better": True, "dtype": "f32+f64",
            "data": "synthetic (seeded generators)",
            "config": {"workload": f"core R=180 cm H=400 cm, {p.n_tet} tets, 200 materials x 5-40 nuclides x "
                                   f"30,000 pts; {int(sizes.sum())} histories in {sizes.size} batches "
                                   f"({int(sizes.min())}..{int(sizes.max())})", "tets": p.n_tet,
-                      "bank_size": banks, "l2": "inputs larger than L2 (mesh tables about 10 GB)"}}
+                      "histories": int(sizes.sum()), "bank_size": banks,
+                      "l2": "inputs larger than L2 (mesh tables about 10 GB)"}}
     res = {}
+    t = Tracker(0)
+    t.load(p)
+    t.set_stream(stream.cuda_stream)
     for name, prec in (("mixed", MC_PREC_MIXED), ("fp64", MC_PREC_FP64)):
-        t = Tracker(0)
-        t.load(p)
-        t.set_stream(stream.cuda_stream)
-        if name == "mixed":
-            out["setup_s"] = time.perf_counter() - t0
-        params, rate = t.autotune(trial=1_000_000, first=10**10, bank_size=banks[name], precision=prec,
-                                  block_size=256, max_seg=64)
-        params["graph"] = True if name == "mixed" else params["graph"]
+        if tune:
+            params, _ = t.autotune(trial=1_000_000, first=10**10, bank_size=banks[name], precision=prec,
+                                   block_size=256, max_seg=64)
+            params["graph"] = True if name == "mixed" else params["graph"]
+        else:
+            params = dict(fixed[name], bank_size=banks[name])
+        t.reset_tally()
         t.run(int(sizes[:3].sum()), first=2 * 10**10, seed=1, precision=prec, accumulate=True,
               batch_sizes=sizes[:3], **params)  # warm-up
+        if name == "mixed":
+            out["setup_s"] = time.perf_counter() - t0
         t.reset_tally()
         torch.cuda.synchronize()
+        clk = ClockSampler(0)
+        clk.start()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0 = time.time()
         e0.record(stream)
         st = t.run(int(sizes.sum()), first=0, seed=1, precision=prec, accumulate=True, batch_sizes=sizes,
                    **params)
         e1.record(stream)
         torch.cuda.synchronize()
+        clocks = clk.stop((c0, time.time()))
         ms = e0.elapsed_time(e1)
         res[name] = {"value": int(sizes.sum()) / (ms / 1e3), "ms": ms, "tuned": params,
                      "segments_per_s": st.n_seg / (ms / 1e3), "segments_per_history": st.n_seg / sizes.sum(),
                      "xs_per_history": st.n_xs / sizes.sum(), "stuck": int(st.n_stuck), "lost": int(st.n_lost),
                      "fallback_fraction": st.n_fallback / max(st.n_seg, 1), "gpu_launches": int(st.n_launch),
-                     "batches_done": t.batches_done()}
+                     "batches_done": t.batches_done(), "clocks": clocks}
         res[name]["sum"] = t.tally(MC_TALLY_SUM)
-        t.close()
+    t.close()
     a, b = res["mixed"].pop("sum"), res["fp64"].pop("sum")
     nz = b > 0
     rel = np.abs(a[nz] - b[nz]) / b[nz]
+    blk = p.tet_block
+    fb = np.bincount(blk, weights=b)
+    mb = np.bincount(blk, weights=a)
+    okb = fb > 0
+    relb = np.abs(mb[okb] - fb[okb]) / fb[okb]
     out.update({"value": res["mixed"]["value"], "mixed": res["mixed"], "fp64": res["fp64"],
                 "speedup_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
                 "flux_rel_diff_mean": float(rel.mean()), "flux_rel_diff_max": float(rel.max()),
-                "flux_rel_diff_note": "SUM tallies, mixed vs FP64 on the same histories, elements with a score"})
-    print(json.dumps(out))
+                "flux_rel_diff_block_max": float(relb.max()),
+                "flux_rel_diff_note": "SUM tallies, mixed vs FP64 on the same histories: per element with a score "
+                                      "(mean, max) and per block (material region, max)"})
+    return out
+
+
+def run_core(args):
+    """Batched large-mesh form (one JSON line)."""
+    print(json.dumps(core_result(args.core_histories, tune=not args.no_tune)))
     return 0
 
 
@@ -337,7 +374,7 @@ def run_cube(args):
     return 0
 
 
-def run_eigen(args):
+def eigen_result(n, K, W, no_mixed=False, cpu=True):
     """k-eigenvalue form (one JSON line): generations of 1e6 particles on the
     fissionable lattice; value = active-generation histories / device time
     of those generations (tracking, estimator sums, bank sort and
@@ -349,14 +386,13 @@ def run_eigen(args):
     from oracle.oracle import Oracle, cpu_threads
     torch.cuda.set_device(0)
     p = problems.eigen_lattice_problem()
-    n, K, W = 1_000_000, max(args.steps, 1), args.warmup
     res = {}
     with Tracker(0) as t:
         t.load(p)
         # walk budget and block from a sweep on this workload (8-32 segments,
         # 128/256 threads): flights here are about 28 segments long
         for name, prec, ms_ in (("fp64", MC_PREC_FP64, 32), ("mixed", MC_PREC_MIXED, 32)):
-            if name == "mixed" and args.no_mixed:
+            if name == "mixed" and no_mixed:
                 continue
             clk = ClockSampler(0)
             clk.start()
@@ -387,26 +423,32 @@ def run_eigen(args):
     sites_ph = f["sites_per_generation"] / n
     b_h = f["segments_per_history"] * B_SEG_FP64 + (f["collisions_per_history"] + 1) * B_XS_EVENT + \
         f["collisions_per_history"] * B_COLL_PICK + sites_ph * (80 + 160 + 64)
-    threads = cpu_threads()
-    o = Oracle(p)
-    n_cpu = 20_000
-    og, _, _, _, odt = o.eigen(n_cpu, 2, 1, seed=1, threads=threads)
     out = {"metric": "histories/s, k-eigenvalue generations", "unit": "histories/s", "n_gpus": 1,
            "value": f["value"], "higher_is_better": True, "dtype": "f64", "steps": K, "warmup": W,
            "data": "synthetic (seeded generators)",
            "config": {"workload": f"eigen lattice 17x17 pins, 50 cm, {p.n_tet} tets, every fuel nuclide "
-                                  "fissionable, reflective sides, vacuum top/bottom; 1e6 particles per generation, "
+                                  "fissionable, reflective sides, vacuum top/bottom; {n} particles per generation, "
                                   f"{W} inactive + {K} active generations", "tets": p.n_tet,
                       "l2": "inputs larger than L2 (mesh planes 261 MB, bank 80 MB)"},
            "fp64": f, "mixed": res.get("mixed"),
            "speedup_mixed_vs_fp64": res["mixed"]["value"] / f["value"] if "mixed" in res else None,
            "roofline_history": {"bytes_per_history": b_h, "achieved": f["value"] * b_h / 1e9, "unit": "GB/s",
                                 "peak": peak, "peak_source": psrc, "frac": f["value"] * b_h / 1e9 / peak,
-                                "formula": "S*164 + (C+1)*64*22 + C*16*15 + sites*(80+160+64), FP64"},
-           "cpu_baseline": {"value": n_cpu * 2 / odt, "unit": "histories/s", "cores": threads, "kind": "port",
-                            "sample": f"{n_cpu} particles x 2 generations of the same problem (C oracle)",
-                            "keff_generation": [float(x) for x in og["k_generation"]]}}
-    print(json.dumps(out))
+                                "formula": "S*164 + (C+1)*64*22 + C*16*15 + sites*(80+160+64), FP64"}}
+    if cpu:
+        threads = cpu_threads()
+        o = Oracle(p)
+        n_cpu = 20_000
+        og, _, _, _, odt = o.eigen(n_cpu, 2, 1, seed=1, threads=threads)
+        out["cpu_baseline"] = {"value": n_cpu * 2 / odt, "unit": "histories/s", "cores": threads, "kind": "port",
+                               "sample": f"{n_cpu} particles x 2 generations of the same problem (C oracle)",
+                               "keff_generation": [float(x) for x in og["k_generation"]]}
+    return out
+
+
+def run_eigen(args):
+    """k-eigenvalue form (one JSON line)."""
+    print(json.dumps(eigen_result(1_000_000, max(args.steps, 1), args.warmup, args.no_mixed)))
     return 0
 
 
@@ -419,36 +461,89 @@ def serve_problems():
     return ps
 
 
-def run_serve(args):
-    """Serving form (one JSON line)."""
+def serve_result(seconds):
+    """Serving form: a seeded Poisson trace (50 requests/s for `seconds` s)
+    through the continuous-batching server (mixed tracker), then the same
+    trace one request at a time in FP64; each with its own clock record."""
     import torch
     from macaw_gb300 import Tracker
     from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED
     from macaw_gb300.serve import Server, poisson_jobs, run_one_at_a_time, run_stream
     torch.cuda.set_device(0)
     ps = serve_problems()
-    jobs = poisson_jobs(ps, rate=50.0, duration=args.serve_seconds, seed=7, hist_range=(1e4, 1e6))
+    jobs = poisson_jobs(ps, rate=50.0, duration=seconds, seed=7, hist_range=(1e4, 1e6))
     srv = Server(ps, precision=MC_PREC_MIXED, hbm_budget=96 << 30, bank=1 << 20, max_slots=8)
     warm = poisson_jobs(ps, rate=50.0, duration=1.0, seed=8, hist_range=(1e4, 1e5))
     run_stream(srv, warm)
+    clk = ClockSampler(0)
+    clk.start()
+    c0 = time.time()
     rep = run_stream(srv, jobs)
+    rep["clocks"] = clk.stop((c0, time.time()))
     slots = list(srv.slots)
     srv.close()
     trackers = [Tracker(0).load(p) for p in ps]
     run_one_at_a_time(trackers, warm[:8], precision=MC_PREC_FP64)
+    clk = ClockSampler(0)
+    clk.start()
+    c0 = time.time()
     base = run_one_at_a_time(trackers, jobs, precision=MC_PREC_FP64)
+    base["clocks"] = clk.stop((c0, time.time()))
     for t in trackers:
         t.close()
     out = {"metric": "serving: histories/s and p50/p99 request latency", "unit": "histories/s",
            "value": rep["histories_per_s"], "n_gpus": 1, "higher_is_better": True, "dtype": "f32+f64",
            "data": "synthetic (seeded generators and arrival trace)",
-           "config": {"workload": f"Poisson 50 requests/s for {args.serve_seconds} s over 8 meshes "
+           "config": {"workload": f"Poisson 50 requests/s for {seconds} s over 8 meshes "
                                   f"({', '.join(str(p.n_tet) for p in ps)} tets), point sources, Watt energies, "
                                   "log-uniform 1e4..1e6 histories", "slots_per_mesh": slots,
                       "requests": rep["requests"], "histories": rep["histories"]},
            "serving": rep, "one_at_a_time_fp64": base,
            "p50_speedup": base["p50_ms"] / rep["p50_ms"], "p99_speedup": base["p99_ms"] / rep["p99_ms"]}
-    print(json.dumps(out))
+    return out
+
+
+def run_serve(args):
+    """Serving form (one JSON line)."""
+    print(json.dumps(serve_result(args.serve_seconds)))
+    return 0
+
+
+def run_profile(args):
+    """Runs one workload once for a profiler (ncu), no timing: one untimed
+    batch (so every kernel's first launch is warm), then `--batches` batches
+    of `--hist` histories through one pipelined call with fixed parameters
+    (the autotuner's choices on the workload unless overridden); prints the
+    run's statistics as JSON.  --workload eigen: one inactive generation,
+    then `--batches` active ones of `--hist` particles in one call.
+
+      python bench.py --profile-run --workload lattice --precision fp64 --hist 200000 --batches 1
+    """
+    from macaw_gb300 import Tracker, problems
+    from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED
+    prec = MC_PREC_MIXED if args.precision == "mixed" else MC_PREC_FP64
+    block = args.block or (64 if prec == MC_PREC_MIXED else 128)
+    max_seg = args.max_seg or (128 if prec == MC_PREC_MIXED else 64)
+    sort = args.sort or (13 if args.workload == "core" else 9)
+    n = args.hist
+    if args.workload == "eigen":
+        p = problems.eigen_lattice_problem(nx=args.pins, ny=args.pins)
+        with Tracker(0) as t:
+            t.load(p)
+            g = t.eigen(n, 1 + args.batches, 1, seed=1, precision=prec, bank_size=n, block_size=block,
+                        max_seg=max_seg, sort_queue=sort, graph=True)
+            print(json.dumps([{k: g[k][i].item() for k in g.dtype.names} for i in range(g.size)]))
+        return 0
+    if args.workload not in ("lattice", "core"):
+        raise SystemExit("--profile-run takes --workload lattice, core or eigen")
+    p = problems.lattice_problem(nx=args.pins, ny=args.pins) if args.workload == "lattice" \
+        else problems.core_problem()
+    with Tracker(0) as t:
+        t.load(p)
+        kw = dict(bank_size=n, block_size=block, max_seg=max_seg, sort_queue=sort, precision=prec)
+        warm = t.run(n, first=0, seed=1, accumulate=True, **kw).as_dict()
+        st = t.run(n * args.batches, first=n, seed=1, accumulate=True, batch_sizes=[n] * args.batches, **kw)
+        print(json.dumps(dict(st.as_dict(), warm=warm)))
     return 0
 
 
@@ -465,8 +560,20 @@ def main():
     ap.add_argument("--workload", default="lattice", choices=["lattice", "cube", "core", "serve", "eigen"])
     ap.add_argument("--core-histories", type=int, default=100_000_000)
     ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default run: leave out the core, serve and eigen sub-objects")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="run one workload once with fixed parameters for a profiler (ncu); see run_profile")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64", help="--profile-run only")
+    ap.add_argument("--batches", type=int, default=2, help="--profile-run only")
+    ap.add_argument("--pins", type=int, default=17, help="--profile-run only: pin cells per lattice side")
+    ap.add_argument("--block", type=int, default=0, help="--profile-run only")
+    ap.add_argument("--max-seg", type=int, default=0, help="--profile-run only: 0 = 128 mixed, 64 fp64")
+    ap.add_argument("--sort", type=int, default=0, help="--profile-run only: 0 = 9 (lattice), 13 (core)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile_run:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "core":
@@ -546,6 +653,14 @@ def main():
     clk = clocks.stop((w0, time.time()))
     value = world * n * K / (ms / 1e3)
     sum64 = t.tally(MC_TALLY_SUM)
+    reduce_ms = None
+    if dist is not None:
+        # the one exchange step of a sharded run: an FP64 sum of the element
+        # tallies over the ranks (after the timed region)
+        from macaw_gb300.shard import reduce_tally
+        r0 = time.perf_counter()
+        sum64 = reduce_tally(sum64)
+        reduce_ms = (time.perf_counter() - r0) * 1e3
     # one more batch with the walk launches timed (CUDA events around each
     # walk launch, which turns graph replay off), for the walk's roofline
     _, pst64 = timed(t, MC_PREC_FP64, params64, W + K, 1, True)
@@ -640,7 +755,9 @@ def main():
     e2e = {"value": world * n * K / e2e_s, "unit": "histories/s",
            "h2d_bytes_per_step": n * SITE_DTYPE.itemsize, "d2h_bytes_per_step": p.n_tet * 8,
            "note": "one pipelined mc_run for the K steps: each step's 1e6 host sites copied in (pinned), each "
-                   "step's SUM tally copied out to pinned host memory as its batch folds",
+                   "step's SUM tally copied out to pinned host memory as its batch folds; the host sites are "
+                   "sampled on the device before the timed region, so source sampling is outside this clock "
+                   "(it is inside the device-timed value)",
            "one_call_per_step": world * n * K / e2e_call_s}
 
     if rank == 0:
@@ -684,14 +801,30 @@ def main():
                                                      st.n_xs / (n * K), B_SEG_FP64),
                 "stuck": int(st.n_stuck), "lost": int(st.n_lost),
                 "roofline": roof, "e2e": e2e, "gpu_launches": int(st.n_launch), "clocks": clk}
+        if reduce_ms is not None:
+            line["tally_reduce_ms"] = reduce_ms
         if mixed is not None:
             line["mixed"] = mixed
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(p, CPU_SAMPLE)
+    t.close()
+    if rank == 0:
+        if world == 1 and not args.no_extra:
+            # the other forms, bounded so the default run stays within minutes
+            # (each sub-object carries its own clock record; the workload
+            # names state its size)
+            extra = {}
+            for key, fn in (("core", lambda: core_result(10_000_000, tune=False)),
+                            ("serve", lambda: serve_result(5.0)),
+                            ("eigen", lambda: eigen_result(1_000_000, 2, 1, cpu=False))):
+                try:
+                    extra[key] = fn()
+                except Exception as e:  # reported, never silently dropped
+                    extra[key] = {"error": f"{type(e).__name__}: {e}"}
+            line.update(extra)
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
-    t.close()
     return 0
 
 

@@ -371,22 +371,32 @@ int mc_batches_done(mc_ctx* ctx, int64_t* out);
  * whole GPU, a serving process that budgets HBM up front, code running where
  * an allocation would stall or fail) use mc_run_noalloc instead: it tracks
  * the same histories in the event form, but its scratch is one fixed array
- * of MC_NOALLOC_MAX_BANK particle slots (about 3.2 MB) compiled into the
- * library, which every GPU that loads the library holds until the process
- * exits.  It calls no cudaMalloc, cudaFree or other allocating routine.
+ * of MC_NOALLOC_MAX_BANK particle slots (212 bytes each plus a control
+ * block: about 3.47 MB) compiled into the library.  It calls no cudaMalloc,
+ * cudaFree or other allocating routine.
  *
+ * - The array and the event-form kernels are put on a device by
+ *   mc_ctx_create (the CUDA driver loads them lazily, so this is done while
+ *   the caller can still let the library take memory): every device that
+ *   has had a context holds the array until the process exits.  The first
+ *   mc_run_noalloc call leaves the device's free memory unchanged.
  * - bank_size must be at most MC_NOALLOC_MAX_BANK (0 means the maximum);
  *   larger values are rejected with MC_ERR_ARG.  Any number of histories
  *   is fine: the bank is refilled as histories end.
  * - tally: caller-owned DEVICE buffer of mc_tally_size doubles; scores are
  *   added to it, so clear it first.  traces: caller-owned DEVICE buffer of
  *   n_histories records when record_traces is set, else NULL.
+ * - Stream: the work runs on the context's stream (mc_ctx_set_stream), with
+ *   no ordering against the caller's other streams.  The caller's tally and
+ *   trace buffers must be ready when the call is made: clear them on the
+ *   context's stream, or synchronize before the call.  The call returns
+ *   after the work has finished.
  * - The mesh, tables, block map, boundary conditions and source must already
  *   be on the device: after the last set-up call, run mc_run once (for
- *   example with n_histories = 0).  Host source sites, accumulate and
- *   profile are rejected (each would need memory or events).
- * - The first call on each device looks up the array's device address
- *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   example with n_histories = 0).  Rejected with MC_ERR_ARG, as each would
+ *   need memory, events or a graph: host source sites, accumulate, profile,
+ *   pipelined batches (n_batches > 1, batch_sizes, batch_sum_out),
+ *   sort_queue > 0, graph, and a context with ray recording on.
  * - All calls on a device share the one array and it keeps the last call's
  *   contents (the library clears what must start at zero).  Calls whose
  *   work overlaps on the GPU race on it: run them one after another. */

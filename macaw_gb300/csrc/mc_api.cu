@@ -3,6 +3,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -427,6 +428,13 @@ int mc_ctx_create(int device, mc_ctx** out) {
     delete c;
     return MC_ERR_NOMEM;
   }
+  // the no-allocation run's scratch array and kernels go on the device now,
+  // while the caller can still let the library take memory
+  std::string err;
+  if (noalloc_prepare(device, err) != MC_OK) {
+    delete c;
+    return MC_ERR_CUDA;
+  }
   *out = c;
   return MC_OK;
 }
@@ -509,10 +517,15 @@ int mc_nuclide_add(mc_ctx* c, int64_t n_pts, const double* E, const double* sig_
   if (!(E[0] > 0.0)) return set_err(c, MC_ERR_ARG, "nuclide energies must be positive");
   for (int64_t i = 0; i + 1 < n_pts; ++i)
     if (!(E[i] < E[i + 1])) return set_err(c, MC_ERR_ARG, "nuclide energy grid must be strictly increasing");
-  for (int64_t i = 0; i < n_pts; ++i)
+  if (!std::isfinite(E[n_pts - 1])) return set_err(c, MC_ERR_ARG, "nuclide energies must be finite");
+  for (int64_t i = 0; i < n_pts; ++i) {
+    if (!std::isfinite(sig_t[i]) || !std::isfinite(sig_s[i]))
+      return set_err(c, MC_ERR_ARG, "cross sections must be finite (point " + std::to_string(i) + ")");
     if (!(sig_t[i] >= 0.0) || !(sig_s[i] >= 0.0) || sig_s[i] > sig_t[i])
-      return set_err(c, MC_ERR_ARG, "cross sections must satisfy 0 <= sigma_s <= sigma_t");
-  if (!(awr > 0.0)) return set_err(c, MC_ERR_ARG, "atomic weight ratio must be positive");
+      return set_err(c, MC_ERR_ARG, "cross sections must satisfy 0 <= sigma_s <= sigma_t (point " +
+                                        std::to_string(i) + ")");
+  }
+  if (!(awr > 0.0) || !std::isfinite(awr)) return set_err(c, MC_ERR_ARG, "atomic weight ratio must be positive");
   Nuclide n;
   n.E.assign(E, E + n_pts);
   n.st.assign(sig_t, sig_t + n_pts);
@@ -549,7 +562,8 @@ int mc_material_add(mc_ctx* c, int32_t material_id, int32_t n, const int32_t* nu
   for (int i = 0; i < n; ++i) {
     if (nuclides[i] < 0 || nuclides[i] >= (int32_t)c->nucs.size())
       return set_err(c, MC_ERR_ARG, "material nuclide index out of range");
-    if (!(densities[i] >= 0.0)) return set_err(c, MC_ERR_ARG, "atom densities must be non-negative");
+    if (!(densities[i] >= 0.0) || !std::isfinite(densities[i]))
+      return set_err(c, MC_ERR_ARG, "atom densities must be finite and non-negative");
   }
   for (const auto& m : c->mats)
     if (m.id == material_id) return set_err(c, MC_ERR_ARG, "duplicate material id");
@@ -607,7 +621,15 @@ int mc_source_set(mc_ctx* c, const mc_source_desc* s) {
 int mc_run(mc_ctx* c, const mc_run_desc* d) {
   if (!c || !d) return MC_ERR_ARG;
   std::lock_guard<std::mutex> g(c->mu);
-  return run_locked(c, d, nullptr, nullptr);
+  const int rc = run_locked(c, d, nullptr, nullptr);
+  // copies of later batches' host sites run on the copy stream and read the
+  // caller's buffer; a run that stopped early may leave some queued, so
+  // every return waits for them (a finished run has already waited)
+  if (d->sites) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->copy_stream);
+  }
+  return rc;
 }
 
 }  // extern "C"
@@ -1479,6 +1501,7 @@ bool ctx_view(mc_ctx* c, CtxView* v) {
   v->two_d = c->two_d;
   v->z2d = c->z2d;
   v->n_mat = (int)c->xs.mat_ids.size();
+  v->rays_on = c->ray_n > 0 && c->ray_cap > 0;
   const bool tables = c->have_mesh && !c->nucs.empty() && !c->mats.empty() && !c->xs_dirty && !c->tmat_dirty &&
                       !c->bc_dirty;
   v->ready = tables && c->have_src;

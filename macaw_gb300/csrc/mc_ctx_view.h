@@ -20,6 +20,7 @@ struct CtxView {
   int two_d = 0;        // 2-D mode and its z coordinate
   double z2d = 0.0;
   float tol = 0.0f;
+  bool rays_on = false; // ray recording is enabled (mc_rays_enable)
   bool ready = false;  // mesh, tables, block map, BCs and source resident on the device
                        // (M, X and S are filled whenever the tables are resident)
   DevMesh M;
@@ -46,5 +47,10 @@ int ctx_prepare(mc_ctx* c);  // puts mesh, tables, block map, BCs on the device
 int ctx_event_state(mc_ctx* c, int64_t cap, CtxEvent* out);
 int ctx_fail(mc_ctx* c, int code, const std::string& msg);
 void ctx_set_serving(mc_ctx* c, bool on);
+// Puts the no-allocation run's fixed scratch array and kernels on the
+// current device (once per device; mc_noalloc.cu).  Called at context
+// creation so that mc_run_noalloc itself never makes the driver commit
+// device memory.
+int noalloc_prepare(int device, std::string& err);
 
 }  // namespace mc

@@ -1127,6 +1127,32 @@ cudaError_t launch_event_finish(const DevMesh& M, const DevXS& X, const DevSourc
   return cudaGetLastError();
 }
 
+// Loads the kernels of the fixed-source event form (no ray recording) on the
+// current device: under lazy module loading a kernel's code is put on the
+// device at its first launch or attribute query, and the no-allocation run
+// must not be the call that does it.
+cudaError_t preload_event_kernels() {
+  cudaFuncAttributes fa;
+  const void* fns[] = {
+      (const void*)k_ev_init,
+      (const void*)k_ev_xs<false>,
+      (const void*)k_ev_advance<MC_PREC_MIXED>,
+      (const void*)k_ev_advance<MC_PREC_FP64>,
+      (const void*)k_ev_advance_mixed<false>,
+      (const void*)k_ev_advance_static<MC_PREC_FP64, false, false>,
+      (const void*)k_ev_collide<false>,
+      (const void*)k_ev_refill,
+      (const void*)k_ev_reset,
+      (const void*)k_ev_finish<MC_PREC_MIXED, false>,
+      (const void*)k_ev_finish<MC_PREC_FP64, false>,
+  };
+  for (const void* f : fns) {
+    const cudaError_t e = cudaFuncGetAttributes(&fa, f);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_sample(const DevXS& X, const DevSource& S, int64_t first, int64_t n,
                           uint64_t master, mc_site* out, cudaStream_t st) {
   k_sample<<<1216, 256, 0, st>>>(X, S, first, n, master, out);

@@ -114,6 +114,9 @@ struct RunArgs {
   int* sort_cnt;     // sort_buckets + 1 counters
 };
 
+// Loads the fixed-source event-form kernels onto the current device.
+cudaError_t preload_event_kernels();
+
 cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
                            int block, int grid, cudaStream_t st);
 

@@ -36,9 +36,14 @@ constexpr size_t kScratchBytes =
     align_up(sizeof(EventCtl)) + align_up(sizeof(unsigned long long) * kNumCounters) +
     align_up(sizeof(double));
 
-// The scratch: every GPU that loads the library holds these bytes until
-// the process exits, and every call on a device shares them.
+// The scratch (212 bytes per particle slot plus the control block and
+// counters: about 3.47 MB at 16,384 slots).  It lives in this translation
+// unit's module, which the CUDA driver loads onto a device the first time
+// host code asks for the array's address; mc_ctx_create does that
+// (noalloc_prepare), so every device that has had a context holds these
+// bytes until the process exits, and every call on a device shares them.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+static_assert(kScratchBytes < 4u * 1024u * 1024u, "no-allocation scratch above 4 MB");
 
 // Device address of g_scratch, looked up once per device (the host-side
 // name g_scratch is only a stand-in and must never be passed to a kernel).
@@ -64,6 +69,34 @@ int scratch_address(int device, void** out, std::string& err) {
   *out = g_scratch_addr[device];
   return MC_OK;
 }
+
+}  // namespace
+
+namespace mc {
+
+// Called by mc_ctx_create with `device` current: resolves the scratch
+// address (loading this module, and with it the array, onto the device) and
+// loads the event-form kernels, once per device.
+int noalloc_prepare(int device, std::string& err) {
+  void* p = nullptr;
+  int rc = scratch_address(device, &p, err);
+  if (rc) return rc;
+  static bool loaded[kMaxDevices] = {};
+  std::lock_guard<std::mutex> g(g_setup_mu);
+  if (!loaded[device]) {
+    const cudaError_t e = preload_event_kernels();
+    if (e != cudaSuccess) {
+      err = std::string("load event kernels: ") + cudaGetErrorString(e);
+      return MC_ERR_CUDA;
+    }
+    loaded[device] = true;
+  }
+  return MC_OK;
+}
+
+}  // namespace mc
+
+namespace {
 
 struct Carve {
   unsigned char* p;
@@ -102,6 +135,13 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   if (d->sites) return fail(MC_ERR_ARG, "mc_run_noalloc: host source sites would need a device copy");
   if (d->accumulate) return fail(MC_ERR_ARG, "mc_run_noalloc: accumulate uses the context's tallies");
   if (d->profile) return fail(MC_ERR_ARG, "mc_run_noalloc: profiling creates events");
+  // what mc_run would honour but this form cannot: reject rather than drop
+  if (d->n_batches > 1 || d->batch_sizes || d->batch_sum_out)
+    return fail(MC_ERR_ARG, "mc_run_noalloc: pipelined batches need per-batch tally slots; run one batch per call");
+  if (d->sort_queue > 0)
+    return fail(MC_ERR_ARG, "mc_run_noalloc: ordering the advance queue needs scratch beyond the fixed array");
+  if (d->graph) return fail(MC_ERR_ARG, "mc_run_noalloc: instantiating a CUDA graph allocates");
+  if (v.rays_on) return fail(MC_ERR_ARG, "mc_run_noalloc: ray recording is on (mc_rays_enable); turn it off");
   if (!tally) return fail(MC_ERR_ARG, "mc_run_noalloc: null tally buffer");
   if (d->record_traces && !traces) return fail(MC_ERR_ARG, "mc_run_noalloc: null trace buffer");
   const int block = d->block_size > 0 ? d->block_size : 256;

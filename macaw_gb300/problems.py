@@ -33,7 +33,37 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import MC_BC_REFLECT, MC_BC_VACUUM, MC_SRC_CYLINDERS, MC_SRC_POINT, MC_SRC_WATT, lib, ptr
+from ._abi import MC_BC_REFLECT, MC_BC_VACUUM, MC_SRC_CYLINDERS, MC_SRC_POINT, MC_SRC_WATT, SIGNATURES
+
+_GEN = None  # library whose mc_gen_* entry points build the problems
+
+
+def use_generator_library(handle) -> None:
+    """Builds problems with another compiled copy of the generator sources
+    (macaw_gb300/csrc/mc_gen.cpp) exposing the same mc_gen_* entry points,
+    instead of the tracker's library (None: back to the tracker's)."""
+    global _GEN
+    if handle is not None:
+        for name, (args, res) in SIGNATURES.items():
+            if name.startswith("mc_gen_"):
+                fn = getattr(handle, name)
+                fn.argtypes = args
+                fn.restype = res
+    _GEN = handle
+
+
+def _lib():
+    if _GEN is not None:
+        return _GEN
+    from ._lib import lib
+    return lib
+
+
+def ptr(a):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "arrays passed to the C ABI must be contiguous"
+    return C.c_void_p(a.ctypes.data)
 
 WATT_A = 0.988e6   # eV
 WATT_B = 2.249e-6  # 1/eV
@@ -114,38 +144,38 @@ def _check(rc: int, what: str) -> None:
 
 def cube_mesh(n: int = 20, L: float = 20.0):
     nv, nt = C.c_int64(), C.c_int64()
-    _check(lib.mc_gen_cube_sizes(n, C.byref(nv), C.byref(nt)), "mc_gen_cube_sizes")
+    _check(_lib().mc_gen_cube_sizes(n, C.byref(nv), C.byref(nt)), "mc_gen_cube_sizes")
     xyz = np.zeros((nv.value, 3), np.float64)
     tv = np.zeros((nt.value, 4), np.int32)
     blk = np.zeros(nt.value, np.int32)
     bid = np.zeros((nt.value, 4), np.int32)
-    _check(lib.mc_gen_cube(n, L, ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_cube")
+    _check(_lib().mc_gen_cube(n, L, ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_cube")
     return xyz, tv, blk, bid
 
 
 def box_mesh(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0)):
     nv, nt = C.c_int64(), C.c_int64()
-    _check(lib.mc_gen_box_sizes(nx, ny, nz, C.byref(nv), C.byref(nt)), "mc_gen_box_sizes")
+    _check(_lib().mc_gen_box_sizes(nx, ny, nz, C.byref(nv), C.byref(nt)), "mc_gen_box_sizes")
     xyz = np.zeros((nv.value, 3), np.float64)
     tv = np.zeros((nt.value, 4), np.int32)
     blk = np.zeros(nt.value, np.int32)
     bid = np.zeros((nt.value, 4), np.int32)
     lo_a = np.ascontiguousarray(lo, np.float64)
     hi_a = np.ascontiguousarray(hi, np.float64)
-    _check(lib.mc_gen_box(nx, ny, nz, ptr(lo_a), ptr(hi_a), ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_box")
+    _check(_lib().mc_gen_box(nx, ny, nz, ptr(lo_a), ptr(hi_a), ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_box")
     return xyz, tv, blk, bid
 
 
 def lattice_mesh(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fuel_rings: int = 2,
                  pitch: float = 1.26, height: float = 50.0, r_fuel: float = 0.41, r_clad: float = 0.475):
     nv, nt = C.c_int64(), C.c_int64()
-    _check(lib.mc_gen_lattice_sizes(nx, ny, nz, n_sec, n_fuel_rings, C.byref(nv), C.byref(nt)),
+    _check(_lib().mc_gen_lattice_sizes(nx, ny, nz, n_sec, n_fuel_rings, C.byref(nv), C.byref(nt)),
            "mc_gen_lattice_sizes")
     xyz = np.zeros((nv.value, 3), np.float64)
     tv = np.zeros((nt.value, 4), np.int32)
     blk = np.zeros(nt.value, np.int32)
     bid = np.zeros((nt.value, 4), np.int32)
-    _check(lib.mc_gen_lattice(nx, ny, nz, n_sec, n_fuel_rings, pitch, height, r_fuel, r_clad,
+    _check(_lib().mc_gen_lattice(nx, ny, nz, n_sec, n_fuel_rings, pitch, height, r_fuel, r_clad,
                               ptr(xyz), ptr(tv), ptr(blk), ptr(bid)), "mc_gen_lattice")
     return xyz, tv, blk, bid
 
@@ -153,14 +183,14 @@ def lattice_mesh(nx: int = 17, ny: int = 17, nz: int = 21, n_sec: int = 16, n_fu
 def core_mesh(pins: int = 17, nz: int = 6, n_sec: int = 8, n_fuel_rings: int = 1, pitch: float = 1.26,
               height: float = 400.0, r_fuel: float = 0.41, r_clad: float = 0.475, radius: float = 180.0):
     nv, nt, npn = C.c_int64(), C.c_int64(), C.c_int64()
-    _check(lib.mc_gen_core_sizes(pins, nz, n_sec, n_fuel_rings, pitch, radius, C.byref(nv), C.byref(nt),
+    _check(_lib().mc_gen_core_sizes(pins, nz, n_sec, n_fuel_rings, pitch, radius, C.byref(nv), C.byref(nt),
                                  C.byref(npn)), "mc_gen_core_sizes")
     xyz = np.zeros((nv.value, 3), np.float64)
     tv = np.zeros((nt.value, 4), np.int32)
     blk = np.zeros(nt.value, np.int32)
     bid = np.zeros((nt.value, 4), np.int32)
     pins_xy = np.zeros((npn.value, 2), np.float64)
-    _check(lib.mc_gen_core(pins, nz, n_sec, n_fuel_rings, pitch, height, r_fuel, r_clad, radius, ptr(xyz), ptr(tv),
+    _check(_lib().mc_gen_core(pins, nz, n_sec, n_fuel_rings, pitch, height, r_fuel, r_clad, radius, ptr(xyz), ptr(tv),
                            ptr(blk), ptr(bid), ptr(pins_xy)), "mc_gen_core")
     return xyz, tv, blk, bid, pins_xy
 
@@ -179,14 +209,14 @@ def make_nuclide(seed: int, index: int, n_pts: int, n_peaks: int = 20,
     st = np.zeros(n_pts)
     ss = np.zeros(n_pts)
     awr = C.c_double()
-    _check(lib.mc_gen_nuclide(seed, index, n_pts, E_min, E_max, n_peaks, ptr(E), ptr(st), ptr(ss),
+    _check(_lib().mc_gen_nuclide(seed, index, n_pts, E_min, E_max, n_peaks, ptr(E), ptr(st), ptr(ss),
                               C.byref(awr)), "mc_gen_nuclide")
     return Nuclide(E, st, ss, awr.value)
 
 
 def make_densities(seed: int, index: int, n: int, lo: float = 1e-4, hi: float = 5e-2) -> np.ndarray:
     out = np.zeros(n)
-    _check(lib.mc_gen_densities(seed, index, n, lo, hi, ptr(out)), "mc_gen_densities")
+    _check(_lib().mc_gen_densities(seed, index, n, lo, hi, ptr(out)), "mc_gen_densities")
     return out
 
 

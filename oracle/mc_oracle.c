@@ -437,6 +437,13 @@ int oracle_add_nuclide(oracle_problem* p, int64_t n_pts, const double* E, const 
   for (int64_t i = 0; i + 1 < n_pts; ++i)
     if (!(E[i] < E[i + 1])) return fail(p, "nuclide energy grid must be strictly increasing");
   if (!(E[0] > 0.0)) return fail(p, "nuclide energies must be positive");
+  if (!isfinite(E[n_pts - 1])) return fail(p, "nuclide energies must be finite");
+  for (int64_t i = 0; i < n_pts; ++i) {
+    if (!isfinite(sig_t[i]) || !isfinite(sig_s[i])) return fail(p, "cross sections must be finite");
+    if (!(sig_t[i] >= 0.0) || !(sig_s[i] >= 0.0) || sig_s[i] > sig_t[i])
+      return fail(p, "cross sections must satisfy 0 <= sigma_s <= sigma_t");
+  }
+  if (!(awr > 0.0) || !isfinite(awr)) return fail(p, "atomic weight ratio must be positive");
   if (p->n_nuc == p->cap_nuc) {
     p->cap_nuc = p->cap_nuc ? 2 * p->cap_nuc : 16;
     p->nucs = (nuclide_t*)realloc(p->nucs, sizeof(nuclide_t) * (size_t)p->cap_nuc);
@@ -846,6 +853,25 @@ static int material_of_block(const oracle_problem* p, int32_t blk)
   return -1;
 }
 
+/* tmat[t] = material_of_block(blk[t]) for every element, through a table
+ * per distinct block id in a dense range (the common case), else directly. */
+static void resolve_materials(oracle_problem* p)
+{
+  int32_t lo = 0, hi = -1;
+  for (int64_t t = 0; t < p->n_tet; ++t) {
+    if (t == 0 || p->blk[t] < lo) lo = p->blk[t];
+    if (t == 0 || p->blk[t] > hi) hi = p->blk[t];
+  }
+  if (p->n_tet > 0 && (int64_t)hi - lo < 1000000) {
+    int32_t* tab = (int32_t*)malloc(sizeof(int32_t) * (size_t)(hi - lo + 1));
+    for (int32_t b = lo; b <= hi; ++b) tab[b - lo] = material_of_block(p, b);
+    for (int64_t t = 0; t < p->n_tet; ++t) p->tmat[t] = tab[p->blk[t] - lo];
+    free(tab);
+    return;
+  }
+  for (int64_t t = 0; t < p->n_tet; ++t) p->tmat[t] = material_of_block(p, p->blk[t]);
+}
+
 typedef struct {
   int64_t n_seg, n_coll, n_leak, n_absorb, n_cutoff, n_stuck, n_lost, n_badxs;
   double leak_w;
@@ -1199,7 +1225,7 @@ static int run_histories(oracle_problem* p, int64_t first, int64_t n, uint64_t s
   if (!p->planes) return fail(p, "no mesh");
   if (prepare_data(p)) return 1;
   if (p->n_mat < 1) return fail(p, "no materials");
-  for (int64_t t = 0; t < p->n_tet; ++t) p->tmat[t] = material_of_block(p, p->blk[t]);
+  resolve_materials(p);
   if (p->rays) memset(p->ray_cnt, 0, sizeof(int32_t) * (size_t)p->ray_n);
   if (n_threads < 1) n_threads = 1;
   lstats tot;
@@ -1354,7 +1380,7 @@ int oracle_eigen_run(oracle_problem* p, int64_t n, int32_t n_gen, int32_t n_inac
   for (int i = 0; i < p->n_nuc; ++i)
     if (p->nucs[i].nusf) any = 1;
   if (!any) return fail(p, "no fissionable nuclide");
-  for (int64_t t = 0; t < p->n_tet; ++t) p->tmat[t] = material_of_block(p, p->blk[t]);
+  resolve_materials(p);
   if (keff0 <= 0.0) keff0 = 1.0;
   if (fa <= 0.0) fa = WATT_A_DEFAULT;
   if (fb <= 0.0) fb = WATT_B_DEFAULT;

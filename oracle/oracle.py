@@ -252,6 +252,12 @@ class Oracle:
         return i, f.value
 
 
+def generator_library() -> C.CDLL:
+    """This library's build of the problem generators (mc_gen_* entry
+    points), for macaw_gb300.problems.use_generator_library."""
+    return lib
+
+
 def cpu_threads() -> int:
     try:
         return len(os.sched_getaffinity(0))

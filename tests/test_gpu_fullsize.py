@@ -1,18 +1,20 @@
 """Full-size workloads: the 2,039,184-tet lattice at 1e7 histories and the
 41,283,792-tet core.
 
-At these sizes the oracle checks a sample: the first 2,000 histories of the
-lattice run must match it trace for trace, bit for bit.  The rest is
-checked through properties that hold at any size: every history ends in
-exactly one state with none stuck or lost, the pipelined batches fold to
-the batch count, and the mixed form stays within the 1e-4 mean relative
-element-flux difference of the FP64 form on the same 1e7 histories.
+At these sizes the oracle checks a sample: 2,000 histories of the lattice
+run, and 2,000 of the core (1,000 born from the source in the assemblies'
+fuel, 1,000 started in the reflector), must match it trace for trace, bit
+for bit.  The rest is checked through properties that hold at any size:
+every history ends in exactly one state with none stuck or lost, the
+pipelined batches fold to the batch count, and the mixed form stays within
+the 1e-4 mean relative element-flux difference of the FP64 form on the same
+histories (1e7 on the lattice, 2e7 on the core).
 """
 import numpy as np
 import pytest
 
 from macaw_gb300 import Tracker, problems
-from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM
+from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM, SITE_DTYPE
 
 from oracle import oracle as O
 
@@ -61,8 +63,62 @@ def test_lattice_sample_matches_the_oracle(lattice):
         assert np.array_equal(tr[f], otr[f]), f
 
 
-def test_core_histories_all_end():
-    p = problems.core_problem()
+@pytest.fixture(scope="module")
+def core():
+    return problems.core_problem()
+
+
+def _isotropic(rng, n):
+    d = rng.normal(size=(n, 3))
+    return d / np.linalg.norm(d, axis=1)[:, None]
+
+
+def test_core_sample_matches_the_oracle(core):
+    n = 2000
+    rng = np.random.default_rng(2024)
+    refl = np.where(core.tet_block >= 196)[0]
+    pick = rng.choice(refl, n // 2, replace=False)
+    with Tracker(0) as t:
+        t.load(core)
+        sites = np.concatenate([t.sample_sites(n // 2, first=0, seed=1), np.zeros(n // 2, SITE_DTYPE)])
+        cen = core.xyz[core.tet_vtx[pick]].mean(axis=1)
+        d = _isotropic(rng, n // 2)
+        for j, k in enumerate(("x", "y", "z")):
+            sites[k][n // 2:] = cen[:, j]
+        for j, k in enumerate(("u", "v", "w")):
+            sites[k][n // 2:] = d[:, j]
+        sites["E"][n // 2:] = 10.0 ** rng.uniform(0.0, 6.5, n // 2)
+        sites["wgt"][n // 2:] = 1.0
+        st = t.run(n, seed=1, precision=MC_PREC_FP64, traces=True, sites=sites, bank_size=n, max_seg=64,
+                   sort_queue=13)
+        tr = t.traces(n)
+    assert st.n_hist == n and st.n_lost == 0 and st.n_stuck == 0
+    _, otr, _, _ = O.Oracle(core).run(n, seed=1, threads=16, sites=sites)
+    for f in ("hash", "status", "n_seg", "n_coll", "elem", "face", "E", "x", "y", "z"):
+        assert np.array_equal(tr[f], otr[f]), f
+
+
+def test_core_mixed_flux_within_1e4_of_fp64(core):
+    sizes = [2_500_000] * 8
+    with Tracker(0) as t:
+        t.load(core)
+        kw = dict(seed=3, accumulate=True, batch_sizes=sizes, sort_queue=13, graph=True)
+        st = t.run(sum(sizes), precision=MC_PREC_FP64, bank_size=2_000_000, max_seg=64, **kw)
+        _accounting(st, sum(sizes))
+        fp64 = t.tally(MC_TALLY_SUM)
+        t.reset_tally()
+        sm = t.run(sum(sizes), precision=MC_PREC_MIXED, bank_size=4_000_000, max_seg=128, **kw)
+        _accounting(sm, sum(sizes))
+        mixed = t.tally(MC_TALLY_SUM)
+    nz = fp64 > 0
+    assert np.all(mixed[~nz] == 0)
+    rel = np.abs(mixed[nz] - fp64[nz]) / fp64[nz]
+    assert rel.mean() <= 1e-4, rel.mean()
+    assert sm.n_fallback < 1e-3 * sm.n_seg
+
+
+def test_core_histories_all_end(core):
+    p = core
     with Tracker(0) as t:
         t.load(p)
         sizes = [300_000, 100_000, 600_000]
