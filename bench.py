@@ -30,8 +30,9 @@ More workloads print their own JSON line (not the default run):
                     180 cm, 400 cm, 41,283,792 tets, 200 materials of 5-40
                     nuclides (30,000-point grids); 1e8 histories in 64
                     batches of log-uniform size (1e5-5e6, rescaled) through
-                    one pipelined, graph-replayed, autotuned call, mixed and
-                    FP64 on the same histories
+                    one pipelined, graph-replayed, autotuned call, and again
+                    through one persistent launch, mixed and FP64 on the
+                    same histories
   --workload eigen  the k-eigenvalue form: the lattice with fissionable fuel,
                     reflective sides (2,039,184 tets, k near 1); 1e6
                     particles per generation, W inactive then K active
@@ -256,6 +257,7 @@ def core_result(total, tune=True, batches=64):
     import torch
     from macaw_gb300 import Tracker, problems
     from macaw_gb300._lib import MC_PREC_FP64, MC_PREC_MIXED, MC_TALLY_SUM
+    from macaw_gb300.tracker import run_persistent
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
     p = problems.core_problem()
@@ -310,6 +312,17 @@ def core_result(total, tune=True, batches=64):
                      "fallback_fraction": st.n_fallback / max(st.n_seg, 1), "gpu_launches": int(st.n_launch),
                      "batches_done": t.batches_done(), "clocks": clocks}
         res[name]["sum"] = t.tally(MC_TALLY_SUM)
+        # the same batches as one persistent launch (one tally slot per batch)
+        firsts = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+        t.reset_tally()
+        clk = ClockSampler(0)
+        clk.start()
+        c0 = time.time()
+        pst, _ = run_persistent([(t, int(f), int(n), 1) for f, n in zip(firsts, sizes)], precision=prec)
+        res[name]["persistent"] = {"value": int(sizes.sum()) / (pst.ms_total / 1e3), "ms": pst.ms_total,
+                                   "segments_per_history": pst.n_seg / sizes.sum(), "stuck": int(pst.n_stuck),
+                                   "lost": int(pst.n_lost), "gpu_launches": int(pst.n_launch),
+                                   "batches_done": t.batches_done(), "clocks": clk.stop((c0, time.time()))}
     t.close()
     a, b = res["mixed"].pop("sum"), res["fp64"].pop("sum")
     nz = b > 0
@@ -324,7 +337,9 @@ def core_result(total, tune=True, batches=64):
                 "flux_rel_diff_mean": float(rel.mean()), "flux_rel_diff_max": float(rel.max()),
                 "flux_rel_diff_block_max": float(relb.max()),
                 "flux_rel_diff_note": "SUM tallies, mixed vs FP64 on the same histories: per element with a score "
-                                      "(mean, max) and per block (material region, max)"})
+                                      "(mean, max) and per block (material region, max)",
+                "forms_note": "each leg: the batches through one pipelined, graph-replayed mc_run (value) and "
+                              "through one persistent launch, mc_run_persistent (persistent)"})
     return out
 
 

@@ -363,6 +363,43 @@ int mc_stats_get(mc_ctx* ctx, mc_stats* out);
 /* Number of completed accumulated batches (OpenMC n_realizations). */
 int mc_batches_done(mc_ctx* ctx, int64_t* out);
 
+/* ---- persistent run: many batches, of one or more problems -------------
+ * Replaces: the batch loop of OpenMCStudy (generateRays / execute /
+ * postExecuteStudy once per batch, src/userobjects/OpenMCStudy.C:218-242,
+ * 366-402) for every batch of a run in one kernel launch; beyond the
+ * reference, batches of different problems (contexts on one device) share
+ * that launch.  Every lane of a persistent grid takes the next history of
+ * the run, tracks it whole with its batch's problem (same arithmetic as the
+ * history and event forms: FP64 histories are bit for bit those of
+ * mc_run), and the lane that ends a batch's last history makes the batch
+ * ready; ready batches are folded (tally / n_histories into the problem's
+ * SUM and SUM_SQ, one batch each, as mc_run with accumulate) by lanes with
+ * nothing else to do.  Each problem's batches take `slots` tally slots in
+ * turn: a history of the problem's k-th batch waits, folding meanwhile,
+ * until batch k - slots is folded; a wait that polls wait_limit times ends
+ * the run with MC_ERR_DEVICE (no lane waits without a limit).  The problems
+ * must be on the device already (mc_run once after the last set-up call);
+ * ray recording is not done here. */
+typedef struct {
+  mc_ctx* ctx;             /* the batch's problem */
+  int64_t first_history;   /* 0-based index of its first history (id = index + 1) */
+  int64_t n_histories;     /* 1 .. 2^31 - 1 */
+  uint64_t seed;           /* master seed */
+} mc_job;
+
+typedef struct {
+  int32_t precision;       /* MC_PREC_* */
+  int32_t block_size;      /* threads per block: a multiple of 32, at most 128 (0: 128) */
+  int32_t slots;           /* tally slots per problem (0: one per batch, no waits) */
+  int32_t record_traces;   /* 1: one mc_trace per history into traces, batches in the order given */
+  int64_t wait_limit;      /* polls (about a microsecond apart) before a wait gives up (0: 10,000,000) */
+  mc_trace* traces;        /* HOST buffer of the run's histories when record_traces */
+} mc_persist_desc;
+
+/* stats (optional) receives the run's counters; each problem's mc_stats_get
+ * returns them too, and mc_batches_done counts its batches. */
+int mc_run_persistent(const mc_persist_desc* desc, int32_t n_jobs, const mc_job* jobs, mc_stats* stats);
+
 /* ---- batch run without device allocation ------------------------------
  * No counterpart in the reference: MaCaw itself never allocates device
  * memory.  mc_run obtains its particle bank, event queues and counters with

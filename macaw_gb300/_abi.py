@@ -54,6 +54,15 @@ class EigenDesc(C.Structure):
                 ("fission_bank_capacity", C.c_int64), ("initial_source", C.c_void_p)]
 
 
+class Job(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("first_history", C.c_int64), ("n_histories", C.c_int64), ("seed", C.c_uint64)]
+
+
+class PersistDesc(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("block_size", C.c_int32), ("slots", C.c_int32),
+                ("record_traces", C.c_int32), ("wait_limit", C.c_int64), ("traces", C.c_void_p)]
+
+
 class Request(C.Structure):
     _fields_ = [("n_histories", C.c_int64), ("seed", C.c_uint64), ("source", SourceDesc)]
 
@@ -117,6 +126,7 @@ SIGNATURES = {
     "mc_serve_result": ([_P, _I64, _P, _I64], C.c_int),
     "mc_serve_status": ([_P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)], C.c_int),
     "mc_serve_close": ([_P], C.c_int),
+    "mc_run_persistent": ([C.POINTER(PersistDesc), _I32, _P, _P], C.c_int),
     "mc_run_noalloc": ([_P, C.POINTER(RunDesc), _P, _P], C.c_int),
     "mc_app_run": ([C.c_char_p, C.c_int, C.c_char_p, C.c_char_p, _I64], C.c_int),
     "mc_app_check": ([C.c_char_p, C.c_char_p, _I64], C.c_int),

@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-f
               "-Xptxas", "-O3"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["mc_kernels.cu", "mc_api.cu", "mc_noalloc.cu", "mc_serve.cu", "mc_eigen.cu"]
+CU_SOURCES = ["mc_kernels.cu", "mc_api.cu", "mc_noalloc.cu", "mc_serve.cu", "mc_eigen.cu", "mc_persist.cu"]
 CXX_SOURCES = ["mc_exodus.cpp", "mc_host.cpp", "mc_gen.cpp", "mc_app.cpp", "mc_tune.cpp"]
 
 

@@ -1491,6 +1491,16 @@ void ctx_set_error(mc_ctx* c, const std::string& msg) { c->err = msg; }
 
 void ctx_set_stats(mc_ctx* c, const mc_stats& s) { c->last = s; }
 
+bool ctx_sums(mc_ctx* c, double** sum, double** sumsq) {
+  *sum = c->d_sum.as<double>();
+  *sumsq = c->d_sumsq.as<double>();
+  return *sum && *sumsq;
+}
+
+void ctx_add_batches(mc_ctx* c, int64_t n) { c->batches += n; }
+
+bool ctx_serving(mc_ctx* c) { return c->serving; }
+
 bool ctx_view(mc_ctx* c, CtxView* v) {
   v->device = c->device;
   v->n_sm = c->n_sm;

@@ -47,6 +47,11 @@ int ctx_prepare(mc_ctx* c);  // puts mesh, tables, block map, BCs on the device
 int ctx_event_state(mc_ctx* c, int64_t cap, CtxEvent* out);
 int ctx_fail(mc_ctx* c, int code, const std::string& msg);
 void ctx_set_serving(mc_ctx* c, bool on);
+// The context's SUM and SUM_SQ tallies (false while not allocated), its
+// count of folded batches, and whether a serving session holds it.
+bool ctx_sums(mc_ctx* c, double** sum, double** sumsq);
+void ctx_add_batches(mc_ctx* c, int64_t n);
+bool ctx_serving(mc_ctx* c);
 // Puts the no-allocation run's fixed scratch array and kernels on the
 // current device (once per device; mc_noalloc.cu).  Called at context
 // creation so that mc_run_noalloc itself never makes the driver commit

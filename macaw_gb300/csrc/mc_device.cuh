@@ -926,9 +926,9 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
   for (int f = 0; f < 4; ++f) {
     if (f == p.fin) continue;
     const double4_32a pl = P[f];
-    const double den = pl.x * p.u + pl.y * p.v + pl.z * p.w;
+    const double den = fma(pl.x, p.u, fma(pl.y, p.v, pl.z * p.w));
     if (den > 0.0) {
-      const double num = pl.w - (pl.x * p.x + pl.y * p.y + pl.z * p.z);
+      const double num = fma(-pl.x, p.x, fma(-pl.y, p.y, fma(-pl.z, p.z, pl.w)));
       if (bf < 0 || num * bden < bnum * den) {
         bf = f;
         bnum = num;
@@ -962,9 +962,9 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
   if (cross) {
     p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
     const double sx = p.x, sy = p.y, sz = p.z;
-    p.x = p.x + L * p.u;
-    p.y = p.y + L * p.v;
-    p.z = p.z + L * p.w;
+    p.x = fma(L, p.u, p.x);
+    p.y = fma(L, p.v, p.y);
+    p.z = fma(L, p.w, p.z);
     if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
     const int nb = side_entry(M.tet[p.elem].nbr, bf);
     if (nb >= 0) {
@@ -976,11 +976,11 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     const int bid = -1 - nb;
     if (bid < M.n_bid && M.bc_type[bid] == 1) {
       const double4_32a pl = P[bf];
-      const double dn = p.u * pl.x + p.v * pl.y + p.w * pl.z;
+      const double dn = fma(p.u, pl.x, fma(p.v, pl.y, p.w * pl.z));
       const double t2 = 2.0 * dn;
-      p.u = p.u - t2 * pl.x;
-      p.v = p.v - t2 * pl.y;
-      p.w = p.w - t2 * pl.z;
+      p.u = fma(-t2, pl.x, p.u);
+      p.v = fma(-t2, pl.y, p.v);
+      p.w = fma(-t2, pl.z, p.w);
       p.fin = -1;
       return 0;
     }
@@ -989,12 +989,12 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     return 2;
   }
   p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
-  const double ex = p.x + L * p.u, ey = p.y + L * p.v, ez = p.z + L * p.w;
+  const double ex = fma(L, p.u, p.x), ey = fma(L, p.v, p.y), ez = fma(L, p.w, p.z);
   const double back = L - dist;
   const double sx = p.x, sy = p.y, sz = p.z;
-  p.x = ex - back * p.u;
-  p.y = ey - back * p.v;
-  p.z = ez - back * p.w;
+  p.x = fma(-back, p.u, ex);
+  p.y = fma(-back, p.v, ey);
+  p.z = fma(-back, p.w, ez);
   ++p.n_coll;
   if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
   p.zero_run = 0;
@@ -1096,8 +1096,8 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   }
   const double4_32a* P = M.planes + 4 * (int64_t)p.elem;
   const double4_32a plb = P[bf];
-  const double bden = plb.x * p.u + plb.y * p.v + plb.z * p.w;
-  const double bnum = plb.w - (plb.x * p.x + plb.y * p.y + plb.z * p.z);
+  const double bden = fma(plb.x, p.u, fma(plb.y, p.v, plb.z * p.w));
+  const double bnum = fma(-plb.x, p.x, fma(-plb.y, p.y, fma(-plb.z, p.z, plb.w)));
   double L = bnum / bden;
   // L > 0 as a sign test on the bits (bden > 0 is certified and bnum is
   // finite, so L is not NaN; -0 clamps to +0 as before)
@@ -1133,9 +1133,9 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   if (cross) {
     p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
     const double sx = p.x, sy = p.y, sz = p.z;
-    p.x = p.x + L * p.u;
-    p.y = p.y + L * p.v;
-    p.z = p.z + L * p.w;
+    p.x = fma(L, p.u, p.x);
+    p.y = fma(L, p.v, p.y);
+    p.z = fma(L, p.w, p.z);
     if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
     const int nb = side_entry(nb4, bf);
     if (nb >= 0) {
@@ -1146,11 +1146,11 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     }
     const int bid = -1 - nb;
     if (bid < M.n_bid && M.bc_type[bid] == 1) {
-      const double dn = p.u * plb.x + p.v * plb.y + p.w * plb.z;
+      const double dn = fma(p.u, plb.x, fma(p.v, plb.y, p.w * plb.z));
       const double t2 = 2.0 * dn;
-      p.u = p.u - t2 * plb.x;
-      p.v = p.v - t2 * plb.y;
-      p.w = p.w - t2 * plb.z;
+      p.u = fma(-t2, plb.x, p.u);
+      p.v = fma(-t2, plb.y, p.v);
+      p.w = fma(-t2, plb.z, p.w);
       p.fin = -1;
       return 5;  // reflected: the caller refreshes its float direction
     }
@@ -1159,12 +1159,12 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     return 2;
   }
   p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
-  const double ex = p.x + L * p.u, ey = p.y + L * p.v, ez = p.z + L * p.w;
+  const double ex = fma(L, p.u, p.x), ey = fma(L, p.v, p.y), ez = fma(L, p.w, p.z);
   const double back = L - dist;
   const double sx = p.x, sy = p.y, sz = p.z;
-  p.x = ex - back * p.u;
-  p.y = ey - back * p.v;
-  p.z = ez - back * p.w;
+  p.x = fma(-back, p.u, ex);
+  p.y = fma(-back, p.v, ey);
+  p.z = fma(-back, p.w, ez);
   ++p.n_coll;
   if (kRays && T.rays) record_ray(T, p, sx, sy, sz, p.x, p.y, p.z);
   p.zero_run = 0;

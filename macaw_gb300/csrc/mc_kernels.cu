@@ -1127,6 +1127,275 @@ cudaError_t launch_event_finish(const DevMesh& M, const DevXS& X, const DevSourc
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Persistent form: one launch runs many batches, of one or more problems.
+// Every lane loops on its own (no barrier, no warp-wide operation):
+//   1. fold work first: a chunk of a batch whose histories have all ended is
+//      added to its problem's SUM/SUM_SQ and cleared in the batch's slot;
+//      the lane that folds a batch's last chunk passes the slot on to the
+//      batch n_slots later;
+//   2. else it takes the next history index of the run (one atomic), finds
+//      its batch, waits (folding meanwhile) until the batch's tally slot is
+//      the batch's turn, and tracks the whole history with the batch's
+//      problem: the same birth, walk and collision functions as the history
+//      and event forms, so FP64 histories are bit for bit the same;
+//   3. the lane that ends a batch's last history puts the batch on the
+//      ready list.
+// A wait for a slot polls at most wait_limit times, about a microsecond
+// apart, then sets the run's error flag and every lane leaves.  A lane with
+// nothing left to do helps fold for a short while and leaves; folds not done
+// when the kernel ends are finished by k_persist_fold_rest.
+
+__device__ __forceinline__ unsigned long long vld(const unsigned long long* p) {
+  return *(const volatile unsigned long long*)p;
+}
+__device__ __forceinline__ int vld(const int* p) { return *(const volatile int*)p; }
+
+__device__ __forceinline__ void persist_fold_chunk(const PersistArgs& a, const PersistProblem& P, const PersistJob& J,
+                                                   int ch) {
+  const int64_t e0 = (int64_t)ch * a.chunk;
+  const int64_t e1 = e0 + a.chunk < P.n_tally ? e0 + a.chunk : P.n_tally;
+  double* slot = P.slots + (int64_t)(J.order % P.n_slots) * P.n_tally;
+  for (int64_t e = e0; e < e1; ++e) {
+    const double v = __ldcg(slot + e);  // scored by atomics at L2: read past L1
+    if (v != 0.0) {
+      const double b = v * J.inv_n;
+      atomicAdd(P.sum + e, b);
+      atomicAdd(P.sumsq + e, b * b);
+      __stcg(slot + e, 0.0);
+    }
+  }
+}
+
+// Claims and folds one chunk of a ready batch; false when none is left.
+__device__ bool persist_fold(const PersistArgs& a, const PersistProblem* sp, unsigned long long* scan_lo) {
+  PersistCtl* c = a.ctl;
+  const unsigned long long ready = vld(&c->ready);
+  if (vld(&c->claimed) >= ready) return false;
+  for (unsigned long long k = vld(scan_lo); k < ready; ++k) {
+    const int j = vld(a.ready_list + k);
+    if (j < 0) continue;  // reserved, not yet written
+    const PersistJob J = a.jobs[j];
+    const PersistProblem& P = sp[J.prob];
+    if (vld(a.chunk_next + j) >= P.n_chunks) {
+      atomicCAS(scan_lo, k, k + 1);  // every chunk of this entry is taken: later scans start past it
+      continue;
+    }
+    const int ch = atomicAdd(a.chunk_next + j, 1);
+    if (ch >= P.n_chunks) continue;
+    if (ch == P.n_chunks - 1) atomicAdd(&c->claimed, 1ULL);
+    persist_fold_chunk(a, P, J, ch);
+    __threadfence();
+    if (atomicAdd(a.chunk_done + j, 1) == P.n_chunks - 1) {
+      // the batch's slot is folded and clear: the batch n_slots later may score into it
+      __threadfence();
+      atomicExch(a.slot_turn + a.slot_base[J.prob] + J.order % P.n_slots, J.order + P.n_slots);
+      atomicAdd(&c->folded, 1ULL);
+    }
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ int persist_job_of(const PersistArgs& a, unsigned long long h) {
+  int lo = 0, hi = a.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((int64_t)h < a.jobs[mid].end) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void persist_set_error(const PersistArgs& a, int job, long long polls) {
+  if (atomicCAS(&a.ctl->error, 0, 1) == 0) {
+    a.ctl->err_job = job;
+    a.ctl->err_polls = polls;
+  }
+}
+
+template <int kPrec>
+__global__ void __launch_bounds__(128) k_persist(PersistArgs a) {
+  MC_COUNTERS(L);
+  __shared__ PersistProblem sp[kMaxPersistProblems];
+  {
+    const int words = (int)(sizeof(PersistProblem) / sizeof(int)) * a.n_probs;
+    const int* src = (const int*)a.probs;
+    int* dst = (int*)sp;
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  PersistCtl* c = a.ctl;
+  unsigned long long* scan_lo = &c->scan_lo;
+  unsigned long long nxs = 0, nfb = 0;
+  for (;;) {
+    if (vld(&c->error)) break;
+    if (persist_fold(a, sp, scan_lo)) continue;
+    const unsigned long long h = atomicAdd(&c->next, 1ULL);
+    if (h >= a.total) break;
+    const int j = persist_job_of(a, h);
+    const PersistJob J = a.jobs[j];
+    const PersistProblem& P = sp[J.prob];
+    // wait until the batch's tally slot is this batch's turn, folding meanwhile
+    const int* turn = a.slot_turn + a.slot_base[J.prob] + J.order % P.n_slots;
+    long long polls = 0;
+    bool gave_up = false;
+    while (vld(turn) < J.order) {
+      if (vld(&c->error)) {
+        gave_up = true;
+        break;
+      }
+      if (persist_fold(a, sp, scan_lo)) continue;
+      if (++polls > a.wait_limit) {
+        persist_set_error(a, j, polls);
+        gave_up = true;
+        break;
+      }
+      __nanosleep(1000);
+    }
+    if (gave_up) break;
+    __threadfence();  // the slot's clearing is visible before this history scores into it
+    double* tally = P.slots + (int64_t)(J.order % P.n_slots) * P.n_tally;
+    // birth: history index J.first + (h - J.start) of the problem, as the
+    // history and event forms number it
+    const int64_t idx = J.first + ((int64_t)h - J.start);
+    const Skip k = skip_ahead((uint64_t)(idx + 1) * kPrnStride);
+    mc_site o;
+    if (kPrec == MC_PREC_MIXED) sample_source32(P.X, P.S, k, J.seed, o);
+    else sample_source(P.X, P.S, k, J.seed, o);
+    if (P.two_d) {
+      o.z = P.z2d;
+      planar_dir(o.u, o.v, o.w);
+    }
+    Particle p;
+    start(P.M, o, idx, k, J.seed, p);
+    p.tag = 0;
+    if (kPrec == MC_PREC_FP64) {
+      float sigt32 = 0.0f;
+      float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
+      while (p.status == kAlive) {
+        const int r = segment_fp64g<true, false, true, false>(P.M, P.X, p, uf, vf, wf, tally, P.ts, sigt32, nxs);
+        if (r == 1) {
+          score_collision(P.X, P.ts, tally, p);
+          collide<false>(P.X, p, P.two_d, EigArgs{});
+        }
+        if (r == 1 || r == 5) {
+          uf = narrow(p.u);
+          vf = narrow(p.v);
+          wf = narrow(p.w);
+        }
+      }
+    } else {
+      Geo32 g;
+      geo_load(p, g);
+      float inv_sig = 0.0f;
+      while (p.status == kAlive) {
+        const int r = segment_mixed<true, false, false>(P.M, P.X, p, g, tally, P.ts, inv_sig, P.tol, nxs, nfb);
+        if (r == 1) {
+          geo_store(g, p);
+          score_collision(P.X, P.ts, tally, p);
+          collide<false>(P.X, p, P.two_d, EigArgs{});
+          geo_load(p, g);
+        }
+      }
+      geo_store(g, p);
+    }
+    // end of the history: closing hash word, counters, trace
+    p.hash = fnv(p.hash, (uint64_t)(16 + p.status));
+    L.add(kCntSeg, (unsigned long long)p.n_seg);
+    L.add(kCntColl, (unsigned long long)p.n_coll);
+    L.add(kCntHist, 1);
+    switch (p.status) {
+      case kLeaked: L.add(kCntLeak, 1); L.add_leak(p.wgt); break;
+      case kAbsorbed: L.add(kCntAbsorb, 1); break;
+      case kCutoff: L.add(kCntCutoff, 1); break;
+      case kStuck: L.add(kCntStuck, 1); break;
+      case kLost: L.add(kCntLost, 1); break;
+      default: L.add(kCntBadXS, 1); break;
+    }
+    if (a.traces) {
+      mc_trace t;
+      t.id = p.id;
+      t.hash = p.hash;
+      t.status = p.status;
+      t.n_seg = p.n_seg;
+      t.n_coll = p.n_coll;
+      t.elem = p.elem;
+      t.face = p.face;
+      t.pad = 0;
+      t.E = p.E;
+      t.x = p.x;
+      t.y = p.y;
+      t.z = p.z;
+      a.traces[h] = t;
+    }
+    __threadfence();  // this history's scores land before the batch can be folded
+    if (atomicSub(a.live + j, 1) == 1) {
+      // the batch's last history: put it on the ready list
+      const unsigned long long pos = atomicAdd(&c->ready, 1ULL);
+      atomicExch(a.ready_list + pos, j);
+    }
+  }
+  // nothing left to take: help fold for a while (the tail's last histories
+  // may still add ready batches), then leave; k_persist_fold_rest folds
+  // whatever is left when the kernel ends
+  for (int idle = 0; idle < 2000 && !vld(&c->error) && vld(&c->folded) < (unsigned long long)a.n_jobs;) {
+    if (persist_fold(a, sp, scan_lo)) {
+      idle = 0;
+      continue;
+    }
+    ++idle;
+    __nanosleep(1000);
+  }
+  L.add(kCntXS, nxs);
+  L.add(kCntFallback, nfb);
+  flush(L, a.counters, a.leak_w);
+}
+
+// Folds the chunks of ready batches that no lane of k_persist claimed.
+__global__ void k_persist_fold_rest(PersistArgs a) {
+  const PersistCtl* c = a.ctl;
+  const int nr = (int)c->ready;
+  for (int k = 0; k < nr; ++k) {
+    const int j = a.ready_list[k];
+    const PersistJob J = a.jobs[j];
+    const PersistProblem& P = a.probs[J.prob];
+    const int from = a.chunk_next[j] < P.n_chunks ? a.chunk_next[j] : P.n_chunks;
+    for (int ch = from + blockIdx.x; ch < P.n_chunks; ch += gridDim.x) {
+      const int64_t e0 = (int64_t)ch * a.chunk;
+      const int64_t e1 = e0 + a.chunk < P.n_tally ? e0 + a.chunk : P.n_tally;
+      double* slot = P.slots + (int64_t)(J.order % P.n_slots) * P.n_tally;
+      for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const double v = slot[e];
+        if (v != 0.0) {
+          const double b = v * J.inv_n;
+          atomicAdd(P.sum + e, b);
+          atomicAdd(P.sumsq + e, b * b);
+          slot[e] = 0.0;
+        }
+      }
+    }
+  }
+}
+
+cudaError_t launch_persistent(const PersistArgs& a, int precision, int block, int grid, cudaStream_t st) {
+  if (precision == MC_PREC_MIXED) k_persist<MC_PREC_MIXED><<<grid, block, 0, st>>>(a);
+  else k_persist<MC_PREC_FP64><<<grid, block, 0, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_persist_fold_rest<<<1216, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+int persistent_blocks_per_sm(int precision, int block) {
+  int n = 0;
+  if (precision == MC_PREC_MIXED)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persist<MC_PREC_MIXED>, block, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persist<MC_PREC_FP64>, block, 0);
+  return n > 0 ? n : 1;
+}
+
 // Loads the kernels of the fixed-source event form (no ray recording) on the
 // current device: under lazy module loading a kernel's code is put on the
 // device at its first launch or attribute query, and the no-allocation run

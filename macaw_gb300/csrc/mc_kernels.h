@@ -117,6 +117,74 @@ struct RunArgs {
 // Loads the fixed-source event-form kernels onto the current device.
 cudaError_t preload_event_kernels();
 
+// ---- persistent run of many batches of one or more problems ------------
+constexpr int kMaxPersistProblems = 8;
+
+// One problem of a persistent run: its device tables, tally definition and
+// the tally slots its batches score into in turn (slot k % n_slots for the
+// problem's k-th batch), folded into its SUM/SUM_SQ.
+struct PersistProblem {
+  DevMesh M;
+  DevXS X;
+  DevSource S;
+  TallySpec ts;
+  int64_t n_tally;
+  double* slots;   // n_slots x n_tally
+  double* sum;
+  double* sumsq;
+  int n_slots;
+  int two_d;
+  double z2d;
+  float tol;
+  int n_chunks;    // fold chunks of one tally
+};
+
+// One batch: global history indices [start, end) of the run; history
+// index first + (h - start) of its problem (particle id one more).
+struct PersistJob {
+  int64_t start, end;
+  int64_t first;
+  uint64_t seed;
+  double inv_n;    // 1 / histories of the batch (SUM is a sum of batch / weight)
+  int prob;
+  int order;       // index of the batch among its problem's batches
+};
+
+struct PersistCtl {
+  unsigned long long next;          // next history index to take
+  unsigned long long ready;         // batches whose histories have all ended (entries in ready list)
+  unsigned long long claimed;       // batches whose fold chunks have all been claimed
+  unsigned long long folded;        // batches folded into SUM/SUM_SQ
+  unsigned long long scan_lo;       // ready-list entries below this have every fold chunk claimed
+  int error;                        // 1: a wait gave up (err_job: the batch it waited on)
+  int err_job;
+  long long err_polls;
+};
+
+struct PersistArgs {
+  const PersistProblem* probs;
+  int n_probs;
+  int n_jobs;
+  const PersistJob* jobs;
+  unsigned long long total;    // histories of all batches
+  int* live;                   // per batch: histories not ended
+  int* chunk_next;             // per batch: fold chunks claimed
+  int* chunk_done;             // per batch: fold chunks done
+  int* ready_list;             // batches in the order they became ready (-1: not yet written)
+  int* slot_turn;              // per problem slot: order of the batch allowed to score into it
+  const int* slot_base;        // per problem: its first entry in slot_turn
+  int chunk;                   // tally values per fold chunk
+  PersistCtl* ctl;
+  mc_trace* traces;            // per history of the run (global index), or null
+  unsigned long long* counters;
+  double* leak_w;
+  long long wait_limit;        // polls a lane makes for a slot or for fold work before giving up
+};
+
+cudaError_t launch_persistent(const PersistArgs& a, int precision, int block, int grid, cudaStream_t st);
+// Blocks of `block` threads of the persistent kernel resident per SM.
+int persistent_blocks_per_sm(int precision, int block);
+
 cudaError_t launch_history(const DevMesh& M, const DevXS& X, const DevSource& S, const RunArgs& a,
                            int block, int grid, cudaStream_t st);
 

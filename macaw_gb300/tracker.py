@@ -12,8 +12,8 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (EIGEN_GEN_DTYPE, FISSION_SITE_DTYPE, MC_MODE_EVENT, MC_PREC_FP64, MC_TALLY_BATCH, MC_TALLY_SUM,
-                   MC_TALLY_SUM_SQ, RAY_SEGMENT_DTYPE, SITE_DTYPE, TRACE_DTYPE, EigenDesc, MCError, RunDesc,
-                   SourceDesc, Stats, TallyDesc, lib, ptr)
+                   MC_TALLY_SUM_SQ, RAY_SEGMENT_DTYPE, SITE_DTYPE, TRACE_DTYPE, EigenDesc, Job, MCError, PersistDesc,
+                   RunDesc, SourceDesc, Stats, TallyDesc, lib, ptr)
 from .problems import Problem, Source, TallyDef
 
 
@@ -272,3 +272,24 @@ class Tracker:
         v = C.c_int64()
         self._ck(lib.mc_batches_done(self._h, C.byref(v)), "mc_batches_done")
         return v.value
+
+
+def run_persistent(jobs, precision: int = MC_PREC_FP64, slots: int = 0, block_size: int = 0,
+                   traces: bool = False, wait_limit: int = 0):
+    """mc_run_persistent: jobs is a list of (tracker, first_history,
+    n_histories, seed), one batch each, in the order their histories are
+    numbered; every batch folds into its tracker's SUM/SUM_SQ.  Returns
+    (Stats, traces of the run's histories in job order or None)."""
+    arr = (Job * len(jobs))()
+    total = 0
+    for i, (t, first, n, seed) in enumerate(jobs):
+        arr[i] = Job(t._h.value if isinstance(t._h, C.c_void_p) else t._h, first, n, seed)
+        total += n
+    tr = np.zeros(total, TRACE_DTYPE) if traces else None
+    d = PersistDesc(precision, block_size, slots, int(traces), wait_limit, None if tr is None else tr.ctypes.data)
+    st = Stats()
+    rc = lib.mc_run_persistent(C.byref(d), len(jobs), arr, C.byref(st))
+    if rc != 0:
+        msg = lib.mc_last_error(jobs[0][0]._h)
+        raise MCError(rc, f"mc_run_persistent: {msg.decode() if msg else ''}")
+    return st, tr

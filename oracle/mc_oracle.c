@@ -1083,15 +1083,18 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
       if (!(sigt > 0.0) || sigt != sigt) { status = ST_BADXS; break; }
     }
     /* exit side: smallest (d - n.x)/(n.u) over sides with n.u > 0, compared
-       by cross-multiplication, ties to the lower side index */
+       by cross-multiplication, ties to the lower side index.  The dot
+       products and the position updates are chains of fused multiply-adds
+       (C99 fma, one rounding each): the same operations the GPU's DFMA
+       performs, in the same order, so both give the same bits. */
     const double* P = p->planes + 16 * (int64_t)elem;
     int bf = -1;
     double bnum = 0.0, bden = 1.0;
     for (int f = 0; f < 4; ++f) {
       const double* pl = P + 4 * f;
-      double den = pl[0] * u[0] + pl[1] * u[1] + pl[2] * u[2];
+      double den = fma(pl[0], u[0], fma(pl[1], u[1], pl[2] * u[2]));
       if (den > 0.0) {
-        double num = pl[3] - (pl[0] * x[0] + pl[1] * x[1] + pl[2] * x[2]);
+        double num = fma(-pl[0], x[0], fma(-pl[1], x[1], fma(-pl[2], x[2], pl[3])));
         if (bf < 0 || num * bden < bnum * den) { bf = f; bnum = num; bden = den; }
       }
     }
@@ -1107,9 +1110,9 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
     s0[0] = x[0]; s0[1] = x[1]; s0[2] = x[2];
     if (dist > L) {
       hash = (hash ^ ((uint64_t)elem * 8ULL + (uint64_t)bf)) * FNV_PRIME;
-      x[0] = x[0] + L * u[0];
-      x[1] = x[1] + L * u[1];
-      x[2] = x[2] + L * u[2];
+      x[0] = fma(L, u[0], x[0]);
+      x[1] = fma(L, u[1], x[1]);
+      x[2] = fma(L, u[2], x[2]);
       record_seg(rec, rec_n, rec_cap, id, n_seg, n_coll, elem, s0, x, E, wgt, strk);
       int32_t nb = p->nbr[4 * (int64_t)elem + bf];
       if (nb >= 0) { elem = nb; continue; }
@@ -1117,11 +1120,11 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
       if (bid < 0) bid = 0;
       if (bid < 1024 && p->bc_type[bid] == 1) {
         const double* pl = P + 4 * bf;
-        double dn = u[0] * pl[0] + u[1] * pl[1] + u[2] * pl[2];
+        double dn = fma(u[0], pl[0], fma(u[1], pl[1], u[2] * pl[2]));
         double t2 = 2.0 * dn;
-        u[0] = u[0] - t2 * pl[0];
-        u[1] = u[1] - t2 * pl[1];
-        u[2] = u[2] - t2 * pl[2];
+        u[0] = fma(-t2, pl[0], u[0]);
+        u[1] = fma(-t2, pl[1], u[1]);
+        u[2] = fma(-t2, pl[2], u[2]);
         continue;
       }
       status = ST_LEAK;
@@ -1131,11 +1134,11 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
     }
     /* collision inside this element */
     hash = (hash ^ ((uint64_t)elem * 8ULL + 4ULL)) * FNV_PRIME;
-    double ex = x[0] + L * u[0], ey = x[1] + L * u[1], ez = x[2] + L * u[2];
+    double ex = fma(L, u[0], x[0]), ey = fma(L, u[1], x[1]), ez = fma(L, u[2], x[2]);
     double back = L - dist;
-    x[0] = ex - back * u[0];
-    x[1] = ey - back * u[1];
-    x[2] = ez - back * u[2];
+    x[0] = fma(-back, u[0], ex);
+    x[1] = fma(-back, u[1], ey);
+    x[2] = fma(-back, u[2], ez);
     ++n_coll;
     record_seg(rec, rec_n, rec_cap, id, n_seg, n_coll, elem, s0, x, E, wgt, strk);
     zero_run = 0;

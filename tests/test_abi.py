@@ -42,7 +42,7 @@ def _header_sizes(tmp_path):
     inc = ROOT / "include"
     src = tmp_path / "sizes.c"
     structs = ["mc_source_desc", "mc_site", "mc_fission_site", "mc_run_desc", "mc_trace", "mc_stats",
-               "mc_tally_desc", "mc_ray_segment", "mc_eigen_desc", "mc_eigen_gen"]
+               "mc_tally_desc", "mc_ray_segment", "mc_eigen_desc", "mc_eigen_gen", "mc_job", "mc_persist_desc"]
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "macaw_gb300.h"\nint main(void){\n' +
                    "".join(f'printf("{n} %zu\\n", sizeof({n}));\n' for n in structs) +
                    'printf("batch_sum_out %zu\\n", offsetof(mc_run_desc, batch_sum_out));\nreturn 0;}\n')
@@ -58,6 +58,8 @@ def test_struct_layouts_match_header_sizes(tmp_path):
     assert C.sizeof(_lib.RunDesc) == h["mc_run_desc"]
     assert _lib.RunDesc.batch_sum_out.offset == h["batch_sum_out"]
     assert C.sizeof(_lib.EigenDesc) == h["mc_eigen_desc"]
+    assert C.sizeof(_lib.Job) == h["mc_job"]
+    assert C.sizeof(_lib.PersistDesc) == h["mc_persist_desc"]
     assert C.sizeof(_lib.TallyDesc) == h["mc_tally_desc"]
     assert C.sizeof(_lib.Stats) == h["mc_stats"]
     assert _lib.TRACE_DTYPE.itemsize == h["mc_trace"]
