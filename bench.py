@@ -552,7 +552,7 @@ def run_profile(args):
     if args.workload not in ("lattice", "core"):
         raise SystemExit("--profile-run takes --workload lattice, core or eigen")
     p = problems.lattice_problem(nx=args.pins, ny=args.pins) if args.workload == "lattice" \
-        else problems.core_problem()
+        else problems.core_problem(pins=args.pins, radius=args.radius)
     with Tracker(0) as t:
         t.load(p)
         kw = dict(bank_size=n, block_size=block, max_seg=max_seg, sort_queue=sort, precision=prec)
@@ -585,6 +585,7 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="--profile-run only")
     ap.add_argument("--max-seg", type=int, default=0, help="--profile-run only: 0 = 128 mixed, 64 fp64")
     ap.add_argument("--sort", type=int, default=0, help="--profile-run only: 0 = 9 (lattice), 13 (core)")
+    ap.add_argument("--radius", type=float, default=180.0, help="--profile-run only: core radius (cm)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_run:

@@ -1172,6 +1172,158 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
 }
 
 // ---------------------------------------------------------------------------
+// The FP64 segment of the compact walk (k_ev_advance_fp64): segment_fp64g's
+// arithmetic and results, bit for bit, with the element's float record
+// (planes R0..R3, entries nb4 and, after a flagged side, the material
+// mnext) already in registers.  As soon as the exit side is certified and
+// the float pretest decides that the particle crosses, the neighbour's
+// record is requested and the line of its FP64 planes prefetched into L1,
+// before this segment's FP64 distance, tally and position update; so the
+// next segment's loads are in flight while they run.  Same return codes as
+// segment_fp64g (0 crossed, 1 collision, 2 ended, 3 XS event, 5 reflected);
+// after the full-search fallback (uncertified exits) the record is reloaded.
+__device__ __forceinline__ void load_tet32(const DevMesh& M, int t, float4& R0, float4& R1, float4& R2, float4& R3,
+                                           int4& nb4) {
+  const Tet32* T = M.tet + t;
+  R0 = __ldg(&T->p[0]);
+  R1 = __ldg(&T->p[1]);
+  R2 = __ldg(&T->p[2]);
+  R3 = __ldg(&T->p[3]);
+  nb4 = __ldg(&T->nbr);
+}
+
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+template <bool kEig>
+__device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, Particle& p, float& uf, float& vf,
+                                             float& wf, float4& R0, float4& R1, float4& R2, float4& R3, int4& nb4,
+                                             int& mnext, double* __restrict__ tally, const TallySpec& T,
+                                             float& sigt32, unsigned long long& n_xs) {
+  if (p.n_seg >= M.max_seg || p.zero_run >= kMaxZeroRun) {
+    p.status = kStuck;
+    return 2;
+  }
+  if (p.mat < 0) {
+    const int mat = mnext;
+    if (mat < 0) {
+      p.status = kBadXS;
+      return 2;
+    }
+    if (!xs_cache_get<kEig>(p, mat)) return 3;
+    p.mat = mat;
+    sigt32 = narrow(p.sigt);
+  }
+  const float xf = narrow(p.x), yf = narrow(p.y), zf = narrow(p.z);
+  const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
+  const float Eden = 7.2e-7f * (fabsf(uf) + fabsf(vf) + fabsf(wf));
+  bool sure = true;
+  int bf = -1;
+  float tb = 3.0e38f, eb = 0.0f, lo_other = 3.0e38f;
+  auto side = [&](const float4& pl, int f) {
+    const float den = fmaf(pl.x, uf, fmaf(pl.y, vf, pl.z * wf));
+    const float num = pl.w - fmaf(pl.x, xf, fmaf(pl.y, yf, pl.z * zf));
+    const float En = 7.2e-7f * (fabsf(pl.w) + xa);
+    const bool other = f != p.fin;
+    if (other && fabsf(den) <= Eden) sure = false;
+    const bool cand = other && den > Eden;
+    const float t = cand ? __fdividef(num, den) : 3.0e38f;
+    const float e =
+        cand ? (__fdividef(En + fabsf(t) * Eden, den - Eden) + 4.8e-7f * fabsf(t)) * 1.001f + 1e-30f : 0.0f;
+    const bool nearer = t < tb;
+    lo_other = fminf(lo_other, nearer ? tb - eb : t - e);
+    bf = nearer ? f : bf;
+    tb = nearer ? t : tb;
+    eb = nearer ? e : eb;
+  };
+  side(R0, 0);
+  side(R1, 1);
+  side(R2, 2);
+  side(R3, 3);
+  if (!sure || bf < 0 || !(tb + eb < lo_other)) {
+    const int r = segment_fp64<false, false, kEig>(M, X, p, tally, T, sigt32, n_xs);
+    if (r == 0 || r == 5) {  // a new element (or a new direction): its record
+      load_tet32(M, p.elem, R0, R1, R2, R3, nb4);
+      if (p.mat < 0) mnext = __ldg(M.tmat + p.elem);
+    }
+    return (r == 0 && p.fin < 0) ? 5 : r;
+  }
+  // one draw per segment: advance the state once, derive both forms
+  p.seed = kPrnMult * p.seed + kPrnAdd;
+  uint64_t wv = ((p.seed >> ((p.seed >> 59u) + 5u)) ^ p.seed) * 12605985483714917081ULL;
+  wv = (wv >> 43u) ^ wv;
+  const float xhi = fmaf((float)(uint32_t)(wv >> 32), 2.3283064365386963e-10f, 2.3283064365386963e-10f) *
+                    1.00000024f;
+  const float lf = -__logf(xhi) * 0.999999f - 1e-6f;
+  const float thr = fmaxf(tb + eb, 0.0f) * sigt32;
+  const bool cross_sure = lf > thr * 1.00001f + 1e-6f;
+  const int nb = side_entry(nb4, bf);
+  const int next = (nb & (kMatChange - 1)) >> 2;
+  const double4_32a plb = M.planes[4 * (int64_t)p.elem + bf];
+  if (cross_sure && nb >= 0) {
+    // the neighbour's record and FP64 planes, requested ahead of this
+    // segment's FP64 work
+    load_tet32(M, next, R0, R1, R2, R3, nb4);
+    if (nb & kMatChange) mnext = __ldg(M.tmat + next);
+    prefetch_l1(M.planes + 4 * (int64_t)next);
+  }
+  const double bden = fma(plb.x, p.u, fma(plb.y, p.v, plb.z * p.w));
+  const double bnum = fma(-plb.x, p.x, fma(-plb.y, p.y, fma(-plb.z, p.z, plb.w)));
+  double L = bnum / bden;
+  if ((long long)dbits(L) <= 0) L = 0.0;
+  bool cross = cross_sure;
+  double dist = 0.0;
+  if (!cross_sure) {
+    const double xi = (double)(wv >> 11) * 0x1.0p-53;
+    dist = -mc::log64(xi) / p.sigt;
+    cross = dist > L;
+    if (cross && nb >= 0) {
+      load_tet32(M, next, R0, R1, R2, R3, nb4);
+      if (nb & kMatChange) mnext = __ldg(M.tmat + next);
+    }
+  }
+  const double score = cross ? L : dist;
+  score_track(T, tally, p.elem, p.E, dbits(p.wgt) == dbits(1.0) ? score : p.wgt * score, p.sigt);
+  if (kEig) p.ktl = p.ktl + p.wgt * score * p.nuf;  // CollisionKernel.C:153-154
+  ++p.n_seg;
+  if (dbits(L) == 0) ++p.zero_run;
+  else p.zero_run = 0;
+  if (cross) {
+    p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + (uint64_t)bf);
+    p.x = fma(L, p.u, p.x);
+    p.y = fma(L, p.v, p.y);
+    p.z = fma(L, p.w, p.z);
+    if (nb >= 0) {
+      if (nb & kMatChange) p.mat = -2;
+      p.elem = next;
+      p.fin = nb & 3;
+      return 0;
+    }
+    const int bid = -1 - nb;
+    if (bid < M.n_bid && M.bc_type[bid] == 1) {
+      const double dn = fma(p.u, plb.x, fma(p.v, plb.y, p.w * plb.z));
+      const double t2 = 2.0 * dn;
+      p.u = fma(-t2, plb.x, p.u);
+      p.v = fma(-t2, plb.y, p.v);
+      p.w = fma(-t2, plb.z, p.w);
+      p.fin = -1;
+      return 5;  // reflected: the caller refreshes its float direction (the record is still this element's)
+    }
+    p.status = kLeaked;
+    p.face = bf;
+    return 2;
+  }
+  p.hash = fnv(p.hash, (uint64_t)p.elem * 8ULL + 4ULL);
+  const double ex = fma(L, p.u, p.x), ey = fma(L, p.v, p.y), ez = fma(L, p.w, p.z);
+  const double back = L - dist;
+  p.x = fma(-back, p.u, ex);
+  p.y = fma(-back, p.v, ey);
+  p.z = fma(-back, p.w, ez);
+  ++p.n_coll;
+  p.zero_run = 0;
+  return 1;
+}
+
+// ---------------------------------------------------------------------------
 // Mixed-precision form.  Position and direction live in float registers for
 // the walk; exits are solved on the float planes; the two nearest exit
 // distances must differ by more than tol (1e-6 of the mesh bounding-box

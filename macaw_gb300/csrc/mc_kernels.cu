@@ -459,6 +459,60 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
   flush(L, a.counters, a.leak_w);
 }
 
+// FP64 segment walk for the default tally (no ray recording): each lane
+// walks the particles of its warp's queue chunks one visit at a time with
+// segment_fp64c, whose element records are loaded one step ahead.
+template <bool kEig>
+__global__ void __launch_bounds__(128) k_ev_advance_fp64(DevMesh M, DevXS X, RunArgs a, Bank B, EventQueues Q,
+                                                         EventCtl* ctl, int par) {
+  MC_COUNTERS(L);
+  const int n = *(volatile int*)&ctl->n_adv[par];
+  const int nxt = par ^ 1;
+  for (;;) {
+    const int i = take_chunk(&ctl->adv_head) + (int)(threadIdx.x & 31);
+    if (__shfl_sync(0xffffffffu, i, 0) >= n) break;
+    if (i >= n) continue;
+    const int s = Q.adv[par][i];
+    Particle p;
+    load(B, s, p, kEig);
+    float4 R0, R1, R2, R3;
+    int4 nb4;
+    load_tet32(M, p.elem, R0, R1, R2, R3, nb4);
+    int mnext = p.mat < 0 ? __ldg(M.tmat + p.elem) : 0;
+    const int seg0 = p.n_seg;
+    unsigned long long nxs = 0;
+    int r = 0, k = 0;
+    float sigt32 = narrow(p.sigt);
+    float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
+    double* const tal = tally_of(a, p.tag);
+    for (;;) {
+      r = segment_fp64c<kEig>(M, X, p, uf, vf, wf, R0, R1, R2, R3, nb4, mnext, tal, a.ts, sigt32, nxs);
+      if (r == 5) {
+        uf = narrow(p.u);
+        vf = narrow(p.v);
+        wf = narrow(p.w);
+        r = 0;
+      }
+      if (r != 0) break;
+      if (a.max_seg > 0 && ++k >= a.max_seg) {
+        r = 4;
+        break;
+      }
+    }
+    L.add(kCntSegWalk, (unsigned long long)(p.n_seg - seg0));
+    if (r == 2) {
+      finish(p, a, L);
+      push_free(Q, ctl, s, B.cap);
+      continue;
+    }
+    store(B, s, p, kEig);
+    if (r == 1) push(Q.coll, &ctl->n_coll, s);
+    else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
+    else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
+  }
+  flush(L, a.counters, a.leak_w);
+}
+
 // Take the next advance-queue entry (one atomic per converged lane group).
 __device__ __forceinline__ int take(int* head) {
   cg::coalesced_group g = cg::coalesced_threads();
@@ -1102,7 +1156,7 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
   } else {
     if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else if (a.ts.rays) k_ev_advance_static<MC_PREC_FP64, true, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else k_ev_advance_static<MC_PREC_FP64, false, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_advance_fp64<false><<<grid, block < 128 ? block : 128, 0, st>>>(M, X, a, B, Q, ctl, par);
   }
   if (adv1) cudaEventRecord(adv1, st);
   if (a.eig.on) k_ev_collide<true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
