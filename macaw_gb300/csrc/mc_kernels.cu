@@ -1462,7 +1462,7 @@ cudaError_t preload_event_kernels() {
       (const void*)k_ev_advance<MC_PREC_MIXED>,
       (const void*)k_ev_advance<MC_PREC_FP64>,
       (const void*)k_ev_advance_mixed<false>,
-      (const void*)k_ev_advance_static<MC_PREC_FP64, false, false>,
+      (const void*)k_ev_advance_fp64<false>,
       (const void*)k_ev_collide<false>,
       (const void*)k_ev_refill,
       (const void*)k_ev_reset,
