@@ -83,18 +83,18 @@ REF_SAMPLE = 100_000
 # DRAM bytes per walked segment of the walk kernels, from ncu captures of
 # every walk launch of a 2 x 2e5-history lattice run (profiles/walk_*_lattice.md);
 # traffic per launch = this x the launch's segments
-ADVANCE_DRAM_BYTES_PER_SEG = 194.2
+ADVANCE_DRAM_BYTES_PER_SEG = 200.0
 MIXED_DRAM_BYTES_PER_SEG = 46.8
 # what bounds each walk instead of HBM, from the same captures' --set full
-# launch: the FP64 walk keeps the FP64 pipe 68% busy (GB300's FP64 rate is a
+# launch: the FP64 walk keeps the FP64 pipe 63% busy (GB300's FP64 rate is a
 # 64th of its FP32 rate); the mixed walk waits on its one dependent record
 # load per segment (L2 hit rate 48%, 29% of the warp slots occupied)
-FP64_PIPE_ACTIVE = 0.677
+FP64_PIPE_ACTIVE = 0.633
 MIXED_L2_HIT = 0.477
 # the same captures' L2 hit rate and warp execution efficiency (active
 # threads per executed instruction / 32), for the report
-FP64_L2_HIT = 0.329
-FP64_WARP_EFF = 22.08 / 32
+FP64_L2_HIT = 0.400
+FP64_WARP_EFF = 21.44 / 32
 MIXED_WARP_EFF = 20.30 / 32
 
 
@@ -442,7 +442,7 @@ def eigen_result(n, K, W, no_mixed=False, cpu=True):
            "value": f["value"], "higher_is_better": True, "dtype": "f64", "steps": K, "warmup": W,
            "data": "synthetic (seeded generators)",
            "config": {"workload": f"eigen lattice 17x17 pins, 50 cm, {p.n_tet} tets, every fuel nuclide "
-                                  "fissionable, reflective sides, vacuum top/bottom; {n} particles per generation, "
+                                  f"fissionable, reflective sides, vacuum top/bottom; {n} particles per generation, "
                                   f"{W} inactive + {K} active generations", "tets": p.n_tet,
                       "l2": "inputs larger than L2 (mesh planes 261 MB, bank 80 MB)"},
            "fp64": f, "mixed": res.get("mixed"),
@@ -783,7 +783,7 @@ def main():
         adv_bytes = walk * B_SEG_FP64
         achieved = adv_bytes / (pst64.ms_advance / 1e3) / 1e9 if pst64.ms_advance > 0 else None
         roof = {"bound": "hbm", "kernel": "k_ev_advance<FP64>" if params64.get("refill")
-                else "k_ev_advance_static<FP64>",
+                else "k_ev_advance_fp64",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": (ADVANCE_DRAM_BYTES_PER_SEG * walk / max(pst64.n_advance_launch, 1))

@@ -998,7 +998,47 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
     Particle p;
     load(B, s, p, kEig);
     unsigned long long nxs = 0, nfb = 0;
-    if (kPrec == MC_PREC_FP64) {
+    if (kPrec == MC_PREC_FP64 && !a.ts.rays) {
+      // the compact FP64 segment: records loaded a step ahead (a tail
+      // history is one long chain of dependent loads); cross-section
+      // events are evaluated inline for the material entered
+      float sigt32 = narrow(p.sigt);
+      float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
+      float4 R0, R1, R2, R3;
+      int4 nb4;
+      load_tet32(M, p.elem, R0, R1, R2, R3, nb4);
+      int mnext = p.mat < 0 ? __ldg(M.tmat + p.elem) : 0;
+      double* const tal = tally_of(a, p.tag);
+      while (p.status == kAlive) {
+        const int r = segment_fp64c<kEig>(M, X, p, uf, vf, wf, R0, R1, R2, R3, nb4, mnext, tal, a.ts, sigt32, nxs);
+        if (r == 3) {
+          const int mat = mnext;  // a material with no cached Sigma_t at this energy
+          double nf = 0.0;
+          const double sg = kEig ? macro_total_nuf(X, mat, p.E, xs_bucket32(X, p.E), nf) : macro_total(X, mat, p.E);
+          ++nxs;
+          if (!(sg > 0.0) || sg != sg) {
+            p.status = kBadXS;
+            break;
+          }
+          p.sigt = sg;
+          if (kEig) p.nuf = nf;
+          xs_cache_put<kEig>(p, mat, sg, nf);
+          p.mat = mat;
+          sigt32 = narrow(sg);
+          continue;
+        }
+        if (r == 1) {
+          score_collision(X, a.ts, tal, p);
+          collide<kEig>(X, p, a.two_d, a.eig);
+          mnext = __ldg(M.tmat + p.elem);  // collide empties the cache: the element's material again
+        }
+        if (r == 1 || r == 5) {
+          uf = narrow(p.u);
+          vf = narrow(p.v);
+          wf = narrow(p.w);
+        }
+      }
+    } else if (kPrec == MC_PREC_FP64) {
       float sigt32 = narrow(p.sigt);
       float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
       while (p.status == kAlive) {
@@ -1148,7 +1188,7 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
     else if (a.precision == MC_PREC_MIXED)
       k_ev_advance_static<MC_PREC_MIXED, false, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else
-      k_ev_advance_static<MC_PREC_FP64, false, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
+      k_ev_advance_fp64<true><<<grid, block < 128 ? block : 128, 0, st>>>(M, X, a, B, Q, ctl, par);
   } else if (a.precision == MC_PREC_MIXED) {
     // the compact walk scores the default tally and records no rays
     if (a.refill || a.ts.general || a.ts.rays) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
