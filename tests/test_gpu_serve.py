@@ -74,3 +74,35 @@ def test_poisson_stream_completes(probs):
     rep = run_stream(srv, jobs)
     srv.close()
     assert rep["requests"] == len(jobs) and rep["p99_ms"] >= rep["p50_ms"] > 0
+
+
+def test_admitted_requests_overlap_on_the_device(probs):
+    """Requests admitted together run together: after one step, several are
+    active in one context's bank at once."""
+    srv = Server(probs[:1], precision=MC_PREC_FP64, bank=4096, max_slots=3)
+    keys = [srv.submit(Job(0, 200_000, 20 + k, (4.0, 4.0, 4.0), 1.0e6)) for k in range(3)]
+    srv.step()
+    queued, active, free = srv.status(0)
+    assert active == 3 and queued == 0 and free == 0
+    drain(srv, keys)
+    srv.close()
+
+
+def test_budget_admission_loads_and_evicts(probs):
+    """With an HBM budget that holds one problem at a time, requests for the
+    other problem wait, the idle problem is evicted and the other loaded;
+    every result equals the request run alone."""
+    from macaw_gb300.serve import footprint
+    budget = max(footprint(p, 2048, 1) for p in probs) + 1024
+    srv = Server(probs, precision=MC_PREC_FP64, bank=2048, max_slots=1, hbm_budget=budget, preload=False)
+    keys = [srv.submit(j) for j in JOBS]
+    together = drain(srv, keys)
+    assert srv.loads >= 2 and srv.evictions >= 1
+    assert srv.peak_bytes <= budget
+    srv.close()
+    for key, job in zip(keys, JOBS):
+        alone = Server(probs, precision=MC_PREC_FP64, bank=2048, max_slots=1)
+        k = alone.submit(job)
+        ref = drain(alone, [k])[k]
+        alone.close()
+        assert close(together[key], ref), f"request {job} differs under eviction"
