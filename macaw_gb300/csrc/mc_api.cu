@@ -98,6 +98,8 @@ struct mc_ctx {
   // 2-D mode (mc_set_2d)
   int two_d = 0;
   double z2d = 0.0;
+  // largest L1 error of an octahedral record's decoded unit normal
+  double oct_err = 0.0;
   // segments a history may walk before it ends as stuck (mc_set_segment_limit;
   // 0: default_segment_limit of the mesh)
   int64_t seg_limit = 0;
@@ -213,6 +215,7 @@ int ensure_device_tables(mc_ctx* c) {
     // folded over the lower half (z < 0), rounded to float; the offset is
     // scaled by the length of the normal the walk decodes from (a, b)
     std::vector<TetOct> oct((size_t)c->mesh.n_tet);
+    double oct_err = 0.0;
     for (int64_t t = 0; t < c->mesh.n_tet; ++t) {
       float ab[8], dd[4];
       for (int f = 0; f < 4; ++f) {
@@ -250,6 +253,10 @@ int ensure_device_tables(mc_ctx* c) {
         oct_normal(best_a, best_b, nx, ny, nz);
         const double len = sqrt((double)nx * nx + (double)ny * ny + (double)nz * nz);
         dd[f] = (float)(q[3] * len);
+        // the decoded normal's direction error (L1), for the FP64 walk's
+        // certified side choice on these records
+        const double err = fabs(nx / len - q[0]) + fabs(ny / len - q[1]) + fabs(nz / len - q[2]);
+        if (err > oct_err) oct_err = err;
       }
       TetOct& o = oct[t];
       o.oct01 = make_float4(ab[0], ab[1], ab[2], ab[3]);
@@ -258,6 +265,7 @@ int ensure_device_tables(mc_ctx* c) {
       o.nbr = rec[t].nbr;
     }
     CK(upload(c->d_teto, oct, c->stream), "upload octahedral records");
+    c->oct_err = oct_err;
     CK(cudaStreamSynchronize(c->stream), "upload tet records");
     c->tmat_dirty = false;
   }
@@ -278,6 +286,8 @@ DevMesh dev_mesh(mc_ctx* c) {
   M.n_bid = (int)c->bc_type.size();
   M.n_tet = c->mesh.n_tet;
   M.max_seg = (int)(c->seg_limit > 0 ? c->seg_limit : default_segment_limit(c->mesh.n_tet));
+  // with margin for the float rounding of the bound itself
+  M.oct_err = (float)(c->oct_err * 1.25 + 1e-9);
   for (int k = 0; k < 3; ++k) {
     M.glo[k] = c->mesh.glo[k];
     M.gh[k] = c->mesh.gh[k];

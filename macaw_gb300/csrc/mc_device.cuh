@@ -99,6 +99,7 @@ struct DevMesh {
   const int* __restrict__ bc_type;      // per boundary id: 0 vacuum, 1 reflect
   int n_bid;
   int max_seg;                          // segments a history may walk before it ends as stuck
+  float oct_err;                        // bound on an octahedral record's unit-normal error (L1)
   int64_t n_tet;
   double glo[3], gh[3], ginv[3];  // locator origin, cell size, 1 / cell size
   int gn[3];
@@ -1173,22 +1174,26 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
 
 // ---------------------------------------------------------------------------
 // The FP64 segment of the compact walk (k_ev_advance_fp64): segment_fp64g's
-// arithmetic and results, bit for bit, with the element's float record
-// (planes R0..R3, entries nb4 and, after a flagged side, the material
-// mnext) already in registers.  As soon as the exit side is certified and
-// the float pretest decides that the particle crosses, the neighbour's
-// record is requested and the line of its FP64 planes prefetched into L1,
-// before this segment's FP64 distance, tally and position update; so the
-// next segment's loads are in flight while they run.  Same return codes as
-// segment_fp64g (0 crossed, 1 collision, 2 ended, 3 XS event, 5 reflected);
-// after the full-search fallback (uncertified exits) the record is reloaded.
-__device__ __forceinline__ void load_tet32(const DevMesh& M, int t, float4& R0, float4& R1, float4& R2, float4& R3,
-                                           int4& nb4) {
-  const Tet32* T = M.tet + t;
-  R0 = __ldg(&T->p[0]);
-  R1 = __ldg(&T->p[1]);
-  R2 = __ldg(&T->p[2]);
-  R3 = __ldg(&T->p[3]);
+// arithmetic and results, bit for bit, with the element's 64-byte
+// octahedral record (O01, O23, D, entries nb4 and, after a flagged side,
+// the material mnext) already in registers.  The exit side is certified on
+// the octahedral planes: their decoded normals m differ from the FP64 unit
+// normals n by at most M.oct_err in |m/|m| - n|_1 (measured on the host
+// over every plane of the mesh), which adds oct_err * (|x| + |d|) to the
+// numerator bound and oct_err * |u| to the denominator bound of the float
+// planes' 12 * 2^-24 (see segment_fp64g).  As soon as the exit side is
+// certified and the float pretest decides that the particle crosses, the
+// neighbour's record is requested and the line of its FP64 planes
+// prefetched into L1, before this segment's FP64 distance, tally and
+// position update; so the next segment's loads are in flight while they
+// run.  Same return codes as segment_fp64g (0 crossed, 1 collision, 2
+// ended, 3 XS event, 5 reflected); after the full-search fallback
+// (uncertified exits) the record is reloaded.
+__device__ __forceinline__ void load_oct(const DevMesh& M, int t, float4& O01, float4& O23, float4& D, int4& nb4) {
+  const TetOct* T = M.teto + t;
+  O01 = __ldg(&T->oct01);
+  O23 = __ldg(&T->oct23);
+  D = __ldg(&T->d);
   nb4 = __ldg(&T->nbr);
 }
 
@@ -1196,7 +1201,7 @@ __device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefe
 
 template <bool kEig>
 __device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, Particle& p, float& uf, float& vf,
-                                             float& wf, float4& R0, float4& R1, float4& R2, float4& R3, int4& nb4,
+                                             float& wf, float4& O01, float4& O23, float4& D, int4& nb4,
                                              int& mnext, double* __restrict__ tally, const TallySpec& T,
                                              float& sigt32, unsigned long long& n_xs) {
   if (p.n_seg >= M.max_seg || p.zero_run >= kMaxZeroRun) {
@@ -1215,14 +1220,15 @@ __device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, P
   }
   const float xf = narrow(p.x), yf = narrow(p.y), zf = narrow(p.z);
   const float xa = fabsf(xf) + fabsf(yf) + fabsf(zf);
-  const float Eden = 7.2e-7f * (fabsf(uf) + fabsf(vf) + fabsf(wf));
+  const float cb = 7.2e-7f + M.oct_err;
+  const float Eden = cb * (fabsf(uf) + fabsf(vf) + fabsf(wf));
   bool sure = true;
   int bf = -1;
   float tb = 3.0e38f, eb = 0.0f, lo_other = 3.0e38f;
   auto side = [&](const float4& pl, int f) {
     const float den = fmaf(pl.x, uf, fmaf(pl.y, vf, pl.z * wf));
     const float num = pl.w - fmaf(pl.x, xf, fmaf(pl.y, yf, pl.z * zf));
-    const float En = 7.2e-7f * (fabsf(pl.w) + xa);
+    const float En = cb * (fabsf(pl.w) + xa);
     const bool other = f != p.fin;
     if (other && fabsf(den) <= Eden) sure = false;
     const bool cand = other && den > Eden;
@@ -1235,14 +1241,14 @@ __device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, P
     tb = nearer ? t : tb;
     eb = nearer ? e : eb;
   };
-  side(R0, 0);
-  side(R1, 1);
-  side(R2, 2);
-  side(R3, 3);
+  side(oct_plane(O01.x, O01.y, D.x), 0);
+  side(oct_plane(O01.z, O01.w, D.y), 1);
+  side(oct_plane(O23.x, O23.y, D.z), 2);
+  side(oct_plane(O23.z, O23.w, D.w), 3);
   if (!sure || bf < 0 || !(tb + eb < lo_other)) {
     const int r = segment_fp64<false, false, kEig>(M, X, p, tally, T, sigt32, n_xs);
     if (r == 0 || r == 5) {  // a new element (or a new direction): its record
-      load_tet32(M, p.elem, R0, R1, R2, R3, nb4);
+      load_oct(M, p.elem, O01, O23, D, nb4);
       if (p.mat < 0) mnext = __ldg(M.tmat + p.elem);
     }
     return (r == 0 && p.fin < 0) ? 5 : r;
@@ -1262,7 +1268,7 @@ __device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, P
   if (cross_sure && nb >= 0) {
     // the neighbour's record and FP64 planes, requested ahead of this
     // segment's FP64 work
-    load_tet32(M, next, R0, R1, R2, R3, nb4);
+    load_oct(M, next, O01, O23, D, nb4);
     if (nb & kMatChange) mnext = __ldg(M.tmat + next);
     prefetch_l1(M.planes + 4 * (int64_t)next);
   }
@@ -1277,7 +1283,7 @@ __device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, P
     dist = -mc::log64(xi) / p.sigt;
     cross = dist > L;
     if (cross && nb >= 0) {
-      load_tet32(M, next, R0, R1, R2, R3, nb4);
+      load_oct(M, next, O01, O23, D, nb4);
       if (nb & kMatChange) mnext = __ldg(M.tmat + next);
     }
   }
@@ -1347,10 +1353,10 @@ __device__ __forceinline__ void geo_store(const Geo32& g, Particle& p) {
   p.u = widen(g.u); p.v = widen(g.v); p.w = widen(g.w);
 }
 
-// FP64 re-solve of the exit side for a float position/direction.
-__device__ __forceinline__ int exit_fp64(const DevMesh& M, int elem, int fin, const Geo32& g,
-                                         double& L) {
-  const double x = g.x, y = g.y, z = g.z, u = g.u, v = g.v, w = g.w;
+// FP64 re-solve of the exit side for a position and direction given in
+// double (the compact walk passes its compensated position x + xl).
+__device__ __forceinline__ int exit_fp64d(const DevMesh& M, int elem, int fin, double x, double y, double z,
+                                          double u, double v, double w, double& L) {
   const double4_32a* P = M.planes + 4 * (int64_t)elem;
   int bf = -1;
   double bnum = 0.0, bden = 1.0;
@@ -1373,6 +1379,11 @@ __device__ __forceinline__ int exit_fp64(const DevMesh& M, int elem, int fin, co
     if (!(L > 0.0)) L = 0.0;
   }
   return bf;
+}
+
+// The same for a float position/direction.
+__device__ __forceinline__ int exit_fp64(const DevMesh& M, int elem, int fin, const Geo32& g, double& L) {
+  return exit_fp64d(M, elem, fin, g.x, g.y, g.z, g.u, g.v, g.w, L);
 }
 
 template <bool kInlineXS, bool kPrefetch = false, bool kEig = false>

@@ -475,9 +475,9 @@ __global__ void __launch_bounds__(128) k_ev_advance_fp64(DevMesh M, DevXS X, Run
     const int s = Q.adv[par][i];
     Particle p;
     load(B, s, p, kEig);
-    float4 R0, R1, R2, R3;
+    float4 O01, O23, D;
     int4 nb4;
-    load_tet32(M, p.elem, R0, R1, R2, R3, nb4);
+    load_oct(M, p.elem, O01, O23, D, nb4);
     int mnext = p.mat < 0 ? __ldg(M.tmat + p.elem) : 0;
     const int seg0 = p.n_seg;
     unsigned long long nxs = 0;
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(128) k_ev_advance_fp64(DevMesh M, DevXS X, Run
     float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
     double* const tal = tally_of(a, p.tag);
     for (;;) {
-      r = segment_fp64c<kEig>(M, X, p, uf, vf, wf, R0, R1, R2, R3, nb4, mnext, tal, a.ts, sigt32, nxs);
+      r = segment_fp64c<kEig>(M, X, p, uf, vf, wf, O01, O23, D, nb4, mnext, tal, a.ts, sigt32, nxs);
       if (r == 5) {
         uf = narrow(p.u);
         vf = narrow(p.v);
@@ -716,9 +716,10 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     float Ls;
     if (bf < 0 || t2 - t1 <= tol || t1 < -tol) {
       L.add(kCntFallback, 1);
-      Geo32 g{x, y, z, u, v, w};
+      // the compensated position (float sum and its rounding error)
       double Ld = 0.0;
-      bf = exit_fp64(M, elem, fin, g, Ld);
+      bf = exit_fp64d(M, elem, fin, widen(x) + widen(xl), widen(y) + widen(yl), widen(z) + widen(zl), widen(u),
+                      widen(v), widen(w), Ld);
       if (bf < 0) {
         r = 2;
         face = -2;
@@ -1004,13 +1005,13 @@ __global__ void __launch_bounds__(256) k_ev_finish(DevMesh M, DevXS X, RunArgs a
       // events are evaluated inline for the material entered
       float sigt32 = narrow(p.sigt);
       float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
-      float4 R0, R1, R2, R3;
+      float4 O01, O23, D;
       int4 nb4;
-      load_tet32(M, p.elem, R0, R1, R2, R3, nb4);
+      load_oct(M, p.elem, O01, O23, D, nb4);
       int mnext = p.mat < 0 ? __ldg(M.tmat + p.elem) : 0;
       double* const tal = tally_of(a, p.tag);
       while (p.status == kAlive) {
-        const int r = segment_fp64c<kEig>(M, X, p, uf, vf, wf, R0, R1, R2, R3, nb4, mnext, tal, a.ts, sigt32, nxs);
+        const int r = segment_fp64c<kEig>(M, X, p, uf, vf, wf, O01, O23, D, nb4, mnext, tal, a.ts, sigt32, nxs);
         if (r == 3) {
           const int mat = mnext;  // a material with no cached Sigma_t at this energy
           double nf = 0.0;
