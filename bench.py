@@ -84,7 +84,7 @@ REF_SAMPLE = 100_000
 # every walk launch of a 2 x 2e5-history lattice run (profiles/walk_*_lattice.md);
 # traffic per launch = this x the launch's segments
 ADVANCE_DRAM_BYTES_PER_SEG = 170.0
-MIXED_DRAM_BYTES_PER_SEG = 50.1
+MIXED_DRAM_BYTES_PER_SEG = 46.8
 # what bounds each walk instead of HBM, from the same captures' --set full
 # launch: the FP64 walk keeps the FP64 pipe 65% busy (GB300's FP64 rate is a
 # 64th of its FP32 rate); the mixed walk waits on its one dependent record

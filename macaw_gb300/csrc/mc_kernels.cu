@@ -716,10 +716,9 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     float Ls;
     if (bf < 0 || t2 - t1 <= tol || t1 < -tol) {
       L.add(kCntFallback, 1);
-      // the compensated position (float sum and its rounding error)
+      Geo32 g{x, y, z, u, v, w};
       double Ld = 0.0;
-      bf = exit_fp64d(M, elem, fin, widen(x) + widen(xl), widen(y) + widen(yl), widen(z) + widen(zl), widen(u),
-                      widen(v), widen(w), Ld);
+      bf = exit_fp64(M, elem, fin, g, Ld);
       if (bf < 0) {
         r = 2;
         face = -2;
