@@ -1364,14 +1364,35 @@ __global__ void __launch_bounds__(128) k_persist(PersistArgs a) {
     Particle p;
     start(P.M, o, idx, k, J.seed, p);
     p.tag = 0;
-    if (kPrec == MC_PREC_FP64) {
+    if (kPrec == MC_PREC_FP64 && p.status == kAlive) {
+      // the compact FP64 segment (records a step ahead), cross sections of
+      // each material entered evaluated inline
       float sigt32 = 0.0f;
       float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
+      float4 O01, O23, D;
+      int4 nb4;
+      load_oct(P.M, p.elem, O01, O23, D, nb4);
+      int mnext = __ldg(P.M.tmat + p.elem);
       while (p.status == kAlive) {
-        const int r = segment_fp64g<true, false, true, false>(P.M, P.X, p, uf, vf, wf, tally, P.ts, sigt32, nxs);
+        const int r = segment_fp64c<false>(P.M, P.X, p, uf, vf, wf, O01, O23, D, nb4, mnext, tally, P.ts, sigt32, nxs);
+        if (r == 3) {
+          const int mat = mnext;
+          const double sg = macro_total(P.X, mat, p.E);
+          ++nxs;
+          if (!(sg > 0.0) || sg != sg) {
+            p.status = kBadXS;
+            break;
+          }
+          p.sigt = sg;
+          xs_cache_put<false>(p, mat, sg, 0.0);
+          p.mat = mat;
+          sigt32 = narrow(sg);
+          continue;
+        }
         if (r == 1) {
           score_collision(P.X, P.ts, tally, p);
           collide<false>(P.X, p, P.two_d, EigArgs{});
+          mnext = __ldg(P.M.tmat + p.elem);
         }
         if (r == 1 || r == 5) {
           uf = narrow(p.u);
@@ -1379,7 +1400,7 @@ __global__ void __launch_bounds__(128) k_persist(PersistArgs a) {
           wf = narrow(p.w);
         }
       }
-    } else {
+    } else if (kPrec == MC_PREC_MIXED) {
       Geo32 g;
       geo_load(p, g);
       float inv_sig = 0.0f;
