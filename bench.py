@@ -83,18 +83,18 @@ REF_SAMPLE = 100_000
 # DRAM bytes per walked segment of the walk kernels, from ncu captures of
 # every walk launch of a 2 x 2e5-history lattice run (profiles/walk_*_lattice.md);
 # traffic per launch = this x the launch's segments
-ADVANCE_DRAM_BYTES_PER_SEG = 170.0
-MIXED_DRAM_BYTES_PER_SEG = 46.8
+ADVANCE_DRAM_BYTES_PER_SEG = 176.5
+MIXED_DRAM_BYTES_PER_SEG = 41.7
 # what bounds each walk instead of HBM, from the same captures' --set full
-# launch: the FP64 walk keeps the FP64 pipe 65% busy (GB300's FP64 rate is a
+# launch: the FP64 walk keeps the FP64 pipe 68% busy (GB300's FP64 rate is a
 # 64th of its FP32 rate); the mixed walk waits on its one dependent record
 # load per segment (L2 hit rate 48%, 29% of the warp slots occupied)
-FP64_PIPE_ACTIVE = 0.645
-MIXED_L2_HIT = 0.477
+FP64_PIPE_ACTIVE = 0.682
+MIXED_L2_HIT = 0.481
 # the same captures' L2 hit rate and warp execution efficiency (active
 # threads per executed instruction / 32), for the report
-FP64_L2_HIT = 0.417
-FP64_WARP_EFF = 22.12 / 32
+FP64_L2_HIT = 0.405
+FP64_WARP_EFF = 22.19 / 32
 MIXED_WARP_EFF = 20.30 / 32
 
 
@@ -268,7 +268,8 @@ def core_result(total, tune=True, batches=64):
     # 11.2M histories/s from 2M to 8M), the FP64 walk does not
     banks = {"mixed": 8_000_000, "fp64": 2_000_000}
     fixed = {"mixed": {"block_size": 256, "max_seg": 128, "sort_queue": 13, "refill": False, "graph": True},
-             "fp64": {"block_size": 256, "max_seg": 64, "sort_queue": 13, "refill": False, "graph": True}}
+             "fp64": {"block_size": 256, "max_seg": 64, "sort_queue": 13, "refill": False, "graph": True,
+                      "walk_blocks": 4}}
     out = {"metric": "histories/s, batched large-mesh form", "unit": "histories/s", "n_gpus": 1,
            "higher_is_better": True, "dtype": "f32+f64",
            "data": "synthetic (seeded generators)",
@@ -555,7 +556,8 @@ def run_profile(args):
         else problems.core_problem(pins=args.pins, radius=args.radius)
     with Tracker(0) as t:
         t.load(p)
-        kw = dict(bank_size=n, block_size=block, max_seg=max_seg, sort_queue=sort, precision=prec)
+        kw = dict(bank_size=n, block_size=block, max_seg=max_seg, sort_queue=sort, precision=prec,
+                  walk_blocks=args.walk_blocks)
         warm = t.run(n, first=0, seed=1, accumulate=True, **kw).as_dict()
         st = t.run(n * args.batches, first=n, seed=1, accumulate=True, batch_sizes=[n] * args.batches, **kw)
         print(json.dumps(dict(st.as_dict(), warm=warm)))
@@ -586,6 +588,8 @@ def main():
     ap.add_argument("--max-seg", type=int, default=0, help="--profile-run only: 0 = 128 mixed, 64 fp64")
     ap.add_argument("--sort", type=int, default=0, help="--profile-run only: 0 = 9 (lattice), 13 (core)")
     ap.add_argument("--radius", type=float, default=180.0, help="--profile-run only: core radius (cm)")
+    ap.add_argument("--walk-blocks", type=int, default=0,
+                    help="--profile-run only: FP64 walk build, 4 or 5 resident blocks per SM (0 = 5)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_run:
@@ -618,7 +622,7 @@ def main():
     p = problems.lattice_problem()
     stream = torch.cuda.Stream()
     # each rank owns a disjoint range of history indices (weak scaling)
-    base = rank * (W + 2 * K + 2) * n
+    base = rank * (W + 2 * K + 5) * n
 
     def barrier():
         if dist is not None:
@@ -635,8 +639,10 @@ def main():
                  "sort_queue": 9, "refill": False, "graph": True}
         if args.no_tune:
             return fixed, None
-        # trials: four pipelined batches of n/2 histories
-        params, rate = t.autotune(trial=2 * n, first=base + (W + 2 * K + 1) * n, bank_size=BANK,
+        # trials: four pipelined batches of n histories, the batch size of
+        # the timed steps (with batches of n/2 the tuner picked a mixed walk
+        # budget 3% slower on the steps)
+        params, rate = t.autotune(trial=4 * n, first=base + (W + 2 * K + 1) * n, bank_size=BANK,
                                   precision=precision, block_size=128, max_seg=64, sort_queue=9)
         return params, rate
 

@@ -150,6 +150,10 @@ typedef struct {
                                    buffer b receives the SUM tally as it stands when batch b has been
                                    folded in (copied while later batches run; pinned buffers let the copy
                                    overlap); needs accumulate */
+  int32_t walk_blocks;     /* event mode, MC_PREC_FP64: resident 128-thread blocks per SM the FP64
+                              walk kernel is compiled for -- 5 (96 registers, 20 warps per SM) or 4
+                              (118 registers, 16 warps); 0 = 5.  mc_autotune picks it per workload */
+  int32_t pad;
 } mc_run_desc;
 
 /* Per-history outcome: element sequence hash, counts, end state. */
@@ -408,8 +412,8 @@ int mc_run_persistent(const mc_persist_desc* desc, int32_t n_jobs, const mc_job*
  * whole GPU, a serving process that budgets HBM up front, code running where
  * an allocation would stall or fail) use mc_run_noalloc instead: it tracks
  * the same histories in the event form, but its scratch is one fixed array
- * of MC_NOALLOC_MAX_BANK particle slots (212 bytes each plus a control
- * block: about 3.47 MB) compiled into the library.  It calls no cudaMalloc,
+ * of MC_NOALLOC_MAX_BANK particle slots (220 bytes each plus a control
+ * block: about 3.60 MB) compiled into the library.  It calls no cudaMalloc,
  * cudaFree or other allocating routine.
  *
  * - The array and the event-form kernels are put on a device by

@@ -43,7 +43,7 @@ class RunDesc(C.Structure):
                 ("record_traces", C.c_int32), ("accumulate", C.c_int32), ("sort_queue", C.c_int32),
                 ("profile", C.c_int32), ("refill", C.c_int32), ("n_batches", C.c_int32), ("graph", C.c_int32),
                 ("tail", C.c_int32), ("sites", C.c_void_p), ("batch_sizes", C.c_void_p),
-                ("batch_sum_out", C.c_void_p)]
+                ("batch_sum_out", C.c_void_p), ("walk_blocks", C.c_int32), ("pad", C.c_int32)]
 
 
 class EigenDesc(C.Structure):

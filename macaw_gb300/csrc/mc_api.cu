@@ -107,8 +107,7 @@ struct mc_ctx {
   int64_t ray_first = 0;       // first_history of the last run that recorded
   long long h_limit = 0;
   // event bank
-  DevBuf b_x, b_y, b_z, b_u, b_v, b_w, b_E, b_wgt, b_sigt, b_seed, b_hash, b_id;
-  DevBuf b_elem, b_mat, b_nseg, b_ncoll, b_zero, b_fin, b_tag, b_cm, b_cs, b_cinv;
+  DevBuf b_rec, b_elem;                // particle records (kBankRec bytes a slot), element indices
   DevBuf b_nuf, b_ktl, b_cn, b_nprog;  // k-eigenvalue runs only
   // k-eigenvalue state (mc_eigen_run): source sites of the next generation,
   // the last generation's fission bank (append order, then sorted),
@@ -349,15 +348,9 @@ DevSource dev_source(mc_ctx* c) {
 int ensure_bank(mc_ctx* c, int64_t cap) {
   if (c->bank_cap == cap) return MC_OK;
   const size_t n = (size_t)cap;
-  DevBuf* d8[] = {&c->b_x, &c->b_y, &c->b_z, &c->b_u, &c->b_v, &c->b_w, &c->b_E,
-                  &c->b_wgt, &c->b_sigt, &c->b_seed, &c->b_hash, &c->b_id};
-  for (DevBuf* b : d8) CK(b->alloc(n * 8), "allocate particle bank");
-  DevBuf* d4[] = {&c->b_elem, &c->b_mat, &c->b_nseg, &c->b_ncoll, &c->b_zero, &c->b_fin, &c->b_tag,
-                  &c->q_xs0, &c->q_xs1, &c->q_adv0, &c->q_adv1, &c->q_coll, &c->q_free};
+  CK(c->b_rec.alloc(n * (size_t)kBankRec), "allocate particle bank");
+  DevBuf* d4[] = {&c->b_elem, &c->q_xs0, &c->q_xs1, &c->q_adv0, &c->q_adv1, &c->q_coll, &c->q_free};
   for (DevBuf* b : d4) CK(b->alloc(n * 4), "allocate particle bank");
-  CK(c->b_cm.alloc(n * 16), "allocate particle bank");
-  CK(c->b_cs.alloc(n * 32), "allocate particle bank");
-  CK(c->b_cinv.alloc(n * 16), "allocate particle bank");
   CK(c->d_ctl.alloc(sizeof(EventCtl)), "allocate event control");
   c->bank_cap = cap;
   return MC_OK;
@@ -375,16 +368,7 @@ int ensure_eig_bank(mc_ctx* c) {
 }
 
 Bank dev_bank(mc_ctx* c) {
-  Bank B{};
-  B.x = c->b_x.as<double>(); B.y = c->b_y.as<double>(); B.z = c->b_z.as<double>();
-  B.u = c->b_u.as<double>(); B.v = c->b_v.as<double>(); B.w = c->b_w.as<double>();
-  B.E = c->b_E.as<double>(); B.wgt = c->b_wgt.as<double>(); B.sigt = c->b_sigt.as<double>();
-  B.seed = c->b_seed.as<uint64_t>(); B.hash = c->b_hash.as<uint64_t>(); B.id = c->b_id.as<int64_t>();
-  B.elem = c->b_elem.as<int>(); B.mat = c->b_mat.as<int>(); B.n_seg = c->b_nseg.as<int>();
-  B.n_coll = c->b_ncoll.as<int>(); B.zero_run = c->b_zero.as<int>();
-  B.cm = c->b_cm.as<int4>(); B.cs = c->b_cs.as<double4_32a>(); B.fin = c->b_fin.as<int>();
-  B.cinv = c->b_cinv.as<float4>();
-  B.tag = c->b_tag.as<int>();
+  Bank B = bank_at(c->b_rec.p, c->b_elem.as<int>(), c->bank_cap);
   if (c->b_cn.p && c->b_cn.bytes >= (size_t)c->bank_cap * 32) {
     B.nuf = c->b_nuf.as<double>();
     B.ktl = c->b_ktl.as<double>();
@@ -662,6 +646,8 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
   if (rc) return rc;
   const int block = d->block_size > 0 ? d->block_size : 256;
   if (block % 32 != 0 || block > 256) return set_err(c, MC_ERR_ARG, "block size must be a multiple of 32, at most 256");
+  if (d->walk_blocks != 0 && d->walk_blocks != 4 && d->walk_blocks != 5)
+    return set_err(c, MC_ERR_ARG, "walk_blocks must be 0, 4 or 5");
   if (d->record_traces) {
     if (c->trace_n < d->n_histories) {
       CK(c->d_traces.alloc(sizeof(mc_trace) * (size_t)std::max<int64_t>(1, d->n_histories)), "allocate traces");
@@ -681,6 +667,7 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
   a.precision = d->precision;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.walk_blocks = d->walk_blocks;
   a.two_d = c->two_d;
   a.z2d = c->z2d;
   a.sort_shift = -1;

@@ -193,6 +193,51 @@ __device__ __forceinline__ void store(const Bank& B, int s, const Particle& p, b
   B.cs[s] = c;
 }
 
+// The fields one visit of the FP64 walk reads: all but the particle id and
+// the eigenvalue site count, which only the end of a history reads.
+__device__ __forceinline__ void load_walk(const Bank& B, int s, Particle& p, bool eig) {
+  if (eig) {
+    p.nuf = B.nuf[s];
+    p.ktl = B.ktl[s];
+    const double4_32a n = B.cn[s];
+    p.cn0 = n.x; p.cn1 = n.y; p.cn2 = n.z; p.cn3 = n.w;
+  }
+  p.x = B.x[s]; p.y = B.y[s]; p.z = B.z[s];
+  p.u = B.u[s]; p.v = B.v[s]; p.w = B.w[s];
+  p.E = B.E[s]; p.wgt = B.wgt[s]; p.sigt = B.sigt[s];
+  p.seed = B.seed[s]; p.hash = B.hash[s];
+  p.elem = B.elem[s]; p.mat = B.mat[s]; p.n_seg = B.n_seg[s]; p.n_coll = B.n_coll[s];
+  p.zero_run = B.zero_run[s];
+  p.fin = B.fin[s];
+  p.tag = B.tag[s];
+  p.cm = B.cm[s];
+  const double4_32a c = B.cs[s];
+  p.cs0 = c.x; p.cs1 = c.y; p.cs2 = c.z; p.cs3 = c.w;
+  p.status = kAlive;
+  p.face = -1;
+}
+
+// The fields one visit of the FP64 walk can change: position, direction
+// (reflections), Sigma_t and material (cache hits on entering a material),
+// RNG state, hash, element, counts and entry side (with nu*Sigma_f and the
+// keff sum in eigenvalue runs).  Energy, id and the cross-section cache
+// stay as they are in the bank: the walk hands a cache miss to the XS
+// kernel instead of filling the cache itself.
+__device__ __forceinline__ void store_walk(const Bank& B, int s, const Particle& p, bool eig) {
+  if (eig) {
+    B.nuf[s] = p.nuf;
+    B.ktl[s] = p.ktl;
+  }
+  B.x[s] = p.x; B.y[s] = p.y; B.z[s] = p.z;
+  B.u[s] = p.u; B.v[s] = p.v; B.w[s] = p.w;
+  B.seed[s] = p.seed; B.hash[s] = p.hash;
+  // the record's third sector written whole (weight and tag unchanged)
+  B.wgt[s] = p.wgt; B.fin[s] = p.fin; B.mat[s] = p.mat; B.n_seg[s] = p.n_seg;
+  B.zero_run[s] = p.zero_run; B.tag[s] = p.tag; B.n_coll[s] = p.n_coll;
+  B.sigt[s] = p.sigt;
+  B.elem[s] = p.elem;
+}
+
 __device__ __forceinline__ void birth(const DevMesh& M, const DevXS& X, const DevSource& S,
                                       const RunArgs& a, int64_t h, Particle& p) {
   // which batch / request of the birth sequence this history belongs to
@@ -462,8 +507,15 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
 // FP64 segment walk for the default tally (no ray recording): each lane
 // walks the particles of its warp's queue chunks one visit at a time with
 // segment_fp64c, whose element records are loaded one step ahead.
-template <bool kEig>
-__global__ void __launch_bounds__(128) k_ev_advance_fp64(DevMesh M, DevXS X, RunArgs a, Bank B, EventQueues Q,
+// kBlocks: resident 128-thread blocks per SM it is compiled for.  Five cap
+// it at 96 registers (a few spilled bytes; the keff score's variant spills
+// more) and give 20 warps per SM, four leave it the registers it takes
+// unconstrained and 16 warps.  Which is faster depends on the workload: on
+// the 2M-tet lattice five ran 78.5M histories/s against 76.8M, on the
+// 41M-tet core four ran 5.57M against 5.37M, and the k-eigenvalue walk
+// ran 20.7M with four against 20.0M with five.
+template <bool kEig, int kBlocks>
+__global__ void __launch_bounds__(128, kBlocks) k_ev_advance_fp64(DevMesh M, DevXS X, RunArgs a, Bank B, EventQueues Q,
                                                          EventCtl* ctl, int par) {
   MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_adv[par];
@@ -474,7 +526,7 @@ __global__ void __launch_bounds__(128) k_ev_advance_fp64(DevMesh M, DevXS X, Run
     if (i >= n) continue;
     const int s = Q.adv[par][i];
     Particle p;
-    load(B, s, p, kEig);
+    load_walk(B, s, p, kEig);
     float4 O01, O23, D;
     int4 nb4;
     load_oct(M, p.elem, O01, O23, D, nb4);
@@ -501,11 +553,13 @@ __global__ void __launch_bounds__(128) k_ev_advance_fp64(DevMesh M, DevXS X, Run
     }
     L.add(kCntSegWalk, (unsigned long long)(p.n_seg - seg0));
     if (r == 2) {
+      p.id = B.id[s];
+      if (kEig) p.n_prog = B.n_prog[s];
       finish(p, a, L);
       push_free(Q, ctl, s, B.cap);
       continue;
     }
-    store(B, s, p, kEig);
+    store_walk(B, s, p, kEig);
     if (r == 1) push(Q.coll, &ctl->n_coll, s);
     else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
     else push(Q.adv[nxt], &ctl->n_adv[nxt], s);
@@ -629,7 +683,7 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   int elem = __ldcs(B.elem + s), fin = __ldcs(B.fin + s), mat = __ldcs(B.mat + s), n_seg = __ldcs(B.n_seg + s),
       zrun = __ldcs(B.zero_run + s);
   const int seg0 = n_seg;
-  uint64_t seed = __ldcs((const unsigned long long*)B.seed + s), hash = __ldcs((const unsigned long long*)B.hash + s);
+  uint64_t seed = __ldcs((const unsigned long long*)(B.seed + s)), hash = __ldcs((const unsigned long long*)(B.hash + s));
   const double wgt = __ldcs(B.wgt + s);
   const bool unit_w = __double_as_longlong(wgt) == __double_as_longlong(1.0);
   double* const tal = tally_of(a, B.tag[s]);
@@ -816,10 +870,16 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   __stcs(B.x + s, widen(x) + widen(xl)); __stcs(B.y + s, widen(y) + widen(yl));
   __stcs(B.z + s, widen(z) + widen(zl));
   __stcs(B.u + s, widen(u)); __stcs(B.v + s, widen(v)); __stcs(B.w + s, widen(w));
-  __stcs(B.elem + s, elem); __stcs(B.fin + s, fin); __stcs(B.mat + s, mat); __stcs(B.n_seg + s, n_seg);
+  __stcs((unsigned long long*)(B.seed + s), (unsigned long long)seed);
+  __stcs((unsigned long long*)(B.hash + s), (unsigned long long)hash);
+  // the changed fields of the record's third sector only: re-reading the
+  // weight, tag and collision count to write the sector whole put a
+  // dependent load before the stores of every visit (164M against 200M
+  // histories/s on the 2M-tet lattice)
+  __stcs(B.fin + s, fin); __stcs(B.mat + s, mat); __stcs(B.n_seg + s, n_seg);
   __stcs(B.zero_run + s, zrun);
-  __stcs((unsigned long long*)B.seed + s, (unsigned long long)seed);
-  __stcs((unsigned long long*)B.hash + s, (unsigned long long)hash);
+  if (r == 1) B.n_coll[s] = B.n_coll[s] + 1;
+  __stcs(B.elem + s, elem);
   if (slot >= 0) {
     const double4_32a c = B.cs[s];
     B.sigt[s] = slot == 0 ? c.x : slot == 1 ? c.y : slot == 2 ? c.z : c.w;
@@ -829,7 +889,6 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
     }
   }
   if (kEig) B.ktl[s] = B.ktl[s] + wgt * widen(kacc);
-  if (r == 1) B.n_coll[s] = B.n_coll[s] + 1;
   if (queue) {
     if (r == 1) push(Q.coll, &ctl->n_coll, s);
     else if (r == 3) push(Q.xs[nxt], &ctl->n_xs[nxt], s);
@@ -1188,7 +1247,7 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
     else if (a.precision == MC_PREC_MIXED)
       k_ev_advance_static<MC_PREC_MIXED, false, true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else
-      k_ev_advance_fp64<true><<<grid, block < 128 ? block : 128, 0, st>>>(M, X, a, B, Q, ctl, par);
+      k_ev_advance_fp64<true, 4><<<grid, block < 128 ? block : 128, 0, st>>>(M, X, a, B, Q, ctl, par);
   } else if (a.precision == MC_PREC_MIXED) {
     // the compact walk scores the default tally and records no rays
     if (a.refill || a.ts.general || a.ts.rays) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
@@ -1196,7 +1255,9 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
   } else {
     if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
     else if (a.ts.rays) k_ev_advance_static<MC_PREC_FP64, true, false><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else k_ev_advance_fp64<false><<<grid, block < 128 ? block : 128, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else if (a.walk_blocks == 4)
+      k_ev_advance_fp64<false, 4><<<grid, block < 128 ? block : 128, 0, st>>>(M, X, a, B, Q, ctl, par);
+    else k_ev_advance_fp64<false, 5><<<grid, block < 128 ? block : 128, 0, st>>>(M, X, a, B, Q, ctl, par);
   }
   if (adv1) cudaEventRecord(adv1, st);
   if (a.eig.on) k_ev_collide<true><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
@@ -1364,35 +1425,18 @@ __global__ void __launch_bounds__(128) k_persist(PersistArgs a) {
     Particle p;
     start(P.M, o, idx, k, J.seed, p);
     p.tag = 0;
-    if (kPrec == MC_PREC_FP64 && p.status == kAlive) {
-      // the compact FP64 segment (records a step ahead), cross sections of
-      // each material entered evaluated inline
+    if (kPrec == MC_PREC_FP64) {
+      // the walk on the float-certified planes with cross sections inline:
+      // whole histories per lane touch the mesh in no order, and the compact
+      // segment's look-ahead loads and L1 prefetches cost more there than
+      // they hide (10M histories of the 41M-tet core: 2.6 s against 3.7 s)
       float sigt32 = 0.0f;
       float uf = narrow(p.u), vf = narrow(p.v), wf = narrow(p.w);
-      float4 O01, O23, D;
-      int4 nb4;
-      load_oct(P.M, p.elem, O01, O23, D, nb4);
-      int mnext = __ldg(P.M.tmat + p.elem);
       while (p.status == kAlive) {
-        const int r = segment_fp64c<false>(P.M, P.X, p, uf, vf, wf, O01, O23, D, nb4, mnext, tally, P.ts, sigt32, nxs);
-        if (r == 3) {
-          const int mat = mnext;
-          const double sg = macro_total(P.X, mat, p.E);
-          ++nxs;
-          if (!(sg > 0.0) || sg != sg) {
-            p.status = kBadXS;
-            break;
-          }
-          p.sigt = sg;
-          xs_cache_put<false>(p, mat, sg, 0.0);
-          p.mat = mat;
-          sigt32 = narrow(sg);
-          continue;
-        }
+        const int r = segment_fp64g<true, false, true, false>(P.M, P.X, p, uf, vf, wf, tally, P.ts, sigt32, nxs);
         if (r == 1) {
           score_collision(P.X, P.ts, tally, p);
           collide<false>(P.X, p, P.two_d, EigArgs{});
-          mnext = __ldg(P.M.tmat + p.elem);
         }
         if (r == 1 || r == 5) {
           uf = narrow(p.u);
@@ -1523,7 +1567,8 @@ cudaError_t preload_event_kernels() {
       (const void*)k_ev_advance<MC_PREC_MIXED>,
       (const void*)k_ev_advance<MC_PREC_FP64>,
       (const void*)k_ev_advance_mixed<false>,
-      (const void*)k_ev_advance_fp64<false>,
+      (const void*)k_ev_advance_fp64<false, 5>,
+      (const void*)k_ev_advance_fp64<false, 4>,
       (const void*)k_ev_collide<false>,
       (const void*)k_ev_refill,
       (const void*)k_ev_reset,

@@ -29,15 +29,42 @@ enum Counter : int {
   kNumCounters
 };
 
-// Particle bank in structure-of-arrays form.
+// Particle bank: one 192-byte record (six 32-byte sectors) per slot, plus
+// the element index in an array of its own.  A walk visits particles in
+// element order, so their slots are scattered: in separate arrays every
+// field a visit touches costs a sector of its own, here the fields a walk
+// visit moves share four sectors.
+//   sector 0: x y z u          sector 1: v w seed hash
+//   sector 2: wgt fin mat n_seg zero_run tag n_coll
+//   sector 3: cross-section cache keys, float 1/Sigma_t of the cached values
+//   sector 4: E sigt id         sector 5: cross-section cache values
+// (the mixed walk reads sectors 0-3 and writes 0-1 and the fields of 2 it
+// changed, the FP64 walk reads 0-5 and writes 0-2 and Sigma_t in 4).  The element array (4 bytes a slot) stays
+// in L2; the queue ordering reads it for every queued particle.
+// k-eigenvalue fields sit in arrays of their own.  RecField<T> addresses
+// one field of every record: B.x[s] is slot s's x, B.x + s its address.
+constexpr int64_t kBankRec = 192;
+
+template <class T>
+struct RecField {
+  unsigned char* base;  // the field in slot 0
+  __host__ __device__ __forceinline__ T& operator[](int64_t s) const {
+    return *reinterpret_cast<T*>(base + s * kBankRec);
+  }
+  __host__ __device__ __forceinline__ T* operator+(int64_t s) const {
+    return reinterpret_cast<T*>(base + s * kBankRec);
+  }
+};
+
 struct Bank {
-  double *x, *y, *z, *u, *v, *w, *E, *wgt, *sigt;
-  uint64_t *seed, *hash;
-  int64_t* id;
-  int *elem, *mat, *n_seg, *n_coll, *zero_run, *fin, *tag;
-  int4* cm;            // cross-section cache keys
-  double4_32a* cs;     // cross-section cache values
-  float4* cinv;        // float 1/Sigma_t of the cached values (mixed-precision walk)
+  RecField<double> x, y, z, u, v, w, E, wgt, sigt;
+  RecField<uint64_t> seed, hash;
+  RecField<int64_t> id;
+  RecField<int> mat, n_seg, n_coll, zero_run, fin, tag;
+  int* elem;                 // element index, one array
+  RecField<int4> cm;         // cross-section cache keys
+  RecField<double4_32a> cs;  // cross-section cache values
+  RecField<float4> cinv;     // float 1/Sigma_t of the cached values (mixed-precision walk)
   // k-eigenvalue runs only (null otherwise): nu*Sigma_f of the current
   // material and of the cached ones, track-length keff sum, sites banked
   double *nuf, *ktl;
@@ -46,15 +73,27 @@ struct Bank {
   int64_t cap;
 };
 
-// True when every array of the bank is set (checked on the host before any
-// launch that uses the bank).
-inline bool bank_complete(const Bank& B) {
-  const void* p[] = {B.x, B.y, B.z, B.u, B.v, B.w, B.E, B.wgt, B.sigt, B.seed, B.hash, B.id, B.elem,
-                     B.mat, B.n_seg, B.n_coll, B.zero_run, B.fin, B.tag, B.cm, B.cs, B.cinv};
-  for (const void* q : p)
-    if (!q) return false;
-  return B.cap > 0;
+// The bank whose records start at rec (cap * kBankRec bytes, 256-byte
+// aligned) with its element array elem (cap ints); the k-eigenvalue
+// arrays are left null.
+inline Bank bank_at(void* rec, int* elem, int64_t cap) {
+  unsigned char* r = static_cast<unsigned char*>(rec);
+  Bank B{};
+  B.x = {r + 0}; B.y = {r + 8}; B.z = {r + 16}; B.u = {r + 24};
+  B.v = {r + 32}; B.w = {r + 40}; B.seed = {r + 48}; B.hash = {r + 56};
+  B.wgt = {r + 64}; B.fin = {r + 72}; B.mat = {r + 76}; B.n_seg = {r + 80};
+  B.zero_run = {r + 84}; B.tag = {r + 88}; B.n_coll = {r + 92};
+  B.elem = elem;
+  B.cm = {r + 96}; B.cinv = {r + 112};
+  B.E = {r + 128}; B.sigt = {r + 136}; B.id = {r + 144};
+  B.cs = {r + 160};
+  B.cap = r ? cap : 0;
+  return B;
 }
+
+// True when the bank's records are set (checked on the host before any
+// launch that uses the bank).
+inline bool bank_complete(const Bank& B) { return B.x.base != nullptr && B.elem != nullptr && B.cap > 0; }
 
 // Event-loop control block (device memory).
 struct EventCtl {
@@ -112,6 +151,7 @@ struct RunArgs {
   int sort_buckets;  // (n_tet >> sort_shift) + 1
   int* sort_tmp;     // bank-capacity scratch for the ordering
   int* sort_cnt;     // sort_buckets + 1 counters
+  int walk_blocks;   // FP64 walk compiled for 4 or 5 resident blocks per SM (0: 5)
 };
 
 // Loads the fixed-source event-form kernels onto the current device.

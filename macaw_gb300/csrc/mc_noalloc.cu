@@ -25,19 +25,16 @@ using namespace mc;
 constexpr size_t kAlign = 256;
 constexpr size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
-// Per particle slot: 12 eight-byte fields, 7 four-byte fields, the XS cache
-// (16 + 32 bytes), its float inverses (16 bytes) and 6 four-byte queue
-// entries.
-constexpr size_t kSlotArrays8 = 12, kSlotArrays4 = 7 + 6;
+// Per particle slot: its kBankRec-byte record, its element index and 6
+// four-byte queue entries.
+constexpr size_t kSlotArrays4 = 1 + 6;
 constexpr size_t kScratchBytes =
-    kSlotArrays8 * align_up(8 * (size_t)MC_NOALLOC_MAX_BANK) +
-    kSlotArrays4 * align_up(4 * (size_t)MC_NOALLOC_MAX_BANK) +
-    2 * align_up(16 * (size_t)MC_NOALLOC_MAX_BANK) + align_up(32 * (size_t)MC_NOALLOC_MAX_BANK) +
+    align_up((size_t)kBankRec * MC_NOALLOC_MAX_BANK) + kSlotArrays4 * align_up(4 * (size_t)MC_NOALLOC_MAX_BANK) +
     align_up(sizeof(EventCtl)) + align_up(sizeof(unsigned long long) * kNumCounters) +
     align_up(sizeof(double));
 
-// The scratch (212 bytes per particle slot plus the control block and
-// counters: about 3.47 MB at 16,384 slots).  It lives in this translation
+// The scratch (220 bytes per particle slot plus the control block and
+// counters: about 3.61 MB at 16,384 slots).  It lives in this translation
 // unit's module, which the CUDA driver loads onto a device the first time
 // host code asks for the array's address; mc_ctx_create does that
 // (noalloc_prepare), so every device that has had a context holds these
@@ -147,6 +144,8 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   const int block = d->block_size > 0 ? d->block_size : 256;
   if (block % 32 != 0 || block > 256)
     return fail(MC_ERR_ARG, "block size must be a multiple of 32, at most 256");
+  if (d->walk_blocks != 0 && d->walk_blocks != 4 && d->walk_blocks != 5)
+    return fail(MC_ERR_ARG, "walk_blocks must be 0, 4 or 5");
 
   cudaError_t e = cudaSetDevice(v.device);
   if (e != cudaSuccess) return fail(MC_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
@@ -157,18 +156,8 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
 
   Carve cv{(unsigned char*)base};
   const size_t n = (size_t)cap;
-  Bank B{};
-  B.x = cv.take<double>(n); B.y = cv.take<double>(n); B.z = cv.take<double>(n);
-  B.u = cv.take<double>(n); B.v = cv.take<double>(n); B.w = cv.take<double>(n);
-  B.E = cv.take<double>(n); B.wgt = cv.take<double>(n); B.sigt = cv.take<double>(n);
-  B.seed = cv.take<uint64_t>(n); B.hash = cv.take<uint64_t>(n); B.id = cv.take<int64_t>(n);
-  B.elem = cv.take<int>(n); B.mat = cv.take<int>(n); B.n_seg = cv.take<int>(n);
-  B.n_coll = cv.take<int>(n); B.zero_run = cv.take<int>(n); B.fin = cv.take<int>(n);
-  B.tag = cv.take<int>(n);
-  B.cm = cv.take<int4>(n);
-  B.cs = cv.take<double4_32a>(n);
-  B.cinv = cv.take<float4>(n);
-  B.cap = cap;
+  unsigned char* rec = cv.take<unsigned char>(n * (size_t)kBankRec);
+  Bank B = bank_at(rec, cv.take<int>(n), cap);
   if (!bank_complete(B)) return fail(MC_ERR_STATE, "internal: particle bank incomplete");
   EventQueues Q{};
   Q.xs[0] = cv.take<int>(n); Q.xs[1] = cv.take<int>(n);
@@ -205,6 +194,7 @@ extern "C" int mc_run_noalloc(mc_ctx* ctx, const mc_run_desc* d, double* tally, 
   a.tol = v.tol;
   a.max_seg = d->max_seg_per_advance;
   a.refill = d->refill;
+  a.walk_blocks = d->walk_blocks;
   a.two_d = v.two_d;
   a.z2d = v.z2d;
   a.sort_shift = -1;  // ordering needs scratch beyond the fixed array

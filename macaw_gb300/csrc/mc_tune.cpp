@@ -1,9 +1,9 @@
 // mc_tune.cpp -- autotuner for the event form's execution parameters.
 //
 // Bank size, block shape, segments per walk launch, the advance-queue
-// ordering granularity, lane refill and CUDA-graph replay all move
-// throughput, and their best
-// values depend on the mesh, the cross sections and the precision form.
+// ordering granularity, lane refill, CUDA-graph replay and the FP64 walk's
+// register budget all move throughput, and their best values depend on the
+// mesh, the cross sections and the precision form.
 // mc_autotune measures them on trial runs of the context's own problem
 // (device time from the CUDA events inside mc_run) by coordinate descent:
 // each parameter in turn over its candidate values, the others held at
@@ -78,6 +78,7 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       // (bank sizes only when the caller left the bank open)
       {4, {0, 1}},                                                 // lane refill
       {5, {0, 1}},                                                 // CUDA-graph event cycles
+      {6, {5, 4}},                                                 // FP64 walk: resident blocks per SM
   };
   auto apply = [](mc_run_desc& d, int kind, int64_t v) {
     switch (kind) {
@@ -86,12 +87,14 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
       case 2: d.sort_queue = (int32_t)v; break;
       case 3: d.bank_size = v; break;
       case 4: d.refill = (int32_t)v; break;
-      default: d.graph = (int32_t)v; break;
+      case 5: d.graph = (int32_t)v; break;
+      default: d.walk_blocks = (int32_t)v; break;
     }
   };
   for (int pass = 0; pass < 2; ++pass) {
     for (const Knob& k : knobs) {
       if (k.kind == 3 && base->bank_size > 0) continue;
+      if (k.kind == 6 && cur.precision != MC_PREC_FP64) continue;
       mc_run_desc keep = cur;
       for (int64_t v : k.values) {
         mc_run_desc trial = keep;
@@ -113,6 +116,7 @@ extern "C" int mc_autotune(mc_ctx* ctx, const mc_run_desc* base, int64_t trial_h
   best->sort_queue = cur.sort_queue;
   best->refill = cur.refill;
   best->graph = cur.graph;
+  best->walk_blocks = cur.walk_blocks;
   best->bank_size = base->bank_size > 0 ? base->bank_size : cur.bank_size;
   if (best_rate) *best_rate = rate;
   return MC_OK;

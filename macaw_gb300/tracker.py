@@ -164,7 +164,7 @@ class Tracker:
             max_seg: int = 0, traces: bool = False, accumulate: bool = False,
             sort_queue: bool = False, profile: bool = False, sites: np.ndarray | None = None,
             refill: bool = False, batch_sizes=None, graph: bool = False, tail: int = 0,
-            batch_results=None) -> Stats:
+            batch_results=None, walk_blocks: int = 0) -> Stats:
         """One batch of n histories, or, with batch_sizes (adding up to n),
         consecutive batches run through one pipeline (needs accumulate).
         batch_results: one float64 array of tally_size() per batch, each
@@ -183,7 +183,7 @@ class Tracker:
                     int(accumulate), int(sort_queue), int(profile), int(refill), 0 if bs is None else bs.size,
                     int(graph), int(tail), None if sites is None else sites.ctypes.data,
                     None if bs is None else bs.ctypes.data,
-                    None if outs is None else C.cast(outs, C.c_void_p))
+                    None if outs is None else C.cast(outs, C.c_void_p), int(walk_blocks))
         self._ck(lib.mc_run(self._h, C.byref(d)), "mc_run")
         return self.stats()
 
@@ -223,12 +223,13 @@ class Tracker:
         d = RunDesc(base.get("first", 0), trial, base.get("bank_size", 0), base.get("seed", 1),
                     base.get("precision", MC_PREC_FP64), MC_MODE_EVENT, base.get("block_size", 0),
                     base.get("max_seg", 0), 0, 0, base.get("sort_queue", 0), 0, base.get("refill", 0), 0,
-                    base.get("graph", 0), 0, None, None)
+                    base.get("graph", 0), 0, None, None, None, base.get("walk_blocks", 0))
         out = RunDesc()
         rate = C.c_double()
         self._ck(lib.mc_autotune(self._h, C.byref(d), trial, C.byref(out), C.byref(rate)), "mc_autotune")
         return ({"bank_size": out.bank_size, "block_size": out.block_size, "max_seg": out.max_seg_per_advance,
-                 "sort_queue": out.sort_queue, "refill": bool(out.refill), "graph": bool(out.graph)},
+                 "sort_queue": out.sort_queue, "refill": bool(out.refill), "graph": bool(out.graph),
+                 "walk_blocks": out.walk_blocks},
                 rate.value)
 
     def sample_sites(self, n: int, first: int = 0, seed: int = 1, out: np.ndarray | None = None) -> np.ndarray:

@@ -77,6 +77,21 @@ def test_event_small_bank_and_segment_budget(cube, cube_oracle):
     assert_tally_close(tally, tally_o)
 
 
+@pytest.mark.parametrize("walk_blocks", [4, 5])
+def test_fp64_walk_register_budgets_bit_exact(cube, cube_oracle, walk_blocks):
+    """Both builds of the FP64 walk kernel (4 or 5 resident blocks per SM)
+    give the oracle's traces; any other value is refused."""
+    tally_o, tr_o, _, _ = cube_oracle
+    with Tracker(0) as t:
+        t.load(cube)
+        t.run(100000, seed=1, mode=MC_MODE_EVENT, bank_size=100000, max_seg=64, traces=True, graph=True,
+              walk_blocks=walk_blocks)
+        assert_traces_equal(t.traces(100000), tr_o)
+        assert_tally_close(t.tally(), tally_o)
+        with pytest.raises(RuntimeError):
+            t.run(1000, seed=1, mode=MC_MODE_EVENT, walk_blocks=3)
+
+
 def test_lattice_small_fp64_bit_exact():
     p = problems.lattice_problem(nx=3, ny=3, nz=4, height=10.0, n_pts=4000)
     tally_o, tr_o, st_o, _ = Oracle(p).run(20000, first=500, seed=3, threads=8)
