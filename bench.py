@@ -83,18 +83,18 @@ REF_SAMPLE = 100_000
 # DRAM bytes per walked segment of the walk kernels, from ncu captures of
 # every walk launch of a 2 x 2e5-history lattice run (profiles/walk_*_lattice.md);
 # traffic per launch = this x the launch's segments
-ADVANCE_DRAM_BYTES_PER_SEG = 176.5
+ADVANCE_DRAM_BYTES_PER_SEG = 176.0
 MIXED_DRAM_BYTES_PER_SEG = 41.7
 # what bounds each walk instead of HBM, from the same captures' --set full
-# launch: the FP64 walk keeps the FP64 pipe 68% busy (GB300's FP64 rate is a
+# launch: the FP64 walk keeps the FP64 pipe 64% busy (GB300's FP64 rate is a
 # 64th of its FP32 rate); the mixed walk waits on its one dependent record
 # load per segment (L2 hit rate 48%, 29% of the warp slots occupied)
-FP64_PIPE_ACTIVE = 0.682
+FP64_PIPE_ACTIVE = 0.644
 MIXED_L2_HIT = 0.481
 # the same captures' L2 hit rate and warp execution efficiency (active
 # threads per executed instruction / 32), for the report
-FP64_L2_HIT = 0.405
-FP64_WARP_EFF = 22.19 / 32
+FP64_L2_HIT = 0.406
+FP64_WARP_EFF = 22.29 / 32
 MIXED_WARP_EFF = 20.30 / 32
 
 

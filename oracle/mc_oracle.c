@@ -80,6 +80,27 @@ uint64_t oracle_init_seed(int64_t id, uint64_t master, int stream)
 }
 
 /* ------------------------------------------------------------------ */
+/* Exit distance num / den of the walk (den > 0): the correctly rounded
+ * float reciprocal of den, one Newton step in double, and the quotient
+ * corrected by its residual (P. Markstein, IBM J. Res. Dev. 34(1), 1990):
+ * within an ulp of the IEEE quotient.  A den whose float lies outside
+ * [2^-100, 2^100] takes the IEEE division.  The device walks compute the
+ * same sequence (exit_quotient), which needs five FP64 operations on the
+ * GPU against a division's more.  In the reference this distance is the
+ * MOOSE ray tracer's segment length, which onSegment reads as
+ * _current_segment_length (src/raykernels/CollisionKernel.C:154,163). */
+double oracle_exit_quotient(double num, double den)
+{
+  const float df = (float)den;
+  const float da = fabsf(df);
+  if (!(da >= 0x1p-100f && da <= 0x1p100f)) return num / den;
+  const double y0 = (double)(1.0f / df);
+  const double y1 = fma(y0, fma(-den, y0, 1.0), y0);
+  const double q0 = num * y1;
+  return fma(fma(-den, q0, num), y1, q0);
+}
+
+/* ------------------------------------------------------------------ */
 /* Natural log from the series ln(m) = 2 atanh((m-1)/(m+1)), m in
  * [sqrt(1/2), sqrt(2)), eleven odd terms, plus e*ln2 split hi/lo.      */
 double oracle_log(double x)
@@ -1099,7 +1120,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
       }
     }
     if (bf < 0) { status = ST_STUCK; break; }
-    double L = bnum / bden;
+    double L = oracle_exit_quotient(bnum, bden);
     if (!(L > 0.0)) L = 0.0;
     double dist = -oracle_log(oracle_prn(&strk)) / sigt;
     double score = (L < dist) ? L : dist;
