@@ -96,11 +96,27 @@ constexpr uint64_t kPrnStride = 152917ULL;
 constexpr int kStreamTracking = 0;
 constexpr int kStreamSource = 2;
 
+// k * 2^-53 for an integer k < 2^53, exactly.  On the device it is built
+// from the bits (the leading one's position gives the exponent) with
+// integer operations: the conversion and the multiply would issue on this
+// GPU's narrow FP64 pipe, and births draw about fifteen numbers each.  Both
+// forms are exact, so they give the same bits.
+MC_HD double unit53(uint64_t k) {
+#ifdef __CUDA_ARCH__
+  if (k == 0) return 0.0;
+  const int p = 63 - __clzll((long long)k);  // leading one, 0..52
+  const uint64_t b = ((uint64_t)(p + 970) << 52) | ((k << (52 - p)) & 0xfffffffffffffULL);
+  return __longlong_as_double((long long)b);
+#else
+  return (double)k * 0x1.0p-53;
+#endif
+}
+
 MC_HD double prn(uint64_t& s) {
   s = kPrnMult * s + kPrnAdd;
   uint64_t w = ((s >> ((s >> 59u) + 5u)) ^ s) * 12605985483714917081ULL;
   w = (w >> 43u) ^ w;
-  return (double)(w >> 11) * 0x1.0p-53;
+  return unit53(w >> 11);
 }
 
 // Affine map seed -> G*seed + C equal to n steps of the LCG.

@@ -1091,7 +1091,7 @@ __device__ __forceinline__ int segment_fp64g(const DevMesh& M, const DevXS& X, P
   if (lf > thr * 1.00001f + 1e-6f) {
     cross = true;
   } else {
-    const double xi = (double)(wv >> 11) * 0x1.0p-53;
+    const double xi = unit53(wv >> 11);
     dist = quotient(-mc::log64(xi), p.sigt);
     cross = dist > L;
   }
@@ -1250,7 +1250,7 @@ __device__ __forceinline__ int segment_fp64c(const DevMesh& M, const DevXS& X, P
   bool cross = cross_sure;
   double dist = 0.0;
   if (!cross_sure) {
-    const double xi = (double)(wv >> 11) * 0x1.0p-53;
+    const double xi = unit53(wv >> 11);
     dist = quotient(-mc::log64(xi), p.sigt);
     cross = dist > L;
     if (cross && nb >= 0) {

@@ -1285,10 +1285,12 @@ cudaError_t launch_event_finish(const DevMesh& M, const DevXS& X, const DevSourc
 // ---------------------------------------------------------------------------
 // Persistent form: one launch runs many batches, of one or more problems.
 // Every lane loops on its own (no barrier, no warp-wide operation):
-//   1. fold work first: a chunk of a batch whose histories have all ended is
-//      added to its problem's SUM/SUM_SQ and cleared in the batch's slot;
-//      the lane that folds a batch's last chunk passes the slot on to the
-//      batch n_slots later;
+//   1. fold work first, when batches share tally slots (fold_in_run): a
+//      chunk of a batch whose histories have all ended is added to its
+//      problem's SUM/SUM_SQ and cleared in the batch's slot; the lane that
+//      folds a batch's last chunk passes the slot on to the batch n_slots
+//      later (with a slot per batch, k_persist_fold_rest folds them all
+//      after the run);
 //   2. else it takes the next history index of the run (one atomic), finds
 //      its batch, waits (folding meanwhile) until the batch's tally slot is
 //      the batch's turn, and tracks the whole history with the batch's
@@ -1385,7 +1387,7 @@ __global__ void __launch_bounds__(128) k_persist(PersistArgs a) {
   unsigned long long nxs = 0, nfb = 0;
   for (;;) {
     if (vld(&c->error)) break;
-    if (persist_fold(a, sp, scan_lo)) continue;
+    if (a.fold_in_run && persist_fold(a, sp, scan_lo)) continue;
     const unsigned long long h = atomicAdd(&c->next, 1ULL);
     if (h >= a.total) break;
     const int j = persist_job_of(a, h);
@@ -1498,7 +1500,7 @@ __global__ void __launch_bounds__(128) k_persist(PersistArgs a) {
   // nothing left to take: help fold for a while (the tail's last histories
   // may still add ready batches), then leave; k_persist_fold_rest folds
   // whatever is left when the kernel ends
-  for (int idle = 0; idle < 2000 && !vld(&c->error) && vld(&c->folded) < (unsigned long long)a.n_jobs;) {
+  for (int idle = 0; a.fold_in_run && idle < 2000 && !vld(&c->error) && vld(&c->folded) < (unsigned long long)a.n_jobs;) {
     if (persist_fold(a, sp, scan_lo)) {
       idle = 0;
       continue;

@@ -219,6 +219,9 @@ struct PersistArgs {
   unsigned long long* counters;
   double* leak_w;
   long long wait_limit;        // polls a lane makes for a slot or for fold work before giving up
+  int fold_in_run;             // 1: some problem has fewer slots than batches, so lanes fold
+                               // ready batches during the run to free their slots; 0: every
+                               // batch has a slot of its own and k_persist_fold_rest folds all
 };
 
 cudaError_t launch_persistent(const PersistArgs& a, int precision, int block, int grid, cudaStream_t st);
