@@ -9,7 +9,6 @@
 //    atomics.  Grids are persistent and loop over the device-side queue
 //    lengths, so the host never needs the counts to launch.
 #include <cooperative_groups.h>
-#include <stdlib.h>
 
 #include "mc_kernels.h"
 
@@ -900,8 +899,8 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
 
 // Mixed-precision segment walk (mixed_visit), each lane walking the
 // particles of its warp's queue chunks one visit at a time.
-template <bool kEig, int kT = 256, int kB = 3>
-__global__ void __launch_bounds__(kT, kB) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B, EventQueues Q,
+template <bool kEig>
+__global__ void __launch_bounds__(256, 3) k_ev_advance_mixed(DevMesh M, RunArgs a, Bank B, EventQueues Q,
                                                              EventCtl* ctl, int par) {
   MC_COUNTERS(L);
   const int n = *(volatile int*)&ctl->n_adv[par];
@@ -1252,8 +1251,6 @@ cudaError_t launch_event_iteration(const DevMesh& M, const DevXS& X, const DevSo
   } else if (a.precision == MC_PREC_MIXED) {
     // the compact walk scores the default tally and records no rays
     if (a.refill || a.ts.general || a.ts.rays) k_ev_advance<MC_PREC_MIXED><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
-    else if (getenv("MC_MIXED_LB") && block <= 128)
-      k_ev_advance_mixed<false, 128, 7><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
     else k_ev_advance_mixed<false><<<grid, block, 0, st>>>(M, a, B, Q, ctl, par);
   } else {
     if (a.refill) k_ev_advance<MC_PREC_FP64><<<grid, block, 0, st>>>(M, X, a, B, Q, ctl, par);
