@@ -70,6 +70,7 @@ _SIG = {
     "oracle_eigen_run": ([_P, _I64, _I32, _I32, _U64, _D, _D, _D, _I64, C.c_int, _P, _P, _P, _P, _I64, _P, _P],
                          C.c_int),
     "oracle_log": ([_D], _D),
+    "oracle_quotient": ([_D, _D], _D),
     "oracle_prn": ([C.POINTER(_U64)], _D),
     "oracle_future_seed": ([_U64, _U64], _U64),
     "oracle_init_seed": ([_I64, _U64, C.c_int], _U64),
@@ -267,6 +268,11 @@ def cpu_threads() -> int:
 
 def log(x: float) -> float:
     return lib.oracle_log(x)
+
+
+def quotient(num: float, den: float) -> float:
+    """num / den as the walks compute it (Markstein's sequence)."""
+    return lib.oracle_quotient(num, den)
 
 
 def prn(seed: int):

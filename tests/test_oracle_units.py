@@ -23,6 +23,26 @@ def test_log_accuracy_and_specials():
     assert O.log(np.inf) == np.inf
 
 
+def test_quotient_within_an_ulp_of_the_ieee_division():
+    """The walks' num / den (float reciprocal, one Newton step, residual
+    correction) stays within an ulp of the correctly rounded quotient, and
+    a denominator outside the float range [2^-100, 2^100] takes the IEEE
+    division itself."""
+    rng = np.random.default_rng(7)
+    num = rng.uniform(-1.0, 1.0, 40000) * np.exp(rng.uniform(-40, 40, 40000))
+    den = rng.uniform(0.0, 1.0, 40000) * np.exp(rng.uniform(-60, 60, 40000)) + 1e-300
+    worst, exact = 0.0, 0
+    for a, b in zip(num, den):
+        q, ref = O.quotient(float(a), float(b)), float(a) / float(b)
+        worst = max(worst, ulp_err(q, ref))
+        exact += q == ref
+    assert worst <= 1.0, worst
+    assert exact / num.size > 0.99  # correctly rounded but in rare near-midpoint cases
+    for b in (2.0 ** -110, 2.0 ** 120, 3e-320):
+        assert O.quotient(1.234, b) == 1.234 / b
+    assert O.quotient(0.0, 3.0) == 0.0
+
+
 def test_prn_range_and_uniformity():
     s = O.init_seed(1, 1, 0)
     v = []
