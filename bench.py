@@ -83,18 +83,18 @@ REF_SAMPLE = 100_000
 # DRAM bytes per walked segment of the walk kernels, from ncu captures of
 # every walk launch of a 2 x 2e5-history lattice run (profiles/walk_*_lattice.md);
 # traffic per launch = this x the launch's segments
-ADVANCE_DRAM_BYTES_PER_SEG = 176.0
+ADVANCE_DRAM_BYTES_PER_SEG = 181.0
 MIXED_DRAM_BYTES_PER_SEG = 41.7
 # what bounds each walk instead of HBM, from the same captures' --set full
-# launch: the FP64 walk keeps the FP64 pipe 64% busy (GB300's FP64 rate is a
+# launch: the FP64 walk keeps the FP64 pipe 60% busy (GB300's FP64 rate is a
 # 64th of its FP32 rate); the mixed walk waits on its one dependent record
 # load per segment (L2 hit rate 48%, 29% of the warp slots occupied)
-FP64_PIPE_ACTIVE = 0.644
+FP64_PIPE_ACTIVE = 0.597
 MIXED_L2_HIT = 0.481
 # the same captures' L2 hit rate and warp execution efficiency (active
 # threads per executed instruction / 32), for the report
-FP64_L2_HIT = 0.406
-FP64_WARP_EFF = 22.29 / 32
+FP64_L2_HIT = 0.400
+FP64_WARP_EFF = 23.37 / 32
 MIXED_WARP_EFF = 20.30 / 32
 
 
@@ -683,9 +683,12 @@ def main():
         r0 = time.perf_counter()
         sum64 = reduce_tally(sum64)
         reduce_ms = (time.perf_counter() - r0) * 1e3
-    # one more batch with the walk launches timed (CUDA events around each
-    # walk launch, which turns graph replay off), for the walk's roofline
-    _, pst64 = timed(t, MC_PREC_FP64, params64, W + K, 1, True)
+    # the K steps once more on the next histories, pipelined as in the timed
+    # region, with the walk launches timed (CUDA events around each walk
+    # launch, which turns graph replay off), for the walk's roofline: a
+    # single batch would time the walk while its queue drains, which is not
+    # the state the timed steps run in
+    _, pst64 = timed(t, MC_PREC_FP64, params64, W + K, K, True)
 
     # --- mixed-precision form on the same histories ---
     mixed = None
@@ -699,8 +702,8 @@ def main():
         mms, mst = timed(tm, MC_PREC_MIXED, paramsm, W, K, False)
         clk_m = clocks_m.stop((w0m, time.time()))
         summ = tm.tally(MC_TALLY_SUM)
-        # one more batch with the walk launches timed, for the walk's roofline
-        _, pst = timed(tm, MC_PREC_MIXED, paramsm, W + K, 1, True)
+        # the K steps once more with the walk launches timed, for the walk's roofline
+        _, pst = timed(tm, MC_PREC_MIXED, paramsm, W + K, K, True)
         nz = sum64 > 0
         rel = np.abs(summ[nz] - sum64[nz]) / sum64[nz]
         mixed = {"value": world * n * K / (mms / 1e3), "unit": "histories/s", "ms_per_step": mms / K,
@@ -723,7 +726,8 @@ def main():
                                  "limiter": {"dependent_record_loads_l2_hit": MIXED_L2_HIT,
                                              "source": "ncu lts__t_sector_hit_rate (profiles/walk_mixed_lattice.md)"},
                                  "l2_hit_rate": MIXED_L2_HIT, "warp_execution_efficiency": MIXED_WARP_EFF,
-                                 "sample": f"one extra profiled batch of {n} histories"}
+                                 "sample": f"{K} more batches of {n} histories pipelined as in the timed region, "
+                                           "each walk launch timed by CUDA events (graph replay off)"}
 
     # --- end to end through the C ABI with host buffers ---
     # One pipelined mc_run streams the K steps: every step's 1e6 source sites
@@ -799,7 +803,8 @@ def main():
                 "algorithmic_bytes_per_segment": B_SEG_FP64,
                 "advance_ms_per_launch": pst64.ms_advance / max(pst64.n_advance_launch, 1),
                 "advance_share_of_step": pst64.ms_advance / pst64.ms_total if pst64.ms_total > 0 else None,
-                "sample": f"one extra profiled batch of {n} histories",
+                "sample": f"{K} more batches of {n} histories pipelined as in the timed region, each walk launch "
+                          "timed by CUDA events (graph replay off)",
                 "traffic_source": "ncu DRAM bytes per walked segment (profiles/walk_fp64_lattice.md) x segments "
                                   "per launch",
                 "limiter": {"fp64_pipe_active": FP64_PIPE_ACTIVE,

@@ -504,6 +504,14 @@ __global__ void __launch_bounds__(256) k_ev_advance_static(DevMesh M, DevXS X, R
   flush(L, a.counters, a.leak_w);
 }
 
+// A fixed-source FP64 visit also ends, for every lane still walking, once
+// fewer than this many lanes of a full warp are: the FP64 pipe issues for
+// all 32 lanes, so a warp kept busy by a few long visits wastes it (the
+// particles are re-queued where they stand).  12-16 lanes ran 98.2-98.7M
+// histories/s on the 2M-tet lattice against 96.8M without; 20 ran 97.2M.
+// The mixed walk, bound by its record loads instead, gained nothing.
+constexpr int kWalkMinLanes = 14;
+
 // FP64 segment walk for the default tally (no ray recording): each lane
 // walks the particles of its warp's queue chunks one visit at a time with
 // segment_fp64c, whose element records are loaded one step ahead.
@@ -523,6 +531,9 @@ __global__ void __launch_bounds__(128, kBlocks) k_ev_advance_fp64(DevMesh M, Dev
   for (;;) {
     const int i = take_chunk(&ctl->adv_head) + (int)(threadIdx.x & 31);
     if (__shfl_sync(0xffffffffu, i, 0) >= n) break;
+    // the lane floor applies to full chunks only: the queue's last, partial
+    // chunk would otherwise end its visits after every segment
+    const int min_lanes = (!kEig && __ballot_sync(0xffffffffu, i < n) == 0xffffffffu) ? kWalkMinLanes : 0;
     if (i >= n) continue;
     const int s = Q.adv[par][i];
     Particle p;
@@ -547,6 +558,10 @@ __global__ void __launch_bounds__(128, kBlocks) k_ev_advance_fp64(DevMesh M, Dev
       }
       if (r != 0) break;
       if (a.max_seg > 0 && ++k >= a.max_seg) {
+        r = 4;
+        break;
+      }
+      if (__popc(__activemask()) < min_lanes) {
         r = 4;
         break;
       }
