@@ -325,9 +325,11 @@ __device__ __forceinline__ void micro_xs(const DevXS& X, int nuc, int k, double 
 
 // Sigma_t = sum_i N_i sigma_t,i(E), in material order (OpenMC
 // Material::calculate_xs, called through event_calculate_xs).
-__device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E, int k) {
+// c: a cursor already at energy E (several materials evaluated at one
+// energy share it, so nuclides of different materials on one grid are
+// located once).
+__device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E, int k, GridCursor& c) {
   double acc = 0.0;
-  GridCursor c;
   const int j1 = __ldg(X.mat_off + mat + 1);
   for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
     double st, ss;
@@ -335,6 +337,11 @@ __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E,
     acc = fma(__ldg(X.mat_dens + j), st, acc);
   }
   return acc;
+}
+
+__device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E, int k) {
+  GridCursor c;
+  return macro_total(X, mat, E, k, c);
 }
 
 __device__ __forceinline__ double macro_total(const DevXS& X, int mat, double E) {
@@ -352,9 +359,9 @@ __device__ __forceinline__ double micro_nusf(const DevXS& X, int nuc, const Grid
 // Sigma_t and nu*Sigma_f = sum over the fissionable nuclides of
 // N_i nu*sigma_f,i(E), both in material order, in one pass (OpenMC
 // Material::calculate_xs fills macro_xs.total and macro_xs.nu_fission).
-__device__ __forceinline__ double macro_total_nuf(const DevXS& X, int mat, double E, int k, double& nuf) {
+__device__ __forceinline__ double macro_total_nuf(const DevXS& X, int mat, double E, int k, double& nuf,
+                                                  GridCursor& c) {
   double acc = 0.0, nf = 0.0;
-  GridCursor c;
   const bool fis = X.nusf && __ldg(X.mat_fiss + mat);
   const int j1 = __ldg(X.mat_off + mat + 1);
   for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
@@ -369,18 +376,31 @@ __device__ __forceinline__ double macro_total_nuf(const DevXS& X, int mat, doubl
   return acc;
 }
 
+__device__ __forceinline__ double macro_total_nuf(const DevXS& X, int mat, double E, int k, double& nuf) {
+  GridCursor c;
+  return macro_total_nuf(X, mat, E, k, nuf, c);
+}
+
 // Mixed-precision Sigma_t: the hash bin from a float log (grid_locate's
 // guards correct a bin that rounding moved by one), the grid interval
 // located in FP64 on the double grid, so the bracketing points are the
 // FP64 ones; the fraction, the interpolation and the sum over nuclides in
 // float.
 
+// The float cursor of macro_total32: the grid located last, its interval
+// and float fraction at the energy of the lookups that share it.
+struct GridCursor32 {
+  int g = -1, i = 0;
+  float f = 0.0f;
+};
+
 template <bool kNuf = false>
-__device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E, int k, float* nuf = nullptr) {
+__device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E, int k, GridCursor32& cur,
+                                               float* nuf = nullptr) {
   float acc = 0.0f, nf = 0.0f;
   const bool fis = kNuf && X.nusf && __ldg(X.mat_fiss + mat);
-  int gc = -1, i = 0;
-  float f = 0.0f;
+  int gc = cur.g, i = cur.i;
+  float f = cur.f;
   const int j1 = __ldg(X.mat_off + mat + 1);
   for (int j = __ldg(X.mat_off + mat); j < j1; ++j) {
     const int nuc = __ldg(X.mat_nuc + j);
@@ -402,8 +422,17 @@ __device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E
       nf = fmaf(N, fmaf(f, fb - fa, fa), nf);
     }
   }
+  cur.g = gc;
+  cur.i = i;
+  cur.f = f;
   if (kNuf) *nuf = nf;
   return acc;
+}
+
+template <bool kNuf = false>
+__device__ __forceinline__ float macro_total32(const DevXS& X, int mat, double E, int k, float* nuf = nullptr) {
+  GridCursor32 cur;
+  return macro_total32<kNuf>(X, mat, E, k, cur, nuf);
 }
 
 // ---------------------------------------------------------------------------

@@ -103,16 +103,18 @@ __device__ __forceinline__ void finish(Particle& p, const RunArgs& a, LocalCount
 // material changes at this energy hit the cache); false if unusable.
 // f32: the mixed-precision form's float interpolation (macro_total32).
 // eig: nu*Sigma_f of each evaluated material too.
+// c, c32: grid cursors shared by every material evaluated at this energy.
 __device__ __forceinline__ double eval_xs(const DevXS& X, int mat, double E, int k, bool f32, bool eig,
-                                          double& nf) {
+                                          double& nf, GridCursor& c, GridCursor32& c32) {
   nf = 0.0;
   if (f32) {
     float n32 = 0.0f;
-    const double s = eig ? widen(macro_total32<true>(X, mat, E, k, &n32)) : widen(macro_total32(X, mat, E, k));
+    const double s = eig ? widen(macro_total32<true>(X, mat, E, k, c32, &n32))
+                         : widen(macro_total32(X, mat, E, k, c32));
     nf = widen(n32);
     return s;
   }
-  return eig ? macro_total_nuf(X, mat, E, k, nf) : macro_total(X, mat, E, k);
+  return eig ? macro_total_nuf(X, mat, E, k, nf, c) : macro_total(X, mat, E, k, c);
 }
 
 __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int n_mat, bool f32, bool eig,
@@ -124,7 +126,9 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
   }
   const int k = xs_bucket32(X, p.E);
   double nf;
-  const double s = eval_xs(X, mat, p.E, k, f32, eig, nf);
+  GridCursor c;
+  GridCursor32 c32;
+  const double s = eval_xs(X, mat, p.E, k, f32, eig, nf, c, c32);
   L.add(kCntXS, 1);
   if (!(s > 0.0) || s != s) {
     p.status = kBadXS;
@@ -138,7 +142,7 @@ __device__ __forceinline__ bool refresh_xs(const DevMesh& M, const DevXS& X, int
     for (int m = 0; m < n_mat; ++m) {
       if (m == mat) continue;
       double onf;
-      const double o = eval_xs(X, m, p.E, k, f32, eig, onf);
+      const double o = eval_xs(X, m, p.E, k, f32, eig, onf, c, c32);
       L.add(kCntXS, 1);
       if (o > 0.0) xs_cache_put<true>(p, m, o, onf);
     }
