@@ -22,11 +22,12 @@ namespace mc {
 #ifdef __CUDACC__
 // float <-> double by integer operations, for the mixed-precision walk and
 // the quotient below: on this GPU a conversion instruction issues on the
-// narrow FP64 pipe, an integer operation on the full-rate ALU.  widen() is exact for every
-// normal float (zero and subnormals give a signed zero); narrow() rounds to
-// nearest even like a conversion for results in the normal float range and
-// gives a signed zero below it (|x| < 2^-126) -- positions, directions and
-// cross sections never leave that range except through zero.
+// narrow FP64 pipe, an integer operation on the full-rate ALU.  widen() is
+// exact for every normal float (zero and subnormals give a signed zero);
+// narrow() rounds to nearest even like a conversion for results in the
+// normal float range and gives a signed zero below it (|x| < 2^-126) --
+// positions, directions and cross sections never leave that range except
+// through zero.
 __device__ __forceinline__ double widen(float f) {
   const uint32_t b = __float_as_uint(f);
   const uint32_t e = (b >> 23) & 0xffu;

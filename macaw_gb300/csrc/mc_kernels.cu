@@ -702,7 +702,8 @@ __device__ __forceinline__ int mixed_visit(const DevMesh& M, const RunArgs& a, c
   int elem = __ldcs(B.elem + s), fin = __ldcs(B.fin + s), mat = __ldcs(B.mat + s), n_seg = __ldcs(B.n_seg + s),
       zrun = __ldcs(B.zero_run + s);
   const int seg0 = n_seg;
-  uint64_t seed = __ldcs((const unsigned long long*)(B.seed + s)), hash = __ldcs((const unsigned long long*)(B.hash + s));
+  uint64_t seed = __ldcs((const unsigned long long*)(B.seed + s));
+  uint64_t hash = __ldcs((const unsigned long long*)(B.hash + s));
   const double wgt = __ldcs(B.wgt + s);
   const bool unit_w = __double_as_longlong(wgt) == __double_as_longlong(1.0);
   double* const tal = tally_of(a, B.tag[s]);
@@ -1519,7 +1520,8 @@ __global__ void __launch_bounds__(128) k_persist(PersistArgs a) {
   // nothing left to take: help fold for a while (the tail's last histories
   // may still add ready batches), then leave; k_persist_fold_rest folds
   // whatever is left when the kernel ends
-  for (int idle = 0; a.fold_in_run && idle < 2000 && !vld(&c->error) && vld(&c->folded) < (unsigned long long)a.n_jobs;) {
+  for (int idle = 0;
+       a.fold_in_run && idle < 2000 && !vld(&c->error) && vld(&c->folded) < (unsigned long long)a.n_jobs;) {
     if (persist_fold(a, sp, scan_lo)) {
       idle = 0;
       continue;
