@@ -1,6 +1,7 @@
 // mc_kernels.h -- launchers for the tracking kernels (host-callable).
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "../../include/macaw_gb300.h"
@@ -39,8 +40,9 @@ enum Counter : int {
 //   sector 3: cross-section cache keys, float 1/Sigma_t of the cached values
 //   sector 4: E sigt id         sector 5: cross-section cache values
 // (the mixed walk reads sectors 0-3 and writes 0-1 and the fields of 2 it
-// changed, the FP64 walk reads 0-5 and writes 0-2 and Sigma_t in 4).  The element array (4 bytes a slot) stays
-// in L2; the queue ordering reads it for every queued particle.
+// changed, the FP64 walk reads 0-5 and writes 0-2 and Sigma_t in 4).  The
+// element array (4 bytes a slot) stays in L2; the queue ordering reads it
+// for every queued particle.
 // k-eigenvalue fields sit in arrays of their own.  RecField<T> addresses
 // one field of every record: B.x[s] is slot s's x, B.x + s its address.
 constexpr int64_t kBankRec = 192;
@@ -73,20 +75,41 @@ struct Bank {
   int64_t cap;
 };
 
+// One slot's record, the layout above (the walks address its fields
+// through RecField, never through this type).
+struct BankRecord {
+  double x, y, z, u;                                  // sector 0
+  double v, w;                                        // sector 1
+  uint64_t seed, hash;
+  double wgt;                                         // sector 2
+  int fin, mat, n_seg, zero_run, tag, n_coll;
+  int4 cm;                                            // sector 3
+  float4 cinv;
+  double E, sigt;                                     // sector 4
+  int64_t id, unused;
+  double4_32a cs;                                     // sector 5
+};
+static_assert(sizeof(BankRecord) == (size_t)kBankRec, "bank record is six 32-byte sectors");
+static_assert(offsetof(BankRecord, wgt) == 64 && offsetof(BankRecord, cm) == 96 &&
+                  offsetof(BankRecord, E) == 128 && offsetof(BankRecord, cs) == 160,
+              "bank record sectors");
+
 // The bank whose records start at rec (cap * kBankRec bytes, 256-byte
 // aligned) with its element array elem (cap ints); the k-eigenvalue
 // arrays are left null.
 inline Bank bank_at(void* rec, int* elem, int64_t cap) {
   unsigned char* r = static_cast<unsigned char*>(rec);
+#define MC_REC(f) {r + offsetof(BankRecord, f)}
   Bank B{};
-  B.x = {r + 0}; B.y = {r + 8}; B.z = {r + 16}; B.u = {r + 24};
-  B.v = {r + 32}; B.w = {r + 40}; B.seed = {r + 48}; B.hash = {r + 56};
-  B.wgt = {r + 64}; B.fin = {r + 72}; B.mat = {r + 76}; B.n_seg = {r + 80};
-  B.zero_run = {r + 84}; B.tag = {r + 88}; B.n_coll = {r + 92};
+  B.x = MC_REC(x); B.y = MC_REC(y); B.z = MC_REC(z); B.u = MC_REC(u);
+  B.v = MC_REC(v); B.w = MC_REC(w); B.seed = MC_REC(seed); B.hash = MC_REC(hash);
+  B.wgt = MC_REC(wgt); B.fin = MC_REC(fin); B.mat = MC_REC(mat); B.n_seg = MC_REC(n_seg);
+  B.zero_run = MC_REC(zero_run); B.tag = MC_REC(tag); B.n_coll = MC_REC(n_coll);
+  B.cm = MC_REC(cm); B.cinv = MC_REC(cinv);
+  B.E = MC_REC(E); B.sigt = MC_REC(sigt); B.id = MC_REC(id);
+  B.cs = MC_REC(cs);
+#undef MC_REC
   B.elem = elem;
-  B.cm = {r + 96}; B.cinv = {r + 112};
-  B.E = {r + 128}; B.sigt = {r + 136}; B.id = {r + 144};
-  B.cs = {r + 160};
   B.cap = r ? cap : 0;
   return B;
 }
