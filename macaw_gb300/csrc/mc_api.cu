@@ -777,16 +777,18 @@ int run_locked(mc_ctx* c, const mc_run_desc* d, const mc_site* dev_sites, const 
   a.live = nullptr;
   // history-form batches all score into slot 0 (one runs at a time);
   // event-form batch b scores into slot b % slots
-  // Host source sites: the first batches' sites are copied in stream order;
+  // Host source sites: the first batch's sites are copied in stream order;
   // in the event form the rest go on the copy stream, one copy per batch,
   // and the birth limit reaches batch b only after the tracker's stream
-  // has waited for b's copy, so the copies overlap the first batches' walks.
+  // has waited for b's copy, so the copies overlap the first batch's walks.
+  // (Copying two batches first ran within the spread on a box whose host
+  // copies were fast, and costs a batch's copy where they are slow.)
   int pre_b = nb;  // batches whose sites are copied in stream order
   if (!dev_sites && d->sites && d->n_histories > 0) {
     CK(cudaStreamSynchronize(c->copy_stream), "copy stream");
     CK(c->d_sites.alloc(std::max(c->d_sites.bytes, sizeof(mc_site) * (size_t)d->n_histories)), "allocate sites");
     a.sites = c->d_sites.as<mc_site>();
-    if (d->mode == MC_MODE_EVENT && nb > 2) pre_b = 2;
+    if (d->mode == MC_MODE_EVENT && nb > 1) pre_b = 1;
     CK(cudaMemcpyAsync(c->d_sites.p, d->sites, sizeof(mc_site) * (size_t)bend[pre_b - 1], cudaMemcpyHostToDevice,
                        c->stream),
        "upload sites");
