@@ -168,7 +168,10 @@ class Tracker:
         """One batch of n histories, or, with batch_sizes (adding up to n),
         consecutive batches run through one pipeline (needs accumulate).
         batch_results: one float64 array of tally_size() per batch, each
-        receiving the SUM tally as it stands once its batch is folded in."""
+        receiving the SUM tally as it stands once its batch is folded in.
+        walk_blocks: the FP64 walk kernel's build, 5 or 4 resident blocks of
+        128 threads per SM (0: 5); results are the same, speed depends on the
+        problem (autotune tries both)."""
         if sites is not None:
             assert sites.dtype == SITE_DTYPE and sites.size >= n and sites.flags["C_CONTIGUOUS"]
         bs = None if batch_sizes is None else np.ascontiguousarray(batch_sizes, np.int64)
